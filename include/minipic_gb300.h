@@ -1,0 +1,175 @@
+/*
+ * minipic_gb300.h -- C ABI of the GB300-native electrostatic PIC step.
+ *
+ * One mpg_ctx owns one CUDA stream on one GPU and the device-resident state
+ * of one PIC run: the tet mesh, the particle list, the field (rhs, phi, E)
+ * and the solver.  Calls on one ctx are serialised on its stream; separate
+ * ctxs are independent.  Every entry point returns an int status (MPG_OK = 0,
+ * negative = error class); mpg_last_error() returns the message.  No C++
+ * exception crosses this boundary and no entry point takes torch types.
+ *
+ * Each entry point names the reference interface it replaces (MiniPIC file:line).
+ * The reference is C++ only; include/minipic_gb300.hpp mirrors its classes
+ * (DataWarehouse, Mesh, ParticleList, ES, PIC, ParticleFill, ParticleMove) on
+ * top of these calls.
+ */
+#ifndef MINIPIC_GB300_H_
+#define MINIPIC_GB300_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define MPG_OK 0
+#define MPG_ERR_ARG (-1)           /* bad argument or size                              */
+#define MPG_ERR_CUDA (-2)          /* a CUDA runtime call failed                        */
+#define MPG_ERR_CAPACITY (-3)      /* particle capacity exceeded (particle_fill.hpp:61) */
+#define MPG_ERR_WALK_LIMIT (-4)    /* a particle exceeded the face-crossing limit       */
+#define MPG_ERR_NAN (-5)           /* non-finite value detected                         */
+#define MPG_ERR_NOT_CONVERGED (-6) /* Krylov solve hit max_iter                         */
+#define MPG_ERR_STATE (-7)         /* call order (e.g. no mesh yet)                     */
+#define MPG_ERR_MESH (-8)          /* mesh generation failed (detJ <= 0, bad split)     */
+#define MPG_ERR_TIMEOUT (-9)       /* a bounded device-side wait ran out                */
+
+/* ---- enums ------------------------------------------------------------- */
+#define MPG_PLAIN 0               /* FP64 throughout, reference semantics               */
+#define MPG_MIXED 1               /* FP32 push/walk, int64 fixed-point deposit, FP32 CG in FP64 refinement */
+
+#define MPG_DEPOSIT_REF_QUARTER 0 /* PIC.cpp:120-137: -w q/4 per node via cubature      */
+#define MPG_DEPOSIT_LINEAR 1      /* -w q lambda_i (linear-basis scatter)               */
+
+#define MPG_SOLVER_BICGSTAB 0     /* CG_solve.hpp:115-206 (x := 0, reference default)   */
+#define MPG_SOLVER_CG 1           /* CG_solve.hpp:54-114                                 */
+
+#define MPG_SPLIT_REF5 5          /* mesh.cpp:195-224 five-tet alternating split         */
+#define MPG_SPLIT_KUHN6 6         /* six Kuhn tets per hex                               */
+
+#define MPG_MAP_NONE 0            /* mesh.cpp:763-792 mappings 0..3                      */
+#define MPG_MAP_JITTER 4          /* interior nodes jittered by U(-j,j)*h per component  */
+
+#define MPG_FIELD_RHS 0
+#define MPG_FIELD_PHI 1
+#define MPG_FIELD_E_TET 2         /* T*3, constant per tet                               */
+#define MPG_FIELD_BACKGROUND 3
+
+typedef struct mpg_ctx mpg_ctx;
+
+/* replaces the brick.txt read of Mesh::Mesh (mesh.cpp:85-89): nx ny nz mapping */
+typedef struct {
+  int nx, ny, nz;
+  int split;       /* MPG_SPLIT_REF5 or MPG_SPLIT_KUHN6 */
+  double lo, hi;   /* box [lo,hi]^3; the reference uses [-1,1] */
+  int mapping;     /* MPG_MAP_* */
+  double jitter;   /* fraction of h, MPG_MAP_JITTER only */
+  uint64_t seed;   /* jitter seed */
+} mpg_mesh_desc;
+
+typedef struct {
+  int precision;         /* MPG_PLAIN / MPG_MIXED */
+  int deposit;           /* MPG_DEPOSIT_*; the mixed form always deposits linearly */
+  int solver;            /* MPG_SOLVER_*; the mixed form always uses refined CG */
+  double tol;            /* relative residual |b-Ax|/|b| (PIC.cpp:251 uses 1e-6) */
+  int max_iter;          /* CG_solve.hpp:144 uses 1000 */
+  int warm_start;        /* CG: start from the previous phi */
+  int kill_on_wall;      /* DataWarehouse::set_kill_particles_on_wall_impact */
+  int max_crossings;     /* face crossings per particle per step before MPG_ERR_WALK_LIMIT */
+  int sort_interval;     /* cell sort every k steps, 0 = never (ParticleList::sort) */
+  double rho_background; /* uniform background charge density (0 = none) */
+  int track_ids;         /* keep a 64-bit id per particle (parity checks) */
+} mpg_config;
+
+typedef struct {
+  double ke;             /* PIC.cpp:255-264 "Total KE" after the move */
+  int64_t n_alive;
+  int64_t n_killed;      /* removed at absorbing walls this step */
+  int64_t n_crossings;   /* face crossings this step */
+  int64_t n_walk_limit;  /* particles stopped by max_crossings */
+  int solver_iters;
+  double solver_resid;   /* relative residual at exit */
+  int status;
+  int steps;
+  /* device time per phase (ms), summed over the steps of the call;
+   * filled when mpg_set_timing(ctx, 1) */
+  double ms_deposit, ms_solve, ms_efield, ms_move, ms_sort;
+} mpg_step_stats;
+
+int mpg_version(void);
+int mpg_device_count(int *n);
+
+/* DataWarehouse::DataWarehouse (data_warehouse.cpp:46-48) */
+int mpg_ctx_create(int device, mpg_ctx **out);
+int mpg_ctx_destroy(mpg_ctx *ctx);
+/* copies the last error message of ctx (or of the last failed create) */
+int mpg_last_error(mpg_ctx *ctx, char *buf, int len);
+int mpg_set_timing(mpg_ctx *ctx, int on);
+
+/* DataWarehouse::create_mesh -> Mesh::Mesh (data_warehouse.cpp:50-54, mesh.cpp:78-714) */
+int mpg_mesh_build(mpg_ctx *ctx, const mpg_mesh_desc *desc);
+int mpg_mesh_sizes(mpg_ctx *ctx, int64_t *n_tets, int64_t *n_nodes, int64_t *n_boundary_nodes);
+/* Mesh public arrays (mesh.hpp:109-154): nodes N*3, elem_to_node T*4,
+ * elem_face_to_elem T*4 (-1 = wall, faces (0,1,3),(1,2,3),(0,3,2),(0,2,1)),
+ * inverse_jacobian T*9, determinate_jacobian T, normals T*12, boundary N.
+ * Host buffers; NULL skips an array. */
+int mpg_mesh_download(mpg_ctx *ctx, double *nodes, int32_t *tets, int32_t *nbrs, double *jinv, double *detj,
+                      double *normals, uint8_t *boundary);
+
+/* ParticleTypeList::add_particle_type (particle_type.hpp:58-84); defaults
+ * 0: e- (-1,1), 1: e+ (1,1), 2: H+ (1,1837); at most 16 species. */
+int mpg_species_set(mpg_ctx *ctx, int index, double q, double m);
+
+/* DataWarehouse::create_ES -> ES::ES (ES.cpp:47-213) plus the step options. */
+int mpg_configure(mpg_ctx *ctx, const mpg_config *cfg);
+/* CSR of the assembled stiffness matrix (Tpetra CrsMatrix of ES.cpp:114) */
+int mpg_csr_sizes(mpg_ctx *ctx, int64_t *n_rows, int64_t *nnz);
+int mpg_csr_download(mpg_ctx *ctx, int32_t *rowptr, int32_t *col, double *val);
+
+/* DataWarehouse::create_particle_list -> ParticleList::ParticleList (particle_list.cpp:44-68) */
+int mpg_particles_reserve(mpg_ctx *ctx, int64_t capacity);
+/* ParticleFill (particle_fill.hpp:59-164): nppe particles per tet, seeded per (elem, i, type) */
+int mpg_fill_ref(mpg_ctx *ctx, int nppe, int type, double density, const double vel[3], double temp);
+/* n particles uniform in volume from a seed, Maxwellian velocities of per-component
+ * sigma vth around drift; weight per particle given */
+int mpg_fill_uniform(mpg_ctx *ctx, int64_t n, uint64_t seed, int type, double weight, const double drift[3],
+                     double vth);
+/* ParticleList accessors x/x_ref/v/ielement/weight/type (particle_list.hpp:68-91):
+ * host arrays, (n,3) row-major for vectors; id may be NULL (ids = index). */
+int mpg_particles_upload(mpg_ctx *ctx, int64_t n, const int32_t *cell, const double *x, const double *xref,
+                         const double *v, const double *w, const int32_t *species, const int64_t *id);
+int mpg_particles_download(mpg_ctx *ctx, int64_t cap, int64_t *n, int32_t *cell, double *x, double *xref, double *v,
+                           double *w, int32_t *species, int64_t *id);
+/* ParticleList::num_particles (particle_list.hpp:165) */
+int mpg_particles_count(mpg_ctx *ctx, int64_t *n);
+/* raw mixed-form state: cellsp = species<<24 | cell (0xFFFFFFFF = dead),
+ * b = barycentric (3 floats), v (3 floats) */
+int mpg_mixed_download(mpg_ctx *ctx, int64_t cap, int64_t *n, uint32_t *cellsp, float *b, float *v);
+int mpg_mixed_upload(mpg_ctx *ctx, int64_t n, const uint32_t *cellsp, const float *b, const float *v);
+/* fixed-point charge accumulator of the mixed form (N int64) and its quantum */
+int mpg_charge_download(mpg_ctx *ctx, int64_t *acc, double *quantum, int64_t *qfix_of_species);
+
+/* ---- the step and its phases (PIC.cpp:245-267) ------------------------- */
+int mpg_weight_charge(mpg_ctx *ctx);                            /* PIC::weight_charge, PIC.cpp:139-160 */
+int mpg_solve(mpg_ctx *ctx, int *iters, double *resid);         /* ES::solve, ES.cpp:216-231           */
+int mpg_weight_efield(mpg_ctx *ctx);                            /* PIC::weight_Efield, PIC.cpp:186-189 */
+int mpg_move(mpg_ctx *ctx, double dt, mpg_step_stats *st);      /* ParticleMove::move, particle_move.hpp:398-404, plus KE */
+int mpg_step(mpg_ctx *ctx, double dt, int n_steps, mpg_step_stats *st); /* PIC::time_step x n_steps */
+int mpg_sort(mpg_ctx *ctx);                                     /* ParticleList::sort, particle_list.cpp:90-146 */
+
+/* ES::rhs / ES::phi / set_analytic_RHS-style access (ES.hpp:53-71) */
+int mpg_get_field(mpg_ctx *ctx, int which, double *host);
+int mpg_set_field(mpg_ctx *ctx, int which, const double *host);
+
+/* Stand-alone CSR solve on caller-owned DEVICE buffers: conjugate gradients
+ * on A x = b (A n x n, CSR with int32 indices, FP64), x holds the start
+ * vector and receives the result.  Scratch (4 n doubles + reduction slots)
+ * is allocated on first use and kept in ctx.  Replaces CG_solve
+ * (CG_solve.hpp:54-114) for callers that hold their own matrix. */
+int mpg_cg_csr(mpg_ctx *ctx, int64_t n, const int32_t *d_rowptr, const int32_t *d_col, const double *d_val,
+               const double *d_b, double *d_x, double tol, int max_iter, int *iters, double *resid);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1250 @@
+// api.cu -- C ABI of the GB300 PIC library (include/minipic_gb300.h).
+//
+// One mpg_ctx = one CUDA stream + the device-resident state of one run.  The
+// orchestration follows PIC::time_step (PIC.cpp:245-267):
+//   plain: deposit -> solve -> E per tet -> push+walk (+KE) -> compaction
+//   mixed: [fixed-point charge -> rhs] -> refined CG -> E per tet ->
+//          fused push+walk+deposit (+KE); cell sort every sort_interval steps
+// No step path copies field or particle data to the host.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "mpg_internal.h"
+#include "mpg_kernels.h"
+
+struct mpg_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  bool timing = false;
+  cudaEvent_t ev[12] = {};
+
+  bool has_mesh = false;
+  HostMesh hm;
+  DevMesh dm;
+
+  SpeciesTable sp{};
+  bool weight_set[MPG_MAX_SPECIES] = {};
+  double quantum = 0.0;
+  bool qfix_valid = false;
+
+  bool configured = false;
+  mpg_config cfg{};
+  int csr_mode = -1;
+  int64_t nnz = 0;
+  int32_t *rowptr = nullptr, *col = nullptr;
+  double *val = nullptr;
+  float *val32 = nullptr;
+  double *rhs = nullptr, *phi = nullptr, *bg = nullptr, *Etet = nullptr;
+  unsigned long long *acc = nullptr;
+  bool acc_valid = false;
+
+  int precision = MPG_PLAIN;  // precision of the allocated particle arrays
+  bool parts_alloc = false;
+  int64_t cap = 0, n = 0, want_cap = 0;
+  int64_t n_live = 0;  // live particles (the mixed form leaves holes until the next sort)
+  int cur = 0;
+  PlainParts pp[2]{};
+  MixedParts mp[2]{};
+  int64_t id_next = 0;
+  int64_t step_count = 0;
+
+  CgWork cg;
+  int64_t cg_n = 0;
+  double *bicg_work = nullptr, *red_dev = nullptr, *red_host = nullptr;
+  uint32_t *sort_cnt = nullptr, *sort_start = nullptr, *scan_scratch = nullptr;
+  int64_t scan_len = 0;
+  uint32_t *d_count = nullptr, *h_count = nullptr;
+  DevStats *d_stats = nullptr, *h_stats = nullptr;
+
+  std::vector<void *> allocs;  // device allocations owned by the ctx
+};
+
+static std::string g_last_create_error;
+
+namespace {
+
+int fail(mpg_ctx *c, int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf;
+  return code;
+}
+
+#define CK(call)                                                                                   \
+  do {                                                                                             \
+    cudaError_t e_ = (call);                                                                       \
+    if (e_ != cudaSuccess) return fail(c, MPG_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_));  \
+  } while (0)
+
+#define CKL()                                                                                      \
+  do {                                                                                             \
+    cudaError_t e_ = cudaGetLastError();                                                           \
+    if (e_ != cudaSuccess) return fail(c, MPG_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(e_)); \
+  } while (0)
+
+template <typename T>
+int dalloc(mpg_ctx *c, T **p, int64_t count) {
+  *p = nullptr;
+  if (count <= 0) count = 1;
+  cudaError_t e = cudaMalloc((void **)p, sizeof(T) * (size_t)count);
+  if (e != cudaSuccess) return fail(c, MPG_ERR_CUDA, "cudaMalloc(%lld bytes): %s", (long long)(sizeof(T) * count),
+                                    cudaGetErrorString(e));
+  c->allocs.push_back(*p);
+  return MPG_OK;
+}
+
+template <typename T>
+void dfree(mpg_ctx *c, T *&p) {
+  if (!p) return;
+  auto it = std::find(c->allocs.begin(), c->allocs.end(), (void *)p);
+  if (it != c->allocs.end()) c->allocs.erase(it);
+  cudaFree(p);
+  p = nullptr;
+}
+
+int check_ctx(mpg_ctx *c) {
+  if (!c) return MPG_ERR_ARG;
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e != cudaSuccess) return fail(c, MPG_ERR_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e));
+  return MPG_OK;
+}
+
+#define ENTER(c)                 \
+  do {                           \
+    int rc_ = check_ctx(c);      \
+    if (rc_) return rc_;         \
+  } while (0)
+#define TRY(x)                   \
+  do {                           \
+    int rc_ = (x);               \
+    if (rc_) return rc_;         \
+  } while (0)
+
+void default_species(SpeciesTable &s) {
+  // particle_type.hpp:65-74
+  for (int i = 0; i < MPG_MAX_SPECIES; ++i) {
+    s.q[i] = -1;
+    s.m[i] = 1;
+  }
+  s.q[0] = -1, s.m[0] = 1;
+  s.q[1] = 1, s.m[1] = 1;
+  s.q[2] = 1, s.m[2] = 1837;
+  for (int i = 0; i < MPG_MAX_SPECIES; ++i) {
+    s.qm[i] = s.q[i] / s.m[i];
+    s.qm_f[i] = (float)s.qm[i];
+    s.w[i] = 0.0;
+    s.qfix[i] = 0;
+    s.half_wm_f[i] = 0.f;
+  }
+}
+
+// scratch of the block scans (compaction over particles, sort over cells)
+int ensure_scan_scratch(mpg_ctx *c) {
+  const int64_t want = scan_scratch_len(std::max<int64_t>(std::max<int64_t>(c->cap, c->hm.T + 1), 1)) + 4;
+  if (c->scan_scratch && c->scan_len >= want) return MPG_OK;
+  dfree(c, c->scan_scratch);
+  TRY(dalloc(c, &c->scan_scratch, want));
+  c->scan_len = want;
+  return MPG_OK;
+}
+
+void free_particles(mpg_ctx *c) {
+  for (int k = 0; k < 2; ++k) {
+    dfree(c, c->pp[k].cell);
+    dfree(c, c->pp[k].x);
+    dfree(c, c->pp[k].xr);
+    dfree(c, c->pp[k].v);
+    dfree(c, c->pp[k].w);
+    dfree(c, c->pp[k].sp);
+    dfree(c, c->pp[k].id);
+    dfree(c, c->mp[k].c);
+    dfree(c, c->mp[k].b);
+    dfree(c, c->mp[k].v);
+    dfree(c, c->mp[k].id);
+    c->pp[k] = PlainParts{};
+    c->mp[k] = MixedParts{};
+  }
+  c->parts_alloc = false;
+  c->cap = 0;
+  c->n = 0;
+}
+
+int alloc_particles(mpg_ctx *c, int64_t cap) {
+  free_particles(c);
+  c->precision = c->cfg.precision;
+  const bool ids = c->cfg.track_ids != 0;
+  for (int k = 0; k < 2; ++k) {
+    if (c->precision == MPG_PLAIN) {
+      PlainParts &P = c->pp[k];
+      TRY(dalloc(c, &P.cell, cap));
+      TRY(dalloc(c, &P.x, 3 * cap));
+      TRY(dalloc(c, &P.xr, 3 * cap));
+      TRY(dalloc(c, &P.v, 3 * cap));
+      TRY(dalloc(c, &P.w, cap));
+      TRY(dalloc(c, &P.sp, cap));
+      if (ids) TRY(dalloc(c, &P.id, cap));
+      P.cap = cap;
+    } else {
+      MixedParts &X = c->mp[k];
+      TRY(dalloc(c, &X.c, cap));
+      TRY(dalloc(c, &X.b, cap));
+      TRY(dalloc(c, &X.v, cap));
+      if (ids) TRY(dalloc(c, &X.id, cap));
+      X.cap = cap;
+    }
+  }
+  c->cap = cap;
+  c->n = 0;
+  c->n_live = 0;
+  c->cur = 0;
+  c->parts_alloc = true;
+  TRY(ensure_scan_scratch(c));
+  c->acc_valid = false;
+  return MPG_OK;
+}
+
+int ensure_particles(mpg_ctx *c) {
+  if (!c->has_mesh) return fail(c, MPG_ERR_STATE, "no mesh: call mpg_mesh_build first");
+  if (!c->configured) return fail(c, MPG_ERR_STATE, "not configured: call mpg_configure first");
+  if (c->parts_alloc && c->precision == c->cfg.precision && c->cap >= c->want_cap) return MPG_OK;
+  if (c->want_cap <= 0) return fail(c, MPG_ERR_STATE, "no particle capacity: call mpg_particles_reserve");
+  return alloc_particles(c, c->want_cap);
+}
+
+// temporary plain buffers (stream-ordered allocations)
+struct TempPlain {
+  PlainParts P{};
+  std::vector<void *> ptrs;
+};
+int temp_plain(mpg_ctx *c, int64_t n, bool ids, TempPlain &t) {
+  auto get = [&](void **p, size_t bytes) -> int {
+    cudaError_t e = cudaMallocAsync(p, bytes ? bytes : 8, c->stream);
+    if (e != cudaSuccess) return fail(c, MPG_ERR_CUDA, "cudaMallocAsync: %s", cudaGetErrorString(e));
+    t.ptrs.push_back(*p);
+    return MPG_OK;
+  };
+  const int64_t m = n > 0 ? n : 1;
+  TRY(get((void **)&t.P.cell, sizeof(int32_t) * m));
+  TRY(get((void **)&t.P.x, sizeof(double) * 3 * m));
+  TRY(get((void **)&t.P.xr, sizeof(double) * 3 * m));
+  TRY(get((void **)&t.P.v, sizeof(double) * 3 * m));
+  TRY(get((void **)&t.P.w, sizeof(double) * m));
+  TRY(get((void **)&t.P.sp, sizeof(int32_t) * m));
+  if (ids) TRY(get((void **)&t.P.id, sizeof(int64_t) * m));
+  t.P.cap = m;
+  return MPG_OK;
+}
+void temp_free(mpg_ctx *c, TempPlain &t) {
+  for (void *p : t.ptrs) cudaFreeAsync(p, c->stream);
+  t.ptrs.clear();
+}
+
+void upload_species_derived(mpg_ctx *c) {
+  for (int i = 0; i < MPG_MAX_SPECIES; ++i) {
+    c->sp.qm[i] = c->sp.q[i] / c->sp.m[i];
+    c->sp.qm_f[i] = (float)c->sp.qm[i];
+    c->sp.half_wm_f[i] = (float)(0.5 * c->sp.w[i] * c->sp.m[i]);
+  }
+}
+
+// fixed-point quantum: the largest |w q| over species maps to 2^30 quanta
+void ensure_qfix(mpg_ctx *c) {
+  if (c->qfix_valid) return;
+  double mx = 0.0;
+  for (int i = 0; i < MPG_MAX_SPECIES; ++i)
+    if (c->weight_set[i]) mx = std::max(mx, fabs(c->sp.w[i] * c->sp.q[i]));
+  c->quantum = mx > 0 ? mx / 1073741824.0 : 1.0;
+  for (int i = 0; i < MPG_MAX_SPECIES; ++i)
+    c->sp.qfix[i] = c->weight_set[i] ? llround(c->sp.w[i] * c->sp.q[i] / c->quantum) : 0;
+  c->qfix_valid = true;
+}
+
+int set_species_weight(mpg_ctx *c, int s, double w) {
+  if (c->weight_set[s] && c->sp.w[s] != w) {
+    if (c->cfg.precision == MPG_MIXED)
+      return fail(c, MPG_ERR_ARG, "mixed form carries one weight per species (species %d: %g vs %g)", s, c->sp.w[s], w);
+  }
+  if (!c->weight_set[s] || c->sp.w[s] != w) {
+    c->sp.w[s] = w;
+    c->weight_set[s] = true;
+    c->qfix_valid = false;
+    c->acc_valid = false;
+    upload_species_derived(c);
+  }
+  return MPG_OK;
+}
+
+int ensure_cg_work(mpg_ctx *c, int64_t n) {
+  if (c->cg_n >= n && c->cg.r) return MPG_OK;
+  dfree(c, c->cg.r);
+  dfree(c, c->cg.p0);
+  dfree(c, c->cg.p1);
+  dfree(c, c->cg.q);
+  dfree(c, c->cg.r32);
+  dfree(c, c->cg.z32);
+  dfree(c, c->cg.q32);
+  dfree(c, c->cg.pa32);
+  dfree(c, c->cg.pb32);
+  dfree(c, c->cg.partials);
+  c->cg.max_blocks = cg_max_blocks(c->device);
+  TRY(dalloc(c, &c->cg.r, n));
+  TRY(dalloc(c, &c->cg.p0, n));
+  TRY(dalloc(c, &c->cg.p1, n));
+  TRY(dalloc(c, &c->cg.q, n));
+  TRY(dalloc(c, &c->cg.r32, n));
+  TRY(dalloc(c, &c->cg.z32, n));
+  TRY(dalloc(c, &c->cg.q32, n));
+  TRY(dalloc(c, &c->cg.pa32, n));
+  TRY(dalloc(c, &c->cg.pb32, n));
+  TRY(dalloc(c, &c->cg.partials, 4 * (int64_t)c->cg.max_blocks));
+  c->cg_n = n;
+  return MPG_OK;
+}
+
+int sync_stats(mpg_ctx *c) {
+  CK(cudaMemcpyAsync(c->h_stats, c->d_stats, sizeof(DevStats), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (c->h_stats->bar_error) return fail(c, MPG_ERR_TIMEOUT, "solver grid barrier timed out");
+  return MPG_OK;
+}
+
+int zero_stats(mpg_ctx *c) {
+  CK(cudaMemsetAsync(c->d_stats, 0, sizeof(DevStats), c->stream));
+  return MPG_OK;
+}
+
+void ev_record(mpg_ctx *c, int i) {
+  if (c->timing) cudaEventRecord(c->ev[i], c->stream);
+}
+double ev_ms(mpg_ctx *c, int a, int b) {
+  float ms = 0.f;
+  if (c->timing && cudaEventElapsedTime(&ms, c->ev[a], c->ev[b]) == cudaSuccess) return ms;
+  return 0.0;
+}
+
+// ---- phases ---------------------------------------------------------------
+int phase_deposit_plain(mpg_ctx *c) {
+  CK(cudaMemsetAsync(c->rhs, 0, sizeof(double) * c->dm.N, c->stream));
+  launch_plain_deposit(c->stream, c->pp[c->cur], c->n, c->dm, c->sp, c->cfg.deposit, c->rhs);
+  launch_rhs_finish(c->stream, c->dm.N, c->rhs, c->bg, c->dm.bnd);
+  CKL();
+  return MPG_OK;
+}
+
+int phase_deposit_mixed(mpg_ctx *c) {
+  if (!c->acc_valid) {
+    ensure_qfix(c);
+    CK(cudaMemsetAsync(c->acc, 0, sizeof(unsigned long long) * c->dm.N, c->stream));
+    launch_mixed_deposit(c->stream, c->mp[c->cur], c->n, c->dm, c->sp, c->acc);
+    c->acc_valid = true;
+  }
+  launch_mixed_convert(c->stream, c->dm.N, c->acc, c->quantum, c->bg, c->dm.bnd, c->rhs);
+  CKL();
+  return MPG_OK;
+}
+
+int phase_solve(mpg_ctx *c) {
+  const int64_t N = c->dm.N;
+  if (c->cfg.precision == MPG_MIXED) {
+    TRY(ensure_cg_work(c, N));
+    if (!c->cfg.warm_start) CK(cudaMemsetAsync(c->phi, 0, sizeof(double) * N, c->stream));
+    int rc = run_cg_mixed(c->stream, c->device, N, c->rowptr, c->col, c->val, c->val32, c->rhs, c->phi, c->cfg.tol,
+                          1e-5, c->cfg.max_iter, c->cg, c->d_stats);
+    if (rc) return fail(c, rc, "mixed CG launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+    return MPG_OK;
+  }
+  if (c->cfg.solver == MPG_SOLVER_CG) {
+    TRY(ensure_cg_work(c, N));
+    if (!c->cfg.warm_start) CK(cudaMemsetAsync(c->phi, 0, sizeof(double) * N, c->stream));
+    int rc = run_cg64(c->stream, c->device, N, c->rowptr, c->col, c->val, c->rhs, c->phi, c->cfg.tol,
+                      c->cfg.max_iter, c->cg, c->d_stats);
+    if (rc) return fail(c, rc, "CG launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+    return MPG_OK;
+  }
+  // reference BiCGStab (host-driven; parity mode)
+  if (!c->bicg_work) TRY(dalloc(c, &c->bicg_work, 5 * N));
+  int it = 0;
+  double res = 0.0;
+  int rc = run_bicgstab(c->stream, N, c->rowptr, c->col, c->val, c->rhs, c->phi, c->cfg.tol, c->cfg.max_iter,
+                        c->bicg_work, c->red_dev, c->red_host, &it, &res);
+  if (rc == MPG_ERR_CUDA) return fail(c, rc, "BiCGStab: %s", cudaGetErrorString(cudaGetLastError()));
+  // record into the device stats so both solver kinds report the same way
+  DevStats tmp;
+  CK(cudaMemcpyAsync(&tmp, c->d_stats, sizeof(DevStats), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  tmp.solver_iters = it;
+  tmp.iters_total += it;
+  tmp.solver_resid = res;
+  tmp.solver_status = rc ? 1 : 0;
+  if (rc) tmp.solver_fail = 1;
+  CK(cudaMemcpyAsync(c->d_stats, &tmp, sizeof(DevStats), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return MPG_OK;
+}
+
+int phase_efield(mpg_ctx *c) {
+  if (c->cfg.precision == MPG_MIXED)
+    launch_efield_mixed(c->stream, c->dm, c->phi);
+  else
+    launch_efield_plain(c->stream, c->dm, c->phi, c->Etet);
+  CKL();
+  return MPG_OK;
+}
+
+int compact_plain(mpg_ctx *c) {
+  const int other = 1 - c->cur;
+  launch_compact_plain(c->stream, c->pp[c->cur], c->n, c->pp[other], c->scan_scratch, c->scan_len, c->d_count);
+  CKL();
+  CK(cudaMemcpyAsync(c->h_count, c->d_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  c->cur = other;
+  c->n = *c->h_count;
+  return MPG_OK;
+}
+
+int sort_mixed(mpg_ctx *c) {
+  const int other = 1 - c->cur;
+  launch_mixed_sort(c->stream, c->mp[c->cur], c->n, c->mp[other], c->dm.T, c->sort_cnt, c->sort_start,
+                    c->scan_scratch, c->scan_len, c->d_count);
+  CKL();
+  c->cur = other;
+  // the new count is read back at the next host sync; slots [count, n) of the
+  // new buffer are marked dead so that the grid bound n stays valid
+  const int64_t n = c->n;
+  if (n > 0) {
+    launch_mark_tail_dead(c->stream, c->mp[c->cur].c, n, c->d_count);
+    CKL();
+  }
+  return MPG_OK;
+}
+
+int finish_counts_mixed(mpg_ctx *c, bool sorted) {
+  if (!sorted) return MPG_OK;
+  CK(cudaMemcpyAsync(c->h_count, c->d_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  c->n = *c->h_count;
+  return MPG_OK;
+}
+
+int one_step(mpg_ctx *c, double dt, mpg_step_stats *acc_st, bool &sorted) {
+  const bool mixed = c->cfg.precision == MPG_MIXED;
+  ev_record(c, 0);
+  TRY(mixed ? phase_deposit_mixed(c) : phase_deposit_plain(c));
+  ev_record(c, 1);
+  TRY(phase_solve(c));
+  ev_record(c, 2);
+  TRY(phase_efield(c));
+  ev_record(c, 3);
+  CK(cudaMemsetAsync(&c->d_stats->ke, 0, sizeof(double), c->stream));
+  if (mixed) {
+    launch_mixed_move(c->stream, c->mp[c->cur], c->n, c->dm, c->sp, (float)dt, c->cfg.kill_on_wall,
+                      c->cfg.max_crossings, c->acc, c->d_stats);
+  } else {
+    launch_plain_move(c->stream, c->pp[c->cur], c->n, c->dm, c->Etet, c->sp, dt, c->cfg.kill_on_wall,
+                      c->cfg.max_crossings, c->d_stats);
+  }
+  CKL();
+  ev_record(c, 4);
+  c->step_count++;
+  if (mixed) {
+    if (c->cfg.sort_interval > 0 && c->step_count % c->cfg.sort_interval == 0) {
+      TRY(sort_mixed(c));
+      sorted = true;
+    }
+  } else {
+    // the plain form compacts whenever particles were removed (particle_list.cpp:148-164)
+    TRY(sync_stats(c));
+    if (c->h_stats->n_killed > 0) {
+      TRY(compact_plain(c));
+      CK(cudaMemsetAsync(&c->d_stats->n_killed, 0, sizeof(unsigned long long), c->stream));
+      acc_st->n_killed += (int64_t)c->h_stats->n_killed;
+    }
+  }
+  ev_record(c, 5);
+  if (c->timing) {
+    CK(cudaEventSynchronize(c->ev[5]));
+    acc_st->ms_deposit += ev_ms(c, 0, 1);
+    acc_st->ms_solve += ev_ms(c, 1, 2);
+    acc_st->ms_efield += ev_ms(c, 2, 3);
+    acc_st->ms_move += ev_ms(c, 3, 4);
+    acc_st->ms_sort += ev_ms(c, 4, 5);
+  }
+  return MPG_OK;
+}
+
+int upload_mesh(mpg_ctx *c) {
+  HostMesh &h = c->hm;
+  DevMesh &d = c->dm;
+  d.T = h.T;
+  d.N = h.N;
+  TRY(dalloc(c, &d.tets, h.T));
+  TRY(dalloc(c, &d.nbrs, h.T));
+  TRY(dalloc(c, &d.jinv, 9 * h.T));
+  TRY(dalloc(c, &d.detj, h.T));
+  TRY(dalloc(c, &d.normals, 12 * h.T));
+  TRY(dalloc(c, &d.grad, 12 * h.T));
+  TRY(dalloc(c, &d.nodes, 3 * h.N));
+  TRY(dalloc(c, &d.bnd, h.N));
+  TRY(dalloc(c, &d.mrec, 3 * h.T));
+  TRY(dalloc(c, &d.mnbr, h.T));
+  TRY(dalloc(c, &d.fill_ratio, h.T));
+  cudaStream_t s = c->stream;
+  CK(cudaMemcpyAsync(d.tets, h.tets.data(), sizeof(int4) * h.T, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d.nbrs, h.nbrs.data(), sizeof(int4) * h.T, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d.jinv, h.jinv.data(), sizeof(double) * 9 * h.T, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d.detj, h.detj.data(), sizeof(double) * h.T, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d.normals, h.normals.data(), sizeof(double) * 12 * h.T, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d.grad, h.grad.data(), sizeof(double) * 12 * h.T, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d.nodes, h.nodes.data(), sizeof(double) * 3 * h.N, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d.bnd, h.bnd.data(), h.N, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d.mnbr, h.nbr_opp.data(), sizeof(uint4) * h.T, cudaMemcpyHostToDevice, s));
+  std::vector<float> rec(12 * h.T), ratio;
+  for (int64_t t = 0; t < h.T; ++t) {
+    for (int q = 0; q < 9; ++q) rec[12 * t + q] = (float)h.jinv[9 * t + q];
+    rec[12 * t + 9] = rec[12 * t + 10] = rec[12 * t + 11] = 0.f;
+  }
+  CK(cudaMemcpyAsync(d.mrec, rec.data(), sizeof(float) * 12 * h.T, cudaMemcpyHostToDevice, s));
+  host_fill_ratio(h, ratio);
+  CK(cudaMemcpyAsync(d.fill_ratio, ratio.data(), sizeof(float) * h.T, cudaMemcpyHostToDevice, s));
+  CK(cudaStreamSynchronize(s));
+  return MPG_OK;
+}
+
+void free_mesh(mpg_ctx *c) {
+  DevMesh &d = c->dm;
+  dfree(c, d.tets);
+  dfree(c, d.nbrs);
+  dfree(c, d.jinv);
+  dfree(c, d.detj);
+  dfree(c, d.normals);
+  dfree(c, d.grad);
+  dfree(c, d.nodes);
+  dfree(c, d.bnd);
+  dfree(c, d.mrec);
+  dfree(c, d.mnbr);
+  dfree(c, d.fill_ratio);
+  d = DevMesh();
+}
+
+void free_field(mpg_ctx *c) {
+  dfree(c, c->rowptr);
+  dfree(c, c->col);
+  dfree(c, c->val);
+  dfree(c, c->val32);
+  dfree(c, c->rhs);
+  dfree(c, c->phi);
+  dfree(c, c->bg);
+  dfree(c, c->Etet);
+  dfree(c, c->acc);
+  dfree(c, c->sort_cnt);
+  dfree(c, c->sort_start);
+  dfree(c, c->scan_scratch);
+  c->scan_len = 0;
+  dfree(c, c->bicg_work);
+  c->configured = false;
+  c->csr_mode = -1;
+}
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+int mpg_version(void) { return 1; }
+
+int mpg_device_count(int *n) {
+  if (!n) return MPG_ERR_ARG;
+  cudaError_t e = cudaGetDeviceCount(n);
+  if (e != cudaSuccess) {
+    *n = 0;
+    g_last_create_error = cudaGetErrorString(e);
+    return MPG_ERR_CUDA;
+  }
+  return MPG_OK;
+}
+
+int mpg_ctx_create(int device, mpg_ctx **out) {
+  if (!out) return MPG_ERR_ARG;
+  *out = nullptr;
+  int nd = 0;
+  cudaError_t e = cudaGetDeviceCount(&nd);
+  if (e != cudaSuccess || nd == 0) {
+    g_last_create_error = std::string("no CUDA device: ") + cudaGetErrorString(e);
+    return MPG_ERR_CUDA;
+  }
+  if (device < 0 || device >= nd) {
+    g_last_create_error = "device index out of range";
+    return MPG_ERR_ARG;
+  }
+  mpg_ctx *c = new (std::nothrow) mpg_ctx();
+  if (!c) return MPG_ERR_ARG;
+  c->device = device;
+  auto bail = [&](const char *what, cudaError_t err) {
+    g_last_create_error = std::string(what) + ": " + cudaGetErrorString(err);
+    delete c;
+    return MPG_ERR_CUDA;
+  };
+  if ((e = cudaSetDevice(device)) != cudaSuccess) return bail("cudaSetDevice", e);
+  if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess)
+    return bail("cudaStreamCreate", e);
+  for (int i = 0; i < 12; ++i)
+    if ((e = cudaEventCreate(&c->ev[i])) != cudaSuccess) return bail("cudaEventCreate", e);
+  if ((e = cudaMalloc(&c->d_stats, sizeof(DevStats))) != cudaSuccess) return bail("cudaMalloc", e);
+  if ((e = cudaMallocHost(&c->h_stats, sizeof(DevStats))) != cudaSuccess) return bail("cudaMallocHost", e);
+  if ((e = cudaMalloc(&c->d_count, sizeof(uint32_t))) != cudaSuccess) return bail("cudaMalloc", e);
+  if ((e = cudaMallocHost(&c->h_count, sizeof(uint32_t))) != cudaSuccess) return bail("cudaMallocHost", e);
+  if ((e = cudaMalloc(&c->red_dev, sizeof(double) * 512)) != cudaSuccess) return bail("cudaMalloc", e);
+  if ((e = cudaMallocHost(&c->red_host, sizeof(double) * 8)) != cudaSuccess) return bail("cudaMallocHost", e);
+  cudaMemsetAsync(c->d_stats, 0, sizeof(DevStats), c->stream);
+  default_species(c->sp);
+  c->cfg.precision = MPG_PLAIN;
+  c->cfg.deposit = MPG_DEPOSIT_REF_QUARTER;
+  c->cfg.solver = MPG_SOLVER_BICGSTAB;
+  c->cfg.tol = 1e-6;
+  c->cfg.max_iter = 1000;
+  c->cfg.max_crossings = 1000;
+  *out = c;
+  return MPG_OK;
+}
+
+int mpg_ctx_destroy(mpg_ctx *c) {
+  if (!c) return MPG_OK;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  for (void *p : c->allocs) cudaFree(p);
+  c->allocs.clear();
+  cudaFree(c->d_stats);
+  cudaFreeHost(c->h_stats);
+  cudaFree(c->d_count);
+  cudaFreeHost(c->h_count);
+  cudaFree(c->red_dev);
+  cudaFreeHost(c->red_host);
+  for (int i = 0; i < 12; ++i)
+    if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+  cudaStreamDestroy(c->stream);
+  delete c;
+  return MPG_OK;
+}
+
+int mpg_last_error(mpg_ctx *c, char *buf, int len) {
+  if (!buf || len <= 0) return MPG_ERR_ARG;
+  const std::string &m = c ? c->err : g_last_create_error;
+  snprintf(buf, (size_t)len, "%s", m.c_str());
+  return MPG_OK;
+}
+
+int mpg_set_timing(mpg_ctx *c, int on) {
+  if (!c) return MPG_ERR_ARG;
+  c->timing = on != 0;
+  return MPG_OK;
+}
+
+int mpg_mesh_build(mpg_ctx *c, const mpg_mesh_desc *d) {
+  ENTER(c);
+  if (!d) return fail(c, MPG_ERR_ARG, "null mesh descriptor");
+  CK(cudaStreamSynchronize(c->stream));
+  free_particles(c);
+  free_field(c);
+  free_mesh(c);
+  c->has_mesh = false;
+  std::string err;
+  int rc = host_mesh_generate(*d, c->hm, err);
+  if (rc) return fail(c, rc, "%s", err.c_str());
+  TRY(upload_mesh(c));
+  c->has_mesh = true;
+  c->step_count = 0;
+  return MPG_OK;
+}
+
+int mpg_mesh_sizes(mpg_ctx *c, int64_t *T, int64_t *N, int64_t *nb) {
+  if (!c) return MPG_ERR_ARG;
+  if (!c->has_mesh) return fail(c, MPG_ERR_STATE, "no mesh");
+  if (T) *T = c->hm.T;
+  if (N) *N = c->hm.N;
+  if (nb) *nb = c->hm.n_bnodes;
+  return MPG_OK;
+}
+
+int mpg_mesh_download(mpg_ctx *c, double *nodes, int32_t *tets, int32_t *nbrs, double *jinv, double *detj,
+                      double *normals, uint8_t *boundary) {
+  ENTER(c);
+  if (!c->has_mesh) return fail(c, MPG_ERR_STATE, "no mesh");
+  const DevMesh &d = c->dm;
+  cudaStream_t s = c->stream;
+  if (nodes) CK(cudaMemcpyAsync(nodes, d.nodes, sizeof(double) * 3 * d.N, cudaMemcpyDeviceToHost, s));
+  if (tets) CK(cudaMemcpyAsync(tets, d.tets, sizeof(int4) * d.T, cudaMemcpyDeviceToHost, s));
+  if (nbrs) CK(cudaMemcpyAsync(nbrs, d.nbrs, sizeof(int4) * d.T, cudaMemcpyDeviceToHost, s));
+  if (jinv) CK(cudaMemcpyAsync(jinv, d.jinv, sizeof(double) * 9 * d.T, cudaMemcpyDeviceToHost, s));
+  if (detj) CK(cudaMemcpyAsync(detj, d.detj, sizeof(double) * d.T, cudaMemcpyDeviceToHost, s));
+  if (normals) CK(cudaMemcpyAsync(normals, d.normals, sizeof(double) * 12 * d.T, cudaMemcpyDeviceToHost, s));
+  if (boundary) CK(cudaMemcpyAsync(boundary, d.bnd, d.N, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return MPG_OK;
+}
+
+int mpg_species_set(mpg_ctx *c, int i, double q, double m) {
+  if (!c) return MPG_ERR_ARG;
+  if (i < 0 || i >= MPG_MAX_SPECIES) return fail(c, MPG_ERR_ARG, "species index %d out of range", i);
+  if (!(m > 0)) return fail(c, MPG_ERR_ARG, "species mass must be positive");
+  c->sp.q[i] = q;
+  c->sp.m[i] = m;
+  upload_species_derived(c);
+  c->qfix_valid = false;
+  c->acc_valid = false;
+  return MPG_OK;
+}
+
+int mpg_configure(mpg_ctx *c, const mpg_config *cfg) {
+  ENTER(c);
+  if (!cfg) return fail(c, MPG_ERR_ARG, "null config");
+  if (!c->has_mesh) return fail(c, MPG_ERR_STATE, "no mesh: call mpg_mesh_build first");
+  if (cfg->precision != MPG_PLAIN && cfg->precision != MPG_MIXED) return fail(c, MPG_ERR_ARG, "bad precision");
+  if (cfg->deposit != MPG_DEPOSIT_REF_QUARTER && cfg->deposit != MPG_DEPOSIT_LINEAR)
+    return fail(c, MPG_ERR_ARG, "bad deposit mode");
+  if (cfg->solver != MPG_SOLVER_BICGSTAB && cfg->solver != MPG_SOLVER_CG) return fail(c, MPG_ERR_ARG, "bad solver");
+  if (!(cfg->tol > 0) || cfg->max_iter < 1 || cfg->max_crossings < 1)
+    return fail(c, MPG_ERR_ARG, "tol, max_iter and max_crossings must be positive");
+  if (cfg->precision == MPG_MIXED && c->hm.T >= (int64_t)MPG_WALL)
+    return fail(c, MPG_ERR_ARG, "mixed form holds cell ids in 24 bits (T < %u)", MPG_WALL);
+  CK(cudaStreamSynchronize(c->stream));
+  const bool realloc_parts = c->parts_alloc && (c->cfg.precision != cfg->precision ||
+                                                (cfg->track_ids != 0) != (c->cfg.track_ids != 0));
+  if (realloc_parts) free_particles(c);
+  c->cfg = *cfg;
+  // the mixed form always solves the symmetric system with refined CG
+  const int mode = (cfg->precision == MPG_MIXED || cfg->solver == MPG_SOLVER_CG) ? 1 : 0;
+  const int64_t N = c->hm.N, T = c->hm.T;
+  if (c->csr_mode != mode) {
+    dfree(c, c->rowptr);
+    dfree(c, c->col);
+    dfree(c, c->val);
+    dfree(c, c->val32);
+    std::vector<int32_t> rp, col;
+    std::vector<double> val;
+    host_csr_assemble(c->hm, mode, rp, col, val);
+    c->nnz = (int64_t)val.size();
+    TRY(dalloc(c, &c->rowptr, N + 1));
+    TRY(dalloc(c, &c->col, c->nnz));
+    TRY(dalloc(c, &c->val, c->nnz));
+    TRY(dalloc(c, &c->val32, c->nnz));
+    std::vector<float> v32(val.begin(), val.end());
+    CK(cudaMemcpyAsync(c->rowptr, rp.data(), sizeof(int32_t) * (N + 1), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->col, col.data(), sizeof(int32_t) * c->nnz, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->val, val.data(), sizeof(double) * c->nnz, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->val32, v32.data(), sizeof(float) * c->nnz, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->csr_mode = mode;
+  }
+  if (!c->rhs) {
+    TRY(dalloc(c, &c->rhs, N));
+    TRY(dalloc(c, &c->phi, N));
+    TRY(dalloc(c, &c->Etet, 3 * T));
+    TRY(dalloc(c, &c->acc, N));
+    TRY(dalloc(c, &c->sort_cnt, T + 1));
+    TRY(dalloc(c, &c->sort_start, T + 1));
+    CK(cudaMemsetAsync(c->phi, 0, sizeof(double) * N, c->stream));
+    CK(cudaMemsetAsync(c->Etet, 0, sizeof(double) * 3 * T, c->stream));
+  }
+  dfree(c, c->bg);
+  if (cfg->rho_background != 0.0) {
+    std::vector<double> bg;
+    host_background(c->hm, cfg->rho_background, bg);
+    TRY(dalloc(c, &c->bg, N));
+    CK(cudaMemcpyAsync(c->bg, bg.data(), sizeof(double) * N, cudaMemcpyHostToDevice, c->stream));
+  }
+  c->configured = true;
+  c->acc_valid = false;
+  CK(cudaStreamSynchronize(c->stream));
+  return MPG_OK;
+}
+
+int mpg_csr_sizes(mpg_ctx *c, int64_t *rows, int64_t *nnz) {
+  if (!c) return MPG_ERR_ARG;
+  if (!c->configured) return fail(c, MPG_ERR_STATE, "not configured");
+  if (rows) *rows = c->hm.N;
+  if (nnz) *nnz = c->nnz;
+  return MPG_OK;
+}
+
+int mpg_csr_download(mpg_ctx *c, int32_t *rowptr, int32_t *col, double *val) {
+  ENTER(c);
+  if (!c->configured) return fail(c, MPG_ERR_STATE, "not configured");
+  if (rowptr)
+    CK(cudaMemcpyAsync(rowptr, c->rowptr, sizeof(int32_t) * (c->hm.N + 1), cudaMemcpyDeviceToHost, c->stream));
+  if (col) CK(cudaMemcpyAsync(col, c->col, sizeof(int32_t) * c->nnz, cudaMemcpyDeviceToHost, c->stream));
+  if (val) CK(cudaMemcpyAsync(val, c->val, sizeof(double) * c->nnz, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return MPG_OK;
+}
+
+int mpg_particles_reserve(mpg_ctx *c, int64_t capacity) {
+  ENTER(c);
+  if (capacity <= 0 || capacity >= (1LL << 31)) return fail(c, MPG_ERR_ARG, "capacity out of range");
+  if (c->parts_alloc && c->n > 0 && !(c->cap == capacity && c->precision == c->cfg.precision))
+    return fail(c, MPG_ERR_STATE, "cannot resize a non-empty particle list");
+  c->want_cap = capacity;
+  if (c->configured && !(c->parts_alloc && c->cap == capacity && c->precision == c->cfg.precision)) {
+    CK(cudaStreamSynchronize(c->stream));
+    return alloc_particles(c, capacity);
+  }
+  return MPG_OK;
+}
+
+int mpg_particles_count(mpg_ctx *c, int64_t *n) {
+  if (!c || !n) return MPG_ERR_ARG;
+  *n = c->parts_alloc ? c->n_live : 0;
+  return MPG_OK;
+}
+
+int mpg_fill_ref(mpg_ctx *c, int nppe, int type, double density, const double vel[3], double temp) {
+  ENTER(c);
+  TRY(ensure_particles(c));
+  if (nppe < 1 || type < 0 || type >= MPG_MAX_SPECIES) return fail(c, MPG_ERR_ARG, "bad nppe or type");
+  const int64_t add = c->hm.T * (int64_t)nppe;
+  if (c->n + add > c->cap)  // particle_fill.hpp:61-64 (the reference prints and skips)
+    return fail(c, MPG_ERR_CAPACITY, "Cannot create that number of particles, no fill performed");
+  const double v0[3] = {0, 0, 0};
+  const double *vel3 = vel ? vel : v0;
+  const double mass = c->sp.m[type];
+  if (c->cfg.precision == MPG_PLAIN) {
+    launch_fill_ref(c->stream, c->pp[c->cur], c->n, nppe, type, density, vel3, temp, mass, c->dm, c->id_next);
+    CKL();
+    c->weight_set[type] = true;
+  } else {
+    TempPlain t;
+    TRY(temp_plain(c, add, c->cfg.track_ids != 0, t));
+    launch_fill_ref(c->stream, t.P, 0, nppe, type, density, vel3, temp, mass, c->dm, c->id_next);
+    MixedParts X = c->mp[c->cur];
+    // shift the destination by n: convert into slots [n, n+add)
+    X.c += c->n;
+    X.b += c->n;
+    X.v += c->n;
+    if (X.id) X.id += c->n;
+    launch_plain_to_mixed(c->stream, t.P, 0, add, X);
+    CKL();
+    temp_free(c, t);
+    double vol = 0.0;
+    for (int64_t i = 0; i < c->hm.T; ++i) vol += c->hm.detj[i] / 6.;
+    TRY(set_species_weight(c, type, density * (vol / c->hm.T) / nppe));
+  }
+  c->n += add;
+  c->n_live += add;
+  c->id_next += add;
+  c->acc_valid = false;
+  CK(cudaStreamSynchronize(c->stream));
+  return MPG_OK;
+}
+
+int mpg_fill_uniform(mpg_ctx *c, int64_t n, uint64_t seed, int type, double weight, const double drift[3],
+                     double vth) {
+  ENTER(c);
+  TRY(ensure_particles(c));
+  if (n < 0 || type < 0 || type >= MPG_MAX_SPECIES) return fail(c, MPG_ERR_ARG, "bad count or type");
+  if (c->n + n > c->cap) return fail(c, MPG_ERR_CAPACITY, "fill of %lld exceeds capacity", (long long)n);
+  if (c->cfg.precision == MPG_MIXED && c->n + n >= (1LL << 32))
+    return fail(c, MPG_ERR_ARG, "too many particles");
+  const double d0[3] = {0, 0, 0};
+  TRY(set_species_weight(c, type, weight));
+  launch_fill_uniform(c->stream, c->cfg.precision == MPG_MIXED, c->pp[c->cur], c->mp[c->cur], c->n, n, seed, type,
+                      weight, drift ? drift : d0, vth, c->dm, c->id_next);
+  CKL();
+  c->n += n;
+  c->n_live += n;
+  c->id_next += n;
+  c->acc_valid = false;
+  CK(cudaStreamSynchronize(c->stream));
+  return MPG_OK;
+}
+
+int mpg_particles_upload(mpg_ctx *c, int64_t n, const int32_t *cell, const double *x, const double *xref,
+                         const double *v, const double *w, const int32_t *species, const int64_t *id) {
+  ENTER(c);
+  TRY(ensure_particles(c));
+  if (n < 0 || n > c->cap) return fail(c, MPG_ERR_CAPACITY, "upload of %lld exceeds capacity", (long long)n);
+  if (n > 0 && (!cell || !xref || !v)) return fail(c, MPG_ERR_ARG, "cell, xref and v are required");
+  cudaStream_t s = c->stream;
+  const bool mixed = c->cfg.precision == MPG_MIXED;
+  // host-side validation of species and weights
+  std::vector<int32_t> spv(n > 0 ? n : 1, 0);
+  if (species)
+    for (int64_t i = 0; i < n; ++i) {
+      if (species[i] < 0 || species[i] >= MPG_MAX_SPECIES) return fail(c, MPG_ERR_ARG, "species out of range");
+      spv[i] = species[i];
+    }
+  for (int64_t i = 0; i < n; ++i)
+    if (cell[i] >= c->hm.T) return fail(c, MPG_ERR_ARG, "cell id %d out of range", cell[i]);
+  std::vector<double> wv(n > 0 ? n : 1, 1.0);
+  if (w)
+    for (int64_t i = 0; i < n; ++i) wv[i] = w[i];
+  if (mixed) {
+    for (int64_t i = 0; i < n; ++i)
+      if (cell[i] >= 0) TRY(set_species_weight(c, spv[i], wv[i]));
+  } else {
+    for (int64_t i = 0; i < n; ++i) c->weight_set[spv[i]] = true;
+  }
+  TempPlain t;
+  TRY(temp_plain(c, n, true, t));
+  double *stage;
+  CK(cudaMallocAsync((void **)&stage, sizeof(double) * 3 * (n > 0 ? n : 1), s));
+  if (n > 0) {
+    CK(cudaMemcpyAsync(t.P.cell, cell, sizeof(int32_t) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(t.P.w, wv.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(t.P.sp, spv.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, s));
+    if (id) {
+      CK(cudaMemcpyAsync(t.P.id, id, sizeof(int64_t) * n, cudaMemcpyHostToDevice, s));
+    } else {
+      std::vector<int64_t> ids(n);
+      for (int64_t i = 0; i < n; ++i) ids[i] = i;
+      CK(cudaMemcpyAsync(t.P.id, ids.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice, s));
+      CK(cudaStreamSynchronize(s));
+    }
+    const double *srcs[3] = {x, xref, v};
+    double *dsts[3] = {t.P.x, t.P.xr, t.P.v};
+    for (int k = 0; k < 3; ++k) {
+      if (!srcs[k]) {
+        CK(cudaMemsetAsync(dsts[k], 0, sizeof(double) * 3 * n, s));
+        continue;
+      }
+      CK(cudaMemcpyAsync(stage, srcs[k], sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
+      launch_rows_to_cols(s, stage, dsts[k], n, t.P.cap);
+    }
+  }
+  if (mixed) {
+    launch_plain_to_mixed(s, t.P, 0, n, c->mp[c->cur]);
+  } else {
+    PlainParts &P = c->pp[c->cur];
+    if (n > 0) {
+      CK(cudaMemcpyAsync(P.cell, t.P.cell, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, s));
+      CK(cudaMemcpyAsync(P.w, t.P.w, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+      CK(cudaMemcpyAsync(P.sp, t.P.sp, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, s));
+      if (P.id) CK(cudaMemcpyAsync(P.id, t.P.id, sizeof(int64_t) * n, cudaMemcpyDeviceToDevice, s));
+      for (int d = 0; d < 3; ++d) {
+        CK(cudaMemcpyAsync(P.x + d * P.cap, t.P.x + d * t.P.cap, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+        CK(cudaMemcpyAsync(P.xr + d * P.cap, t.P.xr + d * t.P.cap, sizeof(double) * n, cudaMemcpyDeviceToDevice,
+                           s));
+        CK(cudaMemcpyAsync(P.v + d * P.cap, t.P.v + d * t.P.cap, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+      }
+    }
+  }
+  CKL();
+  CK(cudaFreeAsync(stage, s));
+  temp_free(c, t);
+  CK(cudaStreamSynchronize(s));
+  c->n = n;
+  c->n_live = 0;
+  for (int64_t i = 0; i < n; ++i) c->n_live += cell[i] >= 0;
+  c->id_next = n;
+  c->acc_valid = false;
+  return MPG_OK;
+}
+
+int mpg_particles_download(mpg_ctx *c, int64_t cap, int64_t *nout, int32_t *cell, double *x, double *xref, double *v,
+                           double *w, int32_t *species, int64_t *id) {
+  ENTER(c);
+  if (!c->parts_alloc) {
+    if (nout) *nout = 0;
+    return MPG_OK;
+  }
+  const int64_t n = c->n;
+  if (nout) *nout = n;
+  if (cap < n) return fail(c, MPG_ERR_CAPACITY, "download buffer holds %lld < %lld", (long long)cap, (long long)n);
+  cudaStream_t s = c->stream;
+  PlainParts P = c->pp[c->cur];
+  TempPlain t;
+  if (c->precision == MPG_MIXED) {
+    TRY(temp_plain(c, n, true, t));
+    launch_mixed_to_plain(s, c->mp[c->cur], n, c->dm, c->sp, t.P);
+    CKL();
+    P = t.P;
+  }
+  double *stage;
+  CK(cudaMallocAsync((void **)&stage, sizeof(double) * 3 * (n > 0 ? n : 1), s));
+  if (n > 0) {
+    if (cell) CK(cudaMemcpyAsync(cell, P.cell, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s));
+    if (w) CK(cudaMemcpyAsync(w, P.w, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    if (species) CK(cudaMemcpyAsync(species, P.sp, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s));
+    if (id && P.id) CK(cudaMemcpyAsync(id, P.id, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, s));
+    double *outs[3] = {x, xref, v};
+    double *srcs[3] = {P.x, P.xr, P.v};
+    for (int k = 0; k < 3; ++k) {
+      if (!outs[k]) continue;
+      launch_cols_to_rows(s, srcs[k], stage, n, P.cap);
+      CK(cudaMemcpyAsync(outs[k], stage, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+    }
+  }
+  CKL();
+  CK(cudaFreeAsync(stage, s));
+  temp_free(c, t);
+  CK(cudaStreamSynchronize(s));
+  if (id && !P.id)
+    for (int64_t i = 0; i < n; ++i) id[i] = i;
+  return MPG_OK;
+}
+
+int mpg_mixed_download(mpg_ctx *c, int64_t cap, int64_t *nout, uint32_t *cellsp, float *b, float *v) {
+  ENTER(c);
+  if (!c->parts_alloc || c->precision != MPG_MIXED) return fail(c, MPG_ERR_STATE, "no mixed particle state");
+  const int64_t n = c->n;
+  if (nout) *nout = n;
+  if (cap < n) return fail(c, MPG_ERR_CAPACITY, "download buffer too small");
+  cudaStream_t s = c->stream;
+  float *sb, *sv;
+  CK(cudaMallocAsync((void **)&sb, sizeof(float) * 3 * (n > 0 ? n : 1), s));
+  CK(cudaMallocAsync((void **)&sv, sizeof(float) * 3 * (n > 0 ? n : 1), s));
+  if (n > 0) {
+    launch_mixed_unpack(s, c->mp[c->cur], n, sb, sv);
+    CKL();
+    if (cellsp) CK(cudaMemcpyAsync(cellsp, c->mp[c->cur].c, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, s));
+    if (b) CK(cudaMemcpyAsync(b, sb, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, s));
+    if (v) CK(cudaMemcpyAsync(v, sv, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, s));
+  }
+  CK(cudaFreeAsync(sb, s));
+  CK(cudaFreeAsync(sv, s));
+  CK(cudaStreamSynchronize(s));
+  return MPG_OK;
+}
+
+int mpg_mixed_upload(mpg_ctx *c, int64_t n, const uint32_t *cellsp, const float *b, const float *v) {
+  ENTER(c);
+  TRY(ensure_particles(c));
+  if (c->precision != MPG_MIXED) return fail(c, MPG_ERR_STATE, "context is not in mixed precision");
+  if (n < 0 || n > c->cap) return fail(c, MPG_ERR_CAPACITY, "upload exceeds capacity");
+  for (int64_t i = 0; i < n; ++i) {
+    if (cellsp[i] == MPG_DEAD) continue;
+    if ((int64_t)(cellsp[i] & 0xFFFFFFu) >= c->hm.T || (cellsp[i] >> 24) >= MPG_MAX_SPECIES)
+      return fail(c, MPG_ERR_ARG, "cellsp[%lld] out of range", (long long)i);
+    if (!c->weight_set[cellsp[i] >> 24])
+      return fail(c, MPG_ERR_STATE, "species %u has no weight (fill or upload it first)", cellsp[i] >> 24);
+  }
+  cudaStream_t s = c->stream;
+  float *sb, *sv;
+  CK(cudaMallocAsync((void **)&sb, sizeof(float) * 3 * (n > 0 ? n : 1), s));
+  CK(cudaMallocAsync((void **)&sv, sizeof(float) * 3 * (n > 0 ? n : 1), s));
+  if (n > 0) {
+    CK(cudaMemcpyAsync(c->mp[c->cur].c, cellsp, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(sb, b, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(sv, v, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, s));
+    launch_mixed_pack(s, sb, sv, c->mp[c->cur], n);
+    CKL();
+  }
+  CK(cudaFreeAsync(sb, s));
+  CK(cudaFreeAsync(sv, s));
+  CK(cudaStreamSynchronize(s));
+  c->n = n;
+  c->n_live = 0;
+  for (int64_t i = 0; i < n; ++i) c->n_live += cellsp[i] != MPG_DEAD;
+  c->acc_valid = false;
+  return MPG_OK;
+}
+
+int mpg_charge_download(mpg_ctx *c, int64_t *acc, double *quantum, int64_t *qfix) {
+  ENTER(c);
+  if (!c->configured) return fail(c, MPG_ERR_STATE, "not configured");
+  if (c->cfg.precision != MPG_MIXED) return fail(c, MPG_ERR_STATE, "charge accumulator exists in the mixed form only");
+  ensure_qfix(c);
+  if (!c->acc_valid && c->parts_alloc) {
+    CK(cudaMemsetAsync(c->acc, 0, sizeof(unsigned long long) * c->dm.N, c->stream));
+    launch_mixed_deposit(c->stream, c->mp[c->cur], c->n, c->dm, c->sp, c->acc);
+    CKL();
+    c->acc_valid = true;
+  }
+  if (acc) CK(cudaMemcpyAsync(acc, c->acc, sizeof(int64_t) * c->dm.N, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (quantum) *quantum = c->quantum;
+  if (qfix)
+    for (int i = 0; i < MPG_MAX_SPECIES; ++i) qfix[i] = c->sp.qfix[i];
+  return MPG_OK;
+}
+
+int mpg_weight_charge(mpg_ctx *c) {
+  ENTER(c);
+  TRY(ensure_particles(c));
+  if (c->cfg.precision == MPG_MIXED) {
+    c->acc_valid = false;
+    TRY(phase_deposit_mixed(c));
+    c->acc_valid = false;  // the conversion consumed (zeroed) the accumulator
+  } else {
+    TRY(phase_deposit_plain(c));
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  return MPG_OK;
+}
+
+int mpg_solve(mpg_ctx *c, int *iters, double *resid) {
+  ENTER(c);
+  if (!c->configured) return fail(c, MPG_ERR_STATE, "not configured");
+  TRY(zero_stats(c));
+  TRY(phase_solve(c));
+  TRY(sync_stats(c));
+  if (iters) *iters = c->h_stats->solver_iters;
+  if (resid) *resid = c->h_stats->solver_resid;
+  if (c->h_stats->solver_status) return fail(c, MPG_ERR_NOT_CONVERGED, "solver reached max_iter");
+  return MPG_OK;
+}
+
+int mpg_weight_efield(mpg_ctx *c) {
+  ENTER(c);
+  if (!c->configured) return fail(c, MPG_ERR_STATE, "not configured");
+  TRY(phase_efield(c));
+  CK(cudaStreamSynchronize(c->stream));
+  return MPG_OK;
+}
+
+int mpg_move(mpg_ctx *c, double dt, mpg_step_stats *st) {
+  ENTER(c);
+  TRY(ensure_particles(c));
+  mpg_step_stats acc{};
+  TRY(zero_stats(c));
+  if (c->cfg.precision == MPG_MIXED) {
+    // the fused kernel also deposits; keep the accumulator consistent
+    CK(cudaMemsetAsync(c->acc, 0, sizeof(unsigned long long) * c->dm.N, c->stream));
+    ensure_qfix(c);
+    launch_mixed_move(c->stream, c->mp[c->cur], c->n, c->dm, c->sp, (float)dt, c->cfg.kill_on_wall,
+                      c->cfg.max_crossings, c->acc, c->d_stats);
+    CKL();
+    c->acc_valid = true;
+    TRY(sync_stats(c));
+  } else {
+    launch_plain_move(c->stream, c->pp[c->cur], c->n, c->dm, c->Etet, c->sp, dt, c->cfg.kill_on_wall,
+                      c->cfg.max_crossings, c->d_stats);
+    CKL();
+    TRY(sync_stats(c));
+    if (c->h_stats->n_killed > 0) TRY(compact_plain(c));
+  }
+  const DevStats &h = *c->h_stats;
+  acc.ke = h.ke;
+  acc.n_killed = (int64_t)h.n_killed;
+  acc.n_crossings = (int64_t)h.n_cross;
+  acc.n_walk_limit = (int64_t)h.n_limit;
+  if (c->cfg.precision == MPG_MIXED)
+    c->n_live -= (int64_t)h.n_killed;
+  else
+    c->n_live = c->n;
+  acc.n_alive = c->n_live;
+  acc.steps = 1;
+  if (st) *st = acc;
+  if (h.n_limit) return fail(c, MPG_ERR_WALK_LIMIT, "%llu particles hit max_crossings", h.n_limit);
+  return MPG_OK;
+}
+
+int mpg_step(mpg_ctx *c, double dt, int n_steps, mpg_step_stats *st) {
+  ENTER(c);
+  TRY(ensure_particles(c));
+  if (n_steps < 0) return fail(c, MPG_ERR_ARG, "n_steps < 0");
+  mpg_step_stats acc{};
+  TRY(zero_stats(c));
+  bool sorted = false;
+  for (int i = 0; i < n_steps; ++i) TRY(one_step(c, dt, &acc, sorted));
+  TRY(sync_stats(c));
+  TRY(finish_counts_mixed(c, sorted));
+  const DevStats &h = *c->h_stats;
+  acc.ke = h.ke;
+  if (c->cfg.precision == MPG_MIXED) {
+    acc.n_killed = (int64_t)h.n_killed;
+  } else {
+    acc.n_killed += (int64_t)h.n_killed;
+  }
+  acc.n_crossings = (int64_t)h.n_cross;
+  acc.n_walk_limit = (int64_t)h.n_limit;
+  acc.solver_iters = h.iters_total;
+  acc.solver_resid = h.solver_resid;
+  acc.steps = n_steps;
+  if (c->cfg.precision == MPG_MIXED)
+    c->n_live -= (int64_t)h.n_killed;
+  else
+    c->n_live = c->n;
+  acc.n_alive = c->n_live;
+  acc.status = h.solver_fail ? MPG_ERR_NOT_CONVERGED : (h.n_limit ? MPG_ERR_WALK_LIMIT : MPG_OK);
+  if (st) *st = acc;
+  if (h.solver_fail) return fail(c, MPG_ERR_NOT_CONVERGED, "a field solve reached max_iter");
+  if (h.n_limit) return fail(c, MPG_ERR_WALK_LIMIT, "%llu particles hit max_crossings", h.n_limit);
+  return MPG_OK;
+}
+
+int mpg_sort(mpg_ctx *c) {
+  ENTER(c);
+  TRY(ensure_particles(c));
+  if (c->cfg.precision == MPG_MIXED) {
+    TRY(sort_mixed(c));
+    TRY(finish_counts_mixed(c, true));
+  }
+  // the plain form keeps the reference Serial order (no sort, PIC.cpp:51-53)
+  CK(cudaStreamSynchronize(c->stream));
+  return MPG_OK;
+}
+
+int mpg_get_field(mpg_ctx *c, int which, double *host) {
+  ENTER(c);
+  if (!c->configured || !host) return fail(c, MPG_ERR_STATE, "not configured");
+  const int64_t N = c->dm.N, T = c->dm.T;
+  cudaStream_t s = c->stream;
+  if (which == MPG_FIELD_RHS) {
+    CK(cudaMemcpyAsync(host, c->rhs, sizeof(double) * N, cudaMemcpyDeviceToHost, s));
+  } else if (which == MPG_FIELD_PHI) {
+    CK(cudaMemcpyAsync(host, c->phi, sizeof(double) * N, cudaMemcpyDeviceToHost, s));
+  } else if (which == MPG_FIELD_BACKGROUND) {
+    if (c->bg)
+      CK(cudaMemcpyAsync(host, c->bg, sizeof(double) * N, cudaMemcpyDeviceToHost, s));
+    else
+      memset(host, 0, sizeof(double) * N);
+  } else if (which == MPG_FIELD_E_TET) {
+    if (c->cfg.precision == MPG_MIXED) {
+      std::vector<float> rec(12 * T);
+      CK(cudaMemcpyAsync(rec.data(), c->dm.mrec, sizeof(float) * 12 * T, cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      for (int64_t t = 0; t < T; ++t)
+        for (int d = 0; d < 3; ++d) host[3 * t + d] = rec[12 * t + 9 + d];
+    } else {
+      CK(cudaMemcpyAsync(host, c->Etet, sizeof(double) * 3 * T, cudaMemcpyDeviceToHost, s));
+    }
+  } else {
+    return fail(c, MPG_ERR_ARG, "unknown field %d", which);
+  }
+  CK(cudaStreamSynchronize(s));
+  return MPG_OK;
+}
+
+int mpg_set_field(mpg_ctx *c, int which, const double *host) {
+  ENTER(c);
+  if (!c->configured || !host) return fail(c, MPG_ERR_STATE, "not configured");
+  const int64_t N = c->dm.N;
+  if (which == MPG_FIELD_RHS)
+    CK(cudaMemcpyAsync(c->rhs, host, sizeof(double) * N, cudaMemcpyHostToDevice, c->stream));
+  else if (which == MPG_FIELD_PHI)
+    CK(cudaMemcpyAsync(c->phi, host, sizeof(double) * N, cudaMemcpyHostToDevice, c->stream));
+  else
+    return fail(c, MPG_ERR_ARG, "field %d is not settable", which);
+  CK(cudaStreamSynchronize(c->stream));
+  return MPG_OK;
+}
+
+int mpg_cg_csr(mpg_ctx *c, int64_t n, const int32_t *d_rowptr, const int32_t *d_col, const double *d_val,
+               const double *d_b, double *d_x, double tol, int max_iter, int *iters, double *resid) {
+  ENTER(c);
+  if (n <= 0 || !d_rowptr || !d_col || !d_val || !d_b || !d_x) return fail(c, MPG_ERR_ARG, "bad CSR arguments");
+  if (!(tol > 0) || max_iter < 1) return fail(c, MPG_ERR_ARG, "tol and max_iter must be positive");
+  TRY(ensure_cg_work(c, n));
+  TRY(zero_stats(c));
+  int rc = run_cg64(c->stream, c->device, n, d_rowptr, d_col, d_val, d_b, d_x, tol, max_iter, c->cg, c->d_stats);
+  if (rc) return fail(c, rc, "CG launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+  TRY(sync_stats(c));
+  if (iters) *iters = c->h_stats->solver_iters;
+  if (resid) *resid = c->h_stats->solver_resid;
+  if (c->h_stats->solver_status) return fail(c, MPG_ERR_NOT_CONVERGED, "CG reached max_iter");
+  return MPG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,910 @@
+// kernels.cu -- particle and field kernels of the GB300 PIC step (sm_103a).
+//
+// Plain form (FP64, reference semantics): one thread per particle, state in
+// component-major SoA so that every load and store of a warp is one coalesced
+// 256-byte transaction per component.  Built with --fmad=false, so the Boris
+// push and the tet walk round exactly like the reference's CPU build
+// (particle_move.hpp:135-225,364-392).
+//
+// Mixed form: cell index + FP32 barycentric coordinates + FP32 velocity
+// (28 bytes per particle), one fused kernel per step that gathers the per-tet
+// E, pushes, walks across faces by carrying barycentrics through a per-face
+// vertex permutation (no re-projection), removes particles at absorbing
+// walls and deposits the new position into an int64 fixed-point node
+// accumulator (order-independent, exact total charge).
+#include <cuda_runtime.h>
+
+#include "mpg_internal.h"
+#include "mpg_kernels.h"
+
+namespace {
+
+constexpr int kThreads = 256;
+
+inline unsigned grid_for(int64_t n, int threads = kThreads) {
+  int64_t g = (n + threads - 1) / threads;
+  return (unsigned)(g < 1 ? 1 : g);
+}
+
+// ---------------------------------------------------------------------------
+// block-level exclusive scan of one uint32 per thread (blockDim = 1024)
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *warp_tot, uint32_t &total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint32_t x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  __syncthreads();
+  if (lane == 31) warp_tot[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = blockDim.x >> 5;
+    uint32_t t = lane < nw ? warp_tot[lane] : 0u;
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    if (lane < nw) warp_tot[lane] = t;  // inclusive warp prefix
+  }
+  __syncthreads();
+  total = warp_tot[(blockDim.x >> 5) - 1];
+  uint32_t before = wid > 0 ? warp_tot[wid - 1] : 0u;
+  return before + x - v;
+}
+
+constexpr int kScanThreads = 1024;
+constexpr int kScanPer = 4;
+constexpr int kScanTile = kScanThreads * kScanPer;
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const uint32_t *__restrict__ in, int64_t n,
+                                                             uint32_t *__restrict__ tile_sum) {
+  __shared__ uint32_t wt[32];
+  const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanPer;
+  uint32_t s = 0;
+  for (int i = 0; i < kScanPer; ++i)
+    if (base + i < n) s += in[base + i];
+  uint32_t tot;
+  block_exclusive_scan(s, wt, tot);
+  if (threadIdx.x == 0) tile_sum[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_sums(uint32_t *tile_sum, int64_t ntiles) {
+  __shared__ uint32_t wt[32];
+  uint32_t carry = 0;
+  for (int64_t b0 = 0; b0 < ntiles; b0 += kScanThreads) {
+    int64_t i = b0 + threadIdx.x;
+    uint32_t v = i < ntiles ? tile_sum[i] : 0u;
+    uint32_t tot;
+    uint32_t ex = block_exclusive_scan(v, wt, tot);
+    if (i < ntiles) tile_sum[i] = carry + ex;
+    carry += tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) tile_sum[ntiles] = carry;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_apply(const uint32_t *__restrict__ in, int64_t n,
+                                                             const uint32_t *__restrict__ tile_off,
+                                                             uint32_t *__restrict__ out, int64_t ntiles) {
+  __shared__ uint32_t wt[32];
+  const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanPer;
+  uint32_t v[kScanPer], s = 0;
+  for (int i = 0; i < kScanPer; ++i) {
+    v[i] = base + i < n ? in[base + i] : 0u;
+    s += v[i];
+  }
+  uint32_t tot;
+  uint32_t ex = block_exclusive_scan(s, wt, tot) + tile_off[blockIdx.x];
+  for (int i = 0; i < kScanPer; ++i) {
+    if (base + i < n) out[base + i] = ex;
+    ex += v[i];
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = tile_off[ntiles];
+}
+
+// ---------------------------------------------------------------------------
+// plain FP64 kernels
+__device__ __forceinline__ void jinv_apply(const double *__restrict__ I, const double a[3], double out[3]) {
+  // mesh.hpp:244-250: ref_vec[i] = sum_j Jinv[i][j] * phys[j], accumulated from 0
+  for (int r = 0; r < 3; ++r) {
+    double s = 0.0;
+    s += I[3 * r + 0] * a[0];
+    s += I[3 * r + 1] * a[1];
+    s += I[3 * r + 2] * a[2];
+    out[r] = s;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_plain_deposit(PlainParts P, int64_t n, const int4 *__restrict__ tets,
+                                                            const double *__restrict__ detj, SpeciesTable S, int mode,
+                                                            double *__restrict__ rhs) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const int e = P.cell[p];
+  if (e < 0) return;
+  const int4 nd = tets[e];
+  const int nodes[4] = {nd.x, nd.y, nd.z, nd.w};
+  const double w = P.w[p], q = S.q[P.sp[p]];
+  if (mode == 0) {
+    // PIC.cpp:125-135: val = sum_c -tot_q * (detJ*w_c * N_i(c))
+    const double A = 0.5854101966249685, B = 0.1381966011250105;
+    const double Pc[4][3] = {{B, B, B}, {A, B, B}, {B, A, B}, {B, B, A}};
+    const double dj = detj[e];
+    const double tot_q = w * q * (6 / dj);
+    const double wm = dj * (1.0 / 24.0);
+    for (int i = 0; i < 4; ++i) {
+      double val = 0;
+      for (int c = 0; c < 4; ++c) {
+        const double Ni = (i == 0) ? (1 - Pc[c][0] - Pc[c][1] - Pc[c][2]) : Pc[c][i - 1];
+        val += -tot_q * (wm * Ni);
+      }
+      atomicAdd(&rhs[nodes[i]], val);
+    }
+  } else {
+    const int64_t cap = P.cap;
+    const double x0 = P.xr[p], x1 = P.xr[cap + p], x2 = P.xr[2 * cap + p];
+    const double wq = w * q;
+    const double lam[4] = {1 - x0 - x1 - x2, x0, x1, x2};
+    for (int i = 0; i < 4; ++i) atomicAdd(&rhs[nodes[i]], -(wq * lam[i]));
+  }
+}
+
+__global__ void k_rhs_finish(int64_t N, double *__restrict__ rhs, const double *__restrict__ bg,
+                             const uint8_t *__restrict__ bnd) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  double r = rhs[i];
+  if (bg) r += bg[i];
+  if (bnd[i]) r = 0.0;  // PIC.cpp:155-158
+  rhs[i] = r;
+}
+
+__global__ void k_efield_plain(int64_t T, const int4 *__restrict__ tets, const double *__restrict__ grad,
+                               const double *__restrict__ phi, double *__restrict__ E) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T) return;
+  const int4 nd = tets[t];
+  const double f[4] = {phi[nd.x], phi[nd.y], phi[nd.z], phi[nd.w]};
+  const double *G = grad + 12 * t;
+  for (int d = 0; d < 3; ++d) {
+    double s = 0.0;
+    for (int i = 0; i < 4; ++i) s += f[i] * G[3 * i + d];
+    E[3 * t + d] = s;
+  }
+}
+
+// find_intersection of particle_move.hpp:135-225 for one sub-step
+__device__ __forceinline__ double plain_intersect(const DevMesh &M, int &e, double x[3], double xr[3], double v[3],
+                                                  double vr[3], double dt, double time_remaining, int kill,
+                                                  bool &killed) {
+  const double local_dt = dt * time_remaining;
+  double scale_fact = 1.0;
+  int face = -1;
+  double dx_ref[3], xf[3];
+  for (int d = 0; d < 3; ++d) {
+    dx_ref[d] = local_dt * vr[d];
+    xf[d] = xr[d] + dx_ref[d];
+  }
+  if (vr[2] < 0 && xf[2] < 0) {
+    face = 3;
+    scale_fact = -xr[2] / (dx_ref[2]);
+  }
+  if (vr[1] < 0 && xf[1] < 0) {
+    const double sfy = -xr[1] / (dx_ref[1]);
+    if (sfy < scale_fact) {
+      face = 0;
+      scale_fact = sfy;
+    }
+  }
+  if (vr[0] < 0 && xf[0] < 0) {
+    const double sfx = -xr[0] / (dx_ref[0]);
+    if (sfx < scale_fact) {
+      face = 2;
+      scale_fact = sfx;
+    }
+  }
+  const double xf_sum = xf[0] + xf[1] + xf[2];
+  const double vr_sum = vr[0] + vr[1] + vr[2];
+  if (vr_sum > 0 && xf_sum > 1) {
+    const double sfs = (1 - xr[0] - xr[1] - xr[2]) / (dx_ref[0] + dx_ref[1] + dx_ref[2]);
+    if (sfs < scale_fact) {
+      face = 1;
+      scale_fact = sfs;
+    }
+  }
+  for (int d = 0; d < 3; ++d) {
+    x[d] = x[d] + scale_fact * local_dt * v[d];
+    xr[d] = xr[d] + scale_fact * local_dt * vr[d];
+  }
+  if (scale_fact < 1) {
+    const int4 nb4 = M.nbrs[e];
+    const int nb = face == 0 ? nb4.x : face == 1 ? nb4.y : face == 2 ? nb4.z : nb4.w;
+    if (nb >= 0) {
+      e = nb;
+      const int n0 = M.tets[e].x;
+      const double delta[3] = {x[0] - M.nodes[3 * n0], x[1] - M.nodes[3 * n0 + 1], x[2] - M.nodes[3 * n0 + 2]};
+      double dref[3];
+      jinv_apply(M.jinv + 9 * (int64_t)e, delta, dref);
+      for (int d = 0; d < 3; ++d) xr[d] = 0.0 + dref[d];
+      jinv_apply(M.jinv + 9 * (int64_t)e, v, vr);
+    } else {
+      if (kill) {
+        killed = true;
+        return 1;
+      }
+      const double *nrm = M.normals + 12 * (int64_t)e + 3 * face;
+      double vdn = 0;
+      for (int d = 0; d < 3; ++d) vdn += v[d] * nrm[d];
+      for (int d = 0; d < 3; ++d) v[d] -= 2 * vdn * nrm[d];
+      jinv_apply(M.jinv + 9 * (int64_t)e, v, vr);
+    }
+  }
+  return scale_fact;
+}
+
+__global__ void __launch_bounds__(kThreads) k_plain_move(PlainParts P, int64_t n, DevMesh M,
+                                                         const double *__restrict__ Etet, SpeciesTable S, double dt,
+                                                         int kill, int max_cross, DevStats *st) {
+  __shared__ double sd[32];
+  __shared__ unsigned long long su[32];
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double ke = 0.0;
+  unsigned long long killed = 0, cross = 0, limit = 0;
+  if (p < n) {
+    int e = P.cell[p];
+    if (e >= 0) {
+      const int64_t cap = P.cap;
+      double x[3] = {P.x[p], P.x[cap + p], P.x[2 * cap + p]};
+      double xr[3] = {P.xr[p], P.xr[cap + p], P.xr[2 * cap + p]};
+      double v[3] = {P.v[p], P.v[cap + p], P.v[2 * cap + p]};
+      const int s = P.sp[p];
+      const double E[3] = {Etet[3 * (int64_t)e], Etet[3 * (int64_t)e + 1], Etet[3 * (int64_t)e + 2]};
+      // Boris push, particle_move.hpp:366-389 (B = 0, PIC.cpp:179)
+      const double scaled_dt = dt * 1.0;
+      const double q_over_m = S.qm[s];
+      const double B[3] = {0.0, 0.0, 0.0};
+      double t[3] = {q_over_m * 0.5 * B[0], q_over_m * 0.5 * B[1], q_over_m * 0.5 * B[2]};
+      for (int d = 0; d < 3; ++d) v[d] += scaled_dt * E[d] * q_over_m * 0.5;
+      double tmp[3] = {v[0], v[1], v[2]};
+      tmp[0] += v[1] * t[2] - v[2] * t[1];
+      tmp[1] += v[2] * t[0] - v[0] * t[2];
+      tmp[2] += v[0] * t[1] - v[1] * t[0];
+      const double t_sqr = t[0] * t[0] + t[1] * t[1] + t[2] * t[2];
+      for (int d = 0; d < 3; ++d) t[d] *= 2. / (1 + t_sqr);
+      v[0] += tmp[1] * t[2] - tmp[2] * t[1];
+      v[1] += tmp[2] * t[0] - tmp[0] * t[2];
+      v[2] += tmp[0] * t[1] - tmp[1] * t[0];
+      for (int d = 0; d < 3; ++d) v[d] += scaled_dt * E[d] * q_over_m * 0.5;
+      double vr[3];
+      jinv_apply(M.jinv + 9 * (int64_t)e, v, vr);
+      // walk, particle_move.hpp:110-121
+      double tr = 1.0;
+      int it = 0;
+      bool dead = false;
+      while (tr > 0) {
+        if (it >= max_cross) {
+          limit = 1;
+          break;
+        }
+        const double sf = plain_intersect(M, e, x, xr, v, vr, dt, tr, kill, dead);
+        tr -= sf * tr;
+        ++it;
+        if (dead) break;
+      }
+      cross = it > 0 ? (unsigned long long)(it - 1) : 0ull;
+      if (dead) {
+        killed = 1;
+        e = -1;
+      } else {
+        // PIC.cpp:193-199
+        const double tot_m = P.w[p] * S.m[s];
+        double v_sqr = 0;
+        for (int d = 0; d < 3; ++d) v_sqr += v[d] * v[d];
+        ke = 0.5 * tot_m * v_sqr;
+      }
+      P.cell[p] = e;
+      P.x[p] = x[0];
+      P.x[cap + p] = x[1];
+      P.x[2 * cap + p] = x[2];
+      P.xr[p] = xr[0];
+      P.xr[cap + p] = xr[1];
+      P.xr[2 * cap + p] = xr[2];
+      P.v[p] = v[0];
+      P.v[cap + p] = v[1];
+      P.v[2 * cap + p] = v[2];
+    }
+  }
+  double bke = block_sum(ke, sd);
+  if (threadIdx.x == 0 && bke != 0.0) atomicAdd(&st->ke, bke);
+  unsigned long long bk = block_sum_u64(killed, su);
+  if (threadIdx.x == 0 && bk) atomicAdd(&st->n_killed, bk);
+  unsigned long long bc = block_sum_u64(cross, su);
+  if (threadIdx.x == 0 && bc) atomicAdd(&st->n_cross, bc);
+  unsigned long long bl = block_sum_u64(limit, su);
+  if (threadIdx.x == 0 && bl) atomicAdd(&st->n_limit, bl);
+}
+
+// stable compaction: count live particles per 4096-particle tile
+__global__ void __launch_bounds__(kScanThreads) k_count_live(const int32_t *__restrict__ cell, int64_t n,
+                                                             uint32_t *__restrict__ tile_cnt) {
+  __shared__ uint32_t wt[32];
+  const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanPer;
+  uint32_t s = 0;
+  for (int i = 0; i < kScanPer; ++i)
+    if (base + i < n && cell[base + i] >= 0) ++s;
+  uint32_t tot;
+  block_exclusive_scan(s, wt, tot);
+  if (threadIdx.x == 0) tile_cnt[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_compact_plain(PlainParts P, int64_t n, PlainParts Q,
+                                                                const uint32_t *__restrict__ tile_off,
+                                                                int64_t ntiles, uint32_t *d_count) {
+  __shared__ uint32_t wt[32];
+  const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanPer;
+  uint32_t s = 0;
+  bool live[kScanPer];
+  for (int i = 0; i < kScanPer; ++i) {
+    live[i] = base + i < n && P.cell[base + i] >= 0;
+    s += live[i];
+  }
+  uint32_t tot;
+  uint32_t dst = block_exclusive_scan(s, wt, tot) + tile_off[blockIdx.x];
+  for (int i = 0; i < kScanPer; ++i) {
+    if (!live[i]) continue;
+    const int64_t a = base + i;
+    Q.cell[dst] = P.cell[a];
+    for (int d = 0; d < 3; ++d) {
+      Q.x[d * Q.cap + dst] = P.x[d * P.cap + a];
+      Q.xr[d * Q.cap + dst] = P.xr[d * P.cap + a];
+      Q.v[d * Q.cap + dst] = P.v[d * P.cap + a];
+    }
+    Q.w[dst] = P.w[a];
+    Q.sp[dst] = P.sp[a];
+    if (P.id) Q.id[dst] = P.id[a];
+    ++dst;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *d_count = tile_off[ntiles];
+}
+
+// ---------------------------------------------------------------------------
+// mixed form
+__device__ __forceinline__ void deposit_fixed(unsigned long long *__restrict__ acc, const int4 nd, float b1, float b2,
+                                              float b3, long long Q) {
+  const float Qf = (float)Q;
+  const long long c1 = __float2ll_rn(b1 * Qf);
+  const long long c2 = __float2ll_rn(b2 * Qf);
+  const long long c3 = __float2ll_rn(b3 * Qf);
+  const long long c0 = Q - c1 - c2 - c3;
+  atomicAdd(acc + nd.x, (unsigned long long)c0);
+  atomicAdd(acc + nd.y, (unsigned long long)c1);
+  atomicAdd(acc + nd.z, (unsigned long long)c2);
+  atomicAdd(acc + nd.w, (unsigned long long)c3);
+}
+
+__global__ void __launch_bounds__(kThreads) k_mixed_deposit(MixedParts P, int64_t n, const int4 *__restrict__ tets,
+                                                            SpeciesTable S, unsigned long long *__restrict__ acc) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const uint32_t cs = P.c[p];
+  if (cs == MPG_DEAD) return;
+  const float4 b = P.b[p];
+  deposit_fixed(acc, tets[cs & 0xFFFFFFu], b.x, b.y, b.z, S.qfix[cs >> 24]);
+}
+
+__global__ void k_mixed_convert(int64_t N, unsigned long long *__restrict__ acc, double quantum,
+                                const double *__restrict__ bg, const uint8_t *__restrict__ bnd,
+                                double *__restrict__ rhs) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const long long a = (long long)acc[i];
+  acc[i] = 0ull;
+  double r = -((double)a * quantum);
+  if (bg) r += bg[i];
+  if (bnd[i]) r = 0.0;
+  rhs[i] = r;
+}
+
+// E per tet from phi: E = sum_k (phi_k - phi_0) * row_{k-1}(J^-1); the phi
+// differences are formed in FP64, the products in FP32.
+__global__ void k_efield_mixed(int64_t T, const int4 *__restrict__ tets, float4 *__restrict__ rec,
+                               const double *__restrict__ phi) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T) return;
+  const int4 nd = tets[t];
+  const double f0 = phi[nd.x];
+  const float d1 = (float)(phi[nd.y] - f0), d2 = (float)(phi[nd.z] - f0), d3 = (float)(phi[nd.w] - f0);
+  const float4 r0 = rec[3 * t], r1 = rec[3 * t + 1];
+  float4 r2 = rec[3 * t + 2];
+  // J^-1 rows: (r0.x r0.y r0.z) (r0.w r1.x r1.y) (r1.z r1.w r2.x)
+  r2.y = __fmaf_rn(d3, r1.z, __fmaf_rn(d2, r0.w, d1 * r0.x));
+  r2.z = __fmaf_rn(d3, r1.w, __fmaf_rn(d2, r1.x, d1 * r0.y));
+  r2.w = __fmaf_rn(d3, r2.x, __fmaf_rn(d2, r1.y, d1 * r0.z));
+  rec[3 * t + 2] = r2;
+}
+
+__global__ void __launch_bounds__(kThreads) k_mixed_move(MixedParts P, int64_t n, const float4 *__restrict__ rec,
+                                                         const uint4 *__restrict__ nbr,
+                                                         const int4 *__restrict__ tets, SpeciesTable S, float dt,
+                                                         int kill, int max_cross, unsigned long long *__restrict__ acc,
+                                                         DevStats *st) {
+  __shared__ double sd[32];
+  __shared__ unsigned long long su[32];
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  float ke = 0.f;
+  unsigned long long killed = 0, cross = 0, limit = 0;
+  if (p < n) {
+    uint32_t cs = P.c[p];
+    if (cs != MPG_DEAD) {
+      const int s = (int)(cs >> 24);
+      uint32_t e = cs & 0xFFFFFFu;
+      const float4 bv = P.b[p];
+      const float2 vv = P.v[p];
+      float l1 = bv.x, l2 = bv.y, l3 = bv.z;
+      float vx = bv.w, vy = vv.x, vz = vv.y;
+      float4 r0 = rec[3 * e], r1 = rec[3 * e + 1], r2 = rec[3 * e + 2];
+      // Boris push with B = 0: the two half kicks of particle_move.hpp:376-387
+      const float hk = 0.5f * dt * S.qm_f[s];
+      vx = __fmaf_rn(hk, r2.y, vx);
+      vy = __fmaf_rn(hk, r2.z, vy);
+      vz = __fmaf_rn(hk, r2.w, vz);
+      vx = __fmaf_rn(hk, r2.y, vx);
+      vy = __fmaf_rn(hk, r2.z, vy);
+      vz = __fmaf_rn(hk, r2.w, vz);
+      float tleft = dt;
+      int entry = -1;  // vertex opposite the face the particle entered through
+      bool dead = false;
+      int it = 0;
+      for (;;) {
+        // barycentric velocity u_k = d lambda_k / dt; u_{1..3} = J^-1 v
+        const float u1 = __fmaf_rn(r0.z, vz, __fmaf_rn(r0.y, vy, r0.x * vx));
+        const float u2 = __fmaf_rn(r1.y, vz, __fmaf_rn(r1.x, vy, r0.w * vx));
+        const float u3 = __fmaf_rn(r2.x, vz, __fmaf_rn(r1.w, vy, r1.z * vx));
+        const float u0 = -(u1 + u2 + u3);
+        const float l0 = 1.0f - l1 - l2 - l3;
+        const float lam[4] = {l0, l1, l2, l3};
+        const float uu[4] = {u0, u1, u2, u3};
+        float tmin = tleft;
+        int kmin = -1;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          if (uu[k] < 0.f && k != entry) {
+            float tk = __fdiv_rn(-lam[k], uu[k]);
+            tk = fmaxf(tk, 0.f);
+            if (tk < tmin) {
+              tmin = tk;
+              kmin = k;
+            }
+          }
+        }
+        if (kmin < 0) {
+          l1 = __fmaf_rn(tleft, u1, l1);
+          l2 = __fmaf_rn(tleft, u2, l2);
+          l3 = __fmaf_rn(tleft, u3, l3);
+          break;
+        }
+        if (it >= max_cross) {
+          limit = 1;
+          break;
+        }
+        ++it;
+        float nl[4] = {__fmaf_rn(tmin, u0, l0), __fmaf_rn(tmin, u1, l1), __fmaf_rn(tmin, u2, l2),
+                       __fmaf_rn(tmin, u3, l3)};
+        nl[kmin] = 0.f;
+        tleft = tleft - tmin;
+        const uint4 nb4 = nbr[e];
+        const uint32_t w = kmin == 0 ? nb4.x : kmin == 1 ? nb4.y : kmin == 2 ? nb4.z : nb4.w;
+        const uint32_t nb = w & 0xFFFFFFu;
+        if (nb == MPG_WALL) {
+          if (kill) {
+            dead = true;
+            l1 = nl[1];
+            l2 = nl[2];
+            l3 = nl[3];
+            break;
+          }
+          // specular reflection off the wall: outward normal is -grad(lambda_k)
+          float gx, gy, gz;
+          if (kmin == 1) {
+            gx = r0.x; gy = r0.y; gz = r0.z;
+          } else if (kmin == 2) {
+            gx = r0.w; gy = r1.x; gz = r1.y;
+          } else if (kmin == 3) {
+            gx = r1.z; gy = r1.w; gz = r2.x;
+          } else {
+            gx = -(r0.x + r0.w + r1.z);
+            gy = -(r0.y + r1.x + r1.w);
+            gz = -(r0.z + r1.y + r2.x);
+          }
+          const float inv = rsqrtf(__fmaf_rn(gz, gz, __fmaf_rn(gy, gy, gx * gx)));
+          gx *= inv;
+          gy *= inv;
+          gz *= inv;
+          const float vdn2 = 2.f * __fmaf_rn(vz, gz, __fmaf_rn(vy, gy, vx * gx));
+          vx = __fmaf_rn(-vdn2, gx, vx);
+          vy = __fmaf_rn(-vdn2, gy, vy);
+          vz = __fmaf_rn(-vdn2, gz, vz);
+          l1 = nl[1];
+          l2 = nl[2];
+          l3 = nl[3];
+          entry = kmin;
+          continue;
+        }
+        const uint32_t perm = w >> 24;
+        float ml[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) ml[(perm >> (2 * j)) & 3u] = nl[j];
+        entry = (int)((perm >> (2 * kmin)) & 3u);
+        ml[entry] = 0.f;
+        e = nb;
+        l1 = ml[1];
+        l2 = ml[2];
+        l3 = ml[3];
+        r0 = rec[3 * e];
+        r1 = rec[3 * e + 1];
+        r2 = rec[3 * e + 2];
+      }
+      cross = (unsigned long long)it;
+      if (dead) {
+        killed = 1;
+        P.c[p] = MPG_DEAD;
+      } else {
+        if (e != (cs & 0xFFFFFFu)) P.c[p] = ((uint32_t)s << 24) | e;
+        P.b[p] = make_float4(l1, l2, l3, vx);
+        P.v[p] = make_float2(vy, vz);
+        ke = S.half_wm_f[s] * __fmaf_rn(vz, vz, __fmaf_rn(vy, vy, vx * vx));
+        deposit_fixed(acc, tets[e], l1, l2, l3, S.qfix[s]);
+      }
+    }
+  }
+  double bke = block_sum((double)ke, sd);
+  if (threadIdx.x == 0 && bke != 0.0) atomicAdd(&st->ke, bke);
+  unsigned long long bk = block_sum_u64(killed, su);
+  if (threadIdx.x == 0 && bk) atomicAdd(&st->n_killed, bk);
+  unsigned long long bc = block_sum_u64(cross, su);
+  if (threadIdx.x == 0 && bc) atomicAdd(&st->n_cross, bc);
+  unsigned long long bl = block_sum_u64(limit, su);
+  if (threadIdx.x == 0 && bl) atomicAdd(&st->n_limit, bl);
+}
+
+__global__ void k_cell_hist(const uint32_t *__restrict__ c, int64_t n, uint32_t *__restrict__ cnt) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const uint32_t cs = c[p];
+  if (cs != MPG_DEAD) atomicAdd(&cnt[cs & 0xFFFFFFu], 1u);
+}
+
+__global__ void k_cell_scatter(MixedParts P, int64_t n, MixedParts Q, const uint32_t *__restrict__ start,
+                               uint32_t *__restrict__ fill) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const uint32_t cs = P.c[p];
+  if (cs == MPG_DEAD) return;
+  const uint32_t e = cs & 0xFFFFFFu;
+  const uint32_t dst = start[e] + atomicAdd(&fill[e], 1u);
+  Q.c[dst] = cs;
+  Q.b[dst] = P.b[p];
+  Q.v[dst] = P.v[p];
+  if (P.id) Q.id[dst] = P.id[p];
+}
+
+__global__ void k_copy_u32(const uint32_t *src, uint32_t *dst) { *dst = *src; }
+
+// slots at or beyond the device count are dead (after a sort the grid bound
+// stays at the old count until the host reads the new one)
+__global__ void k_mark_tail_dead(uint32_t *c, int64_t n, const uint32_t *count) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < n && p >= (int64_t)*count) c[p] = MPG_DEAD;
+}
+
+// ---------------------------------------------------------------------------
+// fills
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z += 0x9E3779B97F4A7C15ULL;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+__device__ __forceinline__ uint64_t draw(uint64_t base, uint64_t ctr) { return mix64(base + mix64(ctr)); }
+__device__ __forceinline__ float f24(uint64_t h) { return (float)(h >> 40) * (1.0f / 16777216.0f); }
+
+__device__ __forceinline__ void ref_to_phys(const DevMesh &M, int e, const double r[3], double out[3]) {
+  // mesh.hpp:182-190
+  const double w[4] = {1 - r[0] - r[1] - r[2], r[0], r[1], r[2]};
+  const int4 nd = M.tets[e];
+  const int ids[4] = {nd.x, nd.y, nd.z, nd.w};
+  out[0] = out[1] = out[2] = 0.0;
+  for (int i = 0; i < 4; ++i)
+    for (int d = 0; d < 3; ++d) out[d] += w[i] * M.nodes[3 * ids[i] + d];
+}
+
+__global__ void k_fill_uniform(int mixed, PlainParts P, MixedParts X, int64_t n0, int64_t n, uint64_t base, int type,
+                               double weight, double dr0, double dr1, double dr2, float vth, DevMesh M, int64_t id0) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const uint64_t c0 = (uint64_t)k << 8;
+  const uint64_t T = (uint64_t)M.T;
+  uint64_t e = 0;
+  for (uint64_t j = 0; j < 128; j += 2) {
+    e = ((draw(base, c0 | j) >> 32) * T) >> 32;
+    if (f24(draw(base, c0 | (j + 1))) < M.fill_ratio[e]) break;
+  }
+  float s = f24(draw(base, c0 | 128));
+  float t = f24(draw(base, c0 | 129));
+  float u = f24(draw(base, c0 | 130));
+  // Rocchini & Cignoni (2000): fold the unit cube onto the unit tet
+  if (s + t > 1.0f) {
+    s = 1.0f - s;
+    t = 1.0f - t;
+  }
+  if (t + u > 1.0f) {
+    const float tmp = u;
+    u = 1.0f - s - t;
+    t = 1.0f - tmp;
+  } else if (s + t + u > 1.0f) {
+    const float tmp = u;
+    u = s + t + u - 1.0f;
+    s = 1.0f - t - tmp;
+  }
+  const float a0 = f24(draw(base, c0 | 131)), a1 = f24(draw(base, c0 | 132));
+  const float a2 = f24(draw(base, c0 | 133)), a3 = f24(draw(base, c0 | 134));
+  const float twopi = 6.28318530717958648f;
+  const float rr0 = sqrtf(-2.0f * logf(1.0f - a0)), rr1 = sqrtf(-2.0f * logf(1.0f - a2));
+  const float g[3] = {rr0 * cosf(twopi * a1), rr0 * sinf(twopi * a1), rr1 * cosf(twopi * a3)};
+  const float drift[3] = {(float)dr0, (float)dr1, (float)dr2};
+  float vf[3];
+  for (int d = 0; d < 3; ++d) vf[d] = drift[d] + vth * g[d];
+  const int64_t dst = n0 + k;
+  if (mixed) {
+    X.c[dst] = ((uint32_t)type << 24) | (uint32_t)e;
+    X.b[dst] = make_float4(s, t, u, vf[0]);
+    X.v[dst] = make_float2(vf[1], vf[2]);
+    if (X.id) X.id[dst] = id0 + k;
+  } else {
+    const double xr[3] = {(double)s, (double)t, (double)u};
+    double xp[3];
+    ref_to_phys(M, (int)e, xr, xp);
+    P.cell[dst] = (int32_t)e;
+    for (int d = 0; d < 3; ++d) {
+      P.x[d * P.cap + dst] = xp[d];
+      P.xr[d * P.cap + dst] = xr[d];
+      P.v[d * P.cap + dst] = (double)vf[d];
+    }
+    P.w[dst] = weight;
+    P.sp[dst] = type;
+    if (P.id) P.id[dst] = id0 + k;
+  }
+}
+
+// particle_fill.hpp:129-164 with the seed of :147 and set_vel of :100-124;
+// particle (elem, ipart) lands at n0 + elem*nppe + ipart (Serial push order)
+__global__ void k_fill_ref(PlainParts P, int64_t n0, int nppe, int type, double density, double v0, double v1,
+                           double v2, double temp, double mass, DevMesh M, int64_t id0) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t total = M.T * (int64_t)nppe;
+  if (k >= total) return;
+  const int64_t elem = k / nppe;
+  const uint64_t ipart = (uint64_t)(k % nppe);
+  const int64_t NG = M.T;
+  uint64_t sd = (uint64_t)elem + (34030 + ipart) * (uint64_t)NG + (uint64_t)(NG * 12345 * (int64_t)type);
+  auto rnd = [&]() -> uint64_t {
+    sd = 6364136223846793005ULL * sd + 1442695040888963407ULL;
+    return sd;
+  };
+  const double dscale = 1. / static_cast<double>(18446744073709551615ULL);
+  auto drand = [&]() -> double { return (double)rnd() * dscale; };
+  for (int i = 0; i < 10; ++i) rnd();
+  // rejection loops of the reference are unbounded; here they stop after
+  // 2^20 tries (acceptance is 1/6 for x_ref and far above 1e-6 for the
+  // Maxwellian at any sane temperature, so the cap is never reached)
+  const int kMaxTries = 1 << 20;
+  double xr[3];
+  int tries = 0;
+  do {
+    xr[0] = drand();
+    xr[1] = drand();
+    xr[2] = drand();
+  } while (xr[0] + xr[1] + xr[2] > 1.0 && ++tries < kMaxTries);
+  double xp[3];
+  ref_to_phys(M, (int)elem, xr, xp);
+  const double vel[3] = {v0, v1, v2};
+  double vp[3];
+  if (temp == 0) {
+    vp[0] = vel[0];
+    vp[1] = vel[1];
+    vp[2] = vel[2];
+  } else if (temp < 0) {
+    vp[0] = vel[0] * (1. + temp * sin(1. * 3.14159265358979323846 * xp[0]));
+    vp[1] = vp[2] = 0.0;
+  } else {
+    for (int k = 0;; ++k) {
+      const double r = drand();
+      const double vmax = sqrt(6 * temp / mass);
+      double vv[3];
+      vv[0] = vmax * 2 * (-.5 + drand());
+      vv[1] = vmax * 2 * (-.5 + drand());
+      vv[2] = vmax * 2 * (-.5 + drand());
+      const double prob = exp(-(vv[0] * vv[0] + vv[1] * vv[1] + vv[2] * vv[2]) / temp);
+      if (r < prob || k >= kMaxTries) {
+        vp[0] = vel[0] + vv[0];
+        vp[1] = vel[1] + vv[1];
+        vp[2] = vel[2] + vv[2];
+        break;
+      }
+    }
+  }
+  const double vol = M.detj[elem] / 6.;
+  const int64_t dst = n0 + k;
+  P.cell[dst] = (int32_t)elem;
+  for (int d = 0; d < 3; ++d) {
+    P.x[d * P.cap + dst] = xp[d];
+    P.xr[d * P.cap + dst] = xr[d];
+    P.v[d * P.cap + dst] = vp[d];
+  }
+  P.w[dst] = density * vol / nppe;
+  P.sp[dst] = type;
+  if (P.id) P.id[dst] = id0 + k;
+}
+
+__global__ void k_rows_to_cols(const double *__restrict__ rows, double *__restrict__ cols, int64_t n, int64_t cap) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  for (int d = 0; d < 3; ++d) cols[d * cap + p] = rows[3 * p + d];
+}
+__global__ void k_cols_to_rows(const double *__restrict__ cols, double *__restrict__ rows, int64_t n, int64_t cap) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  for (int d = 0; d < 3; ++d) rows[3 * p + d] = cols[d * cap + p];
+}
+__global__ void k_mixed_pack(const float *__restrict__ b, const float *__restrict__ v, MixedParts X, int64_t n) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  X.b[p] = make_float4(b[3 * p], b[3 * p + 1], b[3 * p + 2], v[3 * p]);
+  X.v[p] = make_float2(v[3 * p + 1], v[3 * p + 2]);
+}
+__global__ void k_mixed_unpack(MixedParts X, int64_t n, float *__restrict__ b, float *__restrict__ v) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const float4 a = X.b[p];
+  const float2 c = X.v[p];
+  b[3 * p] = a.x;
+  b[3 * p + 1] = a.y;
+  b[3 * p + 2] = a.z;
+  v[3 * p] = a.w;
+  v[3 * p + 1] = c.x;
+  v[3 * p + 2] = c.y;
+}
+__global__ void k_plain_to_mixed(PlainParts P, int64_t n0, int64_t n, MixedParts X) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int64_t p = n0 + k;
+  const int32_t e = P.cell[p];
+  X.c[p] = e < 0 ? MPG_DEAD : (((uint32_t)P.sp[p] << 24) | (uint32_t)e);
+  X.b[p] = make_float4((float)P.xr[p], (float)P.xr[P.cap + p], (float)P.xr[2 * P.cap + p], (float)P.v[p]);
+  X.v[p] = make_float2((float)P.v[P.cap + p], (float)P.v[2 * P.cap + p]);
+  if (X.id) X.id[p] = P.id ? P.id[p] : p;
+}
+__global__ void k_mixed_to_plain(MixedParts X, int64_t n, DevMesh M, SpeciesTable S, PlainParts P) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const uint32_t cs = X.c[p];
+  const float4 a = X.b[p];
+  const float2 c = X.v[p];
+  const double xr[3] = {(double)a.x, (double)a.y, (double)a.z};
+  double xp[3] = {0.0, 0.0, 0.0};
+  const int s = cs == MPG_DEAD ? 0 : (int)(cs >> 24);
+  if (cs != MPG_DEAD) ref_to_phys(M, (int)(cs & 0xFFFFFFu), xr, xp);
+  P.cell[p] = cs == MPG_DEAD ? -1 : (int32_t)(cs & 0xFFFFFFu);
+  const double vv[3] = {(double)a.w, (double)c.x, (double)c.y};
+  for (int d = 0; d < 3; ++d) {
+    P.x[d * P.cap + p] = xp[d];
+    P.xr[d * P.cap + p] = xr[d];
+    P.v[d * P.cap + p] = vv[d];
+  }
+  P.w[p] = S.w[s];
+  P.sp[p] = s;
+  if (P.id) P.id[p] = X.id ? X.id[p] : p;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// launch wrappers
+int64_t scan_scratch_len(int64_t n) { return (n + kScanTile - 1) / kScanTile + 2; }
+
+void scan_u32(cudaStream_t s, const uint32_t *in, uint32_t *out, int64_t n, uint32_t *scratch, int64_t) {
+  const int64_t nt = (n + kScanTile - 1) / kScanTile;
+  const unsigned g = (unsigned)(nt < 1 ? 1 : nt);
+  k_scan_tiles<<<g, kScanThreads, 0, s>>>(in, n, scratch);
+  k_scan_sums<<<1, kScanThreads, 0, s>>>(scratch, g);
+  k_scan_apply<<<g, kScanThreads, 0, s>>>(in, n, scratch, out, g);
+}
+
+void launch_plain_deposit(cudaStream_t s, const PlainParts &P, int64_t n, const DevMesh &M, const SpeciesTable &S,
+                          int mode, double *rhs) {
+  if (n <= 0) return;
+  k_plain_deposit<<<grid_for(n), kThreads, 0, s>>>(P, n, M.tets, M.detj, S, mode, rhs);
+}
+void launch_rhs_finish(cudaStream_t s, int64_t N, double *rhs, const double *bg, const uint8_t *bnd) {
+  k_rhs_finish<<<grid_for(N), kThreads, 0, s>>>(N, rhs, bg, bnd);
+}
+void launch_efield_plain(cudaStream_t s, const DevMesh &M, const double *phi, double *Etet) {
+  k_efield_plain<<<grid_for(M.T), kThreads, 0, s>>>(M.T, M.tets, M.grad, phi, Etet);
+}
+void launch_plain_move(cudaStream_t s, const PlainParts &P, int64_t n, const DevMesh &M, const double *Etet,
+                       const SpeciesTable &S, double dt, int kill, int max_cross, DevStats *st) {
+  if (n <= 0) return;
+  k_plain_move<<<grid_for(n), kThreads, 0, s>>>(P, n, M, Etet, S, dt, kill, max_cross, st);
+}
+void launch_compact_plain(cudaStream_t s, const PlainParts &P, int64_t n, const PlainParts &Q, uint32_t *scratch,
+                          int64_t, uint32_t *d_count) {
+  const int64_t nt = (n + kScanTile - 1) / kScanTile;
+  const unsigned g = (unsigned)(nt < 1 ? 1 : nt);
+  k_count_live<<<g, kScanThreads, 0, s>>>(P.cell, n, scratch);
+  k_scan_sums<<<1, kScanThreads, 0, s>>>(scratch, g);
+  k_compact_plain<<<g, kScanThreads, 0, s>>>(P, n, Q, scratch, g, d_count);
+}
+void launch_mixed_deposit(cudaStream_t s, const MixedParts &P, int64_t n, const DevMesh &M, const SpeciesTable &S,
+                          unsigned long long *acc) {
+  if (n <= 0) return;
+  k_mixed_deposit<<<grid_for(n), kThreads, 0, s>>>(P, n, M.tets, S, acc);
+}
+void launch_mixed_convert(cudaStream_t s, int64_t N, unsigned long long *acc, double quantum, const double *bg,
+                          const uint8_t *bnd, double *rhs) {
+  k_mixed_convert<<<grid_for(N), kThreads, 0, s>>>(N, acc, quantum, bg, bnd, rhs);
+}
+void launch_efield_mixed(cudaStream_t s, const DevMesh &M, const double *phi) {
+  k_efield_mixed<<<grid_for(M.T), kThreads, 0, s>>>(M.T, M.tets, M.mrec, phi);
+}
+void launch_mixed_move(cudaStream_t s, const MixedParts &P, int64_t n, const DevMesh &M, const SpeciesTable &S,
+                       float dt, int kill, int max_cross, unsigned long long *acc, DevStats *st) {
+  if (n <= 0) return;
+  k_mixed_move<<<grid_for(n), kThreads, 0, s>>>(P, n, M.mrec, M.mnbr, M.tets, S, dt, kill, max_cross, acc, st);
+}
+void launch_mixed_sort(cudaStream_t s, const MixedParts &P, int64_t n, const MixedParts &Q, int64_t T, uint32_t *cnt,
+                       uint32_t *start, uint32_t *scratch, int64_t scratch_len, uint32_t *d_count) {
+  cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * T, s);
+  if (n > 0) k_cell_hist<<<grid_for(n), kThreads, 0, s>>>(P.c, n, cnt);
+  scan_u32(s, cnt, start, T, scratch, scratch_len);
+  cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * T, s);
+  if (n > 0) k_cell_scatter<<<grid_for(n), kThreads, 0, s>>>(P, n, Q, start, cnt);
+  k_copy_u32<<<1, 1, 0, s>>>(start + T, d_count);
+}
+void launch_mark_tail_dead(cudaStream_t s, uint32_t *c, int64_t n, const uint32_t *count) {
+  if (n > 0) k_mark_tail_dead<<<grid_for(n), kThreads, 0, s>>>(c, n, count);
+}
+void launch_fill_uniform(cudaStream_t s, int mixed, const PlainParts &P, const MixedParts &X, int64_t n0, int64_t n,
+                         uint64_t seed, int type, double weight, const double drift[3], double vth, const DevMesh &M,
+                         int64_t id0) {
+  if (n <= 0) return;
+  const uint64_t base = mpg_mix64(seed ^ MPG_SALT_FILL);
+  k_fill_uniform<<<grid_for(n), kThreads, 0, s>>>(mixed, P, X, n0, n, base, type, weight, drift[0], drift[1],
+                                                   drift[2], (float)vth, M, id0);
+}
+void launch_fill_ref(cudaStream_t s, const PlainParts &P, int64_t n0, int nppe, int type, double density,
+                     const double vel[3], double temp, double mass, const DevMesh &M, int64_t id0) {
+  const int64_t total = M.T * (int64_t)nppe;
+  if (total <= 0) return;
+  k_fill_ref<<<grid_for(total, 128), 128, 0, s>>>(P, n0, nppe, type, density, vel[0], vel[1], vel[2], temp, mass, M,
+                                                   id0);
+}
+void launch_rows_to_cols(cudaStream_t s, const double *rows, double *cols, int64_t n, int64_t cap) {
+  if (n > 0) k_rows_to_cols<<<grid_for(n), kThreads, 0, s>>>(rows, cols, n, cap);
+}
+void launch_cols_to_rows(cudaStream_t s, const double *cols, double *rows, int64_t n, int64_t cap) {
+  if (n > 0) k_cols_to_rows<<<grid_for(n), kThreads, 0, s>>>(cols, rows, n, cap);
+}
+void launch_mixed_pack(cudaStream_t s, const float *b, const float *v, MixedParts X, int64_t n) {
+  if (n > 0) k_mixed_pack<<<grid_for(n), kThreads, 0, s>>>(b, v, X, n);
+}
+void launch_mixed_unpack(cudaStream_t s, const MixedParts X, int64_t n, float *b, float *v) {
+  if (n > 0) k_mixed_unpack<<<grid_for(n), kThreads, 0, s>>>(X, n, b, v);
+}
+void launch_plain_to_mixed(cudaStream_t s, const PlainParts &P, int64_t n0, int64_t n, const MixedParts &X) {
+  if (n > 0) k_plain_to_mixed<<<grid_for(n), kThreads, 0, s>>>(P, n0, n, X);
+}
+void launch_mixed_to_plain(cudaStream_t s, const MixedParts &X, int64_t n, const DevMesh &M, const SpeciesTable &S,
+                           const PlainParts &P) {
+  if (n > 0) k_mixed_to_plain<<<grid_for(n), kThreads, 0, s>>>(X, n, M, S, P);
+}

@@ -1,0 +1,348 @@
+// mesh_host.cpp -- structured tet mesh, connectivity and P1 stiffness assembly.
+//
+// Host-side setup of the GB300 PIC library (runs once per run, not per step).
+// Replaces Mesh::Mesh (mesh.cpp:78-714) and the assembly of ES::ES
+// (ES.cpp:83-205) for one rank.  Differences in method, not in result:
+//  * face neighbours are found per hex (a tet face either lies inside its hex
+//    or on one of the six hex faces, so the partner is among the <= 24 faces
+//    of one hex) instead of through a std::multimap of all faces
+//    (mesh.cpp:233-405);
+//  * the CSR pattern of a row is a 27-bit mask over the {-1,0,1}^3 node
+//    offsets of the structured grid, so rows come out sorted without a
+//    sort.
+// Node numbering (mesh.cpp:52-54), tet tables (mesh.cpp:211-223), face order
+// (mesh.cpp:239-250), normals (mesh.cpp:650-669), Jacobians (mesh.cpp:671-700),
+// gradients (PIC.cpp:229-241) and the element-order summation of element
+// matrices follow the reference so that the arrays are bit-identical to the
+// CPU restatement.  Built with -ffp-contract=off.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "mpg_internal.h"
+
+namespace {
+
+inline double unit53(uint64_t u) { return (double)(u >> 11) * (1.0 / 9007199254740992.0); }
+
+void apply_mapping(double &x, double &y, double &z, int mapping) {
+  // mesh.cpp:763-792
+  double ox = x, oy = y, oz = z;
+  if (mapping == 1) {
+    double r = (1.0 - fabs(x)) * (1.0 - fabs(y));
+    ox = x * cos(r) - y * sin(r);
+    oy = x * sin(r) + y * cos(r);
+  } else if (mapping == 2) {
+    ox = x * sqrt(1 - .5 * y * y - .5 * z * z + y * y * z * z / 3.);
+    oy = y * sqrt(1 - .5 * x * x - .5 * z * z + x * x * z * z / 3.);
+    oz = z * sqrt(1 - .5 * y * y - .5 * x * x + y * y * x * x / 3.);
+  } else if (mapping == 3) {
+    ox = x * x;
+    if (x < 0) ox = -ox;
+  } else {
+    return;
+  }
+  x = ox;
+  y = oy;
+  z = oz;
+}
+
+const int kFaceNodes[4][3] = {{0, 1, 3}, {1, 2, 3}, {0, 3, 2}, {0, 2, 1}};
+const int kFaceOfOpposite[4] = {1, 2, 0, 3};  // face index whose opposite vertex is k
+
+}  // namespace
+
+int host_mesh_generate(const mpg_mesh_desc &d, HostMesh &m, std::string &err) {
+  if (d.nx < 1 || d.ny < 1 || d.nz < 1) {
+    err = "mesh: nx, ny, nz must be >= 1";
+    return MPG_ERR_ARG;
+  }
+  if (d.split != MPG_SPLIT_REF5 && d.split != MPG_SPLIT_KUHN6) {
+    err = "mesh: split must be 5 or 6";
+    return MPG_ERR_ARG;
+  }
+  if (!(d.hi > d.lo)) {
+    err = "mesh: hi must exceed lo";
+    return MPG_ERR_ARG;
+  }
+  const int64_t nx = d.nx, ny = d.ny, nz = d.nz, per = d.split;
+  const int64_t N = (nx + 1) * (ny + 1) * (nz + 1), T = per * nx * ny * nz;
+  if (N >= (1LL << 31) || T >= (1LL << 31)) {
+    err = "mesh: too large for 32-bit indices";
+    return MPG_ERR_ARG;
+  }
+  m = HostMesh();
+  m.d = d;
+  m.N = N;
+  m.T = T;
+  const int64_t sj = nz + 1, si = (ny + 1) * (nz + 1);
+  const double dx = (d.hi - d.lo) / nx, dy = (d.hi - d.lo) / ny, dz = (d.hi - d.lo) / nz;
+  m.nodes.resize(N * 3);
+  m.bnd.assign(N, 0);
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i <= nx; ++i)
+    for (int64_t j = 0; j <= ny; ++j)
+      for (int64_t k = 0; k <= nz; ++k) {
+        int64_t g = i * si + j * sj + k;
+        m.nodes[3 * g + 0] = d.lo + i * dx;
+        m.nodes[3 * g + 1] = d.lo + j * dy;
+        m.nodes[3 * g + 2] = d.lo + k * dz;
+        m.bnd[g] = (i == 0 || i == nx || j == 0 || j == ny || k == 0 || k == nz) ? 1 : 0;
+      }
+  int64_t nb = 0;
+  for (int64_t g = 0; g < N; ++g) nb += m.bnd[g];
+  m.n_bnodes = nb;
+
+  // ---- tets, hex by hex in (i, j, k) order
+  m.tets.resize(T * 4);
+  static const int kOdd[5][4] = {{3, 1, 0, 5}, {6, 4, 5, 0}, {6, 2, 0, 3}, {5, 7, 6, 3}, {5, 6, 0, 3}};
+  static const int kEven[5][4] = {{2, 3, 1, 7}, {7, 6, 4, 2}, {2, 0, 4, 1}, {4, 5, 7, 1}, {2, 4, 7, 1}};
+  // Kuhn: tet (0, e_a, e_a+e_b, 1) for each axis order (a,b,c); corner bit of x=4, y=2, z=1;
+  // odd orders swap the last two vertices so that detJ > 0.
+  static const int kKuhn[6][4] = {{0, 4, 6, 7}, {0, 4, 7, 5}, {0, 2, 7, 6}, {0, 2, 3, 7}, {0, 1, 5, 7}, {0, 1, 7, 3}};
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < nx; ++i)
+    for (int64_t j = 0; j < ny; ++j)
+      for (int64_t k = 0; k < nz; ++k) {
+        const int64_t base = i * si + j * sj + k;
+        // corner c = 4*di + 2*dj + dk  (mesh.cpp:200-208 ordering)
+        int32_t c[8];
+        for (int q = 0; q < 8; ++q) c[q] = (int32_t)(base + ((q >> 2) & 1) * si + ((q >> 1) & 1) * sj + (q & 1));
+        const int64_t h = (i * ny + j) * nz + k;
+        const int(*tab)[4] = (per == 6) ? kKuhn : (((i + j + k) % 2 != 0) ? kOdd : kEven);
+        for (int t = 0; t < per; ++t)
+          for (int q = 0; q < 4; ++q) m.tets[4 * (h * per + t) + q] = c[tab[t][q]];
+      }
+
+  // ---- face neighbours, per hex
+  m.nbrs.assign(T * 4, -1);
+  int bad = 0;
+#pragma omp parallel for schedule(static) reduction(+ : bad)
+  for (int64_t t = 0; t < T; ++t) {
+    const int64_t h = t / per;
+    const int64_t hi_ = h / (ny * nz), hj = (h / nz) % ny, hk = h % nz;
+    const int64_t corner = hi_ * si + hj * sj + hk;
+    for (int f = 0; f < 4; ++f) {
+      int32_t key[3];
+      int all[3][2] = {{1, 1}, {1, 1}, {1, 1}};  // [axis][offset 0/1] all nodes share it
+      for (int q = 0; q < 3; ++q) {
+        int32_t g = m.tets[4 * t + kFaceNodes[f][q]];
+        key[q] = g;
+        int64_t r = g - corner;
+        int di = (int)(r / si), dj = (int)((r % si) / sj), dk = (int)(r % sj);
+        int off[3] = {di, dj, dk};
+        for (int a = 0; a < 3; ++a) {
+          all[a][0] &= (off[a] == 0);
+          all[a][1] &= (off[a] == 1);
+        }
+      }
+      std::sort(key, key + 3);
+      int64_t nh[3] = {hi_, hj, hk};
+      const int64_t lim[3] = {nx, ny, nz};
+      bool wall = false;
+      for (int a = 0; a < 3; ++a) {
+        if (all[a][0]) {
+          if (nh[a] == 0) wall = true;
+          else nh[a] -= 1;
+        } else if (all[a][1]) {
+          if (nh[a] == lim[a] - 1) wall = true;
+          else nh[a] += 1;
+        }
+      }
+      if (wall) {
+        m.nbrs[4 * t + f] = -1;
+        continue;
+      }
+      const int64_t h2 = (nh[0] * ny + nh[1]) * nz + nh[2];
+      int32_t found = -1;
+      for (int64_t t2 = h2 * per; t2 < (h2 + 1) * per && found < 0; ++t2) {
+        if (t2 == t) continue;
+        for (int f2 = 0; f2 < 4; ++f2) {
+          int32_t k2[3] = {m.tets[4 * t2 + kFaceNodes[f2][0]], m.tets[4 * t2 + kFaceNodes[f2][1]],
+                           m.tets[4 * t2 + kFaceNodes[f2][2]]};
+          std::sort(k2, k2 + 3);
+          if (k2[0] == key[0] && k2[1] == key[1] && k2[2] == key[2]) {
+            found = (int32_t)t2;
+            break;
+          }
+        }
+      }
+      if (found < 0) ++bad;
+      m.nbrs[4 * t + f] = found;
+    }
+  }
+  if (bad) {
+    err = "mesh: unmatched interior face (non-conforming split)";
+    return MPG_ERR_MESH;
+  }
+
+  // ---- node mapping / jitter (mesh.cpp:587-588)
+  if (d.mapping >= 1 && d.mapping <= 3) {
+    for (int64_t g = 0; g < N; ++g) apply_mapping(m.nodes[3 * g], m.nodes[3 * g + 1], m.nodes[3 * g + 2], d.mapping);
+  } else if (d.mapping == MPG_MAP_JITTER) {
+    const uint64_t base = mpg_mix64(d.seed ^ MPG_SALT_JITTER);
+    const double h3[3] = {dx, dy, dz};
+#pragma omp parallel for schedule(static)
+    for (int64_t g = 0; g < N; ++g) {
+      if (m.bnd[g]) continue;
+      for (int q = 0; q < 3; ++q) {
+        double u = unit53(mpg_mix64(base + mpg_mix64(3 * (uint64_t)g + q)));
+        m.nodes[3 * g + q] += (2.0 * u - 1.0) * d.jitter * h3[q];
+      }
+    }
+  } else if (d.mapping != MPG_MAP_NONE) {
+    err = "mesh: unknown mapping";
+    return MPG_ERR_ARG;
+  }
+
+  // ---- per-tet geometry
+  m.normals.resize(T * 12);
+  m.jinv.resize(T * 9);
+  m.detj.resize(T);
+  m.grad.resize(T * 12);
+  static const double ghat[4][3] = {{-1, -1, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  int nonpos = 0;
+#pragma omp parallel for schedule(static) reduction(+ : nonpos)
+  for (int64_t t = 0; t < T; ++t) {
+    const double *X[4];
+    for (int q = 0; q < 4; ++q) X[q] = &m.nodes[3 * m.tets[4 * t + q]];
+    for (int f = 0; f < 4; ++f) {
+      const double *A = X[kFaceNodes[f][0]], *B = X[kFaceNodes[f][1]], *C = X[kFaceNodes[f][2]];
+      const double v1[3] = {A[0] - B[0], A[1] - B[1], A[2] - B[2]};
+      const double v2[3] = {C[0] - B[0], C[1] - B[1], C[2] - B[2]};
+      const double n[3] = {v2[1] * v1[2] - v2[2] * v1[1], v2[2] * v1[0] - v2[0] * v1[2],
+                           v2[0] * v1[1] - v2[1] * v1[0]};
+      const double fac = 1. / sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+      for (int q = 0; q < 3; ++q) m.normals[12 * t + 3 * f + q] = n[q] * fac;
+    }
+    double J[3][3];
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) J[r][c] = X[c + 1][r] - X[0][r];
+    const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+                       J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                       J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+    if (!(det > 0)) ++nonpos;
+    double *I = &m.jinv[9 * t];
+    I[0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) / det;
+    I[1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
+    I[2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
+    I[3] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) / det;
+    I[4] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
+    I[5] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
+    I[6] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) / det;
+    I[7] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
+    I[8] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+    m.detj[t] = det;
+    for (int i = 0; i < 4; ++i)
+      for (int dd = 0; dd < 3; ++dd) {
+        double s = 0.0;
+        for (int k = 0; k < 3; ++k) s += I[3 * k + dd] * ghat[i][k];
+        m.grad[12 * t + 3 * i + dd] = s;
+      }
+  }
+  if (nonpos) {
+    err = "mesh: non-positive Jacobian determinant (mesh.cpp:692)";
+    return MPG_ERR_MESH;
+  }
+
+  // ---- neighbour + vertex permutation per face, indexed by opposite vertex
+  m.nbr_opp.resize(T * 4);
+#pragma omp parallel for schedule(static)
+  for (int64_t t = 0; t < T; ++t)
+    for (int k = 0; k < 4; ++k) {
+      int32_t b = m.nbrs[4 * t + kFaceOfOpposite[k]];
+      if (b < 0) {
+        m.nbr_opp[4 * t + k] = 0xFFFFFFu;
+        continue;
+      }
+      uint32_t perm = 0;
+      int used = 0;
+      for (int j = 0; j < 4; ++j) {
+        if (j == k) continue;
+        int32_t g = m.tets[4 * t + j];
+        int pos = 0;
+        while (m.tets[4 * (int64_t)b + pos] != g) ++pos;
+        perm |= (uint32_t)pos << (2 * j);
+        used |= 1 << pos;
+      }
+      int miss = 0;
+      while (used & (1 << miss)) ++miss;
+      perm |= (uint32_t)miss << (2 * k);
+      m.nbr_opp[4 * t + k] = (perm << 24) | ((uint32_t)b & 0xFFFFFFu);
+    }
+  return MPG_OK;
+}
+
+void host_csr_assemble(const HostMesh &m, int mode, std::vector<int32_t> &rowptr, std::vector<int32_t> &col,
+                       std::vector<double> &val) {
+  const int64_t N = m.N, T = m.T;
+  const int64_t nz = m.d.nz, ny = m.d.ny;
+  const int64_t sj = nz + 1, si = (ny + 1) * (nz + 1);
+  auto offset_index = [&](int32_t r, int32_t c) -> int {
+    // (di,dj,dk) in {-1,0,1}^3 between structured grid nodes
+    int64_t ri = r / si, rj = (r % si) / sj, rk = r % sj;
+    int64_t ci = c / si, cj = (c % si) / sj, ck = c % sj;
+    return (int)((ci - ri + 1) * 9 + (cj - rj + 1) * 3 + (ck - rk + 1));
+  };
+  auto delta = [&](int o) -> int64_t { return (o / 9 - 1) * si + ((o / 3) % 3 - 1) * sj + (o % 3 - 1); };
+  std::vector<uint32_t> mask(N, 0);
+  for (int64_t t = 0; t < T; ++t)
+    for (int a = 0; a < 4; ++a) {
+      int32_t r = m.tets[4 * t + a];
+      if (m.bnd[r]) continue;
+      for (int b = 0; b < 4; ++b) {
+        int32_t c = m.tets[4 * t + b];
+        if (mode == 1 && m.bnd[c]) continue;
+        mask[r] |= 1u << offset_index(r, c);
+      }
+    }
+  for (int64_t r = 0; r < N; ++r)
+    if (m.bnd[r]) mask[r] = 1u << 13;
+  rowptr.assign(N + 1, 0);
+  for (int64_t r = 0; r < N; ++r) rowptr[r + 1] = rowptr[r] + __builtin_popcount(mask[r]);
+  col.resize(rowptr[N]);
+  val.assign(rowptr[N], 0.0);
+#pragma omp parallel for schedule(static)
+  for (int64_t r = 0; r < N; ++r) {
+    int32_t p = rowptr[r];
+    for (int o = 0; o < 27; ++o)
+      if (mask[r] & (1u << o)) col[p++] = (int32_t)(r + delta(o));
+  }
+  const double wcub = 1.0 / 24.0;
+  for (int64_t t = 0; t < T; ++t) {
+    const double *G = &m.grad[12 * t];
+    const double wm = m.detj[t] * wcub;
+    for (int a = 0; a < 4; ++a) {
+      int32_t r = m.tets[4 * t + a];
+      if (m.bnd[r]) continue;
+      for (int b = 0; b < 4; ++b) {
+        int32_t c = m.tets[4 * t + b];
+        if (mode == 1 && m.bnd[c]) continue;
+        double k = 0.0;
+        for (int cub = 0; cub < 4; ++cub)
+          for (int dd = 0; dd < 3; ++dd) k += G[3 * a + dd] * (wm * G[3 * b + dd]);
+        int o = offset_index(r, c);
+        val[rowptr[r] + __builtin_popcount(mask[r] & ((1u << o) - 1u))] += k;
+      }
+    }
+  }
+  for (int64_t r = 0; r < N; ++r)
+    if (m.bnd[r]) val[rowptr[r]] = 1.0;
+}
+
+void host_background(const HostMesh &m, double rho_bg, std::vector<double> &bg) {
+  bg.assign(m.N, 0.0);
+  for (int64_t t = 0; t < m.T; ++t) {
+    const double q = -(rho_bg * (m.detj[t] / 6.0)) * 0.25;
+    for (int a = 0; a < 4; ++a) bg[m.tets[4 * t + a]] += q;
+  }
+  for (int64_t i = 0; i < m.N; ++i)
+    if (m.bnd[i]) bg[i] = 0.0;
+}
+
+void host_fill_ratio(const HostMesh &m, std::vector<float> &ratio) {
+  double dmax = 0.0;
+  for (int64_t t = 0; t < m.T; ++t) dmax = std::max(dmax, m.detj[t]);
+  ratio.resize(m.T);
+  for (int64_t t = 0; t < m.T; ++t) ratio[t] = (float)(m.detj[t] / dmax);
+}

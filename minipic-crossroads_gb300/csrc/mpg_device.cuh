@@ -1,0 +1,112 @@
+// mpg_device.cuh -- device-side layouts and helpers of the GB300 PIC library.
+//
+// All translation units are built with --fmad=false: every FP64 multiply and
+// add rounds separately, like the reference's CPU build.  The single-precision
+// kernels of the mixed form request fused multiply-adds explicitly
+// (__fmaf_rn), so their results are reproducible too.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define MPG_MAX_SPECIES 16
+#define MPG_DEAD 0xFFFFFFFFu
+#define MPG_WALL 0xFFFFFFu
+
+// per-species constants, uploaded with cudaMemcpyToSymbolAsync
+struct SpeciesTable {
+  double q[MPG_MAX_SPECIES];
+  double m[MPG_MAX_SPECIES];
+  double qm[MPG_MAX_SPECIES];
+  double w[MPG_MAX_SPECIES];       // mixed form: weight per species
+  long long qfix[MPG_MAX_SPECIES]; // mixed form: charge w*q in quanta
+  float qm_f[MPG_MAX_SPECIES];
+  float half_wm_f[MPG_MAX_SPECIES];  // 0.5 * w * m for the kinetic energy
+};
+
+// device-side counters of one step; zeroed by the host before a step batch
+struct DevStats {
+  unsigned long long n_killed;
+  unsigned long long n_cross;
+  unsigned long long n_limit;
+  unsigned long long n_nan;
+  double ke;
+  int solver_iters;
+  int solver_status;   // 0 ok, 1 not converged
+  int solver_fail;     // sticky: some solve of the batch did not converge
+  int iters_total;     // summed over the solves of a batch
+  double solver_resid;
+  unsigned int bar_count;
+  unsigned int bar_gen;
+  int bar_error;
+  int pad;
+};
+
+// -------------------------------------------------------------------------
+// grid-wide barrier for cooperative launches.  Every block of the grid is
+// co-resident (cudaLaunchCooperativeKernel guarantees it).  The wait is
+// bounded: after ~2^24 polls (about a second with the back-off) the block
+// raises bar_error and returns false; every later barrier sees the flag and
+// returns false at once, so all blocks leave the kernel.
+__device__ __forceinline__ bool grid_barrier(DevStats *st, unsigned nblocks) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ok = 1;
+    volatile unsigned int *vgen = &st->bar_gen;
+    volatile int *verr = &st->bar_error;
+    const unsigned int g = *vgen;
+    __threadfence();
+    if (atomicAdd(&st->bar_count, 1u) == nblocks - 1) {
+      atomicExch(&st->bar_count, 0u);
+      __threadfence();
+      atomicAdd(&st->bar_gen, 1u);
+    } else {
+      unsigned int spins = 0;
+      while (*vgen == g) {
+        if (*verr) {
+          ok = 0;
+          break;
+        }
+        if (++spins > (1u << 24)) {
+          atomicExch(&st->bar_error, 1);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// block-wide sum of one double per thread (blockDim.x multiple of 32, <= 1024);
+// deterministic for a fixed block size.  Result valid in thread 0.
+__device__ __forceinline__ double block_sum(double v, double *smem32) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) smem32[wid] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0) {
+    const int nw = blockDim.x >> 5;
+    for (int i = 0; i < nw; ++i) s += smem32[i];
+  }
+  return s;
+}
+
+__device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long v, unsigned long long *smem32) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) smem32[wid] = v;
+  __syncthreads();
+  unsigned long long s = 0;
+  if (threadIdx.x == 0) {
+    const int nw = blockDim.x >> 5;
+    for (int i = 0; i < nw; ++i) s += smem32[i];
+  }
+  return s;
+}

@@ -1,0 +1,44 @@
+// mpg_internal.h -- shared declarations of the GB300 PIC library (not installed).
+#pragma once
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "minipic_gb300.h"
+
+// ---------------------------------------------------------------------------
+// Host mesh (built once per run; mesh.cpp:78-714 is the reference).
+struct HostMesh {
+  mpg_mesh_desc d{};
+  int64_t T = 0, N = 0, n_bnodes = 0;
+  std::vector<double> nodes;    // N*3
+  std::vector<int32_t> tets;    // T*4
+  std::vector<int32_t> nbrs;    // T*4, reference face order (0,1,3),(1,2,3),(0,3,2),(0,2,1); -1 wall
+  std::vector<uint32_t> nbr_opp;  // T*4, face opposite local node k: (perm << 24) | nbr, nbr 0xFFFFFF = wall
+  std::vector<double> jinv;     // T*9 row-major J^-1
+  std::vector<double> detj;     // T
+  std::vector<double> normals;  // T*12
+  std::vector<double> grad;     // T*12, grad N_i (x,y,z) per local node
+  std::vector<uint8_t> bnd;     // N
+};
+
+// Returns 0 or an MPG_ERR_* code with err filled.
+int host_mesh_generate(const mpg_mesh_desc &d, HostMesh &m, std::string &err);
+// mode 0 = reference (identity Dirichlet rows, boundary columns kept),
+// mode 1 = symmetric (boundary columns dropped).
+void host_csr_assemble(const HostMesh &m, int mode, std::vector<int32_t> &rowptr, std::vector<int32_t> &col,
+                       std::vector<double> &val);
+void host_background(const HostMesh &m, double rho_bg, std::vector<double> &bg);
+// acceptance ratio vol/vol_max per tet for the volume-uniform fill
+void host_fill_ratio(const HostMesh &m, std::vector<float> &ratio);
+
+// counter-based generator shared by the jitter and the fills (splitmix64 finaliser)
+static inline uint64_t mpg_mix64(uint64_t z) {
+  z += 0x9E3779B97F4A7C15ULL;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+static const uint64_t MPG_SALT_JITTER = 0x6A09E667F3BCC908ULL;
+static const uint64_t MPG_SALT_FILL = 0xBB67AE8584CAA73BULL;

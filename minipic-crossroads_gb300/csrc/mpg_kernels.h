@@ -1,0 +1,105 @@
+// mpg_kernels.h -- launch wrappers of the GB300 PIC kernels (host-callable).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "mpg_device.cuh"
+
+// Plain FP64 particle state: component-major SoA, x[d*cap + p].
+struct PlainParts {
+  int32_t *cell;
+  double *x, *xr, *v;
+  double *w;
+  int32_t *sp;
+  int64_t *id;  // may be null
+  int64_t cap;
+};
+
+// Mixed particle state: cellsp = species<<24 | cell, b = (b1,b2,b3,vx), v = (vy,vz).
+struct MixedParts {
+  uint32_t *c;
+  float4 *b;
+  float2 *v;
+  int64_t *id;  // may be null
+  int64_t cap;
+};
+
+struct DevMesh {
+  int64_t T = 0, N = 0;
+  int4 *tets = nullptr;      // T
+  int4 *nbrs = nullptr;      // T, reference face order, -1 wall
+  double *jinv = nullptr;    // T*9
+  double *detj = nullptr;    // T
+  double *normals = nullptr; // T*12
+  double *grad = nullptr;    // T*12
+  double *nodes = nullptr;   // N*3
+  uint8_t *bnd = nullptr;    // N
+  float4 *mrec = nullptr;    // T*3: J^-1 (9 floats) then E (3 floats)
+  uint4 *mnbr = nullptr;     // T: neighbour + permutation per face (indexed by opposite vertex)
+  float *fill_ratio = nullptr;  // T: vol/vol_max
+};
+
+// ---- plain FP64 path ------------------------------------------------------
+void launch_plain_deposit(cudaStream_t s, const PlainParts &P, int64_t n, const DevMesh &M, const SpeciesTable &S,
+                          int mode, double *rhs);
+void launch_rhs_finish(cudaStream_t s, int64_t N, double *rhs, const double *bg, const uint8_t *bnd);
+void launch_efield_plain(cudaStream_t s, const DevMesh &M, const double *phi, double *Etet);
+void launch_plain_move(cudaStream_t s, const PlainParts &P, int64_t n, const DevMesh &M, const double *Etet,
+                       const SpeciesTable &S, double dt, int kill, int max_cross, DevStats *st);
+// stable compaction of live particles (cell >= 0) from P into Q; returns via *d_count (device)
+void launch_compact_plain(cudaStream_t s, const PlainParts &P, int64_t n, const PlainParts &Q, uint32_t *scratch,
+                          int64_t scratch_len, uint32_t *d_count);
+
+// ---- mixed path -----------------------------------------------------------
+void launch_mixed_deposit(cudaStream_t s, const MixedParts &P, int64_t n, const DevMesh &M, const SpeciesTable &S,
+                          unsigned long long *acc);
+void launch_mixed_convert(cudaStream_t s, int64_t N, unsigned long long *acc, double quantum, const double *bg,
+                          const uint8_t *bnd, double *rhs);
+void launch_efield_mixed(cudaStream_t s, const DevMesh &M, const double *phi);
+void launch_mixed_move(cudaStream_t s, const MixedParts &P, int64_t n, const DevMesh &M, const SpeciesTable &S,
+                       float dt, int kill, int max_cross, unsigned long long *acc, DevStats *st);
+// counting sort by cell: drops dead particles; *d_count receives the new count
+void launch_mixed_sort(cudaStream_t s, const MixedParts &P, int64_t n, const MixedParts &Q, int64_t T,
+                       uint32_t *cnt, uint32_t *start, uint32_t *scratch, int64_t scratch_len, uint32_t *d_count);
+
+void launch_mark_tail_dead(cudaStream_t s, uint32_t *c, int64_t n, const uint32_t *count);
+
+// ---- fills, conversions ---------------------------------------------------
+void launch_fill_uniform(cudaStream_t s, int mixed, const PlainParts &P, const MixedParts &X, int64_t n0, int64_t n,
+                         uint64_t seed, int type, double weight, const double drift[3], double vth, const DevMesh &M,
+                         int64_t id0);
+void launch_fill_ref(cudaStream_t s, const PlainParts &P, int64_t n0, int nppe, int type, double density,
+                     const double vel[3], double temp, double mass, const DevMesh &M, int64_t id0);
+// row-major (n,3) staging <-> component-major plain arrays
+void launch_rows_to_cols(cudaStream_t s, const double *rows, double *cols, int64_t n, int64_t cap);
+void launch_cols_to_rows(cudaStream_t s, const double *cols, double *rows, int64_t n, int64_t cap);
+void launch_mixed_pack(cudaStream_t s, const float *b, const float *v, MixedParts X, int64_t n);
+void launch_mixed_unpack(cudaStream_t s, const MixedParts X, int64_t n, float *b, float *v);
+// plain -> mixed conversion of a state (b = float(xref), v = float(v))
+void launch_plain_to_mixed(cudaStream_t s, const PlainParts &P, int64_t n0, int64_t n, const MixedParts &X);
+// mixed -> plain (x = ref_to_phys(cell, b), xref = b, w = species weight)
+void launch_mixed_to_plain(cudaStream_t s, const MixedParts &X, int64_t n, const DevMesh &M, const SpeciesTable &S,
+                           const PlainParts &P);
+// exclusive scan of n uint32 values into out[0..n] (out[n] = total)
+void scan_u32(cudaStream_t s, const uint32_t *in, uint32_t *out, int64_t n, uint32_t *scratch, int64_t scratch_len);
+int64_t scan_scratch_len(int64_t n);
+
+// ---- solvers (solver.cu) --------------------------------------------------
+struct CgWork {
+  double *r = nullptr, *p0 = nullptr, *p1 = nullptr, *q = nullptr;  // FP64 vectors, n each
+  float *r32 = nullptr, *z32 = nullptr, *q32 = nullptr, *pa32 = nullptr, *pb32 = nullptr;  // mixed inner vectors
+  double *partials = nullptr;  // 4 * max_blocks
+  int max_blocks = 0;
+};
+// plain FP64 CG (CG_solve.hpp:54-114), one cooperative launch; returns 0 or an MPG_ERR_*
+int run_cg64(cudaStream_t s, int device, int64_t n, const int32_t *rowptr, const int32_t *col, const double *val,
+             const double *b, double *x, double tol, int max_iter, CgWork &w, DevStats *st);
+// mixed: FP32 CG inside FP64 iterative refinement, one cooperative launch
+int run_cg_mixed(cudaStream_t s, int device, int64_t n, const int32_t *rowptr, const int32_t *col, const double *val,
+                 const float *val32, const double *b, double *x, double tol, double inner_tol, int max_iter,
+                 CgWork &w, DevStats *st);
+// reference BiCGStab (CG_solve.hpp:115-206), host-driven; returns iterations in *iters
+int run_bicgstab(cudaStream_t s, int64_t n, const int32_t *rowptr, const int32_t *col, const double *val,
+                 const double *b, double *x, double tol, int max_iter, double *work, double *red_dev,
+                 double *red_host, int *iters, double *resid);
+int cg_max_blocks(int device);

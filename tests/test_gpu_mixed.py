@@ -1,0 +1,136 @@
+"""GPU checks of the mixed form (FP32 push/walk, int64 fixed-point deposit,
+FP32 CG inside FP64 refinement).
+
+Bit-exact: fill positions (cell, barycentrics), the fixed-point charge
+accumulator against the oracle's integer restatement, its invariance under
+particle permutation, and the exact total charge.
+Tolerance against the FP64 plain form on the same initial state: phi
+relative error <= 1e-6 over the first steps (stated per check below).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _ctx(mpg, n_side=8, precision=None, jitter=0.2, **cfg):
+    ctx = mpg.Ctx(0)
+    ctx.mesh(n_side, split=mpg.SPLIT_KUHN6, lo=0.0, hi=1.0, mapping=mpg.MAP_JITTER if jitter else 0,
+             jitter=jitter, seed=4)
+    base = dict(precision=mpg.MIXED if precision is None else precision, deposit=mpg.DEPOSIT_LINEAR,
+                solver=mpg.SOLVER_CG, tol=1e-10, warm_start=1, kill_on_wall=1)
+    base.update(cfg)
+    ctx.configure(**base)
+    return ctx
+
+
+def _two_species(ctx, n):
+    ctx.species(0, -1.0, 1.0)
+    ctx.species(1, 1.0, 100.0)
+    ctx.reserve(2 * n)
+    ctx.fill_uniform(n, 11, 0, 1.0 / n, vth=0.05)
+    ctx.fill_uniform(n, 12, 1, 1.0 / n, vth=0.005)
+
+
+def test_mixed_fill_positions_match_oracle(mpg, orc):
+    ctx = _ctx(mpg)
+    m = orc.Mesh(8, split=6, mapping=4, jitter=0.2, seed=4)
+    n = 20000
+    ctx.reserve(n)
+    ctx.fill_uniform(n, 5, 0, 1.0 / n, drift=(0.2, 0, 0), vth=0.02)
+    cs, b, v = ctx.mixed_download()
+    P = orc.Particles(n)
+    P.fill_uniform(m, n, 5, 0, 1.0 / n, drift=(0.2, 0, 0), vth=0.02)
+    assert ((cs & 0xFFFFFF) == P.cell).all() and ((cs >> 24) == 0).all()
+    assert (b == P.xref.astype(np.float32)).all()
+    assert np.abs(v - P.v.astype(np.float32)).max() <= 8 * np.finfo(np.float32).eps * 0.3
+
+
+def test_fixed_point_deposit_bit_exact_and_exact_charge(mpg, orc):
+    ctx = _ctx(mpg)
+    m = orc.Mesh(8, split=6, mapping=4, jitter=0.2, seed=4)
+    _two_species(ctx, 30000)
+    acc, quantum, qfix = ctx.charge()
+    cs, b, v = ctx.mixed_download()
+    oacc = orc.deposit_fixed(m, cs, b, qfix)
+    assert (acc == oacc).all()
+    live = cs != mpg.DEAD
+    assert acc.sum() == sum(int(qfix[s]) for s in (cs[live] >> 24))
+    # order independence: permute the particles and deposit again
+    perm = np.random.default_rng(1).permutation(len(cs))
+    ctx.mixed_upload(cs[perm], b[perm], v[perm])
+    acc2, _, _ = ctx.charge()
+    assert (acc2 == acc).all()
+
+
+def test_mixed_solve_reaches_fp64_tolerance(mpg, orc):
+    ctx = _ctx(mpg, n_side=10, warm_start=0)
+    m = orc.Mesh(10, split=6, mapping=4, jitter=0.2, seed=4)
+    m.assemble(1)
+    rng = np.random.default_rng(7)
+    b = rng.standard_normal(m.N)
+    b[m.boundary == 1] = 0
+    ctx.set_field(mpg.FIELD_RHS, b)
+    it, res = ctx.solve()
+    x = ctx.get_field(mpg.FIELD_PHI)
+    r = b - m.spmv(x)
+    assert np.linalg.norm(r) / np.linalg.norm(b) < 1e-10
+    ox, _, _ = orc.cg(m, b, tol=1e-12)
+    assert np.abs(x - ox).max() <= 1e-8 * np.abs(ox).max()
+
+
+def test_mixed_steps_track_plain_form(mpg):
+    n = 40000
+    mixed = _ctx(mpg, n_side=8)
+    plain = _ctx(mpg, n_side=8, precision=mpg.PLAIN)
+    for c in (mixed, plain):
+        _two_species(c, n)
+    phis = []
+    for s in range(5):
+        sm = mixed.step(0.01, 1)
+        sp = plain.step(0.01, 1)
+        pm = mixed.get_field(mpg.FIELD_PHI)
+        pp = plain.get_field(mpg.FIELD_PHI)
+        err = np.abs(pm - pp).max() / np.abs(pp).max()
+        phis.append(err)
+        assert abs(sm.ke - sp.ke) <= 1e-5 * sp.ke
+        assert abs(sm.n_alive - sp.n_alive) <= max(3, 1e-3 * n)
+    assert max(phis) <= 1e-6, phis
+
+
+def test_mixed_sort_orders_cells_and_drops_dead(mpg):
+    ctx = _ctx(mpg, n_side=6, sort_interval=0)
+    n = 20000
+    ctx.reserve(n)
+    ctx.fill_uniform(n, 8, 0, 1.0 / n, vth=0.5)
+    ctx.step(0.05, 1)
+    cs0, b0, v0 = ctx.mixed_download()
+    live0 = cs0 != mpg.DEAD
+    ctx.sort()
+    cs, b, v = ctx.mixed_download()
+    assert len(cs) == live0.sum()
+    assert (np.diff((cs & 0xFFFFFF).astype(np.int64)) >= 0).all()
+    key0 = np.sort(np.round(b0[live0].astype(np.float64) * 1e7).sum(axis=1))
+    key = np.sort(np.round(b.astype(np.float64) * 1e7).sum(axis=1))
+    assert (key0 == key).all()
+    assert ctx.count() == len(cs)
+
+
+def test_mixed_walk_known_answer(mpg):
+    # one particle moving along +x for one step through a uniform Kuhn mesh
+    ctx = _ctx(mpg, n_side=4, jitter=0.0, kill_on_wall=1)
+    ctx.reserve(1)
+    ctx.fill_uniform(1, 1, 0, 1.0, vth=0.0)
+    cs, b, v = ctx.mixed_download()
+    ctx.species(0, 0.0, 1.0)  # no force
+    v = np.array([[0.1, 0.0, 0.0]], np.float32)
+    ctx.mixed_upload(cs, b, v)
+    d0 = ctx.download()
+    x0 = d0["x"][0]
+    st = ctx.move(1.0)
+    d = ctx.download()
+    if x0[0] + 0.1 < 1.0:
+        assert st.n_killed == 0
+        assert np.allclose(d["x"][0], x0 + [0.1, 0, 0], atol=2e-6)
+    else:
+        assert st.n_killed == 1
