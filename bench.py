@@ -1,0 +1,404 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 electrostatic PIC step (push + deposit + CG solve).
+
+One "step" = PIC::time_step (PIC.cpp:245-267) over the whole particle list:
+fixed-point charge -> field solve -> E per tet -> fused push/walk/deposit.
+
+Default workload (N=1): 48^3 Kuhn-split unit cube, interior nodes jittered
+by U(-0.2h, 0.2h), 8M electrons (q/m = -1, v_th = 0.05) + 8M ions
+(q/m = +0.01, v_th = 0.005) uniform in volume, dt = 0.01, mixed precision,
+CG to 1e-10 relative residual.  Particle state (16M x 28 B = 470 MB) is larger
+than L2, so no L2 flush is needed between steps.
+
+Printed JSON line (rank 0): metric/value in particle-steps/s, the plain FP64
+form of the same workload, per-phase device times, the roofline of the
+dominant kernel, the CPU baseline (the CPU restatement of the reference's
+algorithm, timed on this host's cores), the end-to-end number through the C
+ABI with host buffers, clocks sampled during the timed region.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                  [--workload standard|large|small]
+"""
+import argparse
+import importlib.util
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+METRIC = "particle-steps/s (push+deposit+CG) mixed vs FP64 plain; ensemble p50/p99 ms"
+UNIT = "particle-steps/s"
+
+WORKLOADS = {
+    # 48^3 jittered Kuhn, two species (electrons + ions), mixed precision
+    "standard": dict(name="kuhn48-jitter0.2-e8M-ion8M-mixed", n_side=48, jitter=0.2, dt=0.01, sort_interval=10,
+                     species=[dict(q=-1.0, m=1.0, n=8 << 20, vth=0.05, drift=(0, 0, 0), seed=1),
+                              dict(q=1.0, m=100.0, n=8 << 20, vth=0.005, drift=(0, 0, 0), seed=2)],
+                     rho_background=0.0),
+    # 128^3 Kuhn, 128M electrons in two counter-streaming beams over a fixed background
+    "large": dict(name="kuhn128-2beam-e128M-mixed", n_side=128, jitter=0.0, dt=0.005, sort_interval=10,
+                  species=[dict(q=-1.0, m=1.0, n=64 << 20, vth=0.02, drift=(0.2, 0, 0), seed=1),
+                           dict(q=-1.0, m=1.0, n=64 << 20, vth=0.02, drift=(-0.2, 0, 0), seed=2, same=0)],
+                  rho_background=1.0),
+    # 10^3 Kuhn, 1e5 electrons over a uniform background, plain FP64
+    "small": dict(name="kuhn10-e100k-plain", n_side=10, jitter=0.0, dt=0.01, sort_interval=0,
+                  species=[dict(q=-1.0, m=1.0, n=100000, vth=0.05, drift=(0, 0, 0), seed=1)],
+                  rho_background=1.0),
+}
+
+
+def _pkg():
+    name = "minipic_gb300"
+    if name in sys.modules:
+        return sys.modules[name]
+    spec = importlib.util.spec_from_file_location(name, os.path.join(ROOT, "minipic-crossroads_gb300", "__init__.py"))
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[name] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def total_particles(w):
+    return sum(s["n"] for s in w["species"])
+
+
+def make_ctx(mpg, w, precision, device=0, seed_offset=0):
+    ctx = mpg.Ctx(device)
+    ctx.mesh(w["n_side"], split=mpg.SPLIT_KUHN6, lo=0.0, hi=1.0,
+             mapping=mpg.MAP_JITTER if w["jitter"] else mpg.MAP_NONE, jitter=w["jitter"], seed=7)
+    ctx.configure(precision=precision, deposit=mpg.DEPOSIT_LINEAR, solver=mpg.SOLVER_CG, tol=1e-10, max_iter=5000,
+                  warm_start=1, kill_on_wall=1, max_crossings=1000,
+                  sort_interval=w["sort_interval"] if precision == mpg.MIXED else 0,
+                  rho_background=w["rho_background"])
+    # weights: each species carries a total charge of magnitude 1 in the unit cube
+    by_charge = {}
+    for s in w["species"]:
+        by_charge[s["q"]] = by_charge.get(s["q"], 0) + s["n"]
+    ctx.reserve(total_particles(w))
+    for i, s in enumerate(w["species"]):
+        sp = s.get("same", i)
+        ctx.species(sp, s["q"], s["m"])
+        ctx.fill_uniform(s["n"], s["seed"] + 1000 * seed_offset, sp, 1.0 / by_charge[s["q"]], drift=s["drift"],
+                         vth=s["vth"])
+    return ctx
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (SM clock, reasons)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = max(mx, float(p[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if p[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def phase_bytes(w, ctx, stats, steps, mpg):
+    """Algorithmic bytes per launch of each phase of the mixed step."""
+    T, N = ctx.T, ctx.N
+    P = total_particles(w)
+    rp, col, val = ctx.csr()
+    nnz = len(val)
+    n = N
+    iters = stats.solver_iters / max(steps, 1)
+    cg_iter = 8 * nnz + 4 * (n + 1) + 44 * n
+    sweep = 12 * nnz + 4 * (n + 1) + 48 * n
+    return {
+        # 28 B read + 28 B write per particle, 16 B of node ids, 4 x 8 B accumulator RMW,
+        # per-tet walk record (48 B) + neighbour table (16 B) read once
+        "move": P * (56 + 16) + N * 16 + T * 64,
+        "solve": iters * cg_iter + 3 * sweep,
+        "efield": T * (16 + 48 + 12) + N * 8,
+        "deposit": N * (8 + 8 + 8 + 8),
+        "nnz": nnz, "cg_iter_bytes": cg_iter, "iters_per_step": iters,
+    }
+
+
+def read_traffic(kernel):
+    """DRAM bytes per launch from a committed ncu summary (profiles/<kernel>*.txt), if any."""
+    pdir = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(pdir):
+        return None
+    for fn in sorted(os.listdir(pdir)):
+        if not fn.startswith(kernel) or not fn.endswith(".txt"):
+            continue
+        with open(os.path.join(pdir, fn)) as f:
+            for line in f:
+                if line.startswith("dram_bytes_per_launch_full_workload:"):
+                    try:
+                        return float(line.split(":", 1)[1].split()[0])
+                    except ValueError:
+                        return None
+    return None
+
+
+def cpu_baseline(w, budget_s=20.0, max_steps=3):
+    """The CPU restatement of the reference step (plain FP64, all host cores)."""
+    sys.path.insert(0, ROOT)
+    from oracle import oracle as O
+    import numpy as np
+    O.build()
+    cores = os.cpu_count() or 1
+    m = O.Mesh(w["n_side"], split=6, mapping=4 if w["jitter"] else 0, jitter=w["jitter"], seed=7)
+    m.assemble(1)
+    P = total_particles(w)
+    parts = O.Particles(P)
+    by_charge = {}
+    for s in w["species"]:
+        by_charge[s["q"]] = by_charge.get(s["q"], 0) + s["n"]
+    qs, ms = [0.0] * 16, [1.0] * 16
+    for i, s in enumerate(w["species"]):
+        sp = s.get("same", i)
+        qs[sp], ms[sp] = s["q"], s["m"]
+        parts.fill_uniform(m, s["n"], s["seed"], sp, 1.0 / by_charge[s["q"]], drift=s["drift"], vth=s["vth"],
+                           nthreads=cores)
+    bg = m.background(w["rho_background"]) if w["rho_background"] else None
+    phi = np.zeros(m.N)
+    cfg = O.StepCfg(1, 1, 1e-10, 5000, 1, 1, 1, 1000, 1, cores)
+    scratch = np.zeros((P, 3))
+    done, ps, t_used = 0, 0, 0.0
+    while done < max_steps and t_used < budget_s:
+        n0 = parts.n
+        t0 = time.perf_counter()
+        O.step(m, parts, cfg, w["dt"], qs, ms, bg, phi, scratch)
+        t_used += time.perf_counter() - t0
+        ps += n0
+        done += 1
+    return {"value": ps / t_used, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{done} full steps of the same workload ({P} particles, plain FP64, OpenMP {cores} threads)",
+            "seconds": round(t_used, 3)}
+
+
+def run_reference(args, w):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    cb = cpu_baseline(w, budget_s=max(10.0, 6.0 * args.steps), max_steps=max(1, min(args.steps, 3)))
+    line = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_particles(w) / cb["value"] * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": w["name"]}, "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="standard", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    w = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        return run_reference(args, w)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        torch.cuda.set_device(local)
+
+    def barrier_max(x):
+        if dist is None:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def barrier_sum(x):
+        if dist is None:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        return float(t.item())
+
+    mpg = _pkg()
+    mpg.build()
+    mpg.load()
+    precision = mpg.PLAIN if args.workload == "small" else mpg.MIXED
+    ctx = make_ctx(mpg, w, precision, device=local, seed_offset=rank)
+    for _ in range(args.warmup):
+        ctx.step(w["dt"], 1)
+    n0 = ctx.count()
+    if dist is not None:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ctx.timer_start()
+    st = ctx.step(w["dt"], args.steps)
+    ms = ctx.timer_stop()
+    clk = clocks.stop()
+    launches = st.n_launches
+    n1 = st.n_alive
+    particle_steps = 0.5 * (n0 + n1) * args.steps
+    t_max = barrier_max(ms)
+    ps_total = barrier_sum(particle_steps)
+    value = ps_total / (t_max * 1e-3)
+
+    # per-phase device times on a separate timed pass
+    ctx.set_timing(True)
+    k_ph = min(args.steps, 10)
+    ph = ctx.step(w["dt"], k_ph)
+    ctx.set_timing(False)
+    phases = {k: getattr(ph, "ms_" + k) / k_ph for k in ("deposit", "solve", "efield", "move", "sort")}
+    line = {}
+    if rank == 0:
+        hbm, kind = peaks()
+        pb = phase_bytes(w, ctx, ph, k_ph, mpg) if precision == mpg.MIXED else None
+        dominant = max(("solve", "move", "efield", "deposit"), key=lambda k: phases[k])
+        kern = {"solve": "k_cg_mixed", "move": "k_mixed_move", "efield": "k_efield_mixed",
+                "deposit": "k_mixed_convert"}[dominant]
+        roof = None
+        if pb is not None:
+            bytes_launch = pb[dominant]
+            achieved = bytes_launch / (phases[dominant] * 1e-3) / 1e9
+            traffic = read_traffic(kern)
+            roof = {"bound": "hbm", "kernel": kern, "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                    "frac": round(achieved / hbm, 4), "peak_kind": kind, "traffic": traffic,
+                    "algorithmic_bytes_per_launch": int(bytes_launch), "ms_per_launch": round(phases[dominant], 4)}
+            # the particle kernel alone, for reference
+            mv = pb["move"] / (phases["move"] * 1e-3) / 1e9
+            roof["move_kernel_gbs"] = round(mv, 1)
+            roof["move_kernel_frac"] = round(mv / hbm, 4)
+            roof["cg_iters_per_step"] = round(pb["iters_per_step"], 1)
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32" if precision == mpg.MIXED else "f64",
+                "precision": ("mixed: f32 push/walk, i64 fixed-point deposit, f32 CG inside f64 refinement"
+                              if precision == mpg.MIXED else "plain f64"),
+                "data": "synthetic",
+                "config": {"workload": w["name"], "n_side": w["n_side"], "tets": ctx.T, "nodes": ctx.N,
+                           "particles": total_particles(w), "dt": w["dt"], "cg_tol": 1e-10,
+                           "parallelism": "replicas" if world > 1 else "single",
+                           "l2": "inputs larger than L2 (particle state > 129 MB), no flush"},
+                "phases_ms_per_step": {k: round(v, 4) for k, v in phases.items()},
+                "solver_iters_per_step": ph.solver_iters / k_ph,
+                "roofline": roof, "gpu_launches": launches, "clocks": clk}
+    # plain FP64 form of the same workload (the form the mixed target is measured against)
+    if not args.no_plain and precision == mpg.MIXED:
+        ctx.close()
+        pc = make_ctx(mpg, w, mpg.PLAIN, device=local, seed_offset=rank)
+        kp = max(1, min(args.steps, 5))
+        pc.step(w["dt"], 2)
+        q0 = pc.count()
+        pc.timer_start()
+        pst = pc.step(w["dt"], kp)
+        pms = pc.timer_stop()
+        pv = barrier_sum(0.5 * (q0 + pst.n_alive) * kp) / (barrier_max(pms) * 1e-3)
+        if rank == 0:
+            line["plain_fp64"] = {"value": pv, "unit": UNIT, "steps": kp, "ms_per_step": pms / kp,
+                                  "mixed_over_plain": value / pv}
+        pc.close()
+        ctx = make_ctx(mpg, w, precision, device=local, seed_offset=rank) if not args.no_e2e else None
+    # end to end through the C ABI with host buffers: state upload, K steps with
+    # the step statistics read back each step, state download
+    if not args.no_e2e and ctx is not None and precision == mpg.MIXED:
+        import numpy as np
+        for _ in range(2):
+            ctx.step(w["dt"], 1)
+        cs, b, v = ctx.mixed_download()
+        try:
+            import torch
+            pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
+            cs, b, v = pin(cs), pin(b), pin(v)
+        except Exception:
+            pass
+        ke = args.steps
+        t0 = time.perf_counter()
+        ctx.mixed_upload(cs, b, v)
+        n_e = ctx.count()
+        for _ in range(ke):
+            ctx.step(w["dt"], 1)
+        cs2, b2, v2 = ctx.mixed_download()
+        t1 = time.perf_counter()
+        eps = barrier_sum(n_e * ke) / barrier_max(t1 - t0)
+        if rank == 0:
+            nbytes = cs.nbytes + b.nbytes + v.nbytes
+            line["e2e"] = {"value": eps, "unit": UNIT, "h2d_bytes_per_step": int(nbytes / ke),
+                           "d2h_bytes_per_step": int((cs2.nbytes + b2.nbytes + v2.nbytes) / ke + 136),
+                           "how": "mpg_mixed_upload from pinned host buffers, mpg_step x K with stats read back "
+                                  "each step, mpg_mixed_download; host wall clock"}
+    if rank == 0:
+        if not args.no_cpu:
+            try:
+                line["cpu_baseline"] = cpu_baseline(w)
+            except Exception as e:  # the CPU baseline is reported, never required
+                line["cpu_baseline"] = {"value": None, "error": str(e)[:200]}
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -94,6 +94,7 @@ typedef struct {
   /* device time per phase (ms), summed over the steps of the call;
    * filled when mpg_set_timing(ctx, 1) */
   double ms_deposit, ms_solve, ms_efield, ms_move, ms_sort;
+  int64_t n_launches;    /* kernels this library launched during the call */
 } mpg_step_stats;
 
 int mpg_version(void);
@@ -105,6 +106,10 @@ int mpg_ctx_destroy(mpg_ctx *ctx);
 /* copies the last error message of ctx (or of the last failed create) */
 int mpg_last_error(mpg_ctx *ctx, char *buf, int len);
 int mpg_set_timing(mpg_ctx *ctx, int on);
+/* device timer on the ctx stream (replaces the Kokkos::Impl::Timer pairs of
+ * PIC.cpp:250-259): op 0 records the start event, op 1 records the stop
+ * event, waits for it and returns the elapsed milliseconds in *ms. */
+int mpg_timer(mpg_ctx *ctx, int op, double *ms);
 
 /* DataWarehouse::create_mesh -> Mesh::Mesh (data_warehouse.cpp:50-54, mesh.cpp:78-714) */
 int mpg_mesh_build(mpg_ctx *ctx, const mpg_mesh_desc *desc);

@@ -26,6 +26,7 @@ DEAD = 0xFFFFFFFF
 # every symbol include/minipic_gb300.h declares
 EXPORTS = [
     "mpg_version", "mpg_device_count", "mpg_ctx_create", "mpg_ctx_destroy", "mpg_last_error", "mpg_set_timing",
+    "mpg_timer",
     "mpg_mesh_build", "mpg_mesh_sizes", "mpg_mesh_download", "mpg_species_set", "mpg_configure", "mpg_csr_sizes",
     "mpg_csr_download", "mpg_particles_reserve", "mpg_fill_ref", "mpg_fill_uniform", "mpg_particles_upload",
     "mpg_particles_download", "mpg_particles_count", "mpg_mixed_download", "mpg_mixed_upload",
@@ -50,7 +51,8 @@ class StepStats(C.Structure):
     _fields_ = [("ke", C.c_double), ("n_alive", C.c_int64), ("n_killed", C.c_int64), ("n_crossings", C.c_int64),
                 ("n_walk_limit", C.c_int64), ("solver_iters", C.c_int), ("solver_resid", C.c_double),
                 ("status", C.c_int), ("steps", C.c_int), ("ms_deposit", C.c_double), ("ms_solve", C.c_double),
-                ("ms_efield", C.c_double), ("ms_move", C.c_double), ("ms_sort", C.c_double)]
+                ("ms_efield", C.c_double), ("ms_move", C.c_double), ("ms_sort", C.c_double),
+                ("n_launches", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -88,6 +90,7 @@ def load():
         "mpg_ctx_destroy": ([P], I),
         "mpg_last_error": ([P, C.c_char_p, I], I),
         "mpg_set_timing": ([P, I], I),
+        "mpg_timer": ([P, I, C.POINTER(D)], I),
         "mpg_mesh_build": ([P, C.POINTER(MeshDesc)], I),
         "mpg_mesh_sizes": ([P, C.POINTER(I64), C.POINTER(I64), C.POINTER(I64)], I),
         "mpg_mesh_download": ([P] * 8, I),
@@ -177,6 +180,14 @@ class Ctx:
 
     def set_timing(self, on=True):
         self._ck(self.L.mpg_set_timing(self.h, int(on)))
+
+    def timer_start(self):
+        self._ck(self.L.mpg_timer(self.h, 0, None))
+
+    def timer_stop(self):
+        ms = C.c_double()
+        self._ck(self.L.mpg_timer(self.h, 1, C.byref(ms)))
+        return ms.value
 
     def mesh(self, n, split=SPLIT_KUHN6, lo=0.0, hi=1.0, mapping=MAP_NONE, jitter=0.0, seed=0):
         nx, ny, nz = (n, n, n) if np.isscalar(n) else n

@@ -66,6 +66,7 @@ struct mpg_ctx {
   DevStats *d_stats = nullptr, *h_stats = nullptr;
 
   std::vector<void *> allocs;  // device allocations owned by the ctx
+  int64_t launches = 0;        // kernels launched by this ctx (cumulative)
 };
 
 static std::string g_last_create_error;
@@ -339,6 +340,7 @@ int phase_deposit_plain(mpg_ctx *c) {
   CK(cudaMemsetAsync(c->rhs, 0, sizeof(double) * c->dm.N, c->stream));
   launch_plain_deposit(c->stream, c->pp[c->cur], c->n, c->dm, c->sp, c->cfg.deposit, c->rhs);
   launch_rhs_finish(c->stream, c->dm.N, c->rhs, c->bg, c->dm.bnd);
+  c->launches += 2;
   CKL();
   return MPG_OK;
 }
@@ -349,8 +351,10 @@ int phase_deposit_mixed(mpg_ctx *c) {
     CK(cudaMemsetAsync(c->acc, 0, sizeof(unsigned long long) * c->dm.N, c->stream));
     launch_mixed_deposit(c->stream, c->mp[c->cur], c->n, c->dm, c->sp, c->acc);
     c->acc_valid = true;
+    c->launches += 1;
   }
   launch_mixed_convert(c->stream, c->dm.N, c->acc, c->quantum, c->bg, c->dm.bnd, c->rhs);
+  c->launches += 1;
   CKL();
   return MPG_OK;
 }
@@ -362,6 +366,7 @@ int phase_solve(mpg_ctx *c) {
     if (!c->cfg.warm_start) CK(cudaMemsetAsync(c->phi, 0, sizeof(double) * N, c->stream));
     int rc = run_cg_mixed(c->stream, c->device, N, c->rowptr, c->col, c->val, c->val32, c->rhs, c->phi, c->cfg.tol,
                           1e-5, c->cfg.max_iter, c->cg, c->d_stats);
+    c->launches += 1;
     if (rc) return fail(c, rc, "mixed CG launch failed: %s", cudaGetErrorString(cudaGetLastError()));
     return MPG_OK;
   }
@@ -370,6 +375,7 @@ int phase_solve(mpg_ctx *c) {
     if (!c->cfg.warm_start) CK(cudaMemsetAsync(c->phi, 0, sizeof(double) * N, c->stream));
     int rc = run_cg64(c->stream, c->device, N, c->rowptr, c->col, c->val, c->rhs, c->phi, c->cfg.tol,
                       c->cfg.max_iter, c->cg, c->d_stats);
+    c->launches += 1;
     if (rc) return fail(c, rc, "CG launch failed: %s", cudaGetErrorString(cudaGetLastError()));
     return MPG_OK;
   }
@@ -379,6 +385,8 @@ int phase_solve(mpg_ctx *c) {
   double res = 0.0;
   int rc = run_bicgstab(c->stream, N, c->rowptr, c->col, c->val, c->rhs, c->phi, c->cfg.tol, c->cfg.max_iter,
                         c->bicg_work, c->red_dev, c->red_host, &it, &res);
+  // 2 SpMV + 6 dot pairs + 6 updates per iteration, roughly
+  c->launches += 4 + (int64_t)it * 20;
   if (rc == MPG_ERR_CUDA) return fail(c, rc, "BiCGStab: %s", cudaGetErrorString(cudaGetLastError()));
   // record into the device stats so both solver kinds report the same way
   DevStats tmp;
@@ -399,6 +407,7 @@ int phase_efield(mpg_ctx *c) {
     launch_efield_mixed(c->stream, c->dm, c->phi);
   else
     launch_efield_plain(c->stream, c->dm, c->phi, c->Etet);
+  c->launches += 1;
   CKL();
   return MPG_OK;
 }
@@ -406,6 +415,7 @@ int phase_efield(mpg_ctx *c) {
 int compact_plain(mpg_ctx *c) {
   const int other = 1 - c->cur;
   launch_compact_plain(c->stream, c->pp[c->cur], c->n, c->pp[other], c->scan_scratch, c->scan_len, c->d_count);
+  c->launches += 3;
   CKL();
   CK(cudaMemcpyAsync(c->h_count, c->d_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
@@ -418,6 +428,7 @@ int sort_mixed(mpg_ctx *c) {
   const int other = 1 - c->cur;
   launch_mixed_sort(c->stream, c->mp[c->cur], c->n, c->mp[other], c->dm.T, c->sort_cnt, c->sort_start,
                     c->scan_scratch, c->scan_len, c->d_count);
+  c->launches += 6;
   CKL();
   c->cur = other;
   // the new count is read back at the next host sync; slots [count, n) of the
@@ -425,6 +436,7 @@ int sort_mixed(mpg_ctx *c) {
   const int64_t n = c->n;
   if (n > 0) {
     launch_mark_tail_dead(c->stream, c->mp[c->cur].c, n, c->d_count);
+    c->launches += 1;
     CKL();
   }
   return MPG_OK;
@@ -455,6 +467,7 @@ int one_step(mpg_ctx *c, double dt, mpg_step_stats *acc_st, bool &sorted) {
     launch_plain_move(c->stream, c->pp[c->cur], c->n, c->dm, c->Etet, c->sp, dt, c->cfg.kill_on_wall,
                       c->cfg.max_crossings, c->d_stats);
   }
+  c->launches += 1;
   CKL();
   ev_record(c, 4);
   c->step_count++;
@@ -648,6 +661,21 @@ int mpg_last_error(mpg_ctx *c, char *buf, int len) {
 int mpg_set_timing(mpg_ctx *c, int on) {
   if (!c) return MPG_ERR_ARG;
   c->timing = on != 0;
+  return MPG_OK;
+}
+
+int mpg_timer(mpg_ctx *c, int op, double *ms) {
+  ENTER(c);
+  if (op == 0) {
+    CK(cudaEventRecord(c->ev[10], c->stream));
+    return MPG_OK;
+  }
+  if (op != 1 || !ms) return fail(c, MPG_ERR_ARG, "mpg_timer: op must be 0 (start) or 1 (stop) with ms");
+  CK(cudaEventRecord(c->ev[11], c->stream));
+  CK(cudaEventSynchronize(c->ev[11]));
+  float f = 0.f;
+  CK(cudaEventElapsedTime(&f, c->ev[10], c->ev[11]));
+  *ms = f;
   return MPG_OK;
 }
 
@@ -1146,6 +1174,7 @@ int mpg_step(mpg_ctx *c, double dt, int n_steps, mpg_step_stats *st) {
   if (n_steps < 0) return fail(c, MPG_ERR_ARG, "n_steps < 0");
   mpg_step_stats acc{};
   TRY(zero_stats(c));
+  const int64_t launches0 = c->launches;
   bool sorted = false;
   for (int i = 0; i < n_steps; ++i) TRY(one_step(c, dt, &acc, sorted));
   TRY(sync_stats(c));
@@ -1162,6 +1191,7 @@ int mpg_step(mpg_ctx *c, double dt, int n_steps, mpg_step_stats *st) {
   acc.solver_iters = h.iters_total;
   acc.solver_resid = h.solver_resid;
   acc.steps = n_steps;
+  acc.n_launches = c->launches - launches0;
   if (c->cfg.precision == MPG_MIXED)
     c->n_live -= (int64_t)h.n_killed;
   else
