@@ -43,6 +43,7 @@ struct mpg_ctx {
   int32_t *rowptr = nullptr, *col = nullptr;
   double *val = nullptr;
   float *val32 = nullptr;
+  DiaMatrix dia;  // structured diagonal form of the symmetric matrix (CG paths)
   double *rhs = nullptr, *phi = nullptr, *bg = nullptr, *Etet = nullptr;
   unsigned long long *acc = nullptr;
   bool acc_valid = false;
@@ -364,8 +365,7 @@ int phase_solve(mpg_ctx *c) {
   if (c->cfg.precision == MPG_MIXED) {
     TRY(ensure_cg_work(c, N));
     if (!c->cfg.warm_start) CK(cudaMemsetAsync(c->phi, 0, sizeof(double) * N, c->stream));
-    int rc = run_cg_mixed(c->stream, c->device, N, c->rowptr, c->col, c->val, c->val32, c->rhs, c->phi, c->cfg.tol,
-                          1e-5, c->cfg.max_iter, c->cg, c->d_stats);
+    int rc = run_cg_mixed(c->stream, c->dia, c->rhs, c->phi, c->cfg.tol, 1e-5, c->cfg.max_iter, c->cg, c->d_stats);
     c->launches += 1;
     if (rc) return fail(c, rc, "mixed CG launch failed: %s", cudaGetErrorString(cudaGetLastError()));
     return MPG_OK;
@@ -373,8 +373,7 @@ int phase_solve(mpg_ctx *c) {
   if (c->cfg.solver == MPG_SOLVER_CG) {
     TRY(ensure_cg_work(c, N));
     if (!c->cfg.warm_start) CK(cudaMemsetAsync(c->phi, 0, sizeof(double) * N, c->stream));
-    int rc = run_cg64(c->stream, c->device, N, c->rowptr, c->col, c->val, c->rhs, c->phi, c->cfg.tol,
-                      c->cfg.max_iter, c->cg, c->d_stats);
+    int rc = run_cg64_dia(c->stream, c->dia, c->rhs, c->phi, c->cfg.tol, c->cfg.max_iter, c->cg, c->d_stats);
     c->launches += 1;
     if (rc) return fail(c, rc, "CG launch failed: %s", cudaGetErrorString(cudaGetLastError()));
     return MPG_OK;
@@ -556,6 +555,9 @@ void free_field(mpg_ctx *c) {
   dfree(c, c->col);
   dfree(c, c->val);
   dfree(c, c->val32);
+  dfree(c, c->dia.val64);
+  dfree(c, c->dia.val32);
+  c->dia = DiaMatrix();
   dfree(c, c->rhs);
   dfree(c, c->phi);
   dfree(c, c->bg);
@@ -773,6 +775,39 @@ int mpg_configure(mpg_ctx *c, const mpg_config *cfg) {
     CK(cudaMemcpyAsync(c->val, val.data(), sizeof(double) * c->nnz, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(c->val32, v32.data(), sizeof(float) * c->nnz, cudaMemcpyHostToDevice, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    dfree(c, c->dia.val64);
+    dfree(c, c->dia.val32);
+    c->dia = DiaMatrix();
+    if (mode == 1) {
+      // diagonal offsets present in the interior rows, in column order
+      std::vector<int64_t> offs;
+      for (int64_t r = 0; r < N; ++r) {
+        if (c->hm.bnd[r]) continue;
+        for (int32_t k = rp[r]; k < rp[r + 1]; ++k) offs.push_back((int64_t)col[k] - r);
+      }
+      std::sort(offs.begin(), offs.end());
+      offs.erase(std::unique(offs.begin(), offs.end()), offs.end());
+      if (offs.size() > 27) return fail(c, MPG_ERR_MESH, "matrix is not a structured stencil (%zu offsets)", offs.size());
+      const int nd = (int)offs.size();
+      std::vector<double> d64((size_t)nd * N, 0.0);
+      for (int64_t r = 0; r < N; ++r) {
+        if (c->hm.bnd[r]) continue;
+        for (int32_t k = rp[r]; k < rp[r + 1]; ++k) {
+          const int d = (int)(std::lower_bound(offs.begin(), offs.end(), (int64_t)col[k] - r) - offs.begin());
+          d64[(size_t)d * N + r] = val[k];
+        }
+      }
+      std::vector<float> d32(d64.begin(), d64.end());
+      c->dia.n = N;
+      c->dia.ndiag = nd;
+      for (int d = 0; d < nd; ++d) c->dia.off[d] = (int)offs[d];
+      TRY(dalloc(c, &c->dia.val64, (int64_t)nd * N));
+      TRY(dalloc(c, &c->dia.val32, (int64_t)nd * N));
+      CK(cudaMemcpyAsync(c->dia.val64, d64.data(), sizeof(double) * d64.size(), cudaMemcpyHostToDevice, c->stream));
+      CK(cudaMemcpyAsync(c->dia.val32, d32.data(), sizeof(float) * d32.size(), cudaMemcpyHostToDevice, c->stream));
+      c->dia.bnd = c->dm.bnd;
+      CK(cudaStreamSynchronize(c->stream));
+    }
     c->csr_mode = mode;
   }
   if (!c->rhs) {

@@ -370,27 +370,78 @@ __global__ void __launch_bounds__(kScanThreads) k_compact_plain(PlainParts P, in
 
 // ---------------------------------------------------------------------------
 // mixed form
-__device__ __forceinline__ void deposit_fixed(unsigned long long *__restrict__ acc, const int4 nd, float b1, float b2,
-                                              float b3, long long Q) {
-  const float Qf = (float)Q;
-  const long long c1 = __float2ll_rn(b1 * Qf);
-  const long long c2 = __float2ll_rn(b2 * Qf);
-  const long long c3 = __float2ll_rn(b3 * Qf);
-  const long long c0 = Q - c1 - c2 - c3;
-  atomicAdd(acc + nd.x, (unsigned long long)c0);
-  atomicAdd(acc + nd.y, (unsigned long long)c1);
-  atomicAdd(acc + nd.z, (unsigned long long)c2);
-  atomicAdd(acc + nd.w, (unsigned long long)c3);
+// Fixed-point charge of one particle split over its tet's four nodes:
+// c_k = rint(b_k * Q) for k = 1..3 and c_0 = Q - c_1 - c_2 - c_3, so the four
+// parts sum to the particle's charge exactly.
+//
+// Warp-aggregated: lanes that hold the same cell in a contiguous run (the
+// usual case after a cell sort) add their contributions with a segmented warp
+// scan, and the last lane of each run issues the four atomics.  Without this,
+// a sorted warp sends 32 same-address atomics to one L2 slice, which
+// serialise.  Integer addition is associative, so the result does not depend
+// on the grouping.  Every lane of the warp must call this; lanes with
+// key < 0 contribute nothing.
+__device__ __forceinline__ void deposit_fixed_warp(unsigned long long *__restrict__ acc,
+                                                   const int4 *__restrict__ tets, int key, float b1, float b2,
+                                                   float b3, long long Q) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  long long c0 = 0, c1 = 0, c2 = 0, c3 = 0;
+  if (key >= 0) {
+    const float Qf = (float)Q;
+    c1 = __float2ll_rn(b1 * Qf);
+    c2 = __float2ll_rn(b2 * Qf);
+    c3 = __float2ll_rn(b3 * Qf);
+    c0 = Q - c1 - c2 - c3;
+  }
+  const int prev = __shfl_up_sync(FULL, key, 1);
+  const bool head = lane == 0 || prev != key;
+  const unsigned heads = __ballot_sync(FULL, head);
+  const int seg = 31 - __clz(heads & (FULL >> (31 - lane)));
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int su = __shfl_up_sync(FULL, seg, o);
+    const long long u0 = __shfl_up_sync(FULL, c0, o);
+    const long long u1 = __shfl_up_sync(FULL, c1, o);
+    const long long u2 = __shfl_up_sync(FULL, c2, o);
+    const long long u3 = __shfl_up_sync(FULL, c3, o);
+    if (lane >= o && su == seg) {
+      c0 += u0;
+      c1 += u1;
+      c2 += u2;
+      c3 += u3;
+    }
+  }
+  const int sn = __shfl_down_sync(FULL, seg, 1);
+  const bool tail = lane == 31 || sn != seg;
+  if (tail && key >= 0) {
+    const int4 nd = tets[key];
+    atomicAdd(acc + nd.x, (unsigned long long)c0);
+    atomicAdd(acc + nd.y, (unsigned long long)c1);
+    atomicAdd(acc + nd.z, (unsigned long long)c2);
+    atomicAdd(acc + nd.w, (unsigned long long)c3);
+  }
 }
 
 __global__ void __launch_bounds__(kThreads) k_mixed_deposit(MixedParts P, int64_t n, const int4 *__restrict__ tets,
                                                             SpeciesTable S, unsigned long long *__restrict__ acc) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n) return;
-  const uint32_t cs = P.c[p];
-  if (cs == MPG_DEAD) return;
-  const float4 b = P.b[p];
-  deposit_fixed(acc, tets[cs & 0xFFFFFFu], b.x, b.y, b.z, S.qfix[cs >> 24]);
+  int key = -1;
+  float b1 = 0.f, b2 = 0.f, b3 = 0.f;
+  long long Q = 0;
+  if (p < n) {
+    const uint32_t cs = P.c[p];
+    if (cs != MPG_DEAD) {
+      const float4 b = P.b[p];
+      key = (int)(cs & 0xFFFFFFu);
+      b1 = b.x;
+      b2 = b.y;
+      b3 = b.z;
+      Q = S.qfix[cs >> 24];
+    }
+  }
+  // each lane converts its own charge Q, so runs may mix species
+  deposit_fixed_warp(acc, tets, key, b1, b2, b3, Q);
 }
 
 __global__ void k_mixed_convert(int64_t N, unsigned long long *__restrict__ acc, double quantum,
@@ -434,6 +485,9 @@ __global__ void __launch_bounds__(kThreads) k_mixed_move(MixedParts P, int64_t n
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   float ke = 0.f;
   unsigned long long killed = 0, cross = 0, limit = 0;
+  int dep_key = -1;
+  float d1 = 0.f, d2 = 0.f, d3 = 0.f;
+  long long dq = 0;
   if (p < n) {
     uint32_t cs = P.c[p];
     if (cs != MPG_DEAD) {
@@ -554,10 +608,16 @@ __global__ void __launch_bounds__(kThreads) k_mixed_move(MixedParts P, int64_t n
         P.b[p] = make_float4(l1, l2, l3, vx);
         P.v[p] = make_float2(vy, vz);
         ke = S.half_wm_f[s] * __fmaf_rn(vz, vz, __fmaf_rn(vy, vy, vx * vx));
-        deposit_fixed(acc, tets[e], l1, l2, l3, S.qfix[s]);
+        dep_key = (int)e;
+        d1 = l1;
+        d2 = l2;
+        d3 = l3;
+        dq = S.qfix[s];
       }
     }
   }
+  // deposit of the new position for the next step's field solve
+  deposit_fixed_warp(acc, tets, dep_key, d1, d2, d3, dq);
   double bke = block_sum((double)ke, sd);
   if (threadIdx.x == 0 && bke != 0.0) atomicAdd(&st->ke, bke);
   unsigned long long bk = block_sum_u64(killed, su);

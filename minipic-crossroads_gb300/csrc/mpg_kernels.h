@@ -85,19 +85,34 @@ void scan_u32(cudaStream_t s, const uint32_t *in, uint32_t *out, int64_t n, uint
 int64_t scan_scratch_len(int64_t n);
 
 // ---- solvers (solver.cu) --------------------------------------------------
+// Structured diagonal (DIA) form of the symmetric stiffness matrix: on the
+// structured tet grid every column of row i is i + off[d] for at most 27
+// offsets.  val[d*n + i] holds A(i, i+off[d]) (0 where absent); boundary
+// rows are identity rows and are flagged in bnd.
+struct DiaMatrix {
+  int64_t n = 0;
+  int ndiag = 0;
+  int off[27] = {};
+  double *val64 = nullptr;  // ndiag * n
+  float *val32 = nullptr;   // ndiag * n
+  const uint8_t *bnd = nullptr;
+};
+
 struct CgWork {
   double *r = nullptr, *p0 = nullptr, *p1 = nullptr, *q = nullptr;  // FP64 vectors, n each
   float *r32 = nullptr, *z32 = nullptr, *q32 = nullptr, *pa32 = nullptr, *pb32 = nullptr;  // mixed inner vectors
   double *partials = nullptr;  // 4 * max_blocks
   int max_blocks = 0;
 };
-// plain FP64 CG (CG_solve.hpp:54-114), one cooperative launch; returns 0 or an MPG_ERR_*
+// plain FP64 CG on CSR (CG_solve.hpp:54-114), one cooperative launch; returns 0 or an MPG_ERR_*
 int run_cg64(cudaStream_t s, int device, int64_t n, const int32_t *rowptr, const int32_t *col, const double *val,
              const double *b, double *x, double tol, int max_iter, CgWork &w, DevStats *st);
-// mixed: FP32 CG inside FP64 iterative refinement, one cooperative launch
-int run_cg_mixed(cudaStream_t s, int device, int64_t n, const int32_t *rowptr, const int32_t *col, const double *val,
-                 const float *val32, const double *b, double *x, double tol, double inner_tol, int max_iter,
-                 CgWork &w, DevStats *st);
+// plain FP64 CG on the DIA form (same arithmetic, same summation order as CSR)
+int run_cg64_dia(cudaStream_t s, const DiaMatrix &A, const double *b, double *x, double tol, int max_iter, CgWork &w,
+                 DevStats *st);
+// mixed: FP32 CG inside FP64 iterative refinement on the DIA form, one cooperative launch
+int run_cg_mixed(cudaStream_t s, const DiaMatrix &A, const double *b, double *x, double tol, double inner_tol,
+                 int max_iter, CgWork &w, DevStats *st);
 // reference BiCGStab (CG_solve.hpp:115-206), host-driven; returns iterations in *iters
 int run_bicgstab(cudaStream_t s, int64_t n, const int32_t *rowptr, const int32_t *col, const double *val,
                  const double *b, double *x, double tol, int max_iter, double *work, double *red_dev,

@@ -145,12 +145,125 @@ __global__ void __launch_bounds__(kCgThreads) k_cg64(Cg64Args a) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// DIA kernels.  ND is the compile-time upper bound of the diagonal count
+// (15 for the Kuhn split, 27 in general); nd is the actual count.
+struct Cg64DiaArgs {
+  DiaMatrix A;
+  const double *__restrict__ b;
+  double *x;
+  double *r;
+  double *p0;
+  double *p1;
+  double *q;
+  double *partials;
+  double tol2;
+  int max_iter;
+  DevStats *st;
+};
+
+template <int ND>
+__global__ void __launch_bounds__(kCgThreads) k_cg64_dia(Cg64DiaArgs a) {
+  __shared__ double red[32];
+  __shared__ double bcast;
+  const int nb = gridDim.x, bid = blockIdx.x;
+  const int64_t n = a.A.n;
+  const int nd = a.A.ndiag;
+  const int64_t lo = n * bid / nb, hi = n * (bid + 1) / nb;
+  double *P0 = a.partials, *P1 = a.partials + nb, *P2 = a.partials + 2 * nb;
+  const double *__restrict__ val = a.A.val64;
+  const uint8_t *__restrict__ bnd = a.A.bnd;
+  // r = b - A x (CG_solve.hpp:62-63)
+  double rr = 0.0, bb = 0.0;
+  for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+    double s = 0.0;
+    if (bnd[i]) {
+      s += 1.0 * a.x[i];
+    } else {
+#pragma unroll
+      for (int d = 0; d < ND; ++d) {
+        if (d >= nd) break;
+        s += val[d * n + i] * a.x[i + a.A.off[d]];
+      }
+    }
+    const double ri = -1.0 * s + 1.0 * a.b[i];
+    a.r[i] = ri;
+    rr += ri * ri;
+    bb += a.b[i] * a.b[i];
+  }
+  double t = block_sum(rr, red);
+  if (threadIdx.x == 0) P0[bid] = t;
+  t = block_sum(bb, red);
+  if (threadIdx.x == 0) P1[bid] = t;
+  if (!grid_barrier(a.st, nb)) return;
+  const double rho0 = grid_total(P1, nb, &bcast);
+  double rho = grid_total(P0, nb, &bcast), rho_old = 0.0;
+  int iter = 0, status = 0;
+  if (rho0 == 0.0 || rho == 0.0) {
+    if (rho0 == 0.0)
+      for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) a.x[i] = 0.0;
+  } else {
+    for (;; ++iter) {
+      if (iter >= a.max_iter) {
+        status = 1;
+        break;
+      }
+      const double beta = iter == 0 ? 0.0 : rho / rho_old;
+      double *pk = (iter & 1) ? a.p1 : a.p0;
+      const double *pp = (iter & 1) ? a.p0 : a.p1;
+      const bool first = iter == 0;
+      double pq = 0.0;
+      for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+        const double pki = first ? a.r[i] : beta * pp[i] + 1.0 * a.r[i];
+        double s = 0.0;
+        if (bnd[i]) {
+          s += 1.0 * pki;
+        } else {
+#pragma unroll
+          for (int d = 0; d < ND; ++d) {
+            if (d >= nd) break;
+            const int64_t j = i + a.A.off[d];
+            const double pj = first ? a.r[j] : beta * pp[j] + 1.0 * a.r[j];
+            s += val[d * n + i] * pj;
+          }
+        }
+        pk[i] = pki;
+        a.q[i] = s;
+        pq += pki * s;
+      }
+      t = block_sum(pq, red);
+      if (threadIdx.x == 0) P2[bid] = t;
+      if (!grid_barrier(a.st, nb)) return;
+      const double alpha = rho / grid_total(P2, nb, &bcast);
+      rr = 0.0;
+      for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+        a.x[i] = 1.0 * a.x[i] + alpha * pk[i];
+        const double ri = 1.0 * a.r[i] + -alpha * a.q[i];
+        a.r[i] = ri;
+        rr += ri * ri;
+      }
+      t = block_sum(rr, red);
+      if (threadIdx.x == 0) P0[bid] = t;
+      if (!grid_barrier(a.st, nb)) return;
+      rho_old = rho;
+      rho = grid_total(P0, nb, &bcast);
+      if (rho / rho0 < a.tol2) {
+        ++iter;
+        break;
+      }
+    }
+  }
+  if (bid == 0 && threadIdx.x == 0) {
+    a.st->solver_iters = iter;
+    a.st->solver_status = status;
+    a.st->iters_total += iter;
+    if (status) a.st->solver_fail = 1;
+    a.st->solver_resid = rho0 > 0.0 ? sqrt(rho / rho0) : 0.0;
+  }
+}
+
 struct CgMixedArgs {
-  int64_t n;
-  const int32_t *__restrict__ rowptr;
-  const int32_t *__restrict__ col;
-  const double *__restrict__ val;
-  const float *__restrict__ val32;
+  DiaMatrix A;
   const double *__restrict__ b;
   double *x;
   double *r64;
@@ -166,11 +279,17 @@ struct CgMixedArgs {
   DevStats *st;
 };
 
+template <int ND>
 __global__ void __launch_bounds__(kCgThreads) k_cg_mixed(CgMixedArgs a) {
   __shared__ double red[32];
   __shared__ double bcast;
   const int nb = gridDim.x, bid = blockIdx.x;
-  const int64_t lo = a.n * bid / nb, hi = a.n * (bid + 1) / nb;
+  const int64_t n = a.A.n;
+  const int nd = a.A.ndiag;
+  const int64_t lo = n * bid / nb, hi = n * (bid + 1) / nb;
+  const uint8_t *__restrict__ bnd = a.A.bnd;
+  const double *__restrict__ v64 = a.A.val64;
+  const float *__restrict__ v32 = a.A.val32;
   // partial slots: a slot written in phase k is read after barrier k and may
   // only be rewritten in phase k+2 or later
   double *P0 = a.partials, *P1 = a.partials + nb, *P2 = a.partials + 2 * nb, *P3 = a.partials + 3 * nb;
@@ -185,7 +304,15 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_mixed(CgMixedArgs a) {
     double rr = 0.0;
     for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
       double s = 0.0;
-      for (int32_t k = a.rowptr[i]; k < a.rowptr[i + 1]; ++k) s += a.val[k] * a.x[a.col[k]];
+      if (bnd[i]) {
+        s = a.x[i];
+      } else {
+#pragma unroll
+        for (int d = 0; d < ND; ++d) {
+          if (d >= nd) break;
+          s += v64[d * n + i] * a.x[i + a.A.off[d]];
+        }
+      }
       const double ri = a.b[i] - s;
       a.r64[i] = ri;
       rr += ri * ri;
@@ -223,19 +350,21 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_mixed(CgMixedArgs a) {
       const float beta = k == 0 ? 0.f : (float)(rho / rho_old);
       float *pk = (k & 1) ? a.pb : a.pa;
       const float *pp = (k & 1) ? a.pa : a.pb;
+      const bool first = k == 0;
       double pq = 0.0;
       for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+        const float pki = first ? a.r[i] : __fmaf_rn(beta, pp[i], a.r[i]);
         float s = 0.f;
-        float pki;
-        if (k == 0) {
-          for (int32_t kk = a.rowptr[i]; kk < a.rowptr[i + 1]; ++kk) s = __fmaf_rn(a.val32[kk], a.r[a.col[kk]], s);
-          pki = a.r[i];
+        if (bnd[i]) {
+          s = pki;
         } else {
-          for (int32_t kk = a.rowptr[i]; kk < a.rowptr[i + 1]; ++kk) {
-            const int32_t j = a.col[kk];
-            s = __fmaf_rn(a.val32[kk], __fmaf_rn(beta, pp[j], a.r[j]), s);
+#pragma unroll
+          for (int d = 0; d < ND; ++d) {
+            if (d >= nd) break;
+            const int64_t j = i + a.A.off[d];
+            const float pj = first ? a.r[j] : __fmaf_rn(beta, pp[j], a.r[j]);
+            s = __fmaf_rn(v32[d * n + i], pj, s);
           }
-          pki = __fmaf_rn(beta, pp[i], a.r[i]);
         }
         pk[i] = pki;
         a.q[i] = s;
@@ -309,19 +438,25 @@ __global__ void k_dot_final(const double *__restrict__ part, int nb, double *out
 }  // namespace
 
 int cg_max_blocks(int device) {
-  int sms = 0, occ = 0;
+  int sms = 0, occ = 1 << 30, o = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cg64, kCgThreads, 0);
-  int occ2 = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, k_cg_mixed, kCgThreads, 0);
-  if (occ2 < occ) occ = occ2;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_cg64, kCgThreads, 0);
+  occ = o < occ ? o : occ;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_cg64_dia<15>, kCgThreads, 0);
+  occ = o < occ ? o : occ;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_cg64_dia<27>, kCgThreads, 0);
+  occ = o < occ ? o : occ;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_cg_mixed<15>, kCgThreads, 0);
+  occ = o < occ ? o : occ;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_cg_mixed<27>, kCgThreads, 0);
+  occ = o < occ ? o : occ;
   if (occ < 1) occ = 1;
   return sms * occ;
 }
 
+// one row per thread until every co-resident block is busy
 static int grid_for_rows(int64_t n, int max_blocks) {
-  // at least ~4 rows per thread before adding blocks; never more than co-resident
-  int64_t want = (n + (int64_t)kCgThreads * 4 - 1) / ((int64_t)kCgThreads * 4);
+  int64_t want = (n + kCgThreads - 1) / kCgThreads;
   if (want < 1) want = 1;
   if (want > max_blocks) want = max_blocks;
   return (int)want;
@@ -351,15 +486,31 @@ int run_cg64(cudaStream_t s, int device, int64_t n, const int32_t *rowptr, const
   return e == cudaSuccess ? MPG_OK : MPG_ERR_CUDA;
 }
 
-int run_cg_mixed(cudaStream_t s, int device, int64_t n, const int32_t *rowptr, const int32_t *col, const double *val,
-                 const float *val32, const double *b, double *x, double tol, double inner_tol, int max_iter,
-                 CgWork &w, DevStats *st) {
+int run_cg64_dia(cudaStream_t s, const DiaMatrix &A, const double *b, double *x, double tol, int max_iter, CgWork &w,
+                 DevStats *st) {
+  Cg64DiaArgs a;
+  a.A = A;
+  a.b = b;
+  a.x = x;
+  a.r = w.r;
+  a.p0 = w.p0;
+  a.p1 = w.p1;
+  a.q = w.q;
+  a.partials = w.partials;
+  a.tol2 = tol * tol;
+  a.max_iter = max_iter;
+  a.st = st;
+  const int nb = grid_for_rows(A.n, w.max_blocks);
+  void *args[] = {&a};
+  void *fn = A.ndiag <= 15 ? (void *)k_cg64_dia<15> : (void *)k_cg64_dia<27>;
+  cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(nb), dim3(kCgThreads), args, 0, s);
+  return e == cudaSuccess ? MPG_OK : MPG_ERR_CUDA;
+}
+
+int run_cg_mixed(cudaStream_t s, const DiaMatrix &A, const double *b, double *x, double tol, double inner_tol,
+                 int max_iter, CgWork &w, DevStats *st) {
   CgMixedArgs a;
-  a.n = n;
-  a.rowptr = rowptr;
-  a.col = col;
-  a.val = val;
-  a.val32 = val32;
+  a.A = A;
   a.b = b;
   a.x = x;
   a.r64 = w.r;
@@ -373,10 +524,10 @@ int run_cg_mixed(cudaStream_t s, int device, int64_t n, const int32_t *rowptr, c
   a.inner_tol2 = inner_tol * inner_tol;
   a.max_iter = max_iter;
   a.st = st;
-  (void)device;
-  const int nb = grid_for_rows(n, w.max_blocks);
+  const int nb = grid_for_rows(A.n, w.max_blocks);
   void *args[] = {&a};
-  cudaError_t e = cudaLaunchCooperativeKernel((void *)k_cg_mixed, dim3(nb), dim3(kCgThreads), args, 0, s);
+  void *fn = A.ndiag <= 15 ? (void *)k_cg_mixed<15> : (void *)k_cg_mixed<27>;
+  cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(nb), dim3(kCgThreads), args, 0, s);
   return e == cudaSuccess ? MPG_OK : MPG_ERR_CUDA;
 }
 
