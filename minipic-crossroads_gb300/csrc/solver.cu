@@ -46,16 +46,17 @@ struct Cg64Args {
   DevStats *st;
 };
 
-// sum of partials[0..nb) in block order, computed by warp 0; broadcast via smem
+// sum of partials[0..nb): every thread loads at most one partial (one L2
+// round trip), then a fixed block reduction; all blocks compute the same
+// value bit for bit.  nb <= blockDim.x * 4 is required (checked at launch).
 __device__ __forceinline__ double grid_total(const double *partials, int nb, double *sh) {
-  if (threadIdx.x < 32) {
-    double s = 0.0;
-    for (int i = threadIdx.x; i < nb; i += 32) s += partials[i];
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if (threadIdx.x == 0) *sh = s;
-  }
+  double s = 0.0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) s += partials[i];
+  __shared__ double red2[32];
+  s = block_sum(s, red2);
+  if (threadIdx.x == 0) *sh = s;
   __syncthreads();
-  double v = *sh;
+  const double v = *sh;
   __syncthreads();
   return v;
 }
