@@ -261,13 +261,15 @@ void upload_species_derived(mpg_ctx *c) {
   }
 }
 
-// fixed-point quantum: the largest |w q| over species maps to 2^30 quanta
+// fixed-point quantum: the largest |w q| over species maps to 2^25 quanta
+// (finer than the 24-bit barycentrics it multiplies; a warp's run of 32
+// particles then sums to < 2^30 and is aggregated in int32)
 void ensure_qfix(mpg_ctx *c) {
   if (c->qfix_valid) return;
   double mx = 0.0;
   for (int i = 0; i < MPG_MAX_SPECIES; ++i)
     if (c->weight_set[i]) mx = std::max(mx, fabs(c->sp.w[i] * c->sp.q[i]));
-  c->quantum = mx > 0 ? mx / 1073741824.0 : 1.0;
+  c->quantum = mx > 0 ? mx / 33554432.0 : 1.0;
   for (int i = 0; i < MPG_MAX_SPECIES; ++i)
     c->sp.qfix[i] = c->weight_set[i] ? llround(c->sp.w[i] * c->sp.q[i] / c->quantum) : 0;
   c->qfix_valid = true;
@@ -299,6 +301,8 @@ int ensure_cg_work(mpg_ctx *c, int64_t n) {
   dfree(c, c->cg.q32);
   dfree(c, c->cg.pa32);
   dfree(c, c->cg.pb32);
+  dfree(c, c->cg.r32b);
+  dfree(c, c->cg.q32b);
   dfree(c, c->cg.partials);
   c->cg.max_blocks = cg_max_blocks(c->device);
   TRY(dalloc(c, &c->cg.r, n));
@@ -310,7 +314,10 @@ int ensure_cg_work(mpg_ctx *c, int64_t n) {
   TRY(dalloc(c, &c->cg.q32, n));
   TRY(dalloc(c, &c->cg.pa32, n));
   TRY(dalloc(c, &c->cg.pb32, n));
-  TRY(dalloc(c, &c->cg.partials, 4 * (int64_t)c->cg.max_blocks));
+  TRY(dalloc(c, &c->cg.r32b, n));
+  TRY(dalloc(c, &c->cg.q32b, n));
+  if (c->cg.max_blocks < 1) return fail(c, MPG_ERR_CUDA, "solver kernels cannot be resident (occupancy 0)");
+  TRY(dalloc(c, &c->cg.partials, 8 * (int64_t)c->cg.max_blocks));
   c->cg_n = n;
   return MPG_OK;
 }

@@ -116,6 +116,45 @@ __device__ __forceinline__ void jinv_apply(const double *__restrict__ I, const d
   }
 }
 
+// Block totals without __syncthreads at the end: each warp reduces its lanes,
+// lane 0 adds into shared memory, and the last warp to finish pushes the
+// block's totals to the device counters.  Warps retire independently.
+struct BlockTotals {
+  double ke;
+  unsigned killed, cross, limit, done;
+};
+__device__ __forceinline__ void block_totals_init(BlockTotals *bt) {
+  if (threadIdx.x == 0) {
+    bt->ke = 0.0;
+    bt->killed = bt->cross = bt->limit = bt->done = 0u;
+  }
+  __syncthreads();
+}
+__device__ __forceinline__ void block_totals_push(BlockTotals *bt, double ke, unsigned killed, unsigned cross,
+                                                  unsigned limit, DevStats *st) {
+  const unsigned FULL = 0xffffffffu;
+  for (int o = 16; o > 0; o >>= 1) ke += __shfl_down_sync(FULL, ke, o);
+  killed = __reduce_add_sync(FULL, killed);
+  cross = __reduce_add_sync(FULL, cross);
+  limit = __reduce_add_sync(FULL, limit);
+  if ((threadIdx.x & 31) == 0) {
+    if (ke != 0.0) atomicAdd(&bt->ke, ke);
+    if (killed) atomicAdd(&bt->killed, killed);
+    if (cross) atomicAdd(&bt->cross, cross);
+    if (limit) atomicAdd(&bt->limit, limit);
+    __threadfence_block();
+    const unsigned nw = (blockDim.x + 31) >> 5;
+    if (atomicAdd(&bt->done, 1u) == nw - 1) {
+      __threadfence_block();
+      const volatile BlockTotals *v = bt;
+      if (v->ke != 0.0) atomicAdd(&st->ke, v->ke);
+      if (v->killed) atomicAdd(&st->n_killed, (unsigned long long)v->killed);
+      if (v->cross) atomicAdd(&st->n_cross, (unsigned long long)v->cross);
+      if (v->limit) atomicAdd(&st->n_limit, (unsigned long long)v->limit);
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kThreads) k_plain_deposit(PlainParts P, int64_t n, const int4 *__restrict__ tets,
                                                             const double *__restrict__ detj, SpeciesTable S, int mode,
                                                             double *__restrict__ rhs) {
@@ -246,11 +285,11 @@ __device__ __forceinline__ double plain_intersect(const DevMesh &M, int &e, doub
 __global__ void __launch_bounds__(kThreads) k_plain_move(PlainParts P, int64_t n, DevMesh M,
                                                          const double *__restrict__ Etet, SpeciesTable S, double dt,
                                                          int kill, int max_cross, DevStats *st) {
-  __shared__ double sd[32];
-  __shared__ unsigned long long su[32];
+  __shared__ BlockTotals bt;
+  block_totals_init(&bt);
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   double ke = 0.0;
-  unsigned long long killed = 0, cross = 0, limit = 0;
+  unsigned killed = 0, cross = 0, limit = 0;
   if (p < n) {
     int e = P.cell[p];
     if (e >= 0) {
@@ -292,7 +331,7 @@ __global__ void __launch_bounds__(kThreads) k_plain_move(PlainParts P, int64_t n
         ++it;
         if (dead) break;
       }
-      cross = it > 0 ? (unsigned long long)(it - 1) : 0ull;
+      cross = it > 0 ? (unsigned)(it - 1) : 0u;
       if (dead) {
         killed = 1;
         e = -1;
@@ -315,14 +354,7 @@ __global__ void __launch_bounds__(kThreads) k_plain_move(PlainParts P, int64_t n
       P.v[2 * cap + p] = v[2];
     }
   }
-  double bke = block_sum(ke, sd);
-  if (threadIdx.x == 0 && bke != 0.0) atomicAdd(&st->ke, bke);
-  unsigned long long bk = block_sum_u64(killed, su);
-  if (threadIdx.x == 0 && bk) atomicAdd(&st->n_killed, bk);
-  unsigned long long bc = block_sum_u64(cross, su);
-  if (threadIdx.x == 0 && bc) atomicAdd(&st->n_cross, bc);
-  unsigned long long bl = block_sum_u64(limit, su);
-  if (threadIdx.x == 0 && bl) atomicAdd(&st->n_limit, bl);
+  block_totals_push(&bt, ke, killed, cross, limit, st);
 }
 
 // stable compaction: count live particles per 4096-particle tile
@@ -383,28 +415,44 @@ __global__ void __launch_bounds__(kScanThreads) k_compact_plain(PlainParts P, in
 // key < 0 contribute nothing.
 __device__ __forceinline__ void deposit_fixed_warp(unsigned long long *__restrict__ acc,
                                                    const int4 *__restrict__ tets, int key, float b1, float b2,
-                                                   float b3, long long Q) {
+                                                   float b3, int Q) {
+  // |Q| <= 2^25 quanta, so a run of up to 32 lanes sums to < 2^30 in int32
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
-  long long c0 = 0, c1 = 0, c2 = 0, c3 = 0;
+  int c0 = 0, c1 = 0, c2 = 0, c3 = 0;
   if (key >= 0) {
     const float Qf = (float)Q;
-    c1 = __float2ll_rn(b1 * Qf);
-    c2 = __float2ll_rn(b2 * Qf);
-    c3 = __float2ll_rn(b3 * Qf);
+    c1 = __float2int_rn(b1 * Qf);
+    c2 = __float2int_rn(b2 * Qf);
+    c3 = __float2int_rn(b3 * Qf);
     c0 = Q - c1 - c2 - c3;
   }
   const int prev = __shfl_up_sync(FULL, key, 1);
   const bool head = lane == 0 || prev != key;
   const unsigned heads = __ballot_sync(FULL, head);
+  if (heads == 1u) {
+    // the whole warp holds one cell (typical after a sort): plain reductions
+    c0 = __reduce_add_sync(FULL, c0);
+    c1 = __reduce_add_sync(FULL, c1);
+    c2 = __reduce_add_sync(FULL, c2);
+    c3 = __reduce_add_sync(FULL, c3);
+    if (lane == 0 && key >= 0) {
+      const int4 nd = tets[key];
+      atomicAdd(acc + nd.x, (unsigned long long)(long long)c0);
+      atomicAdd(acc + nd.y, (unsigned long long)(long long)c1);
+      atomicAdd(acc + nd.z, (unsigned long long)(long long)c2);
+      atomicAdd(acc + nd.w, (unsigned long long)(long long)c3);
+    }
+    return;
+  }
   const int seg = 31 - __clz(heads & (FULL >> (31 - lane)));
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
     const int su = __shfl_up_sync(FULL, seg, o);
-    const long long u0 = __shfl_up_sync(FULL, c0, o);
-    const long long u1 = __shfl_up_sync(FULL, c1, o);
-    const long long u2 = __shfl_up_sync(FULL, c2, o);
-    const long long u3 = __shfl_up_sync(FULL, c3, o);
+    const int u0 = __shfl_up_sync(FULL, c0, o);
+    const int u1 = __shfl_up_sync(FULL, c1, o);
+    const int u2 = __shfl_up_sync(FULL, c2, o);
+    const int u3 = __shfl_up_sync(FULL, c3, o);
     if (lane >= o && su == seg) {
       c0 += u0;
       c1 += u1;
@@ -416,10 +464,10 @@ __device__ __forceinline__ void deposit_fixed_warp(unsigned long long *__restric
   const bool tail = lane == 31 || sn != seg;
   if (tail && key >= 0) {
     const int4 nd = tets[key];
-    atomicAdd(acc + nd.x, (unsigned long long)c0);
-    atomicAdd(acc + nd.y, (unsigned long long)c1);
-    atomicAdd(acc + nd.z, (unsigned long long)c2);
-    atomicAdd(acc + nd.w, (unsigned long long)c3);
+    atomicAdd(acc + nd.x, (unsigned long long)(long long)c0);
+    atomicAdd(acc + nd.y, (unsigned long long)(long long)c1);
+    atomicAdd(acc + nd.z, (unsigned long long)(long long)c2);
+    atomicAdd(acc + nd.w, (unsigned long long)(long long)c3);
   }
 }
 
@@ -428,7 +476,7 @@ __global__ void __launch_bounds__(kThreads) k_mixed_deposit(MixedParts P, int64_
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int key = -1;
   float b1 = 0.f, b2 = 0.f, b3 = 0.f;
-  long long Q = 0;
+  int Q = 0;
   if (p < n) {
     const uint32_t cs = P.c[p];
     if (cs != MPG_DEAD) {
@@ -437,7 +485,7 @@ __global__ void __launch_bounds__(kThreads) k_mixed_deposit(MixedParts P, int64_
       b1 = b.x;
       b2 = b.y;
       b3 = b.z;
-      Q = S.qfix[cs >> 24];
+      Q = (int)S.qfix[cs >> 24];
     }
   }
   // each lane converts its own charge Q, so runs may mix species
@@ -480,14 +528,14 @@ __global__ void __launch_bounds__(kThreads) k_mixed_move(MixedParts P, int64_t n
                                                          const int4 *__restrict__ tets, SpeciesTable S, float dt,
                                                          int kill, int max_cross, unsigned long long *__restrict__ acc,
                                                          DevStats *st) {
-  __shared__ double sd[32];
-  __shared__ unsigned long long su[32];
+  __shared__ BlockTotals bt;
+  block_totals_init(&bt);
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   float ke = 0.f;
-  unsigned long long killed = 0, cross = 0, limit = 0;
+  unsigned killed = 0, cross = 0, limit = 0;
   int dep_key = -1;
   float d1 = 0.f, d2 = 0.f, d3 = 0.f;
-  long long dq = 0;
+  int dq = 0;
   if (p < n) {
     uint32_t cs = P.c[p];
     if (cs != MPG_DEAD) {
@@ -519,16 +567,20 @@ __global__ void __launch_bounds__(kThreads) k_mixed_move(MixedParts P, int64_t n
         const float l0 = 1.0f - l1 - l2 - l3;
         const float lam[4] = {l0, l1, l2, l3};
         const float uu[4] = {u0, u1, u2, u3};
-        float tmin = tleft;
+        // earliest exit: face k is reached at t_k = lam_k / (-u_k) for u_k < 0.
+        // Compare t_k < t_best as lam_k * w_best < lam_best * w_k (w = -u > 0),
+        // so a division is needed only for the face actually crossed.
         int kmin = -1;
+        float lbest = 0.f, wbest = 0.f;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           if (uu[k] < 0.f && k != entry) {
-            float tk = __fdiv_rn(-lam[k], uu[k]);
-            tk = fmaxf(tk, 0.f);
-            if (tk < tmin) {
-              tmin = tk;
+            const float lk = fmaxf(lam[k], 0.f), wk = -uu[k];
+            // inside the remaining time?  lam_k < tleft * w_k
+            if (lk < tleft * wk && (kmin < 0 || lk * wbest < lbest * wk)) {
               kmin = k;
+              lbest = lk;
+              wbest = wk;
             }
           }
         }
@@ -543,6 +595,7 @@ __global__ void __launch_bounds__(kThreads) k_mixed_move(MixedParts P, int64_t n
           break;
         }
         ++it;
+        const float tmin = __fdiv_rn(lbest, wbest);
         float nl[4] = {__fmaf_rn(tmin, u0, l0), __fmaf_rn(tmin, u1, l1), __fmaf_rn(tmin, u2, l2),
                        __fmaf_rn(tmin, u3, l3)};
         nl[kmin] = 0.f;
@@ -599,7 +652,7 @@ __global__ void __launch_bounds__(kThreads) k_mixed_move(MixedParts P, int64_t n
         r1 = rec[3 * e + 1];
         r2 = rec[3 * e + 2];
       }
-      cross = (unsigned long long)it;
+      cross = (unsigned)it;
       if (dead) {
         killed = 1;
         P.c[p] = MPG_DEAD;
@@ -612,20 +665,13 @@ __global__ void __launch_bounds__(kThreads) k_mixed_move(MixedParts P, int64_t n
         d1 = l1;
         d2 = l2;
         d3 = l3;
-        dq = S.qfix[s];
+        dq = (int)S.qfix[s];
       }
     }
   }
   // deposit of the new position for the next step's field solve
   deposit_fixed_warp(acc, tets, dep_key, d1, d2, d3, dq);
-  double bke = block_sum((double)ke, sd);
-  if (threadIdx.x == 0 && bke != 0.0) atomicAdd(&st->ke, bke);
-  unsigned long long bk = block_sum_u64(killed, su);
-  if (threadIdx.x == 0 && bk) atomicAdd(&st->n_killed, bk);
-  unsigned long long bc = block_sum_u64(cross, su);
-  if (threadIdx.x == 0 && bc) atomicAdd(&st->n_cross, bc);
-  unsigned long long bl = block_sum_u64(limit, su);
-  if (threadIdx.x == 0 && bl) atomicAdd(&st->n_limit, bl);
+  block_totals_push(&bt, (double)ke, killed, cross, limit, st);
 }
 
 __global__ void k_cell_hist(const uint32_t *__restrict__ c, int64_t n, uint32_t *__restrict__ cnt) {

@@ -43,39 +43,41 @@ struct DevStats {
 
 // -------------------------------------------------------------------------
 // grid-wide barrier for cooperative launches.  Every block of the grid is
-// co-resident (cudaLaunchCooperativeKernel guarantees it).  The wait is
-// bounded: after ~2^24 polls (about a second with the back-off) the block
-// raises bar_error and returns false; every later barrier sees the flag and
-// returns false at once, so all blocks leave the kernel.
-__device__ __forceinline__ bool grid_barrier(DevStats *st, unsigned nblocks) {
+// co-resident (cudaLaunchCooperativeKernel guarantees it).  bar_count only
+// grows: the k-th barrier of a launch completes when it reaches k * nblocks
+// (the host zeroes it before each launch).  Arrival is one release-reduction,
+// the wait is an acquire load, so the block's writes before the barrier are
+// visible to every block after it.  The wait is bounded: after ~2^22 polls
+// (about a second with the back-off) the block raises bar_error and returns
+// false; every later barrier sees the flag and returns false at once, so all
+// blocks leave the kernel.  `epoch` is a per-block counter (thread 0 only).
+__device__ __forceinline__ bool grid_barrier(DevStats *st, unsigned nblocks, unsigned &epoch) {
   __shared__ int ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     ok = 1;
-    volatile unsigned int *vgen = &st->bar_gen;
-    volatile int *verr = &st->bar_error;
-    const unsigned int g = *vgen;
-    __threadfence();
-    if (atomicAdd(&st->bar_count, 1u) == nblocks - 1) {
-      atomicExch(&st->bar_count, 0u);
-      __threadfence();
-      atomicAdd(&st->bar_gen, 1u);
-    } else {
-      unsigned int spins = 0;
-      while (*vgen == g) {
-        if (*verr) {
+    ++epoch;
+    const unsigned target = epoch * nblocks;
+    unsigned *cnt = &st->bar_count;
+    asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(cnt) : "memory");
+    unsigned spins = 0, v;
+    for (;;) {
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(cnt) : "memory");
+      if ((int)(v - target) >= 0) break;
+      ++spins;
+      if ((spins & 255u) == 0) {
+        if (*(volatile int *)&st->bar_error) {
           ok = 0;
           break;
         }
-        if (++spins > (1u << 24)) {
+        if (spins > (1u << 22)) {
           atomicExch(&st->bar_error, 1);
           ok = 0;
           break;
         }
-        __nanosleep(64);
       }
+      if (spins > 32) __nanosleep(20);
     }
-    __threadfence();
   }
   __syncthreads();
   return ok != 0;

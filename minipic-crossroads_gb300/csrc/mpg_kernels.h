@@ -101,7 +101,8 @@ struct DiaMatrix {
 struct CgWork {
   double *r = nullptr, *p0 = nullptr, *p1 = nullptr, *q = nullptr;  // FP64 vectors, n each
   float *r32 = nullptr, *z32 = nullptr, *q32 = nullptr, *pa32 = nullptr, *pb32 = nullptr;  // mixed inner vectors
-  double *partials = nullptr;  // 4 * max_blocks
+  float *r32b = nullptr, *q32b = nullptr;  // second copies of r and q (double buffering)
+  double *partials = nullptr;  // 8 * max_blocks
   int max_blocks = 0;
 };
 // plain FP64 CG on CSR (CG_solve.hpp:54-114), one cooperative launch; returns 0 or an MPG_ERR_*

@@ -27,8 +27,65 @@
 
 namespace {
 
-constexpr int kCgThreads = 512;
+constexpr int kCgThreads = 1024;
+constexpr int kSlots = 4;  // partial sums per phase
 
+// sum of partials[0..nb): every thread loads at most one partial (one L2
+// round trip), then a fixed block reduction; all blocks compute the same
+// value bit for bit.
+__device__ __forceinline__ double grid_total(const double *partials, int nb, double *sh) {
+  double s = 0.0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) s += partials[i];
+  __shared__ double red2[32];
+  s = block_sum(s, red2);
+  if (threadIdx.x == 0) *sh = s;
+  __syncthreads();
+  const double v = *sh;
+  __syncthreads();
+  return v;
+}
+
+// four block sums at once (one pair of __syncthreads); results valid in thread 0
+__device__ __forceinline__ void block_sum4(double v[4], double (*sm)[32]) {
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < 4; ++k) sm[k][wid] = v[k];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      double s = 0.0;
+      for (int i = 0; i < nw; ++i) s += sm[k][i];
+      v[k] = s;
+    }
+  }
+}
+
+// four grid totals at once: slots k = 0..3 of one partial set
+__device__ __forceinline__ void grid_total4(const double *set, int nb, double out[4], double (*sm)[32],
+                                            double *bc) {
+  double v[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int i = threadIdx.x; i < nb; i += blockDim.x)
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v[k] += set[(size_t)k * nb + i];
+  block_sum4(v, sm);
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int k = 0; k < 4; ++k) bc[k] = v[k];
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < 4; ++k) out[k] = bc[k];
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// plain FP64 CG on CSR (used by mpg_cg_csr for caller-owned matrices)
 struct Cg64Args {
   int64_t n;
   const int32_t *__restrict__ rowptr;
@@ -46,24 +103,10 @@ struct Cg64Args {
   DevStats *st;
 };
 
-// sum of partials[0..nb): every thread loads at most one partial (one L2
-// round trip), then a fixed block reduction; all blocks compute the same
-// value bit for bit.  nb <= blockDim.x * 4 is required (checked at launch).
-__device__ __forceinline__ double grid_total(const double *partials, int nb, double *sh) {
-  double s = 0.0;
-  for (int i = threadIdx.x; i < nb; i += blockDim.x) s += partials[i];
-  __shared__ double red2[32];
-  s = block_sum(s, red2);
-  if (threadIdx.x == 0) *sh = s;
-  __syncthreads();
-  const double v = *sh;
-  __syncthreads();
-  return v;
-}
-
-__global__ void __launch_bounds__(kCgThreads) k_cg64(Cg64Args a) {
+__global__ void __launch_bounds__(kCgThreads, 1) k_cg64(Cg64Args a) {
   __shared__ double red[32];
   __shared__ double bcast;
+  unsigned epoch = 0;
   const int nb = gridDim.x, bid = blockIdx.x;
   const int64_t lo = a.n * bid / nb, hi = a.n * (bid + 1) / nb;
   double *P0 = a.partials, *P1 = a.partials + nb, *P2 = a.partials + 2 * nb;
@@ -81,7 +124,7 @@ __global__ void __launch_bounds__(kCgThreads) k_cg64(Cg64Args a) {
   if (threadIdx.x == 0) P0[bid] = t;
   t = block_sum(bb, red);
   if (threadIdx.x == 0) P1[bid] = t;
-  if (!grid_barrier(a.st, nb)) return;
+  if (!grid_barrier(a.st, nb, epoch)) return;
   const double rho0 = grid_total(P1, nb, &bcast);
   double rho = grid_total(P0, nb, &bcast), rho_old = 0.0;
   int iter = 0, status = 0;
@@ -116,7 +159,7 @@ __global__ void __launch_bounds__(kCgThreads) k_cg64(Cg64Args a) {
       }
       t = block_sum(pq, red);
       if (threadIdx.x == 0) P2[bid] = t;
-      if (!grid_barrier(a.st, nb)) return;
+      if (!grid_barrier(a.st, nb, epoch)) return;
       const double alpha = rho / grid_total(P2, nb, &bcast);
       // x += alpha p (:92), r -= alpha q (:96), rho = r.r (:100)
       rr = 0.0;
@@ -128,7 +171,7 @@ __global__ void __launch_bounds__(kCgThreads) k_cg64(Cg64Args a) {
       }
       t = block_sum(rr, red);
       if (threadIdx.x == 0) P0[bid] = t;
-      if (!grid_barrier(a.st, nb)) return;
+      if (!grid_barrier(a.st, nb, epoch)) return;
       rho_old = rho;
       rho = grid_total(P0, nb, &bcast);
       if (rho / rho0 < a.tol2) {
@@ -147,8 +190,9 @@ __global__ void __launch_bounds__(kCgThreads) k_cg64(Cg64Args a) {
 }
 
 // ---------------------------------------------------------------------------
-// DIA kernels.  ND is the compile-time upper bound of the diagonal count
-// (15 for the Kuhn split, 27 in general); nd is the actual count.
+// plain FP64 CG on the DIA form: the CG_solve.hpp:54-114 recurrence, two grid
+// barriers per iteration.  ND is the compile-time bound of the diagonal count
+// (15 for the Kuhn split, 27 in general).
 struct Cg64DiaArgs {
   DiaMatrix A;
   const double *__restrict__ b;
@@ -164,9 +208,10 @@ struct Cg64DiaArgs {
 };
 
 template <int ND>
-__global__ void __launch_bounds__(kCgThreads) k_cg64_dia(Cg64DiaArgs a) {
+__global__ void __launch_bounds__(kCgThreads, 1) k_cg64_dia(Cg64DiaArgs a) {
   __shared__ double red[32];
   __shared__ double bcast;
+  unsigned epoch = 0;
   const int nb = gridDim.x, bid = blockIdx.x;
   const int64_t n = a.A.n;
   const int nd = a.A.ndiag;
@@ -174,7 +219,6 @@ __global__ void __launch_bounds__(kCgThreads) k_cg64_dia(Cg64DiaArgs a) {
   double *P0 = a.partials, *P1 = a.partials + nb, *P2 = a.partials + 2 * nb;
   const double *__restrict__ val = a.A.val64;
   const uint8_t *__restrict__ bnd = a.A.bnd;
-  // r = b - A x (CG_solve.hpp:62-63)
   double rr = 0.0, bb = 0.0;
   for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
     double s = 0.0;
@@ -196,7 +240,7 @@ __global__ void __launch_bounds__(kCgThreads) k_cg64_dia(Cg64DiaArgs a) {
   if (threadIdx.x == 0) P0[bid] = t;
   t = block_sum(bb, red);
   if (threadIdx.x == 0) P1[bid] = t;
-  if (!grid_barrier(a.st, nb)) return;
+  if (!grid_barrier(a.st, nb, epoch)) return;
   const double rho0 = grid_total(P1, nb, &bcast);
   double rho = grid_total(P0, nb, &bcast), rho_old = 0.0;
   int iter = 0, status = 0;
@@ -234,7 +278,7 @@ __global__ void __launch_bounds__(kCgThreads) k_cg64_dia(Cg64DiaArgs a) {
       }
       t = block_sum(pq, red);
       if (threadIdx.x == 0) P2[bid] = t;
-      if (!grid_barrier(a.st, nb)) return;
+      if (!grid_barrier(a.st, nb, epoch)) return;
       const double alpha = rho / grid_total(P2, nb, &bcast);
       rr = 0.0;
       for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
@@ -245,7 +289,7 @@ __global__ void __launch_bounds__(kCgThreads) k_cg64_dia(Cg64DiaArgs a) {
       }
       t = block_sum(rr, red);
       if (threadIdx.x == 0) P0[bid] = t;
-      if (!grid_barrier(a.st, nb)) return;
+      if (!grid_barrier(a.st, nb, epoch)) return;
       rho_old = rho;
       rho = grid_total(P0, nb, &bcast);
       if (rho / rho0 < a.tol2) {
@@ -263,17 +307,32 @@ __global__ void __launch_bounds__(kCgThreads) k_cg64_dia(Cg64DiaArgs a) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Mixed form: FP32 CG inside FP64 iterative refinement.
+//
+// Outer sweep: r64 = b - A64 x (FP64 matrix), stop when |r64| <= tol |b|;
+// inner: FP32 CG on A32 z = r64/|r64| from z = 0 to inner_tol; x += |r64| z.
+//
+// The inner loop is a single-reduction CG: one phase and one grid barrier
+// per iteration.  Phase k+1 forms, for its own rows and on the fly for every
+// neighbour it reads,
+//     r_{k+1} = r_k - alpha_k q_k,  p_{k+1} = beta_{k+1} p_k + r_{k+1},
+//     q_{k+1} = A p_{k+1},          z_{k+1} = z_k + alpha_k p_k,
+// and the four dot products (p,q), (r,q), (q,q), (r,r) of the new vectors.
+// After the barrier alpha_{k+1} = (r,r)/(p,q) uses the exact (r,r); beta for
+// the next phase uses rho_{k+2} = rho - 2 alpha (r,q) + alpha^2 (q,q).
+// r, p, q are double-buffered (neighbours read the old copies while the
+// owner writes the new ones); z is only touched by its owner.
 struct CgMixedArgs {
   DiaMatrix A;
   const double *__restrict__ b;
   double *x;
   double *r64;
-  float *r;
+  float *r[2];
+  float *p[2];
+  float *q[2];
   float *z;
-  float *q;
-  float *pa;
-  float *pb;
-  double *partials;
+  double *partials;  // [2 sets][kSlots][nb]
   double tol2;
   double inner_tol2;
   int max_iter;
@@ -281,9 +340,12 @@ struct CgMixedArgs {
 };
 
 template <int ND>
-__global__ void __launch_bounds__(kCgThreads) k_cg_mixed(CgMixedArgs a) {
+__global__ void __launch_bounds__(kCgThreads, 1) k_cg_mixed(CgMixedArgs a) {
   __shared__ double red[32];
+  __shared__ double red4[4][32];
+  __shared__ double bc4[4];
   __shared__ double bcast;
+  unsigned epoch = 0;
   const int nb = gridDim.x, bid = blockIdx.x;
   const int64_t n = a.A.n;
   const int nd = a.A.ndiag;
@@ -291,17 +353,18 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_mixed(CgMixedArgs a) {
   const uint8_t *__restrict__ bnd = a.A.bnd;
   const double *__restrict__ v64 = a.A.val64;
   const float *__restrict__ v32 = a.A.val32;
-  // partial slots: a slot written in phase k is read after barrier k and may
-  // only be rewritten in phase k+2 or later
-  double *P0 = a.partials, *P1 = a.partials + nb, *P2 = a.partials + 2 * nb, *P3 = a.partials + 3 * nb;
+  // partial sets alternate between phases: a set written in phase k is read
+  // after barrier k and rewritten in phase k+2 at the earliest
+  int phase = 0;
+  auto slot = [&](int set, int k) { return a.partials + ((size_t)(set * kSlots + k)) * nb; };
   double bb = 0.0;
   for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) bb += a.b[i] * a.b[i];
   double t = block_sum(bb, red);
-  if (threadIdx.x == 0) P1[bid] = t;
+  if (threadIdx.x == 0) slot(1, 3)[bid] = t;  // read after the first barrier
   int total_inner = 0, status = 0, sweeps = 0;
   double rho64 = 0.0, rho0 = 0.0;
   for (;; ++sweeps) {
-    // FP64 residual with the FP64 matrix
+    // ---- FP64 residual with the FP64 matrix
     double rr = 0.0;
     for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
       double s = 0.0;
@@ -318,11 +381,13 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_mixed(CgMixedArgs a) {
       a.r64[i] = ri;
       rr += ri * ri;
     }
+    int set = phase & 1;
     t = block_sum(rr, red);
-    if (threadIdx.x == 0) P0[bid] = t;
-    if (!grid_barrier(a.st, nb)) return;
-    if (sweeps == 0) rho0 = grid_total(P1, nb, &bcast);
-    rho64 = grid_total(P0, nb, &bcast);
+    if (threadIdx.x == 0) slot(set, 0)[bid] = t;
+    if (!grid_barrier(a.st, nb, epoch)) return;
+    if (sweeps == 0) rho0 = grid_total(slot(1, 3), nb, &bcast);
+    rho64 = grid_total(slot(set, 0), nb, &bcast);
+    ++phase;
     if (rho0 == 0.0) {
       for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) a.x[i] = 0.0;
       rho64 = 0.0;
@@ -333,67 +398,117 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_mixed(CgMixedArgs a) {
       status = 1;
       break;
     }
-    // inner FP32 CG on A z = r / |r|, from z = 0
+    // ---- inner start: r0 = r64/|r64|, p0 = r0, z = 0
     const double scale = 1.0 / sqrt(rho64);
+    float *r0 = a.r[0], *p0 = a.p[0];
     double rs = 0.0;
     for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
       const float ri = (float)(a.r64[i] * scale);
-      a.r[i] = ri;
+      r0[i] = ri;
+      p0[i] = ri;
       a.z[i] = 0.f;
       rs += (double)ri * (double)ri;
     }
+    set = phase & 1;
     t = block_sum(rs, red);
-    if (threadIdx.x == 0) P3[bid] = t;
-    if (!grid_barrier(a.st, nb)) return;
-    const double rin0 = grid_total(P3, nb, &bcast);
-    double rho = rin0, rho_old = 0.0;
-    for (int k = 0;; ++k) {
-      const float beta = k == 0 ? 0.f : (float)(rho / rho_old);
-      float *pk = (k & 1) ? a.pb : a.pa;
-      const float *pp = (k & 1) ? a.pa : a.pb;
-      const bool first = k == 0;
-      double pq = 0.0;
+    if (threadIdx.x == 0) slot(set, 3)[bid] = t;
+    if (!grid_barrier(a.st, nb, epoch)) return;
+    const double rin0 = grid_total(slot(set, 3), nb, &bcast);
+    ++phase;
+    // ---- q0 = A p0 and the dot products of the start vectors
+    {
+      float *q0 = a.q[0];
+      double pq = 0.0, rq = 0.0, qq = 0.0;
       for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-        const float pki = first ? a.r[i] : __fmaf_rn(beta, pp[i], a.r[i]);
-        float s = 0.f;
+        const float pi = p0[i];
+        float s;
         if (bnd[i]) {
-          s = pki;
+          s = pi;
         } else {
+          s = 0.f;
+#pragma unroll
+          for (int d = 0; d < ND; ++d) {
+            if (d >= nd) break;
+            s = __fmaf_rn(v32[d * n + i], p0[i + a.A.off[d]], s);
+          }
+        }
+        q0[i] = s;
+        pq += (double)pi * (double)s;
+        qq += (double)s * (double)s;
+      }
+      rq = pq;  // r0 = p0
+      set = phase & 1;
+      double t0 = block_sum(pq, red);
+      double t2 = block_sum(qq, red);
+      if (threadIdx.x == 0) {
+        slot(set, 0)[bid] = t0;
+        slot(set, 1)[bid] = t0;
+        slot(set, 2)[bid] = t2;
+      }
+      (void)rq;
+    }
+    if (!grid_barrier(a.st, nb, epoch)) return;
+    double pq = grid_total(slot(phase & 1, 0), nb, &bcast);
+    double rq = grid_total(slot(phase & 1, 1), nb, &bcast);
+    double qq = grid_total(slot(phase & 1, 2), nb, &bcast);
+    double rho = rin0;
+    ++phase;
+    int cur = 0;
+    for (;;) {
+      if (rho <= a.inner_tol2 * rin0 || total_inner >= a.max_iter || !(pq > 0.0)) break;
+      const double alpha = rho / pq;
+      double rho_next = rho - 2.0 * alpha * rq + alpha * alpha * qq;
+      if (rho_next < 0.0) rho_next = 0.0;
+      const float af = (float)alpha, bf = (float)(rho_next / rho);
+      const float *rk = a.r[cur], *pk = a.p[cur], *qk = a.q[cur];
+      float *rn = a.r[cur ^ 1], *pn = a.p[cur ^ 1], *qn = a.q[cur ^ 1];
+      double dpq = 0.0, drq = 0.0, dqq = 0.0, drr = 0.0;
+      for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+        const float ri = __fmaf_rn(-af, qk[i], rk[i]);
+        const float pi = __fmaf_rn(bf, pk[i], ri);
+        a.z[i] = __fmaf_rn(af, pk[i], a.z[i]);
+        float s;
+        if (bnd[i]) {
+          s = pi;
+        } else {
+          s = 0.f;
 #pragma unroll
           for (int d = 0; d < ND; ++d) {
             if (d >= nd) break;
             const int64_t j = i + a.A.off[d];
-            const float pj = first ? a.r[j] : __fmaf_rn(beta, pp[j], a.r[j]);
-            s = __fmaf_rn(v32[d * n + i], pj, s);
+            const float rj = __fmaf_rn(-af, qk[j], rk[j]);
+            s = __fmaf_rn(v32[d * n + i], __fmaf_rn(bf, pk[j], rj), s);
           }
         }
-        pk[i] = pki;
-        a.q[i] = s;
-        pq += (double)pki * (double)s;
+        rn[i] = ri;
+        pn[i] = pi;
+        qn[i] = s;
+        dpq += (double)pi * (double)s;
+        drq += (double)ri * (double)s;
+        dqq += (double)s * (double)s;
+        drr += (double)ri * (double)ri;
       }
-      t = block_sum(pq, red);
-      if (threadIdx.x == 0) P2[bid] = t;
-      if (!grid_barrier(a.st, nb)) return;
-      const float alpha = (float)(rho / grid_total(P2, nb, &bcast));
-      double rr2 = 0.0;
-      for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-        a.z[i] = __fmaf_rn(alpha, pk[i], a.z[i]);
-        const float ri = __fmaf_rn(-alpha, a.q[i], a.r[i]);
-        a.r[i] = ri;
-        rr2 += (double)ri * (double)ri;
-      }
-      t = block_sum(rr2, red);
-      if (threadIdx.x == 0) P0[bid] = t;
-      if (!grid_barrier(a.st, nb)) return;
-      rho_old = rho;
-      rho = grid_total(P0, nb, &bcast);
+      set = phase & 1;
+      double v4[4] = {dpq, drq, dqq, drr};
+      block_sum4(v4, red4);
+      if (threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) slot(set, k)[bid] = v4[k];
+      if (!grid_barrier(a.st, nb, epoch)) return;
+      double tot[4];
+      grid_total4(slot(set, 0), nb, tot, red4, bc4);
+      pq = tot[0];
+      rq = tot[1];
+      qq = tot[2];
+      rho = tot[3];
+      ++phase;
+      cur ^= 1;
       ++total_inner;
-      if (rho <= a.inner_tol2 * rin0 || total_inner >= a.max_iter) break;
     }
-    // x += z * |r|  (FP64)
+    // ---- x += |r64| z  (FP64)
     const double back = sqrt(rho64);
     for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) a.x[i] += (double)a.z[i] * back;
-    if (!grid_barrier(a.st, nb)) return;
+    if (!grid_barrier(a.st, nb, epoch)) return;
   }
   if (bid == 0 && threadIdx.x == 0) {
     a.st->solver_iters = total_inner;
@@ -451,7 +566,7 @@ int cg_max_blocks(int device) {
   occ = o < occ ? o : occ;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_cg_mixed<27>, kCgThreads, 0);
   occ = o < occ ? o : occ;
-  if (occ < 1) occ = 1;
+  if (occ < 1) occ = 0;
   return sms * occ;
 }
 
@@ -461,6 +576,15 @@ static int grid_for_rows(int64_t n, int max_blocks) {
   if (want < 1) want = 1;
   if (want > max_blocks) want = max_blocks;
   return (int)want;
+}
+
+static int coop_launch(cudaStream_t s, void *fn, int nb, void *arg, DevStats *st) {
+  if (nb < 1) return MPG_ERR_CUDA;
+  // the barrier counter starts at zero for every launch
+  if (cudaMemsetAsync(&st->bar_count, 0, sizeof(unsigned), s) != cudaSuccess) return MPG_ERR_CUDA;
+  void *args[] = {arg};
+  cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(nb), dim3(kCgThreads), args, 0, s);
+  return e == cudaSuccess ? MPG_OK : MPG_ERR_CUDA;
 }
 
 int run_cg64(cudaStream_t s, int device, int64_t n, const int32_t *rowptr, const int32_t *col, const double *val,
@@ -481,10 +605,7 @@ int run_cg64(cudaStream_t s, int device, int64_t n, const int32_t *rowptr, const
   a.max_iter = max_iter;
   a.st = st;
   (void)device;
-  const int nb = grid_for_rows(n, w.max_blocks);
-  void *args[] = {&a};
-  cudaError_t e = cudaLaunchCooperativeKernel((void *)k_cg64, dim3(nb), dim3(kCgThreads), args, 0, s);
-  return e == cudaSuccess ? MPG_OK : MPG_ERR_CUDA;
+  return coop_launch(s, (void *)k_cg64, grid_for_rows(n, w.max_blocks), &a, st);
 }
 
 int run_cg64_dia(cudaStream_t s, const DiaMatrix &A, const double *b, double *x, double tol, int max_iter, CgWork &w,
@@ -501,11 +622,8 @@ int run_cg64_dia(cudaStream_t s, const DiaMatrix &A, const double *b, double *x,
   a.tol2 = tol * tol;
   a.max_iter = max_iter;
   a.st = st;
-  const int nb = grid_for_rows(A.n, w.max_blocks);
-  void *args[] = {&a};
   void *fn = A.ndiag <= 15 ? (void *)k_cg64_dia<15> : (void *)k_cg64_dia<27>;
-  cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(nb), dim3(kCgThreads), args, 0, s);
-  return e == cudaSuccess ? MPG_OK : MPG_ERR_CUDA;
+  return coop_launch(s, fn, grid_for_rows(A.n, w.max_blocks), &a, st);
 }
 
 int run_cg_mixed(cudaStream_t s, const DiaMatrix &A, const double *b, double *x, double tol, double inner_tol,
@@ -515,21 +633,20 @@ int run_cg_mixed(cudaStream_t s, const DiaMatrix &A, const double *b, double *x,
   a.b = b;
   a.x = x;
   a.r64 = w.r;
-  a.r = w.r32;
+  a.r[0] = w.r32;
+  a.r[1] = w.r32b;
+  a.p[0] = w.pa32;
+  a.p[1] = w.pb32;
+  a.q[0] = w.q32;
+  a.q[1] = w.q32b;
   a.z = w.z32;
-  a.q = w.q32;
-  a.pa = w.pa32;
-  a.pb = w.pb32;
   a.partials = w.partials;
   a.tol2 = tol * tol;
   a.inner_tol2 = inner_tol * inner_tol;
   a.max_iter = max_iter;
   a.st = st;
-  const int nb = grid_for_rows(A.n, w.max_blocks);
-  void *args[] = {&a};
   void *fn = A.ndiag <= 15 ? (void *)k_cg_mixed<15> : (void *)k_cg_mixed<27>;
-  cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(nb), dim3(kCgThreads), args, 0, s);
-  return e == cudaSuccess ? MPG_OK : MPG_ERR_CUDA;
+  return coop_launch(s, fn, grid_for_rows(A.n, w.max_blocks), &a, st);
 }
 
 // CG_solve.hpp:115-206, one host round trip per dot product
