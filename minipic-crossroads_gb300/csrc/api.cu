@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
@@ -304,7 +305,10 @@ int ensure_cg_work(mpg_ctx *c, int64_t n) {
   dfree(c, c->cg.r32b);
   dfree(c, c->cg.q32b);
   dfree(c, c->cg.partials);
-  c->cg.max_blocks = cg_max_blocks(c->device);
+  // solver launch shape: tunable through MPG_CG_THREADS / MPG_CG_BARRIER
+  if (const char *e = getenv("MPG_CG_THREADS")) c->cg.threads = atoi(e);
+  if (const char *e = getenv("MPG_CG_BARRIER")) c->cg.bar_mode = atoi(e);
+  c->cg.max_blocks = cg_max_blocks(c->device, c->cg.threads == 256 || c->cg.threads == 1024 ? c->cg.threads : 512);
   TRY(dalloc(c, &c->cg.r, n));
   TRY(dalloc(c, &c->cg.p0, n));
   TRY(dalloc(c, &c->cg.p1, n));

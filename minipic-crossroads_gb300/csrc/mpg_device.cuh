@@ -38,7 +38,7 @@ struct DevStats {
   unsigned int bar_count;
   unsigned int bar_gen;
   int bar_error;
-  int pad;
+  int bar_mode;  // 0: fence + volatile polling, 1: release/acquire
 };
 
 // -------------------------------------------------------------------------
@@ -59,10 +59,20 @@ __device__ __forceinline__ bool grid_barrier(DevStats *st, unsigned nblocks, uns
     ++epoch;
     const unsigned target = epoch * nblocks;
     unsigned *cnt = &st->bar_count;
-    asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(cnt) : "memory");
+    const int mode = st->bar_mode;
+    if (mode == 0) {
+      // fence + relaxed arrival, volatile polling, fence
+      __threadfence();
+      atomicAdd(cnt, 1u);
+    } else {
+      asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(cnt) : "memory");
+    }
     unsigned spins = 0, v;
     for (;;) {
-      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(cnt) : "memory");
+      if (mode == 0)
+        v = *(volatile unsigned *)cnt;
+      else
+        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(cnt) : "memory");
       if ((int)(v - target) >= 0) break;
       ++spins;
       if ((spins & 255u) == 0) {
@@ -76,8 +86,9 @@ __device__ __forceinline__ bool grid_barrier(DevStats *st, unsigned nblocks, uns
           break;
         }
       }
-      if (spins > 32) __nanosleep(20);
+      if (spins > 64) __nanosleep(32);
     }
+    if (mode == 0) __threadfence();
   }
   __syncthreads();
   return ok != 0;

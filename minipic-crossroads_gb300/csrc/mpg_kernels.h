@@ -104,6 +104,8 @@ struct CgWork {
   float *r32b = nullptr, *q32b = nullptr;  // second copies of r and q (double buffering)
   double *partials = nullptr;  // 8 * max_blocks
   int max_blocks = 0;
+  int threads = 512;  // block size of the cooperative solver kernels (256, 512 or 1024)
+  int bar_mode = 0;   // grid barrier flavour (0: fence + volatile polling, 1: release/acquire)
 };
 // plain FP64 CG on CSR (CG_solve.hpp:54-114), one cooperative launch; returns 0 or an MPG_ERR_*
 int run_cg64(cudaStream_t s, int device, int64_t n, const int32_t *rowptr, const int32_t *col, const double *val,
@@ -118,4 +120,4 @@ int run_cg_mixed(cudaStream_t s, const DiaMatrix &A, const double *b, double *x,
 int run_bicgstab(cudaStream_t s, int64_t n, const int32_t *rowptr, const int32_t *col, const double *val,
                  const double *b, double *x, double tol, int max_iter, double *work, double *red_dev,
                  double *red_host, int *iters, double *resid);
-int cg_max_blocks(int device);
+int cg_max_blocks(int device, int threads);

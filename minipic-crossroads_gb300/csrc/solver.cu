@@ -27,7 +27,6 @@
 
 namespace {
 
-constexpr int kCgThreads = 1024;
 constexpr int kSlots = 4;  // partial sums per phase
 
 // sum of partials[0..nb): every thread loads at most one partial (one L2
@@ -103,7 +102,8 @@ struct Cg64Args {
   DevStats *st;
 };
 
-__global__ void __launch_bounds__(kCgThreads, 1) k_cg64(Cg64Args a) {
+template <int TH>
+__global__ void __launch_bounds__(TH, 1024 / TH) k_cg64(Cg64Args a) {
   __shared__ double red[32];
   __shared__ double bcast;
   unsigned epoch = 0;
@@ -207,8 +207,8 @@ struct Cg64DiaArgs {
   DevStats *st;
 };
 
-template <int ND>
-__global__ void __launch_bounds__(kCgThreads, 1) k_cg64_dia(Cg64DiaArgs a) {
+template <int ND, int TH>
+__global__ void __launch_bounds__(TH, 1024 / TH) k_cg64_dia(Cg64DiaArgs a) {
   __shared__ double red[32];
   __shared__ double bcast;
   unsigned epoch = 0;
@@ -339,8 +339,8 @@ struct CgMixedArgs {
   DevStats *st;
 };
 
-template <int ND>
-__global__ void __launch_bounds__(kCgThreads, 1) k_cg_mixed(CgMixedArgs a) {
+template <int ND, int TH>
+__global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
   __shared__ double red[32];
   __shared__ double red4[4][32];
   __shared__ double bc4[4];
@@ -553,37 +553,50 @@ __global__ void k_dot_final(const double *__restrict__ part, int nb, double *out
 
 }  // namespace
 
-int cg_max_blocks(int device) {
+// kernel instances: [kind][threads index]; kind 0 = CSR FP64, 1/2 = DIA FP64
+// (15 / 27 diagonals), 3/4 = mixed (15 / 27 diagonals); threads 256, 512, 1024
+static void *kernel_of(int kind, int th) {
+  static void *tab[5][3] = {
+      {(void *)k_cg64<256>, (void *)k_cg64<512>, (void *)k_cg64<1024>},
+      {(void *)k_cg64_dia<15, 256>, (void *)k_cg64_dia<15, 512>, (void *)k_cg64_dia<15, 1024>},
+      {(void *)k_cg64_dia<27, 256>, (void *)k_cg64_dia<27, 512>, (void *)k_cg64_dia<27, 1024>},
+      {(void *)k_cg_mixed<15, 256>, (void *)k_cg_mixed<15, 512>, (void *)k_cg_mixed<15, 1024>},
+      {(void *)k_cg_mixed<27, 256>, (void *)k_cg_mixed<27, 512>, (void *)k_cg_mixed<27, 1024>}};
+  const int ti = th <= 256 ? 0 : th <= 512 ? 1 : 2;
+  return tab[kind][ti];
+}
+
+static int threads_of(const CgWork &w) { return w.threads == 256 || w.threads == 1024 ? w.threads : 512; }
+
+int cg_max_blocks(int device, int threads) {
   int sms = 0, occ = 1 << 30, o = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_cg64, kCgThreads, 0);
-  occ = o < occ ? o : occ;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_cg64_dia<15>, kCgThreads, 0);
-  occ = o < occ ? o : occ;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_cg64_dia<27>, kCgThreads, 0);
-  occ = o < occ ? o : occ;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_cg_mixed<15>, kCgThreads, 0);
-  occ = o < occ ? o : occ;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_cg_mixed<27>, kCgThreads, 0);
-  occ = o < occ ? o : occ;
+  for (int kind = 0; kind < 5; ++kind) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kernel_of(kind, threads), threads, 0);
+    occ = o < occ ? o : occ;
+  }
   if (occ < 1) occ = 0;
   return sms * occ;
 }
 
 // one row per thread until every co-resident block is busy
-static int grid_for_rows(int64_t n, int max_blocks) {
-  int64_t want = (n + kCgThreads - 1) / kCgThreads;
+static int grid_for_rows(int64_t n, int max_blocks, int threads) {
+  int64_t want = (n + threads - 1) / threads;
   if (want < 1) want = 1;
   if (want > max_blocks) want = max_blocks;
   return (int)want;
 }
 
-static int coop_launch(cudaStream_t s, void *fn, int nb, void *arg, DevStats *st) {
+static int coop_launch(cudaStream_t s, void *fn, int nb, int threads, void *arg, DevStats *st, int bar_mode) {
   if (nb < 1) return MPG_ERR_CUDA;
+  static const int modes[2] = {0, 1};
   // the barrier counter starts at zero for every launch
   if (cudaMemsetAsync(&st->bar_count, 0, sizeof(unsigned), s) != cudaSuccess) return MPG_ERR_CUDA;
+  if (cudaMemcpyAsync(&st->bar_mode, &modes[bar_mode ? 1 : 0], sizeof(int), cudaMemcpyHostToDevice, s) !=
+      cudaSuccess)
+    return MPG_ERR_CUDA;
   void *args[] = {arg};
-  cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(nb), dim3(kCgThreads), args, 0, s);
+  cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(nb), dim3(threads), args, 0, s);
   return e == cudaSuccess ? MPG_OK : MPG_ERR_CUDA;
 }
 
@@ -605,7 +618,8 @@ int run_cg64(cudaStream_t s, int device, int64_t n, const int32_t *rowptr, const
   a.max_iter = max_iter;
   a.st = st;
   (void)device;
-  return coop_launch(s, (void *)k_cg64, grid_for_rows(n, w.max_blocks), &a, st);
+  const int th = threads_of(w);
+  return coop_launch(s, kernel_of(0, th), grid_for_rows(n, w.max_blocks, th), th, &a, st, w.bar_mode);
 }
 
 int run_cg64_dia(cudaStream_t s, const DiaMatrix &A, const double *b, double *x, double tol, int max_iter, CgWork &w,
@@ -622,8 +636,9 @@ int run_cg64_dia(cudaStream_t s, const DiaMatrix &A, const double *b, double *x,
   a.tol2 = tol * tol;
   a.max_iter = max_iter;
   a.st = st;
-  void *fn = A.ndiag <= 15 ? (void *)k_cg64_dia<15> : (void *)k_cg64_dia<27>;
-  return coop_launch(s, fn, grid_for_rows(A.n, w.max_blocks), &a, st);
+  const int th = threads_of(w);
+  return coop_launch(s, kernel_of(A.ndiag <= 15 ? 1 : 2, th), grid_for_rows(A.n, w.max_blocks, th), th, &a, st,
+                     w.bar_mode);
 }
 
 int run_cg_mixed(cudaStream_t s, const DiaMatrix &A, const double *b, double *x, double tol, double inner_tol,
@@ -645,8 +660,9 @@ int run_cg_mixed(cudaStream_t s, const DiaMatrix &A, const double *b, double *x,
   a.inner_tol2 = inner_tol * inner_tol;
   a.max_iter = max_iter;
   a.st = st;
-  void *fn = A.ndiag <= 15 ? (void *)k_cg_mixed<15> : (void *)k_cg_mixed<27>;
-  return coop_launch(s, fn, grid_for_rows(A.n, w.max_blocks), &a, st);
+  const int th = threads_of(w);
+  return coop_launch(s, kernel_of(A.ndiag <= 15 ? 3 : 4, th), grid_for_rows(A.n, w.max_blocks, th), th, &a, st,
+                     w.bar_mode);
 }
 
 // CG_solve.hpp:115-206, one host round trip per dot product
