@@ -25,6 +25,20 @@
 #include "minipic_gb300.h"
 #include "mpg_kernels.h"
 
+#ifdef MPG_CG_PROFILE
+// optional phase timing of the mixed inner loop (compile with -DMPG_CG_PROFILE):
+// [0] compute, [1] barrier wait, [2] grid totals, [3] iterations; block 0 only
+__device__ unsigned long long g_cg_prof[8];
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+extern "C" int mpg_probe_cg_profile(unsigned long long *out) {
+  return cudaMemcpyFromSymbol(out, g_cg_prof, sizeof(g_cg_prof)) == cudaSuccess ? 0 : -2;
+}
+#endif
+
 namespace {
 
 constexpr int kSlots = 4;  // partial sums per phase
@@ -460,6 +474,9 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
       double rho_next = rho - 2.0 * alpha * rq + alpha * alpha * qq;
       if (rho_next < 0.0) rho_next = 0.0;
       const float af = (float)alpha, bf = (float)(rho_next / rho);
+#ifdef MPG_CG_PROFILE
+      const unsigned long long tA = gtimer();
+#endif
       const float *rk = a.r[cur], *pk = a.p[cur], *qk = a.q[cur];
       float *rn = a.r[cur ^ 1], *pn = a.p[cur ^ 1], *qn = a.q[cur ^ 1];
       double dpq = 0.0, drq = 0.0, dqq = 0.0, drr = 0.0;
@@ -494,9 +511,24 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
       if (threadIdx.x == 0)
 #pragma unroll
         for (int k = 0; k < 4; ++k) slot(set, k)[bid] = v4[k];
+#ifdef MPG_CG_PROFILE
+      const unsigned long long tB = gtimer();
+#endif
       if (!grid_barrier(a.st, nb, epoch)) return;
+#ifdef MPG_CG_PROFILE
+      const unsigned long long tC = gtimer();
+#endif
       double tot[4];
       grid_total4(slot(set, 0), nb, tot, red4, bc4);
+#ifdef MPG_CG_PROFILE
+      if (bid == 0 && threadIdx.x == 0) {
+        const unsigned long long tD = gtimer();
+        g_cg_prof[0] += tB - tA;
+        g_cg_prof[1] += tC - tB;
+        g_cg_prof[2] += tD - tC;
+        g_cg_prof[3] += 1;
+      }
+#endif
       pq = tot[0];
       rq = tot[1];
       qq = tot[2];
