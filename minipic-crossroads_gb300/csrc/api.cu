@@ -799,7 +799,8 @@ int mpg_configure(mpg_ctx *c, const mpg_config *cfg) {
       std::sort(offs.begin(), offs.end());
       offs.erase(std::unique(offs.begin(), offs.end()), offs.end());
       if (offs.size() > 27) return fail(c, MPG_ERR_MESH, "matrix is not a structured stencil (%zu offsets)", offs.size());
-      const int nd = (int)offs.size();
+      // pad to the kernel's diagonal count (15 or 27) with zero diagonals at offset 0
+      const int nd = offs.size() <= 15 ? 15 : 27;
       std::vector<double> d64((size_t)nd * N, 0.0);
       for (int64_t r = 0; r < N; ++r) {
         if (c->hm.bnd[r]) continue;
@@ -811,7 +812,7 @@ int mpg_configure(mpg_ctx *c, const mpg_config *cfg) {
       std::vector<float> d32(d64.begin(), d64.end());
       c->dia.n = N;
       c->dia.ndiag = nd;
-      for (int d = 0; d < nd; ++d) c->dia.off[d] = (int)offs[d];
+      for (int d = 0; d < nd; ++d) c->dia.off[d] = d < (int)offs.size() ? (int)offs[d] : 0;
       TRY(dalloc(c, &c->dia.val64, (int64_t)nd * N));
       TRY(dalloc(c, &c->dia.val32, (int64_t)nd * N));
       CK(cudaMemcpyAsync(c->dia.val64, d64.data(), sizeof(double) * d64.size(), cudaMemcpyHostToDevice, c->stream));

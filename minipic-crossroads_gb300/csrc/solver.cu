@@ -205,8 +205,10 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg64(Cg64Args a) {
 
 // ---------------------------------------------------------------------------
 // plain FP64 CG on the DIA form: the CG_solve.hpp:54-114 recurrence, two grid
-// barriers per iteration.  ND is the compile-time bound of the diagonal count
-// (15 for the Kuhn split, 27 in general).
+// barriers per iteration.  ND is the exact diagonal count (15 for the Kuhn
+// split, 27 in general; the host pads with zero diagonals of offset 0), so
+// the diagonal loop unrolls without branches and all gathers of a row can be
+// in flight at once.
 struct Cg64DiaArgs {
   DiaMatrix A;
   const double *__restrict__ b;
@@ -228,7 +230,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg64_dia(Cg64DiaArgs a) {
   unsigned epoch = 0;
   const int nb = gridDim.x, bid = blockIdx.x;
   const int64_t n = a.A.n;
-  const int nd = a.A.ndiag;
+  (void)a.A.ndiag;
   const int64_t lo = n * bid / nb, hi = n * (bid + 1) / nb;
   double *P0 = a.partials, *P1 = a.partials + nb, *P2 = a.partials + 2 * nb;
   const double *__restrict__ val = a.A.val64;
@@ -241,7 +243,6 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg64_dia(Cg64DiaArgs a) {
     } else {
 #pragma unroll
       for (int d = 0; d < ND; ++d) {
-        if (d >= nd) break;
         s += val[d * n + i] * a.x[i + a.A.off[d]];
       }
     }
@@ -280,8 +281,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg64_dia(Cg64DiaArgs a) {
         } else {
 #pragma unroll
           for (int d = 0; d < ND; ++d) {
-            if (d >= nd) break;
-            const int64_t j = i + a.A.off[d];
+                const int64_t j = i + a.A.off[d];
             const double pj = first ? a.r[j] : beta * pp[j] + 1.0 * a.r[j];
             s += val[d * n + i] * pj;
           }
@@ -362,7 +362,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
   unsigned epoch = 0;
   const int nb = gridDim.x, bid = blockIdx.x;
   const int64_t n = a.A.n;
-  const int nd = a.A.ndiag;
+  (void)a.A.ndiag;
   const int64_t lo = n * bid / nb, hi = n * (bid + 1) / nb;
   const uint8_t *__restrict__ bnd = a.A.bnd;
   const double *__restrict__ v64 = a.A.val64;
@@ -387,8 +387,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
       } else {
 #pragma unroll
         for (int d = 0; d < ND; ++d) {
-          if (d >= nd) break;
-          s += v64[d * n + i] * a.x[i + a.A.off[d]];
+            s += v64[d * n + i] * a.x[i + a.A.off[d]];
         }
       }
       const double ri = a.b[i] - s;
@@ -442,8 +441,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
           s = 0.f;
 #pragma unroll
           for (int d = 0; d < ND; ++d) {
-            if (d >= nd) break;
-            s = __fmaf_rn(v32[d * n + i], p0[i + a.A.off[d]], s);
+                s = __fmaf_rn(v32[d * n + i], p0[i + a.A.off[d]], s);
           }
         }
         q0[i] = s;
@@ -491,8 +489,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
           s = 0.f;
 #pragma unroll
           for (int d = 0; d < ND; ++d) {
-            if (d >= nd) break;
-            const int64_t j = i + a.A.off[d];
+                const int64_t j = i + a.A.off[d];
             const float rj = __fmaf_rn(-af, qk[j], rk[j]);
             s = __fmaf_rn(v32[d * n + i], __fmaf_rn(bf, pk[j], rj), s);
           }
