@@ -26,14 +26,11 @@
 #include "mpg_kernels.h"
 
 #ifdef MPG_CG_PROFILE
-// optional phase timing of the mixed inner loop (compile with -DMPG_CG_PROFILE):
-// [0] compute, [1] barrier wait, [2] grid totals, [3] iterations; block 0 only
+// optional phase timing of the mixed inner loop (compile with -DMPG_CG_PROFILE),
+// in SM cycles of block 0: [0] compute, [1] barrier wait, [2] grid totals,
+// [3] iterations, [4] row loop only, [5] block reduction + partial store
 __device__ unsigned long long g_cg_prof[8];
-__device__ __forceinline__ unsigned long long gtimer() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
+__device__ __forceinline__ unsigned long long gtimer() { return (unsigned long long)clock64(); }
 extern "C" int mpg_probe_cg_profile(unsigned long long *out) {
   return cudaMemcpyFromSymbol(out, g_cg_prof, sizeof(g_cg_prof)) == cudaSuccess ? 0 : -2;
 }
@@ -502,6 +499,9 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
         dqq += (double)s * (double)s;
         drr += (double)ri * (double)ri;
       }
+#ifdef MPG_CG_PROFILE
+      const unsigned long long tL = gtimer();
+#endif
       set = phase & 1;
       double v4[4] = {dpq, drq, dqq, drr};
       block_sum4(v4, red4);
@@ -524,6 +524,8 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
         g_cg_prof[1] += tC - tB;
         g_cg_prof[2] += tD - tC;
         g_cg_prof[3] += 1;
+        g_cg_prof[4] += tL - tA;
+        g_cg_prof[5] += tB - tL;
       }
 #endif
       pq = tot[0];
