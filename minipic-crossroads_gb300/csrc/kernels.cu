@@ -116,42 +116,50 @@ __device__ __forceinline__ void jinv_apply(const double *__restrict__ I, const d
   }
 }
 
-// Block totals without __syncthreads at the end: each warp reduces its lanes,
-// lane 0 adds into shared memory, and the last warp to finish pushes the
-// block's totals to the device counters.  Warps retire independently.
+// Block totals without __syncthreads at the end: each warp reduces its lanes
+// (kinetic energy in float-float, counters with integer reductions), lane 0
+// stores the warp's share, and the last warp to finish sums the shares and
+// pushes one set of device atomics per block.  Warps retire independently and
+// no FP64 arithmetic runs per warp.
 struct BlockTotals {
-  double ke;
+  ff ke[32];
   unsigned killed, cross, limit, done;
 };
 __device__ __forceinline__ void block_totals_init(BlockTotals *bt) {
-  if (threadIdx.x == 0) {
-    bt->ke = 0.0;
-    bt->killed = bt->cross = bt->limit = bt->done = 0u;
-  }
+  if (threadIdx.x < 32) bt->ke[threadIdx.x] = ff{0.f, 0.f};
+  if (threadIdx.x == 0) bt->killed = bt->cross = bt->limit = bt->done = 0u;
   __syncthreads();
 }
-__device__ __forceinline__ void block_totals_push(BlockTotals *bt, double ke, unsigned killed, unsigned cross,
+__device__ __forceinline__ void block_totals_push(BlockTotals *bt, ff ke, unsigned killed, unsigned cross,
                                                   unsigned limit, DevStats *st) {
   const unsigned FULL = 0xffffffffu;
-  for (int o = 16; o > 0; o >>= 1) ke += __shfl_down_sync(FULL, ke, o);
+  for (int o = 16; o > 0; o >>= 1) ke = ff_add(ke, ff_shfl_down(ke, o));
   killed = __reduce_add_sync(FULL, killed);
   cross = __reduce_add_sync(FULL, cross);
   limit = __reduce_add_sync(FULL, limit);
-  if ((threadIdx.x & 31) == 0) {
-    if (ke != 0.0) atomicAdd(&bt->ke, ke);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const unsigned nw = (blockDim.x + 31) >> 5;
+  unsigned last = 0;
+  if (lane == 0) {
+    bt->ke[wid] = ke;
     if (killed) atomicAdd(&bt->killed, killed);
     if (cross) atomicAdd(&bt->cross, cross);
     if (limit) atomicAdd(&bt->limit, limit);
     __threadfence_block();
-    const unsigned nw = (blockDim.x + 31) >> 5;
-    if (atomicAdd(&bt->done, 1u) == nw - 1) {
-      __threadfence_block();
-      const volatile BlockTotals *v = bt;
-      if (v->ke != 0.0) atomicAdd(&st->ke, v->ke);
-      if (v->killed) atomicAdd(&st->n_killed, (unsigned long long)v->killed);
-      if (v->cross) atomicAdd(&st->n_cross, (unsigned long long)v->cross);
-      if (v->limit) atomicAdd(&st->n_limit, (unsigned long long)v->limit);
-    }
+    last = atomicAdd(&bt->done, 1u) == nw - 1;
+  }
+  last = __shfl_sync(FULL, last, 0);
+  if (!last) return;
+  __threadfence_block();
+  const volatile BlockTotals *v = bt;
+  ff s = lane < (int)nw ? ff{v->ke[lane].hi, v->ke[lane].lo} : ff{0.f, 0.f};
+  for (int o = 16; o > 0; o >>= 1) s = ff_add(s, ff_shfl_down(s, o));
+  if (lane == 0) {
+    const double e = (double)s.hi + (double)s.lo;
+    if (e != 0.0) atomicAdd(&st->ke, e);
+    if (v->killed) atomicAdd(&st->n_killed, (unsigned long long)v->killed);
+    if (v->cross) atomicAdd(&st->n_cross, (unsigned long long)v->cross);
+    if (v->limit) atomicAdd(&st->n_limit, (unsigned long long)v->limit);
   }
 }
 
@@ -354,7 +362,9 @@ __global__ void __launch_bounds__(kThreads) k_plain_move(PlainParts P, int64_t n
       P.v[2 * cap + p] = v[2];
     }
   }
-  block_totals_push(&bt, ke, killed, cross, limit, st);
+  // kinetic energy of this particle as float-float (exact split of the double)
+  const float ke_hi = (float)ke;
+  block_totals_push(&bt, ff{ke_hi, (float)(ke - (double)ke_hi)}, killed, cross, limit, st);
 }
 
 // stable compaction: count live particles per 4096-particle tile
@@ -671,7 +681,7 @@ __global__ void __launch_bounds__(kThreads) k_mixed_move(MixedParts P, int64_t n
   }
   // deposit of the new position for the next step's field solve
   deposit_fixed_warp(acc, tets, dep_key, d1, d2, d3, dq);
-  block_totals_push(&bt, (double)ke, killed, cross, limit, st);
+  block_totals_push(&bt, ff{ke, 0.f}, killed, cross, limit, st);
 }
 
 __global__ void k_cell_hist(const uint32_t *__restrict__ c, int64_t n, uint32_t *__restrict__ cnt) {

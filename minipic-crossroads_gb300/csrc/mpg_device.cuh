@@ -95,7 +95,9 @@ __device__ __forceinline__ bool grid_barrier(DevStats *st, unsigned nblocks, uns
 }
 
 // block-wide sum of one double per thread (blockDim.x multiple of 32, <= 1024);
-// deterministic for a fixed block size.  Result valid in thread 0.
+// deterministic for a fixed block size.  Result valid in thread 0.  The last
+// stage runs in warp 0 as a shuffle tree (FP64 is a slow pipe on this chip, so
+// no thread sums serially).
 __device__ __forceinline__ double block_sum(double v, double *smem32) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -103,11 +105,71 @@ __device__ __forceinline__ double block_sum(double v, double *smem32) {
   if (lane == 0) smem32[wid] = v;
   __syncthreads();
   double s = 0.0;
-  if (threadIdx.x == 0) {
+  if (wid == 0) {
     const int nw = blockDim.x >> 5;
-    for (int i = 0; i < nw; ++i) s += smem32[i];
+    s = lane < nw ? smem32[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
   }
   return s;
+}
+
+// ---------------------------------------------------------------------------
+// float-float ("double-single") arithmetic: a value is hi + lo with |lo| <=
+// ulp(hi)/2, about 44 significant bits, built from FP32 operations only
+// (Knuth's TwoSum and the FMA-based exact product).  Used for the dot products
+// of the mixed solver, where FP64 would run on the slow FP64 pipe.  The
+// translation unit is built with --fmad=false, so no operation below is
+// contracted behind our back.
+struct ff {
+  float hi, lo;
+};
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+  const float s = a.hi + b.hi;
+  const float bb = s - a.hi;
+  float e = (a.hi - (s - bb)) + (b.hi - bb);
+  e += a.lo + b.lo;
+  const float hi = s + e;
+  return {hi, e - (hi - s)};
+}
+__device__ __forceinline__ ff ff_prod(float a, float b) {
+  const float p = a * b;
+  return {p, __fmaf_rn(a, b, -p)};
+}
+__device__ __forceinline__ ff ff_mulf(ff a, float b) {
+  const float p = a.hi * b;
+  const float e = __fmaf_rn(a.hi, b, -p) + a.lo * b;
+  const float hi = p + e;
+  return {hi, e - (hi - p)};
+}
+__device__ __forceinline__ ff ff_shfl_down(ff a, int o) {
+  return {__shfl_down_sync(0xffffffffu, a.hi, o), __shfl_down_sync(0xffffffffu, a.lo, o)};
+}
+// block-wide float-float sums of K values per thread; results valid in all
+// threads (broadcast through shared memory).  sm must hold K*32 ff.
+template <int K>
+__device__ __forceinline__ void block_sum_ff(ff v[K], ff *sm) {
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] = ff_add(v[k], ff_shfl_down(v[k], o));
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < K; ++k) sm[k * 32 + wid] = v[k];
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      ff s = lane < nw ? sm[k * 32 + lane] : ff{0.f, 0.f};
+      for (int o = 16; o > 0; o >>= 1) s = ff_add(s, ff_shfl_down(s, o));
+      if (lane == 0) sm[k * 32] = s;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < K; ++k) v[k] = sm[k * 32];
+  __syncthreads();
 }
 
 __device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long v, unsigned long long *smem32) {

@@ -55,45 +55,6 @@ __device__ __forceinline__ double grid_total(const double *partials, int nb, dou
   return v;
 }
 
-// four block sums at once (one pair of __syncthreads); results valid in thread 0
-__device__ __forceinline__ void block_sum4(double v[4], double (*sm)[32]) {
-  for (int o = 16; o > 0; o >>= 1)
-#pragma unroll
-    for (int k = 0; k < 4; ++k) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  __syncthreads();
-  if (lane == 0)
-#pragma unroll
-    for (int k = 0; k < 4; ++k) sm[k][wid] = v[k];
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    const int nw = blockDim.x >> 5;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      double s = 0.0;
-      for (int i = 0; i < nw; ++i) s += sm[k][i];
-      v[k] = s;
-    }
-  }
-}
-
-// four grid totals at once: slots k = 0..3 of one partial set
-__device__ __forceinline__ void grid_total4(const double *set, int nb, double out[4], double (*sm)[32],
-                                            double *bc) {
-  double v[4] = {0.0, 0.0, 0.0, 0.0};
-  for (int i = threadIdx.x; i < nb; i += blockDim.x)
-#pragma unroll
-    for (int k = 0; k < 4; ++k) v[k] += set[(size_t)k * nb + i];
-  block_sum4(v, sm);
-  if (threadIdx.x == 0)
-#pragma unroll
-    for (int k = 0; k < 4; ++k) bc[k] = v[k];
-  __syncthreads();
-#pragma unroll
-  for (int k = 0; k < 4; ++k) out[k] = bc[k];
-  __syncthreads();
-}
-
 // ---------------------------------------------------------------------------
 // plain FP64 CG on CSR (used by mpg_cg_csr for caller-owned matrices)
 struct Cg64Args {
@@ -353,25 +314,39 @@ struct CgMixedArgs {
 template <int ND, int TH>
 __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
   __shared__ double red[32];
-  __shared__ double red4[4][32];
-  __shared__ double bc4[4];
+  __shared__ ff smf[4 * 32];
   __shared__ double bcast;
   unsigned epoch = 0;
   const int nb = gridDim.x, bid = blockIdx.x;
   const int64_t n = a.A.n;
-  (void)a.A.ndiag;
   const int64_t lo = n * bid / nb, hi = n * (bid + 1) / nb;
   const uint8_t *__restrict__ bnd = a.A.bnd;
   const double *__restrict__ v64 = a.A.val64;
   const float *__restrict__ v32 = a.A.val32;
-  // partial sets alternate between phases: a set written in phase k is read
-  // after barrier k and rewritten in phase k+2 at the earliest
+  // FP64 partials of the outer phases; float-float partials (stored as float2)
+  // of the inner phases.  Sets alternate: a set written in phase k is read
+  // after barrier k and rewritten in phase k+2 at the earliest.
   int phase = 0;
-  auto slot = [&](int set, int k) { return a.partials + ((size_t)(set * kSlots + k)) * nb; };
+  auto slot64 = [&](int set, int k) { return a.partials + ((size_t)(set * kSlots + k)) * nb; };
+  auto slotff = [&](int set, int k) { return reinterpret_cast<float2 *>(slot64(set, k)); };
+  auto put_ff = [&](int set, const ff *v, int K) {
+    if (threadIdx.x == 0)
+      for (int k = 0; k < K; ++k) slotff(set, k)[bid] = make_float2(v[k].hi, v[k].lo);
+  };
+  auto total_ff = [&](int set, ff *out, int K) {
+    ff v[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    for (int i = threadIdx.x; i < nb; i += blockDim.x)
+      for (int k = 0; k < K; ++k) {
+        const float2 t = slotff(set, k)[i];
+        v[k] = ff_add(v[k], ff{t.x, t.y});
+      }
+    block_sum_ff<4>(v, smf);
+    for (int k = 0; k < K; ++k) out[k] = v[k];
+  };
   double bb = 0.0;
   for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) bb += a.b[i] * a.b[i];
   double t = block_sum(bb, red);
-  if (threadIdx.x == 0) slot(1, 3)[bid] = t;  // read after the first barrier
+  if (threadIdx.x == 0) slot64(1, 3)[bid] = t;  // read after the first barrier
   int total_inner = 0, status = 0, sweeps = 0;
   double rho64 = 0.0, rho0 = 0.0;
   for (;; ++sweeps) {
@@ -383,9 +358,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
         s = a.x[i];
       } else {
 #pragma unroll
-        for (int d = 0; d < ND; ++d) {
-            s += v64[d * n + i] * a.x[i + a.A.off[d]];
-        }
+        for (int d = 0; d < ND; ++d) s += v64[d * n + i] * a.x[i + a.A.off[d]];
       }
       const double ri = a.b[i] - s;
       a.r64[i] = ri;
@@ -393,10 +366,10 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
     }
     int set = phase & 1;
     t = block_sum(rr, red);
-    if (threadIdx.x == 0) slot(set, 0)[bid] = t;
+    if (threadIdx.x == 0) slot64(set, 0)[bid] = t;
     if (!grid_barrier(a.st, nb, epoch)) return;
-    if (sweeps == 0) rho0 = grid_total(slot(1, 3), nb, &bcast);
-    rho64 = grid_total(slot(set, 0), nb, &bcast);
+    if (sweeps == 0) rho0 = grid_total(slot64(1, 3), nb, &bcast);
+    rho64 = grid_total(slot64(set, 0), nb, &bcast);
     ++phase;
     if (rho0 == 0.0) {
       for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) a.x[i] = 0.0;
@@ -408,27 +381,27 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
       status = 1;
       break;
     }
-    // ---- inner start: r0 = r64/|r64|, p0 = r0, z = 0
+    // ---- inner start: r0 = r64/|r64|, p0 = r0, z = 0, q0 = A p0
     const double scale = 1.0 / sqrt(rho64);
     float *r0 = a.r[0], *p0 = a.p[0];
-    double rs = 0.0;
+    ff rs = {0.f, 0.f};
     for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
       const float ri = (float)(a.r64[i] * scale);
       r0[i] = ri;
       p0[i] = ri;
       a.z[i] = 0.f;
-      rs += (double)ri * (double)ri;
+      rs = ff_add(rs, ff_prod(ri, ri));
     }
     set = phase & 1;
-    t = block_sum(rs, red);
-    if (threadIdx.x == 0) slot(set, 3)[bid] = t;
+    block_sum_ff<1>(&rs, smf);
+    put_ff(set, &rs, 1);
     if (!grid_barrier(a.st, nb, epoch)) return;
-    const double rin0 = grid_total(slot(set, 3), nb, &bcast);
+    ff rin0;
+    total_ff(set, &rin0, 1);
     ++phase;
-    // ---- q0 = A p0 and the dot products of the start vectors
     {
       float *q0 = a.q[0];
-      double pq = 0.0, rq = 0.0, qq = 0.0;
+      ff pq = {0.f, 0.f}, qq = {0.f, 0.f};
       for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
         const float pi = p0[i];
         float s;
@@ -437,44 +410,37 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
         } else {
           s = 0.f;
 #pragma unroll
-          for (int d = 0; d < ND; ++d) {
-                s = __fmaf_rn(v32[d * n + i], p0[i + a.A.off[d]], s);
-          }
+          for (int d = 0; d < ND; ++d) s = __fmaf_rn(v32[d * n + i], p0[i + a.A.off[d]], s);
         }
         q0[i] = s;
-        pq += (double)pi * (double)s;
-        qq += (double)s * (double)s;
+        pq = ff_add(pq, ff_prod(pi, s));
+        qq = ff_add(qq, ff_prod(s, s));
       }
-      rq = pq;  // r0 = p0
       set = phase & 1;
-      double t0 = block_sum(pq, red);
-      double t2 = block_sum(qq, red);
-      if (threadIdx.x == 0) {
-        slot(set, 0)[bid] = t0;
-        slot(set, 1)[bid] = t0;
-        slot(set, 2)[bid] = t2;
-      }
-      (void)rq;
+      ff v3[3] = {pq, pq, qq};  // (r0, q0) = (p0, q0)
+      block_sum_ff<3>(v3, smf);
+      put_ff(set, v3, 3);
     }
     if (!grid_barrier(a.st, nb, epoch)) return;
-    double pq = grid_total(slot(phase & 1, 0), nb, &bcast);
-    double rq = grid_total(slot(phase & 1, 1), nb, &bcast);
-    double qq = grid_total(slot(phase & 1, 2), nb, &bcast);
-    double rho = rin0;
+    ff tot[4];
+    total_ff(phase & 1, tot, 3);
+    ff pq = tot[0], rq = tot[1], qq = tot[2], rho = rin0;
     ++phase;
     int cur = 0;
+    const float stop = (float)a.inner_tol2 * rin0.hi;
     for (;;) {
-      if (rho <= a.inner_tol2 * rin0 || total_inner >= a.max_iter || !(pq > 0.0)) break;
-      const double alpha = rho / pq;
-      double rho_next = rho - 2.0 * alpha * rq + alpha * alpha * qq;
-      if (rho_next < 0.0) rho_next = 0.0;
-      const float af = (float)alpha, bf = (float)(rho_next / rho);
+      if (rho.hi <= stop || total_inner >= a.max_iter || !(pq.hi > 0.f)) break;
+      // scalars in float / float-float (identical in every thread)
+      const float af = rho.hi / pq.hi;
+      ff rn = ff_add(rho, ff_mulf(rq, -2.f * af));
+      rn = ff_add(rn, ff_mulf(ff_mulf(qq, af), af));
+      const float bf = rn.hi > 0.f ? rn.hi / rho.hi : 0.f;
 #ifdef MPG_CG_PROFILE
       const unsigned long long tA = gtimer();
 #endif
       const float *rk = a.r[cur], *pk = a.p[cur], *qk = a.q[cur];
-      float *rn = a.r[cur ^ 1], *pn = a.p[cur ^ 1], *qn = a.q[cur ^ 1];
-      double dpq = 0.0, drq = 0.0, dqq = 0.0, drr = 0.0;
+      float *rnx = a.r[cur ^ 1], *pnx = a.p[cur ^ 1], *qnx = a.q[cur ^ 1];
+      ff dpq = {0.f, 0.f}, drq = {0.f, 0.f}, dqq = {0.f, 0.f}, drr = {0.f, 0.f};
       for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
         const float ri = __fmaf_rn(-af, qk[i], rk[i]);
         const float pi = __fmaf_rn(bf, pk[i], ri);
@@ -486,28 +452,26 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
           s = 0.f;
 #pragma unroll
           for (int d = 0; d < ND; ++d) {
-                const int64_t j = i + a.A.off[d];
+            const int64_t j = i + a.A.off[d];
             const float rj = __fmaf_rn(-af, qk[j], rk[j]);
             s = __fmaf_rn(v32[d * n + i], __fmaf_rn(bf, pk[j], rj), s);
           }
         }
-        rn[i] = ri;
-        pn[i] = pi;
-        qn[i] = s;
-        dpq += (double)pi * (double)s;
-        drq += (double)ri * (double)s;
-        dqq += (double)s * (double)s;
-        drr += (double)ri * (double)ri;
+        rnx[i] = ri;
+        pnx[i] = pi;
+        qnx[i] = s;
+        dpq = ff_add(dpq, ff_prod(pi, s));
+        drq = ff_add(drq, ff_prod(ri, s));
+        dqq = ff_add(dqq, ff_prod(s, s));
+        drr = ff_add(drr, ff_prod(ri, ri));
       }
 #ifdef MPG_CG_PROFILE
       const unsigned long long tL = gtimer();
 #endif
       set = phase & 1;
-      double v4[4] = {dpq, drq, dqq, drr};
-      block_sum4(v4, red4);
-      if (threadIdx.x == 0)
-#pragma unroll
-        for (int k = 0; k < 4; ++k) slot(set, k)[bid] = v4[k];
+      ff v4[4] = {dpq, drq, dqq, drr};
+      block_sum_ff<4>(v4, smf);
+      put_ff(set, v4, 4);
 #ifdef MPG_CG_PROFILE
       const unsigned long long tB = gtimer();
 #endif
@@ -515,8 +479,11 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
 #ifdef MPG_CG_PROFILE
       const unsigned long long tC = gtimer();
 #endif
-      double tot[4];
-      grid_total4(slot(set, 0), nb, tot, red4, bc4);
+      total_ff(set, tot, 4);
+      pq = tot[0];
+      rq = tot[1];
+      qq = tot[2];
+      rho = tot[3];
 #ifdef MPG_CG_PROFILE
       if (bid == 0 && threadIdx.x == 0) {
         const unsigned long long tD = gtimer();
@@ -528,10 +495,6 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
         g_cg_prof[5] += tB - tL;
       }
 #endif
-      pq = tot[0];
-      rq = tot[1];
-      qq = tot[2];
-      rho = tot[3];
       ++phase;
       cur ^= 1;
       ++total_inner;
