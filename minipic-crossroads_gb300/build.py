@@ -50,21 +50,25 @@ def _run(cmd):
     return p.stdout
 
 
-def build(force=False, verbose=False, ptxas_info=False):
-    os.makedirs(BUILD, exist_ok=True)
+def build(force=False, verbose=False, ptxas_info=False, out_dir=None, extra_nvcc=()):
+    """Compile the library (and the driver) into out_dir (default _build/)."""
+    out = out_dir or BUILD
+    lib = os.path.join(out, "libminipic_gb300.so")
+    driver = os.path.join(out, "minipic_gb300")
+    os.makedirs(out, exist_ok=True)
     hdrs = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(INCLUDE, "minipic_gb300.h")]
     jobs = []
     objs = []
     for src in CU_SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src + ".o")
+        o = os.path.join(out, src + ".o")
         objs.append(o)
         if force or _newer(o, [s] + hdrs):
-            extra = ["-Xptxas", "-v"] if ptxas_info else []
+            extra = (["-Xptxas", "-v"] if ptxas_info else []) + list(extra_nvcc)
             jobs.append([nvcc()] + ARCH + NVCC_FLAGS + extra + ["-c", s, "-o", o])
     for src in CXX_SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src + ".o")
+        o = os.path.join(out, src + ".o")
         objs.append(o)
         if force or _newer(o, [s] + hdrs):
             jobs.append(["g++"] + CXX_FLAGS + ["-c", s, "-o", o])
@@ -75,13 +79,13 @@ def build(force=False, verbose=False, ptxas_info=False):
     if verbose:
         for o in outs:
             sys.stdout.write(o)
-    if force or jobs or not os.path.exists(LIB):
-        _run([nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-Xcompiler", "-fopenmp", "-lgomp"])
+    if force or jobs or not os.path.exists(lib):
+        _run([nvcc()] + ARCH + ["-shared", "-o", lib] + objs + ["-Xcompiler", "-fopenmp", "-lgomp"])
     drv_src = os.path.join(CSRC, "main.cpp")
-    if os.path.exists(drv_src) and (force or _newer(DRIVER, [drv_src, LIB, os.path.join(INCLUDE, "minipic_gb300.hpp")])):
-        _run(["g++", "-O2", "-std=c++17", "-I" + INCLUDE, drv_src, "-o", DRIVER, "-L" + BUILD, "-lminipic_gb300",
-              "-Wl,-rpath," + BUILD])
-    return LIB
+    if os.path.exists(drv_src) and (force or _newer(driver, [drv_src, lib, os.path.join(INCLUDE, "minipic_gb300.hpp")])):
+        _run(["g++", "-O2", "-std=c++17", "-I" + INCLUDE, drv_src, "-o", driver, "-L" + out, "-lminipic_gb300",
+              "-Wl,-rpath," + out])
+    return lib
 
 
 if __name__ == "__main__":
