@@ -174,6 +174,35 @@ int mpg_set_field(mpg_ctx *ctx, int which, const double *host);
 int mpg_cg_csr(mpg_ctx *ctx, int64_t n, const int32_t *d_rowptr, const int32_t *d_col, const double *d_val,
                const double *d_b, double *d_x, double tol, int max_iter, int *iters, double *resid);
 
+/* Allocation-free variant of mpg_cg_csr.  No counterpart in the reference.
+ *
+ * For callers that cannot allocate device memory at the point of the call:
+ * code that hands all device memory to its own pool or to another framework,
+ * real-time loops that must not pay an allocation, or a host that only lends
+ * out device pointers.  The call allocates nothing (no cudaMalloc, no
+ * cudaFree, no allocating library routine) and needs no mpg_ctx: its scratch
+ * (the CG vectors r, p, p', q, the per-block partial sums and the barrier
+ * counters, 4 n doubles plus ~256 KB) is one file-scope static device array
+ * of the library, sized for n <= MPG_NOALLOC_MAX_N rows (about 4.3 MB, held
+ * on every GPU that loads the library until the process exits).  Larger n is
+ * rejected with MPG_ERR_CAPACITY before anything runs.
+ *
+ * Same arguments and result as mpg_cg_csr, plus the stream to run on
+ * (a cudaStream_t passed as void*, NULL = the default stream); the caller
+ * owns and passes the CSR matrix, b and x (device pointers).  The first call
+ * on a device looks up the array's device address and the solver's
+ * co-residency limit for that device (the device current at the call); make
+ * that first call before any stream capture.  All calls share the one array:
+ * calls that overlap on the GPU (on different streams or host threads) race
+ * and give wrong results; serialise them.  The array keeps the last call's
+ * contents; the call clears the counters it needs at its start.  Status
+ * only (it has no ctx to hold a message): MPG_ERR_CAPACITY n too large,
+ * MPG_ERR_ARG bad argument, MPG_ERR_CUDA, MPG_ERR_TIMEOUT,
+ * MPG_ERR_NOT_CONVERGED. */
+#define MPG_NOALLOC_MAX_N 131072
+int mpg_cg_csr_noalloc(void *stream, int64_t n, const int32_t *d_rowptr, const int32_t *d_col, const double *d_val,
+                       const double *d_b, double *d_x, double tol, int max_iter, int *iters, double *resid);
+
 #ifdef __cplusplus
 }
 #endif

@@ -31,8 +31,9 @@ EXPORTS = [
     "mpg_csr_download", "mpg_particles_reserve", "mpg_fill_ref", "mpg_fill_uniform", "mpg_particles_upload",
     "mpg_particles_download", "mpg_particles_count", "mpg_mixed_download", "mpg_mixed_upload",
     "mpg_charge_download", "mpg_weight_charge", "mpg_solve", "mpg_weight_efield", "mpg_move", "mpg_step",
-    "mpg_sort", "mpg_get_field", "mpg_set_field", "mpg_cg_csr",
+    "mpg_sort", "mpg_get_field", "mpg_set_field", "mpg_cg_csr", "mpg_cg_csr_noalloc",
 ]
+NOALLOC_MAX_N = 131072
 
 
 class MeshDesc(C.Structure):
@@ -116,6 +117,7 @@ def load():
         "mpg_get_field": ([P, I, P], I),
         "mpg_set_field": ([P, I, P], I),
         "mpg_cg_csr": ([P, I64, P, P, P, P, P, D, I, C.POINTER(I), C.POINTER(D)], I),
+        "mpg_cg_csr_noalloc": ([P, I64, P, P, P, P, P, D, I, C.POINTER(I), C.POINTER(D)], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

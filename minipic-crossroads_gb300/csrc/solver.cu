@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <mutex>
 
 #include "minipic_gb300.h"
 #include "mpg_kernels.h"
@@ -719,4 +720,90 @@ int run_bicgstab(cudaStream_t s, int64_t n, const int32_t *rp, const int32_t *co
   *resid_out = rho0 > 0 ? sqrt(resid / rho0) : 0.0;
   if (cudaGetLastError() != cudaSuccess) return MPG_ERR_CUDA;
   return iter >= max_iter ? MPG_ERR_NOT_CONVERGED : MPG_OK;
+}
+
+// ===========================================================================
+// Allocation-free CG on a caller's CSR matrix (mpg_cg_csr_noalloc).
+//
+// The scratch of the solve lives in one file-scope static device array: the
+// device-side counters (DevStats, 256 B), the per-block partial sums (8 x
+// kNoAllocMaxBlocks doubles) and the vectors r, p, p', q (MPG_NOALLOC_MAX_N
+// doubles each).  Host code never uses the array's name as an address: the
+// first call on a device (with that device current) asks the runtime for the
+// array's device address with cudaGetSymbolAddress and caches it per device.
+namespace {
+constexpr int kNoAllocMaxBlocks = 4096;
+constexpr size_t kNoAllocStatsBytes = 256;
+constexpr size_t kNoAllocPartials = 8 * (size_t)kNoAllocMaxBlocks;
+constexpr size_t kNoAllocBytes =
+    kNoAllocStatsBytes + sizeof(double) * (kNoAllocPartials + 4 * (size_t)MPG_NOALLOC_MAX_N);
+static_assert(sizeof(DevStats) <= kNoAllocStatsBytes, "DevStats must fit its scratch slot");
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+namespace {
+struct NoAllocDevice {
+  bool ready = false;
+  unsigned char *base = nullptr;  // device address of g_noalloc_scratch on this device
+  int max_blocks = 0;
+};
+constexpr int kNoAllocDevices = 64;
+NoAllocDevice g_noalloc_dev[kNoAllocDevices];
+std::mutex g_noalloc_mu;
+}  // namespace
+
+extern "C" int mpg_cg_csr_noalloc(void *stream, int64_t n, const int32_t *d_rowptr, const int32_t *d_col,
+                                  const double *d_val, const double *d_b, double *d_x, double tol, int max_iter,
+                                  int *iters, double *resid) {
+  if (n > MPG_NOALLOC_MAX_N) return MPG_ERR_CAPACITY;  // the static scratch holds MPG_NOALLOC_MAX_N rows
+  if (n <= 0) return MPG_ERR_ARG;
+  if (!d_rowptr || !d_col || !d_val || !d_b || !d_x || !(tol > 0) || max_iter < 1) return MPG_ERR_ARG;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= kNoAllocDevices) return MPG_ERR_CUDA;
+  NoAllocDevice nd;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    NoAllocDevice &d = g_noalloc_dev[dev];
+    if (!d.ready) {
+      // one-time set-up on this device (the device is current)
+      void *p = nullptr;
+      e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (e != cudaSuccess || !p) return MPG_ERR_CUDA;
+      int mb = cg_max_blocks(dev, 512);
+      if (mb > kNoAllocMaxBlocks) mb = kNoAllocMaxBlocks;
+      if (mb < 1) return MPG_ERR_CUDA;
+      d.base = static_cast<unsigned char *>(p);
+      d.max_blocks = mb;
+      d.ready = true;
+    }
+    nd = d;
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  DevStats *st = reinterpret_cast<DevStats *>(nd.base);
+  double *dbl = reinterpret_cast<double *>(nd.base + kNoAllocStatsBytes);
+  CgWork w;
+  w.partials = dbl;
+  w.r = dbl + kNoAllocPartials;
+  w.p0 = w.r + MPG_NOALLOC_MAX_N;
+  w.p1 = w.p0 + MPG_NOALLOC_MAX_N;
+  w.q = w.p1 + MPG_NOALLOC_MAX_N;
+  w.max_blocks = nd.max_blocks;
+  w.threads = 512;
+  w.bar_mode = 0;
+  // the array keeps the previous call's contents: clear the counters
+  e = cudaMemsetAsync(st, 0, sizeof(DevStats), s);
+  if (e != cudaSuccess) return MPG_ERR_CUDA;
+  int rc = run_cg64(s, dev, n, d_rowptr, d_col, d_val, d_b, d_x, tol, max_iter, w, st);
+  if (rc) return rc;
+  DevStats h;
+  e = cudaMemcpyAsync(&h, st, sizeof(DevStats), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return MPG_ERR_CUDA;
+  if (h.bar_error) return MPG_ERR_TIMEOUT;
+  if (iters) *iters = h.solver_iters;
+  if (resid) *resid = h.solver_resid;
+  if (h.solver_status) return MPG_ERR_NOT_CONVERGED;
+  return MPG_OK;
 }
