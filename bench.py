@@ -151,15 +151,21 @@ def peaks():
 
 
 def phase_bytes(w, ctx, stats, steps, mpg):
-    """Algorithmic bytes per launch of each phase of the mixed step."""
+    """Algorithmic bytes per launch of each phase of the mixed step.
+
+    Solver (structured diagonal operator, nd = 15 diagonals on the Kuhn grid):
+    per inner iteration 4*nd bytes of FP32 coefficients per row (none with the
+    constant stencil of an unjittered mesh) + 16 B of vector reads (r, q, p, z)
+    + 16 B of vector writes; per refinement sweep (about 3 per solve) the FP64
+    residual reads 8*nd + 16 B and writes 8 B per row, the restart 20 B.
+    """
     T, N = ctx.T, ctx.N
     P = total_particles(w)
-    rp, col, val = ctx.csr()
-    nnz = len(val)
-    n = N
+    nd = 15
     iters = stats.solver_iters / max(steps, 1)
-    cg_iter = 8 * nnz + 4 * (n + 1) + 44 * n
-    sweep = 12 * nnz + 4 * (n + 1) + 48 * n
+    coef = 0 if w["jitter"] == 0 else 4 * nd
+    cg_iter = (coef + 32) * N
+    sweep = (8 * nd + 24 + 20) * N
     return {
         # 28 B read + 28 B write per particle, 16 B of node ids, 4 x 8 B accumulator RMW,
         # per-tet walk record (48 B) + neighbour table (16 B) read once
@@ -167,7 +173,7 @@ def phase_bytes(w, ctx, stats, steps, mpg):
         "solve": iters * cg_iter + 3 * sweep,
         "efield": T * (16 + 48 + 12) + N * 8,
         "deposit": N * (8 + 8 + 8 + 8),
-        "nnz": nnz, "cg_iter_bytes": cg_iter, "iters_per_step": iters,
+        "cg_iter_bytes": cg_iter, "iters_per_step": iters,
     }
 
 

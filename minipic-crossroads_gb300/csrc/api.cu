@@ -818,6 +818,33 @@ int mpg_configure(mpg_ctx *c, const mpg_config *cfg) {
       CK(cudaMemcpyAsync(c->dia.val64, d64.data(), sizeof(double) * d64.size(), cudaMemcpyHostToDevice, c->stream));
       CK(cudaMemcpyAsync(c->dia.val32, d32.data(), sizeof(float) * d32.size(), cudaMemcpyHostToDevice, c->stream));
       c->dia.bnd = c->dm.bnd;
+      // constant-stencil test: every stored entry of every interior row equals
+      // its diagonal's reference value to within FP32 resolution, and every
+      // absent entry of an interior row is a (dropped) boundary column
+      {
+        std::vector<double> ref(nd, 0.0);
+        std::vector<char> have(nd, 0);
+        bool uniform = true;
+        for (int64_t r = 0; r < N && uniform; ++r) {
+          if (c->hm.bnd[r]) continue;
+          for (int d = 0; d < (int)offs.size(); ++d) {
+            const double v = d64[(size_t)d * N + r];
+            if (v == 0.0) {
+              if (!c->hm.bnd[r + offs[d]]) uniform = false;
+              continue;
+            }
+            if (!have[d]) {
+              ref[d] = v;
+              have[d] = 1;
+            } else if (fabs(v - ref[d]) > 1e-7 * fabs(ref[d])) {
+              uniform = false;
+              break;
+            }
+          }
+        }
+        c->dia.constant = uniform ? 1 : 0;
+        for (int d = 0; d < nd; ++d) c->dia.cst[d] = uniform ? (float)ref[d] : 0.f;
+      }
       CK(cudaStreamSynchronize(c->stream));
     }
     c->csr_mode = mode;

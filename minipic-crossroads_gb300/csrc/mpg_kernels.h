@@ -96,6 +96,13 @@ struct DiaMatrix {
   double *val64 = nullptr;  // ndiag * n
   float *val32 = nullptr;   // ndiag * n
   const uint8_t *bnd = nullptr;
+  // Uniform meshes: every interior row holds the same coefficients (to FP32
+  // precision), so the FP32 inner operator of the mixed solver can be this
+  // stencil and read no matrix at all.  A missing entry of a row next to the
+  // boundary multiplies a boundary entry of the inner vectors, which is
+  // exactly zero, so the stencil gives the same products there.
+  int constant = 0;
+  float cst[27] = {};
 };
 
 struct CgWork {

@@ -312,7 +312,9 @@ struct CgMixedArgs {
   DevStats *st;
 };
 
-template <int ND, int TH>
+// CST: the inner FP32 operator is the constant stencil a.A.cst (uniform
+// meshes); otherwise the stored FP32 diagonals.
+template <int ND, int TH, bool CST>
 __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
   __shared__ double red[32];
   __shared__ ff smf[4 * 32];
@@ -351,11 +353,14 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
   int total_inner = 0, status = 0, sweeps = 0;
   double rho64 = 0.0, rho0 = 0.0;
   for (;; ++sweeps) {
-    // ---- FP64 residual with the FP64 matrix
+    // ---- FP64 residual with the FP64 matrix.  Boundary rows are identity
+    // rows, so x_i = b_i there is exact; setting it keeps the boundary entries
+    // of every inner vector exactly zero (which the constant stencil relies on).
     double rr = 0.0;
     for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
       double s = 0.0;
       if (bnd[i]) {
+        a.x[i] = a.b[i];
         s = a.x[i];
       } else {
 #pragma unroll
@@ -411,7 +416,8 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
         } else {
           s = 0.f;
 #pragma unroll
-          for (int d = 0; d < ND; ++d) s = __fmaf_rn(v32[d * n + i], p0[i + a.A.off[d]], s);
+          for (int d = 0; d < ND; ++d)
+            s = __fmaf_rn(CST ? a.A.cst[d] : v32[d * n + i], p0[i + a.A.off[d]], s);
         }
         q0[i] = s;
         pq = ff_add(pq, ff_prod(pi, s));
@@ -455,7 +461,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
           for (int d = 0; d < ND; ++d) {
             const int64_t j = i + a.A.off[d];
             const float rj = __fmaf_rn(-af, qk[j], rk[j]);
-            s = __fmaf_rn(v32[d * n + i], __fmaf_rn(bf, pk[j], rj), s);
+            s = __fmaf_rn(CST ? a.A.cst[d] : v32[d * n + i], __fmaf_rn(bf, pk[j], rj), s);
           }
         }
         rnx[i] = ri;
@@ -550,13 +556,18 @@ __global__ void k_dot_final(const double *__restrict__ part, int nb, double *out
 
 // kernel instances: [kind][threads index]; kind 0 = CSR FP64, 1/2 = DIA FP64
 // (15 / 27 diagonals), 3/4 = mixed (15 / 27 diagonals); threads 256, 512, 1024
+// kernel instances: [kind][threads index]; kind 0 = CSR FP64, 1/2 = DIA FP64
+// (15 / 27 diagonals), 3/4 = mixed (15 / 27 diagonals), 5/6 = mixed with the
+// constant stencil (15 / 27 diagonals); threads 256, 512, 1024
 static void *kernel_of(int kind, int th) {
-  static void *tab[5][3] = {
+  static void *tab[7][3] = {
       {(void *)k_cg64<256>, (void *)k_cg64<512>, (void *)k_cg64<1024>},
       {(void *)k_cg64_dia<15, 256>, (void *)k_cg64_dia<15, 512>, (void *)k_cg64_dia<15, 1024>},
       {(void *)k_cg64_dia<27, 256>, (void *)k_cg64_dia<27, 512>, (void *)k_cg64_dia<27, 1024>},
-      {(void *)k_cg_mixed<15, 256>, (void *)k_cg_mixed<15, 512>, (void *)k_cg_mixed<15, 1024>},
-      {(void *)k_cg_mixed<27, 256>, (void *)k_cg_mixed<27, 512>, (void *)k_cg_mixed<27, 1024>}};
+      {(void *)k_cg_mixed<15, 256, false>, (void *)k_cg_mixed<15, 512, false>, (void *)k_cg_mixed<15, 1024, false>},
+      {(void *)k_cg_mixed<27, 256, false>, (void *)k_cg_mixed<27, 512, false>, (void *)k_cg_mixed<27, 1024, false>},
+      {(void *)k_cg_mixed<15, 256, true>, (void *)k_cg_mixed<15, 512, true>, (void *)k_cg_mixed<15, 1024, true>},
+      {(void *)k_cg_mixed<27, 256, true>, (void *)k_cg_mixed<27, 512, true>, (void *)k_cg_mixed<27, 1024, true>}};
   const int ti = th <= 256 ? 0 : th <= 512 ? 1 : 2;
   return tab[kind][ti];
 }
@@ -566,7 +577,7 @@ static int threads_of(const CgWork &w) { return w.threads == 256 || w.threads ==
 int cg_max_blocks(int device, int threads) {
   int sms = 0, occ = 1 << 30, o = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  for (int kind = 0; kind < 5; ++kind) {
+  for (int kind = 0; kind < 7; ++kind) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kernel_of(kind, threads), threads, 0);
     occ = o < occ ? o : occ;
   }
@@ -656,8 +667,8 @@ int run_cg_mixed(cudaStream_t s, const DiaMatrix &A, const double *b, double *x,
   a.max_iter = max_iter;
   a.st = st;
   const int th = threads_of(w);
-  return coop_launch(s, kernel_of(A.ndiag <= 15 ? 3 : 4, th), grid_for_rows(A.n, w.max_blocks, th), th, &a, st,
-                     w.bar_mode);
+  const int kind = (A.ndiag <= 15 ? 3 : 4) + (A.constant ? 2 : 0);
+  return coop_launch(s, kernel_of(kind, th), grid_for_rows(A.n, w.max_blocks, th), th, &a, st, w.bar_mode);
 }
 
 // CG_solve.hpp:115-206, one host round trip per dot product
