@@ -174,6 +174,69 @@ int mpg_set_field(mpg_ctx *ctx, int which, const double *host);
 int mpg_cg_csr(mpg_ctx *ctx, int64_t n, const int32_t *d_rowptr, const int32_t *d_col, const double *d_val,
                const double *d_b, double *d_x, double tol, int max_iter, int *iters, double *resid);
 
+/* ---- batched ensemble / serving (no counterpart in the reference) --------
+ * Many independent runs (each: Kuhn-split unit cube n^3, one species,
+ * volume-uniform fill, absorbing walls, mixed precision) resident on one GPU
+ * and advanced together: one launch per phase of the step for all active runs
+ * (charge conversion, field solve, E field, fused push/walk/deposit), the
+ * step captured in a CUDA graph.  The field operator of a batched run is the
+ * uniform Kuhn stencil of its mesh (constant coefficients, FP32 inside FP64
+ * refinement).  Runs are admitted against a device-memory budget, step
+ * until their requested step count and are retired to free their slot.
+ * A run's results do not depend on which other runs share the batch. */
+typedef struct mpg_batch mpg_batch;
+
+typedef struct {
+  int n_side;            /* mesh: n^3 cubes, 6 Kuhn tets each, unit cube */
+  int64_t n_particles;   /* uniform in volume */
+  uint64_t seed;         /* fill seed */
+  double q, m;           /* species charge and mass */
+  double weight;         /* weight per particle */
+  double vth;            /* Maxwellian sigma per component */
+  double drift[3];
+  double rho_background; /* uniform background charge density */
+  double dt;
+  double tol;            /* relative residual of the field solve */
+  int max_iter;
+  int steps;             /* the run finishes after this many steps */
+} mpg_run_desc;
+
+typedef struct {
+  int active;            /* admitted and not finished */
+  int finished;
+  int steps_done;
+  int64_t n_alive;
+  double ke;             /* kinetic energy after the last step */
+  int solver_iters;      /* of the last step */
+  double solver_resid;
+  int status;
+  int64_t bytes;         /* device memory charged to the run */
+} mpg_run_info;
+
+typedef struct {
+  int active_runs;       /* runs stepped by the last call */
+  int64_t particle_steps;
+  double ms;             /* device time of the call */
+  double ms_last_step;   /* device time of its last step */
+  int64_t n_launches;
+  int graph;             /* 1 if the steps ran from a captured CUDA graph */
+  int status;
+} mpg_batch_stats;
+
+int mpg_batch_create(int device, int64_t budget_bytes, int max_runs, int64_t particle_capacity, mpg_batch **out);
+int mpg_batch_destroy(mpg_batch *b);
+int mpg_batch_last_error(mpg_batch *b, char *buf, int len);
+/* block size of the batched solver (256, 512, 1024) and cell-sort interval */
+int mpg_batch_set_tuning(mpg_batch *b, int cg_threads, int sort_interval);
+/* MPG_ERR_CAPACITY when the budget, the particle capacity or the slots are exhausted */
+int mpg_batch_admit(mpg_batch *b, const mpg_run_desc *desc, int *slot);
+int mpg_batch_step(mpg_batch *b, int n_steps, mpg_batch_stats *st);
+int mpg_batch_run_info(mpg_batch *b, int slot, mpg_run_info *info);
+int mpg_batch_run_phi(mpg_batch *b, int slot, double *phi);
+/* raw particle state of a run (local cell, barycentrics, velocity), any order */
+int mpg_batch_run_particles(mpg_batch *b, int slot, int64_t cap, int64_t *n, uint32_t *cell, float *b3, float *v3);
+int mpg_batch_retire(mpg_batch *b, int slot);
+
 /* Allocation-free variant of mpg_cg_csr.  No counterpart in the reference.
  *
  * For callers that cannot allocate device memory at the point of the call:

@@ -32,6 +32,8 @@ EXPORTS = [
     "mpg_particles_download", "mpg_particles_count", "mpg_mixed_download", "mpg_mixed_upload",
     "mpg_charge_download", "mpg_weight_charge", "mpg_solve", "mpg_weight_efield", "mpg_move", "mpg_step",
     "mpg_sort", "mpg_get_field", "mpg_set_field", "mpg_cg_csr", "mpg_cg_csr_noalloc",
+    "mpg_batch_create", "mpg_batch_destroy", "mpg_batch_last_error", "mpg_batch_set_tuning", "mpg_batch_admit",
+    "mpg_batch_step", "mpg_batch_run_info", "mpg_batch_run_phi", "mpg_batch_run_particles", "mpg_batch_retire",
 ]
 NOALLOC_MAX_N = 131072
 
@@ -57,6 +59,24 @@ class StepStats(C.Structure):
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class RunDesc(C.Structure):
+    _fields_ = [("n_side", C.c_int), ("n_particles", C.c_int64), ("seed", C.c_uint64), ("q", C.c_double),
+                ("m", C.c_double), ("weight", C.c_double), ("vth", C.c_double), ("drift", C.c_double * 3),
+                ("rho_background", C.c_double), ("dt", C.c_double), ("tol", C.c_double), ("max_iter", C.c_int),
+                ("steps", C.c_int)]
+
+
+class RunInfo(C.Structure):
+    _fields_ = [("active", C.c_int), ("finished", C.c_int), ("steps_done", C.c_int), ("n_alive", C.c_int64),
+                ("ke", C.c_double), ("solver_iters", C.c_int), ("solver_resid", C.c_double), ("status", C.c_int),
+                ("bytes", C.c_int64)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("active_runs", C.c_int), ("particle_steps", C.c_int64), ("ms", C.c_double),
+                ("ms_last_step", C.c_double), ("n_launches", C.c_int64), ("graph", C.c_int), ("status", C.c_int)]
 
 
 def lib_path():
@@ -118,6 +138,16 @@ def load():
         "mpg_set_field": ([P, I, P], I),
         "mpg_cg_csr": ([P, I64, P, P, P, P, P, D, I, C.POINTER(I), C.POINTER(D)], I),
         "mpg_cg_csr_noalloc": ([P, I64, P, P, P, P, P, D, I, C.POINTER(I), C.POINTER(D)], I),
+        "mpg_batch_create": ([I, I64, I, I64, C.POINTER(P)], I),
+        "mpg_batch_destroy": ([P], I),
+        "mpg_batch_last_error": ([P, C.c_char_p, I], I),
+        "mpg_batch_set_tuning": ([P, I, I], I),
+        "mpg_batch_admit": ([P, C.POINTER(RunDesc), C.POINTER(I)], I),
+        "mpg_batch_step": ([P, I, C.POINTER(BatchStats)], I),
+        "mpg_batch_run_info": ([P, I, C.POINTER(RunInfo)], I),
+        "mpg_batch_run_phi": ([P, I, P], I),
+        "mpg_batch_run_particles": ([P, I, I64, C.POINTER(I64), P, P, P], I),
+        "mpg_batch_retire": ([P, I], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -330,3 +360,80 @@ class Ctx:
 
     def set_field(self, which, a):
         self._ck(self.L.mpg_set_field(self.h, which, ptr(np.ascontiguousarray(a, np.float64))))
+
+
+class Batch:
+    """Many independent runs resident on one GPU, stepped together (mpg_batch_*)."""
+
+    def __init__(self, device=0, budget_bytes=8 << 30, max_runs=255, particle_capacity=1 << 24):
+        self.L = load()
+        h = C.c_void_p()
+        rc = self.L.mpg_batch_create(device, int(budget_bytes), int(max_runs), int(particle_capacity), C.byref(h))
+        if rc != OK:
+            raise MpgError(rc, "mpg_batch_create failed")
+        self.h = h
+        self.n_nodes = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.mpg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, rc, allow=()):
+        if rc != OK and rc not in allow:
+            buf = C.create_string_buffer(512)
+            self.L.mpg_batch_last_error(self.h, buf, 512)
+            raise MpgError(rc, buf.value.decode())
+        return rc
+
+    def tuning(self, cg_threads=512, sort_interval=10):
+        self._ck(self.L.mpg_batch_set_tuning(self.h, cg_threads, sort_interval))
+
+    def admit(self, n_side, n_particles, seed, q=-1.0, m=1.0, weight=None, vth=0.05, drift=(0.0, 0.0, 0.0),
+              rho_background=None, dt=0.01, tol=1e-10, max_iter=5000, steps=100, allow=()):
+        w = (1.0 / n_particles) if weight is None else weight
+        rho = (-q * w * n_particles) if rho_background is None else rho_background
+        d = RunDesc(n_side, int(n_particles), seed, q, m, w, vth, (C.c_double * 3)(*drift), rho, dt, tol, max_iter,
+                    steps)
+        slot = C.c_int(-1)
+        rc = self._ck(self.L.mpg_batch_admit(self.h, C.byref(d), C.byref(slot)), allow=allow)
+        if rc != OK:
+            return None
+        self.n_nodes[slot.value] = (n_side + 1) ** 3
+        return slot.value
+
+    def step(self, n=1, allow=()):
+        st = BatchStats()
+        rc = self._ck(self.L.mpg_batch_step(self.h, n, C.byref(st)), allow=allow)
+        st.rc = rc
+        return st
+
+    def info(self, slot):
+        r = RunInfo()
+        self._ck(self.L.mpg_batch_run_info(self.h, slot, C.byref(r)))
+        return r
+
+    def phi(self, slot):
+        a = np.zeros(self.n_nodes[slot])
+        self._ck(self.L.mpg_batch_run_phi(self.h, slot, ptr(a)))
+        return a
+
+    def particles(self, slot):
+        n = C.c_int64()
+        self._ck(self.L.mpg_batch_run_particles(self.h, slot, 0, C.byref(n), None, None, None), allow=(ERR_CAPACITY,))
+        cap = max(n.value, 1)
+        cell = np.zeros(cap, np.uint32)
+        b = np.zeros((cap, 3), np.float32)
+        v = np.zeros((cap, 3), np.float32)
+        self._ck(self.L.mpg_batch_run_particles(self.h, slot, cap, C.byref(n), ptr(cell), ptr(b), ptr(v)))
+        return cell[: n.value], b[: n.value], v[: n.value]
+
+    def retire(self, slot):
+        self._ck(self.L.mpg_batch_retire(self.h, slot))
+        self.n_nodes.pop(slot, None)

@@ -1,0 +1,88 @@
+"""GPU checks of the batched ensemble engine (mpg_batch_*).
+
+A run's field and particle state must not depend on which runs share the
+batch: stepped alone or in a mix, phi and the particle set are bit-identical
+(kinetic energy, a floating-point sum over particles in block order, agrees to
+1e-6).  Against the single-run mixed path on the same mesh and fill (which
+uses the assembled per-row FP64 matrix in the outer residual instead of the
+uniform stencil): phi within 1e-7 relative, kinetic energy within 1e-5.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _sorted_state(cell, b, v):
+    key = np.lexsort((v[:, 2], v[:, 1], v[:, 0], b[:, 2], b[:, 1], b[:, 0], cell))
+    return cell[key], b[key], v[key]
+
+
+def test_run_alone_equals_run_in_mix(mpg):
+    mix = mpg.Batch(0, budget_bytes=4 << 30, particle_capacity=1 << 20)
+    alone = mpg.Batch(0, budget_bytes=4 << 30, particle_capacity=1 << 20)
+    mix.tuning(512, 3)
+    alone.tuning(512, 3)
+    a = mix.admit(8, 20000, 11, vth=0.08, steps=20)
+    s_mix = mix.admit(12, 60000, 22, vth=0.05, steps=20)
+    c = mix.admit(10, 30000, 33, vth=0.1, drift=(0.1, 0, 0), steps=20)
+    s_alone = alone.admit(12, 60000, 22, vth=0.05, steps=20)
+    for _ in range(8):
+        st = mix.step(1)
+        assert st.rc == 0
+        assert alone.step(1).rc == 0
+    p1, p2 = mix.phi(s_mix), alone.phi(s_alone)
+    assert (p1.view(np.uint64) == p2.view(np.uint64)).all()
+    x1 = _sorted_state(*mix.particles(s_mix))
+    x2 = _sorted_state(*alone.particles(s_alone))
+    assert len(x1[0]) == len(x2[0])
+    for u, w in zip(x1, x2):
+        assert (u == w).all()
+    i1, i2 = mix.info(s_mix), alone.info(s_alone)
+    assert i1.n_alive == i2.n_alive and i1.steps_done == i2.steps_done == 8
+    assert i1.solver_iters == i2.solver_iters
+    assert abs(i1.ke - i2.ke) <= 1e-6 * i2.ke
+    assert mix.info(a).steps_done == 8 and mix.info(c).steps_done == 8
+
+
+def test_batch_run_matches_single_run(mpg):
+    n_side, n, seed, dt = 10, 40000, 5, 0.01
+    bt = mpg.Batch(0, budget_bytes=4 << 30, particle_capacity=1 << 20)
+    bt.tuning(512, 0)
+    s = bt.admit(n_side, n, seed, vth=0.05, dt=dt, steps=10)
+    ctx = mpg.Ctx(0)
+    ctx.mesh(n_side, split=mpg.SPLIT_KUHN6)
+    ctx.configure(precision=mpg.MIXED, deposit=mpg.DEPOSIT_LINEAR, solver=mpg.SOLVER_CG, tol=1e-10, max_iter=5000,
+                  warm_start=1, kill_on_wall=1, rho_background=1.0)
+    ctx.reserve(n)
+    ctx.fill_uniform(n, seed, 0, 1.0 / n, vth=0.05)
+    for k in range(5):
+        bst = bt.step(1)
+        sst = ctx.step(dt, 1)
+        bi = bt.info(s)
+        assert abs(bi.ke - sst.ke) <= 1e-5 * sst.ke, (k, bi.ke, sst.ke)
+        assert abs(bi.n_alive - sst.n_alive) <= 2
+    pb = bt.phi(s)
+    pc = ctx.get_field(mpg.FIELD_PHI)
+    assert np.abs(pb - pc).max() <= 1e-7 * np.abs(pc).max()
+
+
+def test_budget_slots_finish_and_reuse(mpg):
+    bt = mpg.Batch(0, budget_bytes=64 << 20, max_runs=2, particle_capacity=200000)
+    s0 = bt.admit(8, 10000, 1, steps=3)
+    s1 = bt.admit(8, 10000, 2, steps=5)
+    assert bt.admit(8, 10000, 3, steps=5, allow=(mpg.ERR_CAPACITY,)) is None   # no free slot
+    st = bt.step(4)
+    assert st.rc == 0
+    i0, i1 = bt.info(s0), bt.info(s1)
+    assert i0.finished == 1 and i0.steps_done == 3 and i0.active == 0
+    assert i1.steps_done == 4 and i1.active == 1
+    bt.retire(s0)
+    s2 = bt.admit(8, 10000, 4, steps=2)
+    assert s2 == s0                      # slot reused, old particles gone
+    cell, b, v = bt.particles(s2)
+    assert len(cell) == 10000
+    bt.step(2)
+    assert bt.info(s2).finished == 1 and bt.info(s1).finished == 1
+    big = mpg.Batch(0, budget_bytes=1 << 20, particle_capacity=1000)
+    assert big.admit(16, 500, 1, allow=(mpg.ERR_CAPACITY,)) is None       # budget
