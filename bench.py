@@ -17,7 +17,16 @@ algorithm, timed on this host's cores), the end-to-end number through the C
 ABI with host buffers, clocks sampled during the timed region.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                  [--workload standard|large|small]
+                  [--workload standard|large|small|ensemble|serving]
+
+Ensemble: 256 independent runs (n^3 Kuhn meshes, n uniform in [8,32];
+particle counts log-uniform in [1e4, 2e6]; v_th uniform in [0.02, 0.1]; seeds
+1000+i; 100 steps each) advanced together by the batch engine, with the
+solver block size and sort interval picked by a short autotuning pass.
+Serving: Poisson arrivals (20 runs/s for --serve-seconds, default 60) of the
+same run mix, 5% of them 64^3 meshes with 16M particles, 50-500 steps each,
+admitted against a 150 GB device budget; time advances with the measured
+device time of the batch steps (a virtual clock).
 """
 import argparse
 import importlib.util
@@ -195,6 +204,179 @@ def read_traffic(kernel):
     return None
 
 
+# ---------------------------------------------------------------------------
+# ensemble and serving
+def ensemble_trace(count=256, seed=2026):
+    import math
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    runs = []
+    for i in range(count):
+        n = int(rng.integers(8, 33))
+        P = int(round(math.exp(rng.uniform(math.log(1e4), math.log(2e6)))))
+        runs.append(dict(n_side=n, n_particles=P, seed=1000 + i, vth=float(rng.uniform(0.02, 0.1)), steps=100))
+    return runs
+
+
+def serving_trace(seconds=60.0, rate=20.0, seed=2027):
+    import math
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    t, runs, i = 0.0, [], 0
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > seconds:
+            break
+        if rng.uniform() < 0.05:
+            n, P = 64, 16 << 20
+        else:
+            n = int(rng.integers(8, 33))
+            P = int(round(math.exp(rng.uniform(math.log(1e4), math.log(2e6)))))
+        runs.append(dict(arrival=t, n_side=n, n_particles=P, seed=5000 + i, vth=float(rng.uniform(0.02, 0.1)),
+                         steps=int(rng.integers(50, 501))))
+        i += 1
+    return runs
+
+
+def batch_admit(bt, r, steps=None):
+    return bt.admit(r["n_side"], r["n_particles"], r["seed"], vth=r["vth"], dt=0.01, tol=1e-10, max_iter=5000,
+                    steps=r["steps"] if steps is None else steps, allow=(-3,))
+
+
+def autotune(mpg, runs, device=0):
+    """Pick the batch solver's block size and the sort interval on a sample."""
+    sample = runs[: min(24, len(runs))]
+    cap = sum(r["n_particles"] for r in sample)
+    results = []
+    for th, si in ((256, 10), (512, 10), (1024, 10), (512, 5), (512, 20)):
+        bt = mpg.Batch(device, budget_bytes=64 << 30, particle_capacity=cap)
+        bt.tuning(th, si)
+        for r in sample:
+            batch_admit(bt, r, steps=1000)
+        bt.step(2)
+        st = bt.step(8)
+        results.append((st.particle_steps / max(st.ms, 1e-9), th, si))
+        bt.close()
+    best = max(results)
+    return {"cg_threads": best[1], "sort_interval": best[2],
+            "tried": [{"cg_threads": th, "sort_interval": si, "particle_steps_per_ms": round(v, 1)}
+                      for v, th, si in results]}
+
+
+def plain_sequential_rate(mpg, runs, k=6, steps=3, device=0):
+    """particle-steps/s of the plain FP64 form running sample runs one after another."""
+    import numpy as np
+    rng = np.random.default_rng(7)
+    idx = rng.choice(len(runs), size=min(k, len(runs)), replace=False)
+    ps, ms = 0.0, 0.0
+    for i in idx:
+        r = runs[int(i)]
+        ctx = mpg.Ctx(device)
+        ctx.mesh(r["n_side"], split=mpg.SPLIT_KUHN6)
+        ctx.configure(precision=mpg.PLAIN, deposit=mpg.DEPOSIT_LINEAR, solver=mpg.SOLVER_CG, tol=1e-10,
+                      max_iter=5000, warm_start=1, kill_on_wall=1, rho_background=1.0)
+        ctx.reserve(r["n_particles"])
+        ctx.fill_uniform(r["n_particles"], r["seed"], 0, 1.0 / r["n_particles"], vth=r["vth"])
+        ctx.step(0.01, 1)
+        n0 = ctx.count()
+        ctx.timer_start()
+        ctx.step(0.01, steps)
+        ms += ctx.timer_stop()
+        ps += n0 * steps
+        ctx.close()
+    return ps / (ms * 1e-3), [int(i) for i in idx]
+
+
+def run_ensemble(mpg, args, device=0):
+    import numpy as np
+    runs = ensemble_trace()
+    tune = autotune(mpg, runs, device)
+    cap = sum(r["n_particles"] for r in runs)
+    bt = mpg.Batch(device, budget_bytes=150 << 30, max_runs=256, particle_capacity=cap)
+    bt.tuning(tune["cg_threads"], tune["sort_interval"])
+    t0 = time.perf_counter()
+    for r in runs:
+        assert batch_admit(bt, r) is not None
+    t_admit = time.perf_counter() - t0
+    lat, ps, ms, graph = [], 0, 0.0, 0
+    clocks = ClockSampler(device)
+    clocks.start()
+    while True:
+        st = bt.step(1)
+        if st.active_runs == 0:
+            break
+        lat.append(st.ms)
+        ps += st.particle_steps
+        ms += st.ms
+        graph = max(graph, st.graph)
+    clk = clocks.stop()
+    bt.close()
+    seq, sample = plain_sequential_rate(mpg, runs)
+    value = ps / (ms * 1e-3)
+    return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": len(lat), "warmup": 0,
+            "ms_per_step": ms / max(len(lat), 1), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "ensemble256-kuhn8to32-1e4to2e6-mixed", "runs": len(runs),
+                       "particles": cap, "steps_per_run": 100},
+            "ensemble": {"p50_step_ms": float(np.percentile(lat, 50)), "p99_step_ms": float(np.percentile(lat, 99)),
+                         "batch_steps": len(lat), "admission_s": round(t_admit, 2), "graph": graph,
+                         "autotune": tune, "plain_sequential_particle_steps_per_s": seq,
+                         "plain_sequential_sample": sample, "speedup_vs_plain_sequential": value / seq},
+            "clocks": clk}
+
+
+def run_serving(mpg, args, device=0):
+    import numpy as np
+    runs = serving_trace(seconds=args.serve_seconds)
+    tune = autotune(mpg, [r for r in runs if r["n_side"] < 64], device)
+    cap = 200 << 20
+    bt = mpg.Batch(device, budget_bytes=150 << 30, max_runs=256, particle_capacity=cap)
+    bt.tuning(tune["cg_threads"], tune["sort_interval"])
+    clock = 0.0          # virtual seconds: device time of the batch steps
+    pending = list(runs)
+    resident = {}        # slot -> run
+    lat, done, ps, busy = [], [], 0, 0.0
+    admitted_wait = []
+    while pending or resident:
+        # admit every arrived run that fits (first come, first served)
+        while pending and pending[0]["arrival"] <= clock:
+            slot = batch_admit(bt, pending[0])
+            if slot is None:
+                break
+            admitted_wait.append(clock - pending[0]["arrival"])
+            resident[slot] = pending.pop(0)
+        if not resident:
+            clock = pending[0]["arrival"]
+            continue
+        st = bt.step(1)
+        dt_s = st.ms * 1e-3
+        clock += dt_s
+        busy += dt_s
+        lat.append(st.ms)
+        ps += st.particle_steps
+        for slot in list(resident):
+            inf = bt.info(slot)
+            if inf.finished:
+                r = resident.pop(slot)
+                done.append(clock - r["arrival"])
+                bt.retire(slot)
+    bt.close()
+    seq, sample = plain_sequential_rate(mpg, [r for r in runs if r["n_side"] < 64])
+    value = ps / busy
+    return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": len(lat), "warmup": 0,
+            "ms_per_step": busy * 1e3 / max(len(lat), 1), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "serving-poisson20-%ds-mixed" % int(args.serve_seconds), "runs": len(runs),
+                       "budget_bytes": 150 << 30},
+            "serving": {"p50_step_ms": float(np.percentile(lat, 50)), "p99_step_ms": float(np.percentile(lat, 99)),
+                        "completion_s": clock, "arrival_window_s": args.serve_seconds,
+                        "run_latency_p50_s": float(np.percentile(done, 50)),
+                        "run_latency_p99_s": float(np.percentile(done, 99)),
+                        "admission_wait_p99_s": float(np.percentile(admitted_wait, 99)),
+                        "autotune": tune, "plain_sequential_particle_steps_per_s": seq,
+                        "speedup_vs_plain_sequential": value / seq}}
+
+
 def cpu_baseline(w, budget_s=20.0, max_steps=3):
     """The CPU restatement of the reference step (plain FP64, all host cores)."""
     sys.path.insert(0, ROOT)
@@ -252,11 +434,23 @@ def main():
     ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="standard", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="standard", choices=sorted(WORKLOADS) + ["ensemble", "serving"])
+    ap.add_argument("--serve-seconds", type=float, default=60.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
+    if args.workload in ("ensemble", "serving"):
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no batched or serving mode; "
+                              "its CPU step is timed by the standard workload"}))
+            return 0
+        mpg = _pkg()
+        mpg.build()
+        mpg.load()
+        line = run_ensemble(mpg, args) if args.workload == "ensemble" else run_serving(mpg, args)
+        print(json.dumps(line), flush=True)
+        return 0
     w = WORKLOADS[args.workload]
     if args.impl == "reference":
         return run_reference(args, w)

@@ -223,6 +223,7 @@ typedef struct {
   int status;
 } mpg_batch_stats;
 
+/* max_runs <= 256 resident runs; particle_capacity < 2^32 for all runs together */
 int mpg_batch_create(int device, int64_t budget_bytes, int max_runs, int64_t particle_capacity, mpg_batch **out);
 int mpg_batch_destroy(mpg_batch *b);
 int mpg_batch_last_error(mpg_batch *b, char *buf, int len);

@@ -365,7 +365,7 @@ class Ctx:
 class Batch:
     """Many independent runs resident on one GPU, stepped together (mpg_batch_*)."""
 
-    def __init__(self, device=0, budget_bytes=8 << 30, max_runs=255, particle_capacity=1 << 24):
+    def __init__(self, device=0, budget_bytes=8 << 30, max_runs=256, particle_capacity=1 << 24):
         self.L = load()
         h = C.c_void_p()
         rc = self.L.mpg_batch_create(device, int(budget_bytes), int(max_runs), int(particle_capacity), C.byref(h))

@@ -40,7 +40,7 @@
 
 namespace {
 
-constexpr int kMaxSlots = 255;
+constexpr int kMaxSlots = 256;  // the 8-bit run field of cellsp
 constexpr int kND = 15;      // Kuhn stencil
 constexpr int kMaxParts = 64;  // CTAs of one run in the solver
 
@@ -911,6 +911,8 @@ int mpg_batch_admit(mpg_batch *b, const mpg_run_desc *d, int *slot) {
   if (b->used + need > b->budget) return bfail(b, MPG_ERR_CAPACITY, "device-memory budget exhausted");
   if (b->n + d->n_particles > b->cap && b->n > 0) BTRY(batch_sort(b));
   if (b->n + d->n_particles > b->cap) return bfail(b, MPG_ERR_CAPACITY, "particle capacity exhausted");
+  if (6LL * d->n_side * d->n_side * d->n_side >= (int64_t)MPG_WALL)
+    return bfail(b, MPG_ERR_ARG, "run mesh too large for 24-bit cell ids");
   // mesh and stencil on the host
   mpg_mesh_desc md{};
   md.nx = md.ny = md.nz = d->n_side;
