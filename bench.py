@@ -439,6 +439,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-ensemble", action="store_true")
     args = ap.parse_args()
     if args.workload in ("ensemble", "serving"):
         if args.impl == "reference":
@@ -587,6 +588,11 @@ def main():
                            "d2h_bytes_per_step": int((cs2.nbytes + b2.nbytes + v2.nbytes) / ke + 136),
                            "how": "mpg_mixed_upload from pinned host buffers, mpg_step x K with stats read back "
                                   "each step, mpg_mixed_download; host wall clock"}
+    if rank == 0 and not args.no_ensemble and args.workload == "standard" and world == 1:
+        # the ensemble part of the metric: 256 runs in the batch engine
+        ens = run_ensemble(mpg, args, device=local)
+        line["ensemble"] = dict(ens["ensemble"], value=ens["value"], unit=UNIT, workload=ens["config"]["workload"],
+                                particles=ens["config"]["particles"], steps=ens["steps"])
     if rank == 0:
         if not args.no_cpu:
             try:
