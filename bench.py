@@ -75,12 +75,17 @@ def total_particles(w):
     return sum(s["n"] for s in w["species"])
 
 
+# CG initial guess of the single-run workloads (both forms): 2 = linear
+# extrapolation from the last two solutions, 1 = the previous solution
+WARM_START = 2
+
+
 def make_ctx(mpg, w, precision, device=0, seed_offset=0):
     ctx = mpg.Ctx(device)
     ctx.mesh(w["n_side"], split=mpg.SPLIT_KUHN6, lo=0.0, hi=1.0,
              mapping=mpg.MAP_JITTER if w["jitter"] else mpg.MAP_NONE, jitter=w["jitter"], seed=7)
     ctx.configure(precision=precision, deposit=mpg.DEPOSIT_LINEAR, solver=mpg.SOLVER_CG, tol=1e-10, max_iter=5000,
-                  warm_start=1, kill_on_wall=1, max_crossings=1000,
+                  warm_start=WARM_START, kill_on_wall=1, max_crossings=1000,
                   sort_interval=w["sort_interval"] if precision == mpg.MIXED else 0,
                   rho_background=w["rho_background"])
     # weights: each species carries a total charge of magnitude 1 in the unit cube
@@ -440,7 +445,11 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true")
+    ap.add_argument("--warm-start", type=int, default=2, choices=[0, 1, 2],
+                    help="CG initial guess: 0 zero, 1 previous phi, 2 extrapolated from the last two")
     args = ap.parse_args()
+    global WARM_START
+    WARM_START = args.warm_start
     if args.workload in ("ensemble", "serving"):
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the reference has no batched or serving mode; "
@@ -539,6 +548,7 @@ def main():
                 "data": "synthetic",
                 "config": {"workload": w["name"], "n_side": w["n_side"], "tets": ctx.T, "nodes": ctx.N,
                            "particles": total_particles(w), "dt": w["dt"], "cg_tol": 1e-10,
+                           "cg_initial_guess": ["zero", "previous phi", "extrapolated 2*phi[n-1]-phi[n-2]"][WARM_START],
                            "parallelism": "replicas" if world > 1 else "single",
                            "l2": "inputs larger than L2 (particle state > 129 MB), no flush"},
                 "phases_ms_per_step": {k: round(v, 4) for k, v in phases.items()},

@@ -40,17 +40,27 @@ def main():
     ctx.step(w["dt"], 3)
     L = mpg.load()
     L.mpg_probe_cg_profile.argtypes = [ctypes.c_void_p]
+    L.mpg_probe_cg_profile_blocks.argtypes = [ctypes.c_void_p]
     p0 = (ctypes.c_ulonglong * 8)()
+    b0 = (ctypes.c_ulonglong * 3072)()
     L.mpg_probe_cg_profile(p0)
+    L.mpg_probe_cg_profile_blocks(b0)
     ctx.step(w["dt"], args.steps)
     p1 = (ctypes.c_ulonglong * 8)()
+    b1 = (ctypes.c_ulonglong * 3072)()
     L.mpg_probe_cg_profile(p1)
+    L.mpg_probe_cg_profile_blocks(b1)
     d = [p1[i] - p0[i] for i in range(6)]
     it = max(d[3], 1)
     f = 2.07e3  # SM cycles per microsecond at the 2070 MHz maximum clock
+    per_block = {}
+    for j, name in enumerate(("compute_reduce_us", "barrier_us", "totals_us")):
+        v = sorted((b1[3 * k + j] - b0[3 * k + j]) / it / f for k in range(1024) if b1[3 * k + j] > b0[3 * k + j])
+        if v:
+            per_block[name] = {"blocks": len(v), "min": v[0], "median": v[len(v) // 2], "max": v[-1]}
     print(json.dumps({"iterations": d[3], "row_loop_us": d[4] / it / f, "reduce_store_us": d[5] / it / f,
                       "barrier_us": d[1] / it / f, "totals_us": d[2] / it / f,
-                      "threads": os.environ.get("MPG_CG_THREADS", "512")}))
+                      "threads": os.environ.get("MPG_CG_THREADS", "512"), "per_block": per_block}))
 
 
 if __name__ == "__main__":

@@ -46,6 +46,8 @@ struct mpg_ctx {
   float *val32 = nullptr;
   DiaMatrix dia;  // structured diagonal form of the symmetric matrix (CG paths)
   double *rhs = nullptr, *phi = nullptr, *bg = nullptr, *Etet = nullptr;
+  double *phi_prev = nullptr;  // previous solution (warm_start 2)
+  int phi_hist = 0;            // solutions held in phi / phi_prev (0, 1, 2)
   unsigned long long *acc = nullptr;
   bool acc_valid = false;
 
@@ -297,29 +299,18 @@ int ensure_cg_work(mpg_ctx *c, int64_t n) {
   dfree(c, c->cg.p0);
   dfree(c, c->cg.p1);
   dfree(c, c->cg.q);
-  dfree(c, c->cg.r32);
-  dfree(c, c->cg.z32);
-  dfree(c, c->cg.q32);
-  dfree(c, c->cg.pa32);
-  dfree(c, c->cg.pb32);
-  dfree(c, c->cg.r32b);
-  dfree(c, c->cg.q32b);
+  dfree(c, c->cg.v4);
   dfree(c, c->cg.partials);
   // solver launch shape: tunable through MPG_CG_THREADS / MPG_CG_BARRIER
   if (const char *e = getenv("MPG_CG_THREADS")) c->cg.threads = atoi(e);
   if (const char *e = getenv("MPG_CG_BARRIER")) c->cg.bar_mode = atoi(e);
+  if (const char *e = getenv("MPG_CG_BLOCKS")) c->cg.block_cap = atoi(e);
   c->cg.max_blocks = cg_max_blocks(c->device, c->cg.threads == 256 || c->cg.threads == 1024 ? c->cg.threads : 512);
   TRY(dalloc(c, &c->cg.r, n));
   TRY(dalloc(c, &c->cg.p0, n));
   TRY(dalloc(c, &c->cg.p1, n));
   TRY(dalloc(c, &c->cg.q, n));
-  TRY(dalloc(c, &c->cg.r32, n));
-  TRY(dalloc(c, &c->cg.z32, n));
-  TRY(dalloc(c, &c->cg.q32, n));
-  TRY(dalloc(c, &c->cg.pa32, n));
-  TRY(dalloc(c, &c->cg.pb32, n));
-  TRY(dalloc(c, &c->cg.r32b, n));
-  TRY(dalloc(c, &c->cg.q32b, n));
+  TRY(dalloc(c, &c->cg.v4, 2 * n));
   if (c->cg.max_blocks < 1) return fail(c, MPG_ERR_CUDA, "solver kernels cannot be resident (occupancy 0)");
   TRY(dalloc(c, &c->cg.partials, 8 * (int64_t)c->cg.max_blocks));
   c->cg_n = n;
@@ -371,22 +362,41 @@ int phase_deposit_mixed(mpg_ctx *c) {
   return MPG_OK;
 }
 
-int phase_solve(mpg_ctx *c) {
-  const int64_t N = c->dm.N;
-  if (c->cfg.precision == MPG_MIXED) {
-    TRY(ensure_cg_work(c, N));
+// Initial guess of the CG solves: zero (warm_start 0), the previous phi (1),
+// or the linear extrapolation 2 phi_{n-1} - phi_{n-2} of the last two
+// solutions (2; the previous phi until two exist).
+int initial_guess(mpg_ctx *c, int64_t N) {
+  if (c->cfg.warm_start != 2) {
+    // phi_prev is not kept up to date in these modes
+    c->phi_hist = 0;
     if (!c->cfg.warm_start) CK(cudaMemsetAsync(c->phi, 0, sizeof(double) * N, c->stream));
-    int rc = run_cg_mixed(c->stream, c->dia, c->rhs, c->phi, c->cfg.tol, 1e-5, c->cfg.max_iter, c->cg, c->d_stats);
-    c->launches += 1;
-    if (rc) return fail(c, rc, "mixed CG launch failed: %s", cudaGetErrorString(cudaGetLastError()));
     return MPG_OK;
   }
-  if (c->cfg.solver == MPG_SOLVER_CG) {
+  if (!c->phi_prev) {
+    TRY(dalloc(c, &c->phi_prev, N));
+    c->phi_hist = c->phi_hist > 1 ? 1 : c->phi_hist;
+  }
+  if (c->phi_hist >= 2) {
+    launch_extrapolate(c->stream, N, c->phi, c->phi_prev);
+    c->launches += 1;
+  } else if (c->phi_hist == 1) {
+    CK(cudaMemcpyAsync(c->phi_prev, c->phi, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
+  }
+  return MPG_OK;
+}
+
+int phase_solve(mpg_ctx *c) {
+  const int64_t N = c->dm.N;
+  if (c->cfg.precision == MPG_MIXED || c->cfg.solver == MPG_SOLVER_CG) {
     TRY(ensure_cg_work(c, N));
-    if (!c->cfg.warm_start) CK(cudaMemsetAsync(c->phi, 0, sizeof(double) * N, c->stream));
-    int rc = run_cg64_dia(c->stream, c->dia, c->rhs, c->phi, c->cfg.tol, c->cfg.max_iter, c->cg, c->d_stats);
+    TRY(initial_guess(c, N));
+    int rc = c->cfg.precision == MPG_MIXED
+                 ? run_cg_mixed(c->stream, c->dia, c->rhs, c->phi, c->cfg.tol, 1e-5, c->cfg.max_iter, c->cg,
+                                c->d_stats)
+                 : run_cg64_dia(c->stream, c->dia, c->rhs, c->phi, c->cfg.tol, c->cfg.max_iter, c->cg, c->d_stats);
     c->launches += 1;
     if (rc) return fail(c, rc, "CG launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+    if (c->phi_hist < 2) ++c->phi_hist;
     return MPG_OK;
   }
   // reference BiCGStab (host-driven; parity mode)
@@ -571,6 +581,8 @@ void free_field(mpg_ctx *c) {
   c->dia = DiaMatrix();
   dfree(c, c->rhs);
   dfree(c, c->phi);
+  dfree(c, c->phi_prev);
+  c->phi_hist = 0;
   dfree(c, c->bg);
   dfree(c, c->Etet);
   dfree(c, c->acc);
@@ -1327,9 +1339,10 @@ int mpg_set_field(mpg_ctx *c, int which, const double *host) {
   const int64_t N = c->dm.N;
   if (which == MPG_FIELD_RHS)
     CK(cudaMemcpyAsync(c->rhs, host, sizeof(double) * N, cudaMemcpyHostToDevice, c->stream));
-  else if (which == MPG_FIELD_PHI)
+  else if (which == MPG_FIELD_PHI) {
     CK(cudaMemcpyAsync(c->phi, host, sizeof(double) * N, cudaMemcpyHostToDevice, c->stream));
-  else
+    c->phi_hist = 1;  // the given phi is the only history
+  } else
     return fail(c, MPG_ERR_ARG, "field %d is not settable", which);
   CK(cudaStreamSynchronize(c->stream));
   return MPG_OK;

@@ -607,6 +607,14 @@ __global__ void k_copy_u32(const uint32_t *src, uint32_t *dst) { *dst = *src; }
 
 // slots at or beyond the device count are dead (after a sort the grid bound
 // stays at the old count until the host reads the new one)
+__global__ void k_extrapolate(int64_t n, double *__restrict__ phi, double *__restrict__ prev) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double a = phi[i];
+  phi[i] = 2.0 * a - prev[i];
+  prev[i] = a;
+}
+
 __global__ void k_mark_tail_dead(uint32_t *c, int64_t n, const uint32_t *count) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p < n && p >= (int64_t)*count) c[p] = MPG_DEAD;
@@ -887,6 +895,9 @@ void launch_mixed_sort(cudaStream_t s, const MixedParts &P, int64_t n, const Mix
 }
 void launch_mark_tail_dead(cudaStream_t s, uint32_t *c, int64_t n, const uint32_t *count) {
   if (n > 0) k_mark_tail_dead<<<grid_for(n), kThreads, 0, s>>>(c, n, count);
+}
+void launch_extrapolate(cudaStream_t s, int64_t n, double *phi, double *prev) {
+  if (n > 0) k_extrapolate<<<grid_for(n), kThreads, 0, s>>>(n, phi, prev);
 }
 void launch_fill_uniform(cudaStream_t s, int mixed, const PlainParts &P, const MixedParts &X, int64_t n0, int64_t n,
                          uint64_t seed, int type, double weight, const double drift[3], double vth, const DevMesh &M,

@@ -63,6 +63,8 @@ void launch_mixed_sort(cudaStream_t s, const MixedParts &P, int64_t n, const Mix
                        uint32_t *cnt, uint32_t *start, uint32_t *scratch, int64_t scratch_len, uint32_t *d_count);
 
 void launch_mark_tail_dead(cudaStream_t s, uint32_t *c, int64_t n, const uint32_t *count);
+// phi <- 2 phi - prev, prev <- old phi (initial guess from the last two solutions)
+void launch_extrapolate(cudaStream_t s, int64_t n, double *phi, double *prev);
 
 // ---- fills, conversions ---------------------------------------------------
 void launch_fill_uniform(cudaStream_t s, int mixed, const PlainParts &P, const MixedParts &X, int64_t n0, int64_t n,
@@ -107,12 +109,12 @@ struct DiaMatrix {
 
 struct CgWork {
   double *r = nullptr, *p0 = nullptr, *p1 = nullptr, *q = nullptr;  // FP64 vectors, n each
-  float *r32 = nullptr, *z32 = nullptr, *q32 = nullptr, *pa32 = nullptr, *pb32 = nullptr;  // mixed inner vectors
-  float *r32b = nullptr, *q32b = nullptr;  // second copies of r and q (double buffering)
+  float4 *v4 = nullptr;  // mixed inner vectors {r, p, q, z} per node, two copies (2n)
   double *partials = nullptr;  // 8 * max_blocks
   int max_blocks = 0;
   int threads = 512;  // block size of the cooperative solver kernels (256, 512 or 1024)
   int bar_mode = 0;   // grid barrier flavour (0: fence + volatile polling, 1: release/acquire)
+  int block_cap = 0;  // > 0: at most this many blocks in the mixed solver's grid
 };
 // plain FP64 CG on CSR (CG_solve.hpp:54-114), one cooperative launch; returns 0 or an MPG_ERR_*
 int run_cg64(cudaStream_t s, int device, int64_t n, const int32_t *rowptr, const int32_t *col, const double *val,

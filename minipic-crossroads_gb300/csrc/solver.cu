@@ -31,9 +31,14 @@
 // in SM cycles of block 0: [0] compute, [1] barrier wait, [2] grid totals,
 // [3] iterations, [4] row loop only, [5] block reduction + partial store
 __device__ unsigned long long g_cg_prof[8];
+// per block (up to 1024): [0] compute + block reduction, [1] barrier wait, [2] grid totals
+__device__ unsigned long long g_cg_prof_blk[1024 * 3];
 __device__ __forceinline__ unsigned long long gtimer() { return (unsigned long long)clock64(); }
 extern "C" int mpg_probe_cg_profile(unsigned long long *out) {
   return cudaMemcpyFromSymbol(out, g_cg_prof, sizeof(g_cg_prof)) == cudaSuccess ? 0 : -2;
+}
+extern "C" int mpg_probe_cg_profile_blocks(unsigned long long *out) {
+  return cudaMemcpyFromSymbol(out, g_cg_prof_blk, sizeof(g_cg_prof_blk)) == cudaSuccess ? 0 : -2;
 }
 #endif
 
@@ -301,10 +306,7 @@ struct CgMixedArgs {
   const double *__restrict__ b;
   double *x;
   double *r64;
-  float *r[2];
-  float *p[2];
-  float *q[2];
-  float *z;
+  float4 *v[2];  // inner vectors per node {r, p, q, z}, double-buffered
   double *partials;  // [2 sets][kSlots][nb]
   double tol2;
   double inner_tol2;
@@ -312,15 +314,23 @@ struct CgMixedArgs {
   DevStats *st;
 };
 
+// Block records each of the first four warps' threads loads in the inner
+// all-reduce; the launch caps the grid at 128 * kRecOf(TH) blocks.
+__host__ __device__ constexpr int kRecOf(int th) { return th <= 256 ? 5 : th <= 512 ? 3 : 2; }
+
 // CST: the inner FP32 operator is the constant stencil a.A.cst (uniform
 // meshes); otherwise the stored FP32 diagonals.
 template <int ND, int TH, bool CST>
 __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
+  constexpr int kRec = kRecOf(TH);
   __shared__ double red[32];
   __shared__ ff smf[4 * 32];
+  __shared__ float smw[4 * 32];
+  __shared__ ff smt[4];
   __shared__ double bcast;
   unsigned epoch = 0;
   const int nb = gridDim.x, bid = blockIdx.x;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwarps = TH / 32;
   const int64_t n = a.A.n;
   const int64_t lo = n * bid / nb, hi = n * (bid + 1) / nb;
   const uint8_t *__restrict__ bnd = a.A.bnd;
@@ -332,6 +342,8 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
   int phase = 0;
   auto slot64 = [&](int set, int k) { return a.partials + ((size_t)(set * kSlots + k)) * nb; };
   auto slotff = [&](int set, int k) { return reinterpret_cast<float2 *>(slot64(set, k)); };
+  // inner iterations: one 32-byte record (4 float-float values) per block
+  auto slotrec = [&](int set) { return reinterpret_cast<float4 *>(slot64(set, 0)); };
   auto put_ff = [&](int set, const ff *v, int K) {
     if (threadIdx.x == 0)
       for (int k = 0; k < K; ++k) slotff(set, k)[bid] = make_float2(v[k].hi, v[k].lo);
@@ -389,13 +401,11 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
     }
     // ---- inner start: r0 = r64/|r64|, p0 = r0, z = 0, q0 = A p0
     const double scale = 1.0 / sqrt(rho64);
-    float *r0 = a.r[0], *p0 = a.p[0];
+    float4 *v0 = a.v[0];
     ff rs = {0.f, 0.f};
     for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
       const float ri = (float)(a.r64[i] * scale);
-      r0[i] = ri;
-      p0[i] = ri;
-      a.z[i] = 0.f;
+      v0[i] = make_float4(ri, ri, 0.f, 0.f);
       rs = ff_add(rs, ff_prod(ri, ri));
     }
     set = phase & 1;
@@ -406,10 +416,9 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
     total_ff(set, &rin0, 1);
     ++phase;
     {
-      float *q0 = a.q[0];
       ff pq = {0.f, 0.f}, qq = {0.f, 0.f};
       for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-        const float pi = p0[i];
+        const float pi = v0[i].y;
         float s;
         if (bnd[i]) {
           s = pi;
@@ -417,9 +426,10 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
           s = 0.f;
 #pragma unroll
           for (int d = 0; d < ND; ++d)
-            s = __fmaf_rn(CST ? a.A.cst[d] : v32[d * n + i], p0[i + a.A.off[d]], s);
+            s = __fmaf_rn(CST ? a.A.cst[d] : v32[d * n + i], v0[i + a.A.off[d]].y, s);
         }
-        q0[i] = s;
+        // only q is written: other blocks read this node's p concurrently
+        reinterpret_cast<float *>(v0 + i)[2] = s;
         pq = ff_add(pq, ff_prod(pi, s));
         qq = ff_add(qq, ff_prod(s, s));
       }
@@ -445,13 +455,15 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
 #ifdef MPG_CG_PROFILE
       const unsigned long long tA = gtimer();
 #endif
-      const float *rk = a.r[cur], *pk = a.p[cur], *qk = a.q[cur];
-      float *rnx = a.r[cur ^ 1], *pnx = a.p[cur ^ 1], *qnx = a.q[cur ^ 1];
+      const float4 *vk = a.v[cur];
+      float4 *vnx = a.v[cur ^ 1];
       ff dpq = {0.f, 0.f}, drq = {0.f, 0.f}, dqq = {0.f, 0.f}, drr = {0.f, 0.f};
       for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-        const float ri = __fmaf_rn(-af, qk[i], rk[i]);
-        const float pi = __fmaf_rn(bf, pk[i], ri);
-        a.z[i] = __fmaf_rn(af, pk[i], a.z[i]);
+        // one 16-byte load per node: {r, p, q, z} of the current iterate
+        const float4 w = vk[i];
+        const float ri = __fmaf_rn(-af, w.z, w.x);
+        const float pi = __fmaf_rn(bf, w.y, ri);
+        const float zi = __fmaf_rn(af, w.y, w.w);
         float s;
         if (bnd[i]) {
           s = pi;
@@ -459,14 +471,12 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
           s = 0.f;
 #pragma unroll
           for (int d = 0; d < ND; ++d) {
-            const int64_t j = i + a.A.off[d];
-            const float rj = __fmaf_rn(-af, qk[j], rk[j]);
-            s = __fmaf_rn(CST ? a.A.cst[d] : v32[d * n + i], __fmaf_rn(bf, pk[j], rj), s);
+            const float4 u = vk[i + a.A.off[d]];
+            const float rj = __fmaf_rn(-af, u.z, u.x);
+            s = __fmaf_rn(CST ? a.A.cst[d] : v32[d * n + i], __fmaf_rn(bf, u.y, rj), s);
           }
         }
-        rnx[i] = ri;
-        pnx[i] = pi;
-        qnx[i] = s;
+        vnx[i] = make_float4(ri, pi, s, zi);
         dpq = ff_add(dpq, ff_prod(pi, s));
         drq = ff_add(drq, ff_prod(ri, s));
         dqq = ff_add(dqq, ff_prod(s, s));
@@ -476,9 +486,33 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
       const unsigned long long tL = gtimer();
 #endif
       set = phase & 1;
-      ff v4[4] = {dpq, drq, dqq, drr};
-      block_sum_ff<4>(v4, smf);
-      put_ff(set, v4, 4);
+      {
+        // block partials: FP32 warp trees (each thread holds its rows'
+        // float-float sums; a 32-term FP32 tree keeps ~2e-7 relative), then
+        // one warp adds the warp sums in float-float and posts them
+        float w4[4] = {dpq.hi + dpq.lo, drq.hi + drq.lo, dqq.hi + dqq.lo, drr.hi + drr.lo};
+        for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+          for (int k = 0; k < 4; ++k) w4[k] += __shfl_down_sync(0xffffffffu, w4[k], o);
+        if (lane == 0)
+#pragma unroll
+          for (int k = 0; k < 4; ++k) smw[k * 32 + wid] = w4[k];
+        __syncthreads();
+        if (wid == 0) {
+          ff t[4];
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            t[k] = ff{lane < nwarps ? smw[k * 32 + lane] : 0.f, 0.f};
+            for (int o = 16; o > 0; o >>= 1) t[k] = ff_add(t[k], ff_shfl_down(t[k], o));
+          }
+          if (lane == 0) {
+            // one 32-byte record per block
+            float4 *rec = slotrec(set) + 2 * bid;
+            rec[0] = make_float4(t[0].hi, t[0].lo, t[1].hi, t[1].lo);
+            rec[1] = make_float4(t[2].hi, t[2].lo, t[3].hi, t[3].lo);
+          }
+        }
+      }
 #ifdef MPG_CG_PROFILE
       const unsigned long long tB = gtimer();
 #endif
@@ -486,12 +520,59 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
 #ifdef MPG_CG_PROFILE
       const unsigned long long tC = gtimer();
 #endif
-      total_ff(set, tot, 4);
-      pq = tot[0];
-      rq = tot[1];
-      qq = tot[2];
-      rho = tot[3];
+      // grid totals: the first four warps load every block record up front
+      // (thread t: records t, t + 128, ...; one L2 round trip), add them in
+      // float-float, reduce across lanes and across the four warps.  Same
+      // order in every block, so every block gets the same totals.
+      if (wid < 4) {
+        const float4 *rec = slotrec(set);
+        float4 x[kRec], y[kRec];
+#pragma unroll
+        for (int j = 0; j < kRec; ++j) {
+          const int i = threadIdx.x + 128 * j;
+          if (i < nb) {
+            x[j] = rec[2 * i];
+            y[j] = rec[2 * i + 1];
+          } else {
+            x[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+            y[j] = x[j];
+          }
+        }
+        ff t[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+#pragma unroll
+        for (int j = 0; j < kRec; ++j) {
+          t[0] = ff_add(t[0], ff{x[j].x, x[j].y});
+          t[1] = ff_add(t[1], ff{x[j].z, x[j].w});
+          t[2] = ff_add(t[2], ff{y[j].x, y[j].y});
+          t[3] = ff_add(t[3], ff{y[j].z, y[j].w});
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          for (int o = 16; o > 0; o >>= 1) t[k] = ff_add(t[k], ff_shfl_down(t[k], o));
+          if (lane == 0) smf[k * 32 + wid] = t[k];
+        }
+      }
+      __syncthreads();
+      if (wid == 0) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          ff u = lane < 4 ? smf[k * 32 + lane] : ff{0.f, 0.f};
+          for (int o = 2; o > 0; o >>= 1) u = ff_add(u, ff_shfl_down(u, o));
+          if (lane == 0) smt[k] = u;
+        }
+      }
+      __syncthreads();
+      pq = smt[0];
+      rq = smt[1];
+      qq = smt[2];
+      rho = smt[3];
 #ifdef MPG_CG_PROFILE
+      if (threadIdx.x == 0 && bid < 1024) {
+        const unsigned long long tE = gtimer();
+        g_cg_prof_blk[3 * bid + 0] += tB - tA;
+        g_cg_prof_blk[3 * bid + 1] += tC - tB;
+        g_cg_prof_blk[3 * bid + 2] += tE - tC;
+      }
       if (bid == 0 && threadIdx.x == 0) {
         const unsigned long long tD = gtimer();
         g_cg_prof[0] += tB - tA;
@@ -508,7 +589,8 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
     }
     // ---- x += |r64| z  (FP64)
     const double back = sqrt(rho64);
-    for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) a.x[i] += (double)a.z[i] * back;
+    const float4 *vz = a.v[cur];
+    for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) a.x[i] += (double)vz[i].w * back;
     if (!grid_barrier(a.st, nb, epoch)) return;
   }
   if (bid == 0 && threadIdx.x == 0) {
@@ -654,13 +736,8 @@ int run_cg_mixed(cudaStream_t s, const DiaMatrix &A, const double *b, double *x,
   a.b = b;
   a.x = x;
   a.r64 = w.r;
-  a.r[0] = w.r32;
-  a.r[1] = w.r32b;
-  a.p[0] = w.pa32;
-  a.p[1] = w.pb32;
-  a.q[0] = w.q32;
-  a.q[1] = w.q32b;
-  a.z = w.z32;
+  a.v[0] = w.v4;
+  a.v[1] = w.v4 + A.n;
   a.partials = w.partials;
   a.tol2 = tol * tol;
   a.inner_tol2 = inner_tol * inner_tol;
@@ -668,7 +745,9 @@ int run_cg_mixed(cudaStream_t s, const DiaMatrix &A, const double *b, double *x,
   a.st = st;
   const int th = threads_of(w);
   const int kind = (A.ndiag <= 15 ? 3 : 4) + (A.constant ? 2 : 0);
-  return coop_launch(s, kernel_of(kind, th), grid_for_rows(A.n, w.max_blocks, th), th, &a, st, w.bar_mode);
+  int cap = 128 * kRecOf(th) < w.max_blocks ? 128 * kRecOf(th) : w.max_blocks;
+  if (w.block_cap > 0 && w.block_cap < cap) cap = w.block_cap;
+  return coop_launch(s, kernel_of(kind, th), grid_for_rows(A.n, cap, th), th, &a, st, w.bar_mode);
 }
 
 // CG_solve.hpp:115-206, one host round trip per dot product

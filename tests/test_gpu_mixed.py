@@ -134,3 +134,31 @@ def test_mixed_walk_known_answer(mpg):
         assert np.allclose(d["x"][0], x0 + [0.1, 0, 0], atol=2e-6)
     else:
         assert st.n_killed == 1
+
+
+@pytest.mark.parametrize("form", ["mixed", "plain"])
+def test_extrapolated_initial_guess_same_solution(mpg, form):
+    # warm_start 2 starts each solve at 2 phi[n-1] - phi[n-2]; the converged
+    # phi must agree with the previous-phi start to the solver tolerance
+    # (both stop at |b - A x| <= 1e-10 |b|; phi differences stay below
+    # 1e-8 max|phi| over the first steps), and KE to 1e-9 relative
+    n = 40000
+    prec = mpg.MIXED if form == "mixed" else mpg.PLAIN
+    a = _ctx(mpg, n_side=8, precision=prec, warm_start=1)
+    b = _ctx(mpg, n_side=8, precision=prec, warm_start=2)
+    for c in (a, b):
+        _two_species(c, n)
+    ia = ib = 0
+    for s in range(6):
+        sa = a.step(0.01, 1)
+        sb = b.step(0.01, 1)
+        pa = a.get_field(mpg.FIELD_PHI)
+        pb = b.get_field(mpg.FIELD_PHI)
+        assert np.abs(pa - pb).max() <= 1e-8 * np.abs(pa).max(), s
+        assert abs(sa.ke - sb.ke) <= 1e-9 * sa.ke
+        assert sa.n_alive == sb.n_alive
+        if s >= 2:
+            ia += sa.solver_iters
+            ib += sb.solver_iters
+    # the extrapolated start is closer: never more iterations in total
+    assert ib <= ia, (ia, ib)
