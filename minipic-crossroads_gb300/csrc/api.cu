@@ -50,6 +50,7 @@ struct mpg_ctx {
   int phi_hist = 0;            // solutions held in phi / phi_prev (0, 1, 2)
   unsigned long long *acc = nullptr;
   bool acc_valid = false;
+  bool needs_sort = false;  // particles added or replaced since the last cell sort
 
   int precision = MPG_PLAIN;  // precision of the allocated particle arrays
   bool parts_alloc = false;
@@ -445,6 +446,7 @@ int compact_plain(mpg_ctx *c) {
 }
 
 int sort_mixed(mpg_ctx *c) {
+  c->needs_sort = false;
   const int other = 1 - c->cur;
   launch_mixed_sort(c->stream, c->mp[c->cur], c->n, c->mp[other], c->dm.T, c->sort_cnt, c->sort_start,
                     c->scan_scratch, c->scan_len, c->d_count);
@@ -472,6 +474,12 @@ int finish_counts_mixed(mpg_ctx *c, bool sorted) {
 
 int one_step(mpg_ctx *c, double dt, mpg_step_stats *acc_st, bool &sorted) {
   const bool mixed = c->cfg.precision == MPG_MIXED;
+  if (mixed && c->cfg.sort_interval > 0 && c->needs_sort) {
+    // freshly filled or uploaded particles are in arbitrary cell order: sort
+    // before the first step instead of after sort_interval steps
+    TRY(sort_mixed(c));
+    sorted = true;
+  }
   ev_record(c, 0);
   TRY(mixed ? phase_deposit_mixed(c) : phase_deposit_plain(c));
   ev_record(c, 1);
@@ -578,6 +586,7 @@ void free_field(mpg_ctx *c) {
   dfree(c, c->val32);
   dfree(c, c->dia.val64);
   dfree(c, c->dia.val32);
+  dfree(c, c->dia.dis);
   c->dia = DiaMatrix();
   dfree(c, c->rhs);
   dfree(c, c->phi);
@@ -800,6 +809,7 @@ int mpg_configure(mpg_ctx *c, const mpg_config *cfg) {
     CK(cudaStreamSynchronize(c->stream));
     dfree(c, c->dia.val64);
     dfree(c, c->dia.val32);
+    dfree(c, c->dia.dis);
     c->dia = DiaMatrix();
     if (mode == 1) {
       // diagonal offsets present in the interior rows, in column order
@@ -830,25 +840,28 @@ int mpg_configure(mpg_ctx *c, const mpg_config *cfg) {
       CK(cudaMemcpyAsync(c->dia.val64, d64.data(), sizeof(double) * d64.size(), cudaMemcpyHostToDevice, c->stream));
       CK(cudaMemcpyAsync(c->dia.val32, d32.data(), sizeof(float) * d32.size(), cudaMemcpyHostToDevice, c->stream));
       c->dia.bnd = c->dm.bnd;
-      // constant-stencil test: every stored entry of every interior row equals
-      // its diagonal's reference value to within FP32 resolution, and every
-      // absent entry of an interior row is a (dropped) boundary column
+      // constant-stencil test: for every interior row, every entry whose
+      // column is an interior node equals its diagonal's reference value to
+      // within 1e-7 of the largest entry (couplings that are zero in exact
+      // arithmetic come out as rounding noise of either sign); entries of
+      // boundary columns are dropped, and the stencil multiplies them by the
+      // exactly zero boundary entries of the inner vectors
       {
+        double amax = 0.0;
+        for (size_t k = 0; k < d64.size(); ++k) amax = std::max(amax, fabs(d64[k]));
+        const double atol = 1e-7 * amax;
         std::vector<double> ref(nd, 0.0);
         std::vector<char> have(nd, 0);
-        bool uniform = true;
+        bool uniform = amax > 0.0;
         for (int64_t r = 0; r < N && uniform; ++r) {
           if (c->hm.bnd[r]) continue;
           for (int d = 0; d < (int)offs.size(); ++d) {
+            if (c->hm.bnd[r + offs[d]]) continue;
             const double v = d64[(size_t)d * N + r];
-            if (v == 0.0) {
-              if (!c->hm.bnd[r + offs[d]]) uniform = false;
-              continue;
-            }
             if (!have[d]) {
               ref[d] = v;
               have[d] = 1;
-            } else if (fabs(v - ref[d]) > 1e-7 * fabs(ref[d])) {
+            } else if (fabs(v - ref[d]) > atol) {
               uniform = false;
               break;
             }
@@ -856,6 +869,29 @@ int mpg_configure(mpg_ctx *c, const mpg_config *cfg) {
         }
         c->dia.constant = uniform ? 1 : 0;
         for (int d = 0; d < nd; ++d) c->dia.cst[d] = uniform ? (float)ref[d] : 0.f;
+      }
+      // Non-uniform meshes: the FP32 inner operator of the mixed solver is the
+      // symmetrically Jacobi-scaled matrix D^-1/2 A D^-1/2 (unit diagonal; the
+      // FP64 outer residual keeps A itself).  MPG_CG_JACOBI=0 turns it off.
+      const char *jenv = getenv("MPG_CG_JACOBI");
+      const int center = (int)(std::lower_bound(offs.begin(), offs.end(), (int64_t)0) - offs.begin());
+      if (!c->dia.constant && !(jenv && atoi(jenv) == 0) && center < (int)offs.size() && offs[center] == 0) {
+        std::vector<double> dis(N, 1.0);
+        for (int64_t r = 0; r < N; ++r) {
+          const double dr = d64[(size_t)center * N + r];
+          if (!c->hm.bnd[r] && dr > 0.0) dis[r] = 1.0 / std::sqrt(dr);
+        }
+        for (int64_t r = 0; r < N; ++r) {
+          if (c->hm.bnd[r]) continue;
+          for (int d = 0; d < (int)offs.size(); ++d) {
+            const double v = d64[(size_t)d * N + r];
+            if (v != 0.0) d32[(size_t)d * N + r] = (float)(v * dis[r] * dis[r + offs[d]]);
+          }
+        }
+        TRY(dalloc(c, &c->dia.dis, N));
+        CK(cudaMemcpyAsync(c->dia.dis, dis.data(), sizeof(double) * N, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(c->dia.val32, d32.data(), sizeof(float) * d32.size(), cudaMemcpyHostToDevice,
+                           c->stream));
       }
       CK(cudaStreamSynchronize(c->stream));
     }
@@ -957,6 +993,7 @@ int mpg_fill_ref(mpg_ctx *c, int nppe, int type, double density, const double ve
   c->n_live += add;
   c->id_next += add;
   c->acc_valid = false;
+  c->needs_sort = true;
   CK(cudaStreamSynchronize(c->stream));
   return MPG_OK;
 }
@@ -978,6 +1015,7 @@ int mpg_fill_uniform(mpg_ctx *c, int64_t n, uint64_t seed, int type, double weig
   c->n_live += n;
   c->id_next += n;
   c->acc_valid = false;
+  c->needs_sort = true;
   CK(cudaStreamSynchronize(c->stream));
   return MPG_OK;
 }
@@ -1061,6 +1099,7 @@ int mpg_particles_upload(mpg_ctx *c, int64_t n, const int32_t *cell, const doubl
   for (int64_t i = 0; i < n; ++i) c->n_live += cell[i] >= 0;
   c->id_next = n;
   c->acc_valid = false;
+  c->needs_sort = true;
   return MPG_OK;
 }
 
@@ -1161,6 +1200,7 @@ int mpg_mixed_upload(mpg_ctx *c, int64_t n, const uint32_t *cellsp, const float 
   c->n_live = 0;
   for (int64_t i = 0; i < n; ++i) c->n_live += cellsp[i] != MPG_DEAD;
   c->acc_valid = false;
+  c->needs_sort = true;
   return MPG_OK;
 }
 

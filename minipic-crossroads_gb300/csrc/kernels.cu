@@ -13,6 +13,7 @@
 // walls and deposits the new position into an int64 fixed-point node
 // accumulator (order-independent, exact total charge).
 #include <cuda_runtime.h>
+#include <stdlib.h>
 
 #include "mpg_internal.h"
 #include "mpg_kernels.h"
@@ -582,6 +583,87 @@ __global__ void __launch_bounds__(kThreads) k_mixed_move(MixedParts P, int64_t n
   block_totals_push(&bt, ff{ke, 0.f}, killed, cross, limit, st);
 }
 
+// Persistent form of the move: the grid is one wave of resident blocks and
+// each warp walks 32-particle chunks c, c + W, c + 2W, ... (W = warps in the
+// grid).  The next chunk's particle record is loaded before the current chunk
+// is processed, so its DRAM latency overlaps the push, walk and deposit of
+// the current one; block totals are formed once per block.  Per particle the
+// arithmetic is that of k_mixed_move.
+__global__ void __launch_bounds__(kThreads) k_mixed_move_persistent(MixedParts P, int64_t n,
+                                                                    const float4 *__restrict__ rec,
+                                                                    const uint4 *__restrict__ nbr,
+                                                                    const int4 *__restrict__ tets, SpeciesTable S,
+                                                                    float dt, int kill, int max_cross,
+                                                                    unsigned long long *__restrict__ acc,
+                                                                    DevStats *st) {
+  __shared__ BlockTotals bt;
+  block_totals_init(&bt);
+  const int lane = threadIdx.x & 31;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int64_t nchunks = (n + 31) >> 5;
+  ff ke = {0.f, 0.f};
+  unsigned killed = 0, cross = 0, limit = 0;
+  int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  // prefetched record of this lane's particle in chunk c
+  uint32_t cs_n = MPG_DEAD;
+  float4 bv_n = make_float4(0.f, 0.f, 0.f, 0.f);
+  float2 vv_n = make_float2(0.f, 0.f);
+  {
+    const int64_t p = c * 32 + lane;
+    if (c < nchunks && p < n) {
+      cs_n = P.c[p];
+      bv_n = P.b[p];
+      vv_n = P.v[p];
+    }
+  }
+  for (; c < nchunks; c += nw) {
+    const int64_t p = c * 32 + lane;
+    const uint32_t cs = cs_n;
+    const float4 bv = bv_n;
+    const float2 vv = vv_n;
+    {
+      const int64_t q = (c + nw) * 32 + lane;
+      cs_n = MPG_DEAD;
+      if (c + nw < nchunks && q < n) {
+        cs_n = P.c[q];
+        bv_n = P.b[q];
+        vv_n = P.v[q];
+      }
+    }
+    int dep_key = -1;
+    float d1 = 0.f, d2 = 0.f, d3 = 0.f;
+    int dq = 0;
+    if (p < n && cs != MPG_DEAD) {
+      const int s = (int)(cs >> 24);
+      uint32_t e = cs & 0xFFFFFFu;
+      float l1 = bv.x, l2 = bv.y, l3 = bv.z;
+      float vx = bv.w, vy = vv.x, vz = vv.y;
+      bool dead, lim;
+      const int it = mixed_walk(rec, nbr, e, l1, l2, l3, vx, vy, vz, 0.5f * dt * S.qm_f[s], dt, kill, max_cross,
+                                dead, lim);
+      limit += lim ? 1u : 0u;
+      cross += (unsigned)it;
+      if (dead) {
+        killed += 1;
+        P.c[p] = MPG_DEAD;
+      } else {
+        if (e != (cs & 0xFFFFFFu)) P.c[p] = ((uint32_t)s << 24) | e;
+        P.b[p] = make_float4(l1, l2, l3, vx);
+        P.v[p] = make_float2(vy, vz);
+        ke = ff_add(ke, ff{S.half_wm_f[s] * __fmaf_rn(vz, vz, __fmaf_rn(vy, vy, vx * vx)), 0.f});
+        dep_key = (int)e;
+        d1 = l1;
+        d2 = l2;
+        d3 = l3;
+        dq = (int)S.qfix[s];
+      }
+    }
+    // every lane of the warp is here (c is uniform across the warp)
+    deposit_fixed_warp(acc, tets, dep_key, d1, d2, d3, dq);
+  }
+  block_totals_push(&bt, ke, killed, cross, limit, st);
+}
+
 __global__ void k_cell_hist(const uint32_t *__restrict__ c, int64_t n, uint32_t *__restrict__ cnt) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
@@ -879,10 +961,32 @@ void launch_mixed_convert(cudaStream_t s, int64_t N, unsigned long long *acc, do
 void launch_efield_mixed(cudaStream_t s, const DevMesh &M, const double *phi) {
   k_efield_mixed<<<grid_for(M.T), kThreads, 0, s>>>(M.T, M.tets, M.mrec, phi);
 }
+// resident blocks of the persistent move kernel on the current device (one wave)
+static unsigned move_wave_blocks() {
+  static int cached[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  if (!cached[dev]) {
+    int sms = 0, occ = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mixed_move_persistent, kThreads, 0);
+    cached[dev] = (sms > 0 ? sms : 1) * (occ > 0 ? occ : 1);
+  }
+  return (unsigned)cached[dev];
+}
 void launch_mixed_move(cudaStream_t s, const MixedParts &P, int64_t n, const DevMesh &M, const SpeciesTable &S,
                        float dt, int kill, int max_cross, unsigned long long *acc, DevStats *st) {
   if (n <= 0) return;
-  k_mixed_move<<<grid_for(n), kThreads, 0, s>>>(P, n, M.mrec, M.mnbr, M.tets, S, dt, kill, max_cross, acc, st);
+  static const char *env = getenv("MPG_MOVE_KERNEL");
+  if (env && atoi(env) == 0) {
+    k_mixed_move<<<grid_for(n), kThreads, 0, s>>>(P, n, M.mrec, M.mnbr, M.tets, S, dt, kill, max_cross, acc, st);
+    return;
+  }
+  const unsigned wave = move_wave_blocks();
+  const unsigned want = grid_for(n);
+  k_mixed_move_persistent<<<want < wave ? want : wave, kThreads, 0, s>>>(P, n, M.mrec, M.mnbr, M.tets, S, dt, kill,
+                                                                         max_cross, acc, st);
 }
 void launch_mixed_sort(cudaStream_t s, const MixedParts &P, int64_t n, const MixedParts &Q, int64_t T, uint32_t *cnt,
                        uint32_t *start, uint32_t *scratch, int64_t scratch_len, uint32_t *d_count) {

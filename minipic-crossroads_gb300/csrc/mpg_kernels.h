@@ -96,7 +96,8 @@ struct DiaMatrix {
   int ndiag = 0;
   int off[27] = {};
   double *val64 = nullptr;  // ndiag * n
-  float *val32 = nullptr;   // ndiag * n
+  float *val32 = nullptr;   // ndiag * n; the FP32 inner operator (Jacobi-scaled when dis is set)
+  double *dis = nullptr;    // n: D^-1/2 of the symmetric Jacobi scaling of val32, or null
   const uint8_t *bnd = nullptr;
   // Uniform meshes: every interior row holds the same coefficients (to FP32
   // precision), so the FP32 inner operator of the mixed solver can be this

@@ -403,8 +403,9 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
     const double scale = 1.0 / sqrt(rho64);
     float4 *v0 = a.v[0];
     ff rs = {0.f, 0.f};
+    const double *__restrict__ dis = a.A.dis;  // Jacobi scaling of the inner system, or null
     for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-      const float ri = (float)(a.r64[i] * scale);
+      const float ri = (float)(dis ? a.r64[i] * scale * dis[i] : a.r64[i] * scale);
       v0[i] = make_float4(ri, ri, 0.f, 0.f);
       rs = ff_add(rs, ff_prod(ri, ri));
     }
@@ -590,7 +591,8 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
     // ---- x += |r64| z  (FP64)
     const double back = sqrt(rho64);
     const float4 *vz = a.v[cur];
-    for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) a.x[i] += (double)vz[i].w * back;
+    for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x)
+      a.x[i] += dis ? (double)vz[i].w * back * dis[i] : (double)vz[i].w * back;
     if (!grid_barrier(a.st, nb, epoch)) return;
   }
   if (bid == 0 && threadIdx.x == 0) {

@@ -63,9 +63,12 @@ def test_fixed_point_deposit_bit_exact_and_exact_charge(mpg, orc):
     assert (acc2 == acc).all()
 
 
-def test_mixed_solve_reaches_fp64_tolerance(mpg, orc):
-    ctx = _ctx(mpg, n_side=10, warm_start=0)
-    m = orc.Mesh(10, split=6, mapping=4, jitter=0.2, seed=4)
+@pytest.mark.parametrize("jitter", [0.2, 0.0])
+def test_mixed_solve_reaches_fp64_tolerance(mpg, orc, jitter):
+    # jitter 0.2: stored FP32 operator with Jacobi scaling; jitter 0: uniform
+    # mesh, constant-stencil FP32 operator
+    ctx = _ctx(mpg, n_side=10, warm_start=0, jitter=jitter)
+    m = orc.Mesh(10, split=6, mapping=4 if jitter else 0, jitter=jitter, seed=4)
     m.assemble(1)
     rng = np.random.default_rng(7)
     b = rng.standard_normal(m.N)
