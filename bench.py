@@ -191,21 +191,27 @@ def phase_bytes(w, ctx, stats, steps, mpg):
     }
 
 
-def read_traffic(kernel):
-    """DRAM bytes per launch from a committed ncu summary (profiles/<kernel>*.txt), if any."""
+def read_traffic(kernel, workload):
+    """DRAM bytes per launch of `kernel` on `workload` from a committed ncu
+    summary (profiles/<kernel>*.txt with a matching "workload:" line), if any."""
     pdir = os.path.join(ROOT, "profiles")
     if not os.path.isdir(pdir):
         return None
     for fn in sorted(os.listdir(pdir)):
         if not fn.startswith(kernel) or not fn.endswith(".txt"):
             continue
+        wl, val = None, None
         with open(os.path.join(pdir, fn)) as f:
             for line in f:
-                if line.startswith("dram_bytes_per_launch_full_workload:"):
+                if line.startswith("workload:"):
+                    wl = line.split(":", 1)[1].split()[0]
+                elif line.startswith("dram_bytes_per_launch_full_workload:"):
                     try:
-                        return float(line.split(":", 1)[1].split()[0])
+                        val = float(line.split(":", 1)[1].split()[0])
                     except ValueError:
-                        return None
+                        val = None
+        if wl == workload and val is not None:
+            return val
     return None
 
 
@@ -445,8 +451,8 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true")
-    ap.add_argument("--warm-start", type=int, default=2, choices=[0, 1, 2],
-                    help="CG initial guess: 0 zero, 1 previous phi, 2 extrapolated from the last two")
+    ap.add_argument("--warm-start", type=int, default=2, choices=[0, 1, 2, 3],
+                    help="CG initial guess: 0 zero, 1 previous phi, 2/3 linear/quadratic extrapolation")
     args = ap.parse_args()
     global WARM_START
     WARM_START = args.warm_start
@@ -525,13 +531,13 @@ def main():
         hbm, kind = peaks()
         pb = phase_bytes(w, ctx, ph, k_ph, mpg) if precision == mpg.MIXED else None
         dominant = max(("solve", "move", "efield", "deposit"), key=lambda k: phases[k])
-        kern = {"solve": "k_cg_mixed", "move": "k_mixed_move", "efield": "k_efield_mixed",
+        kern = {"solve": "k_cg_mixed", "move": "k_mixed_move_persistent", "efield": "k_efield_mixed",
                 "deposit": "k_mixed_convert"}[dominant]
         roof = None
         if pb is not None:
             bytes_launch = pb[dominant]
             achieved = bytes_launch / (phases[dominant] * 1e-3) / 1e9
-            traffic = read_traffic(kern)
+            traffic = read_traffic(kern, w["name"])
             roof = {"bound": "hbm", "kernel": kern, "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                     "frac": round(achieved / hbm, 4), "peak_kind": kind, "traffic": traffic,
                     "algorithmic_bytes_per_launch": int(bytes_launch), "ms_per_launch": round(phases[dominant], 4)}
@@ -548,7 +554,8 @@ def main():
                 "data": "synthetic",
                 "config": {"workload": w["name"], "n_side": w["n_side"], "tets": ctx.T, "nodes": ctx.N,
                            "particles": total_particles(w), "dt": w["dt"], "cg_tol": 1e-10,
-                           "cg_initial_guess": ["zero", "previous phi", "extrapolated 2*phi[n-1]-phi[n-2]"][WARM_START],
+                           "cg_initial_guess": ["zero", "previous phi", "extrapolated 2*phi[n-1]-phi[n-2]",
+                                                "extrapolated 3*phi[n-1]-3*phi[n-2]+phi[n-3]"][WARM_START],
                            "parallelism": "replicas" if world > 1 else "single",
                            "l2": "inputs larger than L2 (particle state > 129 MB), no flush"},
                 "phases_ms_per_step": {k: round(v, 4) for k, v in phases.items()},

@@ -73,7 +73,8 @@ typedef struct {
   int solver;            /* MPG_SOLVER_*; the mixed form always uses refined CG */
   double tol;            /* relative residual |b-Ax|/|b| (PIC.cpp:251 uses 1e-6) */
   int max_iter;          /* CG_solve.hpp:144 uses 1000 */
-  int warm_start;        /* CG initial guess: 0 zero, 1 the previous phi, 2 2*phi[n-1] - phi[n-2] */
+  int warm_start;        /* CG initial guess: 0 zero, 1 the previous phi, 2 2*phi[n-1] - phi[n-2],
+                            3 3*phi[n-1] - 3*phi[n-2] + phi[n-3] */
   int kill_on_wall;      /* DataWarehouse::set_kill_particles_on_wall_impact */
   int max_crossings;     /* face crossings per particle per step before MPG_ERR_WALK_LIMIT */
   int sort_interval;     /* cell sort every k steps, 0 = never (ParticleList::sort) */

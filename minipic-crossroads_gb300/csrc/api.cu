@@ -46,11 +46,13 @@ struct mpg_ctx {
   float *val32 = nullptr;
   DiaMatrix dia;  // structured diagonal form of the symmetric matrix (CG paths)
   double *rhs = nullptr, *phi = nullptr, *bg = nullptr, *Etet = nullptr;
-  double *phi_prev = nullptr;  // previous solution (warm_start 2)
-  int phi_hist = 0;            // solutions held in phi / phi_prev (0, 1, 2)
+  double *phi_prev = nullptr;   // previous solution (warm_start 2, 3)
+  double *phi_prev2 = nullptr;  // the one before (warm_start 3)
+  int phi_hist = 0;             // solutions held in phi / phi_prev / phi_prev2 (0 .. 3)
   unsigned long long *acc = nullptr;
   bool acc_valid = false;
   bool needs_sort = false;  // particles added or replaced since the last cell sort
+  double inner_tol = 1e-5;  // relative residual target of the mixed solver's FP32 inner CG
 
   int precision = MPG_PLAIN;  // precision of the allocated particle arrays
   bool parts_alloc = false;
@@ -306,6 +308,7 @@ int ensure_cg_work(mpg_ctx *c, int64_t n) {
   if (const char *e = getenv("MPG_CG_THREADS")) c->cg.threads = atoi(e);
   if (const char *e = getenv("MPG_CG_BARRIER")) c->cg.bar_mode = atoi(e);
   if (const char *e = getenv("MPG_CG_BLOCKS")) c->cg.block_cap = atoi(e);
+  if (const char *e = getenv("MPG_CG_INNER_TOL")) c->inner_tol = atof(e);
   c->cg.max_blocks = cg_max_blocks(c->device, c->cg.threads == 256 || c->cg.threads == 1024 ? c->cg.threads : 512);
   TRY(dalloc(c, &c->cg.r, n));
   TRY(dalloc(c, &c->cg.p0, n));
@@ -364,21 +367,28 @@ int phase_deposit_mixed(mpg_ctx *c) {
 }
 
 // Initial guess of the CG solves: zero (warm_start 0), the previous phi (1),
-// or the linear extrapolation 2 phi_{n-1} - phi_{n-2} of the last two
-// solutions (2; the previous phi until two exist).
+// the linear extrapolation 2 phi_{n-1} - phi_{n-2} of the last two solutions
+// (2), or the quadratic one 3 phi_{n-1} - 3 phi_{n-2} + phi_{n-3} (3); the
+// extrapolations use the lower orders until enough solutions exist.
 int initial_guess(mpg_ctx *c, int64_t N) {
-  if (c->cfg.warm_start != 2) {
-    // phi_prev is not kept up to date in these modes
+  const int ws = c->cfg.warm_start;
+  if (ws != 2 && ws != 3) {
+    // the history buffers are not kept up to date in these modes
     c->phi_hist = 0;
-    if (!c->cfg.warm_start) CK(cudaMemsetAsync(c->phi, 0, sizeof(double) * N, c->stream));
+    if (!ws) CK(cudaMemsetAsync(c->phi, 0, sizeof(double) * N, c->stream));
     return MPG_OK;
   }
   if (!c->phi_prev) {
     TRY(dalloc(c, &c->phi_prev, N));
     c->phi_hist = c->phi_hist > 1 ? 1 : c->phi_hist;
   }
-  if (c->phi_hist >= 2) {
-    launch_extrapolate(c->stream, N, c->phi, c->phi_prev);
+  if (ws == 3 && !c->phi_prev2) {
+    TRY(dalloc(c, &c->phi_prev2, N));
+    c->phi_hist = c->phi_hist > 2 ? 2 : c->phi_hist;
+  }
+  const int order = std::min(c->phi_hist, ws) - 1;  // 0: copy only, 1: linear, 2: quadratic
+  if (order >= 1) {
+    launch_extrapolate(c->stream, N, c->phi, c->phi_prev, order == 2 ? c->phi_prev2 : nullptr);
     c->launches += 1;
   } else if (c->phi_hist == 1) {
     CK(cudaMemcpyAsync(c->phi_prev, c->phi, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
@@ -392,12 +402,12 @@ int phase_solve(mpg_ctx *c) {
     TRY(ensure_cg_work(c, N));
     TRY(initial_guess(c, N));
     int rc = c->cfg.precision == MPG_MIXED
-                 ? run_cg_mixed(c->stream, c->dia, c->rhs, c->phi, c->cfg.tol, 1e-5, c->cfg.max_iter, c->cg,
+                 ? run_cg_mixed(c->stream, c->dia, c->rhs, c->phi, c->cfg.tol, c->inner_tol, c->cfg.max_iter, c->cg,
                                 c->d_stats)
                  : run_cg64_dia(c->stream, c->dia, c->rhs, c->phi, c->cfg.tol, c->cfg.max_iter, c->cg, c->d_stats);
     c->launches += 1;
     if (rc) return fail(c, rc, "CG launch failed: %s", cudaGetErrorString(cudaGetLastError()));
-    if (c->phi_hist < 2) ++c->phi_hist;
+    if (c->phi_hist < 3) ++c->phi_hist;
     return MPG_OK;
   }
   // reference BiCGStab (host-driven; parity mode)
@@ -591,6 +601,7 @@ void free_field(mpg_ctx *c) {
   dfree(c, c->rhs);
   dfree(c, c->phi);
   dfree(c, c->phi_prev);
+  dfree(c, c->phi_prev2);
   c->phi_hist = 0;
   dfree(c, c->bg);
   dfree(c, c->Etet);

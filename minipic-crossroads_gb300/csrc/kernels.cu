@@ -689,11 +689,17 @@ __global__ void k_copy_u32(const uint32_t *src, uint32_t *dst) { *dst = *src; }
 
 // slots at or beyond the device count are dead (after a sort the grid bound
 // stays at the old count until the host reads the new one)
-__global__ void k_extrapolate(int64_t n, double *__restrict__ phi, double *__restrict__ prev) {
+__global__ void k_extrapolate(int64_t n, double *__restrict__ phi, double *__restrict__ prev,
+                              double *__restrict__ prev2) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const double a = phi[i];
-  phi[i] = 2.0 * a - prev[i];
+  const double a = phi[i], b = prev[i];
+  if (prev2) {
+    phi[i] = 3.0 * (a - b) + prev2[i];
+    prev2[i] = b;
+  } else {
+    phi[i] = 2.0 * a - b;
+  }
   prev[i] = a;
 }
 
@@ -1000,8 +1006,8 @@ void launch_mixed_sort(cudaStream_t s, const MixedParts &P, int64_t n, const Mix
 void launch_mark_tail_dead(cudaStream_t s, uint32_t *c, int64_t n, const uint32_t *count) {
   if (n > 0) k_mark_tail_dead<<<grid_for(n), kThreads, 0, s>>>(c, n, count);
 }
-void launch_extrapolate(cudaStream_t s, int64_t n, double *phi, double *prev) {
-  if (n > 0) k_extrapolate<<<grid_for(n), kThreads, 0, s>>>(n, phi, prev);
+void launch_extrapolate(cudaStream_t s, int64_t n, double *phi, double *prev, double *prev2) {
+  if (n > 0) k_extrapolate<<<grid_for(n), kThreads, 0, s>>>(n, phi, prev, prev2);
 }
 void launch_fill_uniform(cudaStream_t s, int mixed, const PlainParts &P, const MixedParts &X, int64_t n0, int64_t n,
                          uint64_t seed, int type, double weight, const double drift[3], double vth, const DevMesh &M,

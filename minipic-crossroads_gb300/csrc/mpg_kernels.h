@@ -63,8 +63,9 @@ void launch_mixed_sort(cudaStream_t s, const MixedParts &P, int64_t n, const Mix
                        uint32_t *cnt, uint32_t *start, uint32_t *scratch, int64_t scratch_len, uint32_t *d_count);
 
 void launch_mark_tail_dead(cudaStream_t s, uint32_t *c, int64_t n, const uint32_t *count);
-// phi <- 2 phi - prev, prev <- old phi (initial guess from the last two solutions)
-void launch_extrapolate(cudaStream_t s, int64_t n, double *phi, double *prev);
+// initial guess from the last solutions: phi <- 2 phi - prev (prev2 null) or
+// phi <- 3 phi - 3 prev + prev2; the history shifts by one
+void launch_extrapolate(cudaStream_t s, int64_t n, double *phi, double *prev, double *prev2);
 
 // ---- fills, conversions ---------------------------------------------------
 void launch_fill_uniform(cudaStream_t s, int mixed, const PlainParts &P, const MixedParts &X, int64_t n0, int64_t n,

@@ -139,8 +139,9 @@ def test_mixed_walk_known_answer(mpg):
         assert st.n_killed == 1
 
 
+@pytest.mark.parametrize("ws", [2, 3])
 @pytest.mark.parametrize("form", ["mixed", "plain"])
-def test_extrapolated_initial_guess_same_solution(mpg, form):
+def test_extrapolated_initial_guess_same_solution(mpg, form, ws):
     # warm_start 2 starts each solve at 2 phi[n-1] - phi[n-2]; the converged
     # phi must agree with the previous-phi start to the solver tolerance
     # (both stop at |b - A x| <= 1e-10 |b|; phi differences stay below
@@ -148,7 +149,7 @@ def test_extrapolated_initial_guess_same_solution(mpg, form):
     n = 40000
     prec = mpg.MIXED if form == "mixed" else mpg.PLAIN
     a = _ctx(mpg, n_side=8, precision=prec, warm_start=1)
-    b = _ctx(mpg, n_side=8, precision=prec, warm_start=2)
+    b = _ctx(mpg, n_side=8, precision=prec, warm_start=ws)
     for c in (a, b):
         _two_species(c, n)
     ia = ib = 0
