@@ -274,6 +274,36 @@ def autotune(mpg, runs, device=0):
                       for v, th, si in results]}
 
 
+def accuracy_vs_plain(mpg, w, device=0, steps=3):
+    """Error of the mixed form against the FP64 plain form on the same fills:
+    max |phi_mixed - phi_plain| / max |phi_plain| after each of `steps` steps,
+    the relative KE difference, and whether the mixed form's fixed-point
+    charge (the accumulator the fused move leaves for the next solve) sums
+    exactly to the particles' quanta."""
+    import numpy as np
+    m = make_ctx(mpg, w, mpg.MIXED, device=device)
+    p = make_ctx(mpg, w, mpg.PLAIN, device=device)
+    errs, ke = [], 0.0
+    for _ in range(steps):
+        sm = m.step(w["dt"], 1)
+        sp = p.step(w["dt"], 1)
+        pm = m.get_field(mpg.FIELD_PHI)
+        pp = p.get_field(mpg.FIELD_PHI)
+        errs.append(float(np.abs(pm - pp).max() / max(np.abs(pp).max(), 1e-300)))
+        ke = max(ke, abs(sm.ke - sp.ke) / max(abs(sp.ke), 1e-300))
+    acc, _, qfix = m.charge()
+    cs, _, _ = m.mixed_download()
+    live = cs != mpg.DEAD
+    species = (cs[live] >> 24).astype(np.int64)
+    expect = int(np.bincount(species, minlength=len(qfix)).astype(object).dot(qfix.astype(object)))
+    exact = int(acc.astype(object).sum()) == expect
+    m.close()
+    p.close()
+    return {"steps": steps, "phi_rel_err_max": max(errs), "phi_rel_err_per_step": errs, "ke_rel_diff_max": ke,
+            "charge_exact": bool(exact), "how": "same fills, both forms stepped side by side; "
+            "max|phi_mixed-phi_plain|/max|phi_plain|"}
+
+
 def plain_sequential_rate(mpg, runs, k=6, steps=3, device=0):
     """particle-steps/s of the plain FP64 form running sample runs one after another."""
     import numpy as np
@@ -564,6 +594,7 @@ def main():
     # plain FP64 form of the same workload (the form the mixed target is measured against)
     if not args.no_plain and precision == mpg.MIXED:
         ctx.close()
+        ctx = None
         pc = make_ctx(mpg, w, mpg.PLAIN, device=local, seed_offset=rank)
         kp = max(1, min(args.steps, 5))
         pc.step(w["dt"], 2)
@@ -576,7 +607,11 @@ def main():
             line["plain_fp64"] = {"value": pv, "unit": UNIT, "steps": kp, "ms_per_step": pms / kp,
                                   "mixed_over_plain": value / pv}
         pc.close()
-        ctx = make_ctx(mpg, w, precision, device=local, seed_offset=rank) if not args.no_e2e else None
+        # error of the mixed form against the FP64 plain form on the same inputs
+        if rank == 0:
+            line["accuracy_vs_plain_fp64"] = accuracy_vs_plain(mpg, w, device=local)
+        if not args.no_e2e:
+            ctx = make_ctx(mpg, w, precision, device=local, seed_offset=rank)
     # end to end through the C ABI with host buffers: state upload, K steps with
     # the step statistics read back each step, state download
     if not args.no_e2e and ctx is not None and precision == mpg.MIXED:
