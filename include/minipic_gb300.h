@@ -65,6 +65,9 @@ typedef struct {
   int mapping;     /* MPG_MAP_* */
   double jitter;   /* fraction of h, MPG_MAP_JITTER only */
   uint64_t seed;   /* jitter seed */
+  int periodic;    /* 1: periodic in x (Mesh::Mesh(..., periodic), mesh.cpp:61-76,178-189);
+                      the x = hi plane nodes off the y/z walls are ghosts of the x = lo plane,
+                      nx >= 2 (even for MPG_SPLIT_REF5, mesh.cpp:91-94) */
 } mpg_mesh_desc;
 
 typedef struct {
@@ -121,6 +124,11 @@ int mpg_mesh_sizes(mpg_ctx *ctx, int64_t *n_tets, int64_t *n_nodes, int64_t *n_b
  * Host buffers; NULL skips an array. */
 int mpg_mesh_download(mpg_ctx *ctx, double *nodes, int32_t *tets, int32_t *nbrs, double *jinv, double *detj,
                       double *normals, uint8_t *boundary);
+/* Periodic meshes: Mesh::elem_face_periodic T*4 (+1 on both sides of an x = lo/hi
+ * face, 0 elsewhere; mesh.cpp:369-392) and Mesh::node_pairs N (the x = lo node a
+ * ghost node stands for, -1 otherwise; mesh.cpp:178-189).  NULL skips an array;
+ * both are all zero / all -1 on a non-periodic mesh. */
+int mpg_mesh_periodic_download(mpg_ctx *ctx, int8_t *face_periodic, int32_t *node_pairs);
 
 /* ParticleTypeList::add_particle_type (particle_type.hpp:58-84); defaults
  * 0: e- (-1,1), 1: e+ (1,1), 2: H+ (1,1837); at most 16 species. */

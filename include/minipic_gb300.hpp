@@ -127,7 +127,15 @@ class Mesh {  // mesh.hpp:59-267 (single rank; node/elem gids == lids)
     check(c->ctx, mpg_mesh_download(c->ctx, nodes_.data(), tets_.data(), nbrs_.data(), jinv_.data(), detj_.data(),
                                     normals_.data(), bnd_.data()),
           "mpg_mesh_download");
+    is_periodic = d.periodic != 0;
+    fper_.resize(4 * T);
+    pairs_.resize(N);
+    check(c->ctx, mpg_mesh_periodic_download(c->ctx, fper_.data(), pairs_.data()), "mpg_mesh_periodic_download");
   }
+  // mesh.hpp:149-154 (periodic meshes): +1 on both sides of an x face, and
+  // the x = lo node a ghost node of the x = hi plane stands for (-1 otherwise)
+  int elem_face_periodic(LO e, int f) const { return fper_[4 * e + f]; }
+  GO node_pairs(LO i) const { return pairs_[i]; }
   VECTOR nodes(LO i) const { return {nodes_[3 * i], nodes_[3 * i + 1], nodes_[3 * i + 2]}; }
   LO elem_to_node_lids(LO e, int i) const { return tets_[4 * e + i]; }
   GO elem_to_node_gids(LO e, int i) const { return tets_[4 * e + i]; }
@@ -191,7 +199,8 @@ class Mesh {  // mesh.hpp:59-267 (single rank; node/elem gids == lids)
   std::shared_ptr<Context> ctx_;
   mpg_mesh_desc desc_{};
   std::vector<double> nodes_, jinv_, detj_, normals_;
-  std::vector<int32_t> tets_, nbrs_;
+  std::vector<int32_t> tets_, nbrs_, pairs_;
+  std::vector<int8_t> fper_;
   std::vector<uint8_t> bnd_;
 };
 
@@ -337,9 +346,9 @@ class DataWarehouse {  // data_warehouse.hpp:51-90
   DataWarehouse(const DataWarehouse &) = delete;
   DataWarehouse &operator=(const DataWarehouse &) = delete;
 
-  // mesh.cpp:85-89 brick file: "nx ny nz mapping" -> five-tet split of [-1,1]^3
+  // mesh.cpp:85-89 brick file: "nx ny nz mapping" -> five-tet split of [-1,1]^3;
+  // periodic: x = -1 and x = 1 identified (mesh.cpp:61-76,178-189; even nx)
   void create_mesh(std::string &in_name, bool periodic = false) {
-    if (periodic) throw std::runtime_error("periodic meshes are not supported by this build");
     std::ifstream in(in_name.c_str());
     mpg_mesh_desc d{};
     int mapping = 0;
@@ -349,6 +358,7 @@ class DataWarehouse {  // data_warehouse.hpp:51-90
     d.lo = -1.0;
     d.hi = 1.0;
     d.mapping = mapping;
+    d.periodic = periodic ? 1 : 0;
     create_mesh(d);
   }
   void create_mesh(const mpg_mesh_desc &d) { mesh_ = std::make_unique<Mesh>(ctx_, d); }

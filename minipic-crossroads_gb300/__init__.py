@@ -27,7 +27,8 @@ DEAD = 0xFFFFFFFF
 EXPORTS = [
     "mpg_version", "mpg_device_count", "mpg_ctx_create", "mpg_ctx_destroy", "mpg_last_error", "mpg_set_timing",
     "mpg_timer",
-    "mpg_mesh_build", "mpg_mesh_sizes", "mpg_mesh_download", "mpg_species_set", "mpg_configure", "mpg_csr_sizes",
+    "mpg_mesh_build", "mpg_mesh_sizes", "mpg_mesh_download", "mpg_mesh_periodic_download", "mpg_species_set",
+    "mpg_configure", "mpg_csr_sizes",
     "mpg_csr_download", "mpg_particles_reserve", "mpg_fill_ref", "mpg_fill_uniform", "mpg_particles_upload",
     "mpg_particles_download", "mpg_particles_count", "mpg_mixed_download", "mpg_mixed_upload",
     "mpg_charge_download", "mpg_weight_charge", "mpg_solve", "mpg_weight_efield", "mpg_move", "mpg_step",
@@ -40,7 +41,8 @@ NOALLOC_MAX_N = 131072
 
 class MeshDesc(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("split", C.c_int), ("lo", C.c_double),
-                ("hi", C.c_double), ("mapping", C.c_int), ("jitter", C.c_double), ("seed", C.c_uint64)]
+                ("hi", C.c_double), ("mapping", C.c_int), ("jitter", C.c_double), ("seed", C.c_uint64),
+                ("periodic", C.c_int)]
 
 
 class Config(C.Structure):
@@ -115,6 +117,7 @@ def load():
         "mpg_mesh_build": ([P, C.POINTER(MeshDesc)], I),
         "mpg_mesh_sizes": ([P, C.POINTER(I64), C.POINTER(I64), C.POINTER(I64)], I),
         "mpg_mesh_download": ([P] * 8, I),
+        "mpg_mesh_periodic_download": ([P] * 3, I),
         "mpg_species_set": ([P, I, D, D], I),
         "mpg_configure": ([P, C.POINTER(Config)], I),
         "mpg_csr_sizes": ([P, C.POINTER(I64), C.POINTER(I64)], I),
@@ -221,9 +224,9 @@ class Ctx:
         self._ck(self.L.mpg_timer(self.h, 1, C.byref(ms)))
         return ms.value
 
-    def mesh(self, n, split=SPLIT_KUHN6, lo=0.0, hi=1.0, mapping=MAP_NONE, jitter=0.0, seed=0):
+    def mesh(self, n, split=SPLIT_KUHN6, lo=0.0, hi=1.0, mapping=MAP_NONE, jitter=0.0, seed=0, periodic=0):
         nx, ny, nz = (n, n, n) if np.isscalar(n) else n
-        d = MeshDesc(nx, ny, nz, split, lo, hi, mapping, jitter, seed)
+        d = MeshDesc(nx, ny, nz, split, lo, hi, mapping, jitter, seed, int(periodic))
         self._ck(self.L.mpg_mesh_build(self.h, C.byref(d)))
         T, N, nb = C.c_int64(), C.c_int64(), C.c_int64()
         self._ck(self.L.mpg_mesh_sizes(self.h, C.byref(T), C.byref(N), C.byref(nb)))
@@ -239,6 +242,13 @@ class Ctx:
                                                     ("nodes", "tets", "nbrs", "jinv", "detj", "normals",
                                                      "boundary")]))
         return out
+
+    def periodic_arrays(self):
+        """(face_periodic (T,4) int8, node_pairs (N,) int32) of a periodic mesh."""
+        fp = np.zeros((self.T, 4), np.int8)
+        pr = np.zeros(self.N, np.int32)
+        self._ck(self.L.mpg_mesh_periodic_download(self.h, ptr(fp), ptr(pr)))
+        return fp, pr
 
     def species(self, i, q, m):
         self._ck(self.L.mpg_species_set(self.h, i, q, m))

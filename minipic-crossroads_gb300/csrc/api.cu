@@ -74,6 +74,7 @@ struct mpg_ctx {
 
   std::vector<void *> allocs;  // device allocations owned by the ctx
   int64_t launches = 0;        // kernels launched by this ctx (cumulative)
+  int64_t csr_rows = 0;        // rows of the assembled CSR
 };
 
 static std::string g_last_create_error;
@@ -346,7 +347,7 @@ double ev_ms(mpg_ctx *c, int a, int b) {
 int phase_deposit_plain(mpg_ctx *c) {
   CK(cudaMemsetAsync(c->rhs, 0, sizeof(double) * c->dm.N, c->stream));
   launch_plain_deposit(c->stream, c->pp[c->cur], c->n, c->dm, c->sp, c->cfg.deposit, c->rhs);
-  launch_rhs_finish(c->stream, c->dm.N, c->rhs, c->bg, c->dm.bnd);
+  launch_rhs_finish(c->stream, c->dm, c->rhs, c->bg);
   c->launches += 2;
   CKL();
   return MPG_OK;
@@ -360,7 +361,7 @@ int phase_deposit_mixed(mpg_ctx *c) {
     c->acc_valid = true;
     c->launches += 1;
   }
-  launch_mixed_convert(c->stream, c->dm.N, c->acc, c->quantum, c->bg, c->dm.bnd, c->rhs);
+  launch_mixed_convert(c->stream, c->dm, c->acc, c->quantum, c->bg, c->rhs);
   c->launches += 1;
   CKL();
   return MPG_OK;
@@ -407,6 +408,11 @@ int phase_solve(mpg_ctx *c) {
                  : run_cg64_dia(c->stream, c->dia, c->rhs, c->phi, c->cfg.tol, c->cfg.max_iter, c->cg, c->d_stats);
     c->launches += 1;
     if (rc) return fail(c, rc, "CG launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+    if (c->dm.fper) {
+      // the symmetric periodic system leaves the ghost plane out
+      launch_periodic_copy(c->stream, c->dm, c->phi);
+      c->launches += 1;
+    }
     if (c->phi_hist < 3) ++c->phi_hist;
     return MPG_OK;
   }
@@ -419,6 +425,9 @@ int phase_solve(mpg_ctx *c) {
   // 2 SpMV + 6 dot pairs + 6 updates per iteration, roughly
   c->launches += 4 + (int64_t)it * 20;
   if (rc == MPG_ERR_CUDA) return fail(c, rc, "BiCGStab: %s", cudaGetErrorString(cudaGetLastError()));
+  // the reference system holds phi_ghost = phi_pair only to the solver
+  // tolerance; the ghost plane takes the pair values exactly
+  launch_periodic_copy(c->stream, c->dm, c->phi);
   // record into the device stats so both solver kinds report the same way
   DevStats tmp;
   CK(cudaMemcpyAsync(&tmp, c->d_stats, sizeof(DevStats), cudaMemcpyDeviceToHost, c->stream));
@@ -540,6 +549,15 @@ int upload_mesh(mpg_ctx *c) {
   DevMesh &d = c->dm;
   d.T = h.T;
   d.N = h.N;
+  d.nsolve = h.nsolve;
+  d.plane = (int64_t)(h.d.ny + 1) * (h.d.nz + 1);
+  d.xflip = h.d.lo + h.d.hi;
+  d.xshift = (h.d.periodic && h.d.mapping == MPG_MAP_JITTER) ? h.d.hi - h.d.lo : 0.0;
+  d.fper = nullptr;
+  if (h.d.periodic) {
+    TRY(dalloc(c, &d.fper, 4 * h.T));
+    CK(cudaMemcpyAsync(d.fper, h.fper.data(), 4 * h.T, cudaMemcpyHostToDevice, c->stream));
+  }
   TRY(dalloc(c, &d.tets, h.T));
   TRY(dalloc(c, &d.nbrs, h.T));
   TRY(dalloc(c, &d.jinv, 9 * h.T));
@@ -575,6 +593,7 @@ int upload_mesh(mpg_ctx *c) {
 
 void free_mesh(mpg_ctx *c) {
   DevMesh &d = c->dm;
+  dfree(c, d.fper);
   dfree(c, d.tets);
   dfree(c, d.nbrs);
   dfree(c, d.jinv);
@@ -767,6 +786,23 @@ int mpg_mesh_download(mpg_ctx *c, double *nodes, int32_t *tets, int32_t *nbrs, d
   return MPG_OK;
 }
 
+int mpg_mesh_periodic_download(mpg_ctx *c, int8_t *face_periodic, int32_t *node_pairs) {
+  ENTER(c);
+  if (!c->has_mesh) return fail(c, MPG_ERR_STATE, "no mesh");
+  const HostMesh &h = c->hm;
+  // the face flags the device walk reads; the pairs live on the host only
+  if (face_periodic) {
+    if (c->dm.fper) {
+      CK(cudaMemcpyAsync(face_periodic, c->dm.fper, 4 * c->dm.T, cudaMemcpyDeviceToHost, c->stream));
+      CK(cudaStreamSynchronize(c->stream));
+    } else {
+      memset(face_periodic, 0, 4 * c->dm.T);
+    }
+  }
+  if (node_pairs) memcpy(node_pairs, h.pair.data(), sizeof(int32_t) * h.pair.size());
+  return MPG_OK;
+}
+
 int mpg_species_set(mpg_ctx *c, int i, double q, double m) {
   if (!c) return MPG_ERR_ARG;
   if (i < 0 || i >= MPG_MAX_SPECIES) return fail(c, MPG_ERR_ARG, "species index %d out of range", i);
@@ -799,6 +835,25 @@ int mpg_configure(mpg_ctx *c, const mpg_config *cfg) {
   // the mixed form always solves the symmetric system with refined CG
   const int mode = (cfg->precision == MPG_MIXED || cfg->solver == MPG_SOLVER_CG) ? 1 : 0;
   const int64_t N = c->hm.N, T = c->hm.T;
+  // rows of the assembled system: all nodes, or (symmetric form of a periodic
+  // mesh) the nodes of the x < hi planes, the ghost plane being last in order
+  const int64_t R = mode == 1 ? c->hm.nsolve : N;
+  const bool per = c->hm.d.periodic != 0;
+  // periodic stencils wrap around in x: an offset or index modulo R
+  auto wrap_off = [&](int64_t o) -> int64_t {
+    if (per) {
+      if (o > R / 2) o -= R;
+      else if (o < -R / 2) o += R;
+    }
+    return o;
+  };
+  auto wrap_idx = [&](int64_t j) -> int64_t {
+    if (per) {
+      if (j < 0) j += R;
+      else if (j >= R) j -= R;
+    }
+    return j;
+  };
   if (c->csr_mode != mode) {
     dfree(c, c->rowptr);
     dfree(c, c->col);
@@ -808,12 +863,13 @@ int mpg_configure(mpg_ctx *c, const mpg_config *cfg) {
     std::vector<double> val;
     host_csr_assemble(c->hm, mode, rp, col, val);
     c->nnz = (int64_t)val.size();
-    TRY(dalloc(c, &c->rowptr, N + 1));
+    c->csr_rows = R;
+    TRY(dalloc(c, &c->rowptr, R + 1));
     TRY(dalloc(c, &c->col, c->nnz));
     TRY(dalloc(c, &c->val, c->nnz));
     TRY(dalloc(c, &c->val32, c->nnz));
     std::vector<float> v32(val.begin(), val.end());
-    CK(cudaMemcpyAsync(c->rowptr, rp.data(), sizeof(int32_t) * (N + 1), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->rowptr, rp.data(), sizeof(int32_t) * (R + 1), cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(c->col, col.data(), sizeof(int32_t) * c->nnz, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(c->val, val.data(), sizeof(double) * c->nnz, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(c->val32, v32.data(), sizeof(float) * c->nnz, cudaMemcpyHostToDevice, c->stream));
@@ -825,29 +881,31 @@ int mpg_configure(mpg_ctx *c, const mpg_config *cfg) {
     if (mode == 1) {
       // diagonal offsets present in the interior rows, in column order
       std::vector<int64_t> offs;
-      for (int64_t r = 0; r < N; ++r) {
+      for (int64_t r = 0; r < R; ++r) {
         if (c->hm.bnd[r]) continue;
-        for (int32_t k = rp[r]; k < rp[r + 1]; ++k) offs.push_back((int64_t)col[k] - r);
+        for (int32_t k = rp[r]; k < rp[r + 1]; ++k) offs.push_back(wrap_off((int64_t)col[k] - r));
       }
       std::sort(offs.begin(), offs.end());
       offs.erase(std::unique(offs.begin(), offs.end()), offs.end());
       if (offs.size() > 27) return fail(c, MPG_ERR_MESH, "matrix is not a structured stencil (%zu offsets)", offs.size());
       // pad to the kernel's diagonal count (15 or 27) with zero diagonals at offset 0
       const int nd = offs.size() <= 15 ? 15 : 27;
-      std::vector<double> d64((size_t)nd * N, 0.0);
-      for (int64_t r = 0; r < N; ++r) {
+      std::vector<double> d64((size_t)nd * R, 0.0);
+      for (int64_t r = 0; r < R; ++r) {
         if (c->hm.bnd[r]) continue;
         for (int32_t k = rp[r]; k < rp[r + 1]; ++k) {
-          const int d = (int)(std::lower_bound(offs.begin(), offs.end(), (int64_t)col[k] - r) - offs.begin());
-          d64[(size_t)d * N + r] = val[k];
+          const int d =
+              (int)(std::lower_bound(offs.begin(), offs.end(), wrap_off((int64_t)col[k] - r)) - offs.begin());
+          d64[(size_t)d * R + r] = val[k];
         }
       }
       std::vector<float> d32(d64.begin(), d64.end());
-      c->dia.n = N;
+      c->dia.n = R;
+      c->dia.nwrap = per ? R : 0;
       c->dia.ndiag = nd;
       for (int d = 0; d < nd; ++d) c->dia.off[d] = d < (int)offs.size() ? (int)offs[d] : 0;
-      TRY(dalloc(c, &c->dia.val64, (int64_t)nd * N));
-      TRY(dalloc(c, &c->dia.val32, (int64_t)nd * N));
+      TRY(dalloc(c, &c->dia.val64, (int64_t)nd * R));
+      TRY(dalloc(c, &c->dia.val32, (int64_t)nd * R));
       CK(cudaMemcpyAsync(c->dia.val64, d64.data(), sizeof(double) * d64.size(), cudaMemcpyHostToDevice, c->stream));
       CK(cudaMemcpyAsync(c->dia.val32, d32.data(), sizeof(float) * d32.size(), cudaMemcpyHostToDevice, c->stream));
       c->dia.bnd = c->dm.bnd;
@@ -864,11 +922,11 @@ int mpg_configure(mpg_ctx *c, const mpg_config *cfg) {
         std::vector<double> ref(nd, 0.0);
         std::vector<char> have(nd, 0);
         bool uniform = amax > 0.0;
-        for (int64_t r = 0; r < N && uniform; ++r) {
+        for (int64_t r = 0; r < R && uniform; ++r) {
           if (c->hm.bnd[r]) continue;
           for (int d = 0; d < (int)offs.size(); ++d) {
-            if (c->hm.bnd[r + offs[d]]) continue;
-            const double v = d64[(size_t)d * N + r];
+            if (c->hm.bnd[wrap_idx(r + offs[d])]) continue;
+            const double v = d64[(size_t)d * R + r];
             if (!have[d]) {
               ref[d] = v;
               have[d] = 1;
@@ -887,20 +945,20 @@ int mpg_configure(mpg_ctx *c, const mpg_config *cfg) {
       const char *jenv = getenv("MPG_CG_JACOBI");
       const int center = (int)(std::lower_bound(offs.begin(), offs.end(), (int64_t)0) - offs.begin());
       if (!c->dia.constant && !(jenv && atoi(jenv) == 0) && center < (int)offs.size() && offs[center] == 0) {
-        std::vector<double> dis(N, 1.0);
-        for (int64_t r = 0; r < N; ++r) {
-          const double dr = d64[(size_t)center * N + r];
+        std::vector<double> dis(R, 1.0);
+        for (int64_t r = 0; r < R; ++r) {
+          const double dr = d64[(size_t)center * R + r];
           if (!c->hm.bnd[r] && dr > 0.0) dis[r] = 1.0 / std::sqrt(dr);
         }
-        for (int64_t r = 0; r < N; ++r) {
+        for (int64_t r = 0; r < R; ++r) {
           if (c->hm.bnd[r]) continue;
           for (int d = 0; d < (int)offs.size(); ++d) {
-            const double v = d64[(size_t)d * N + r];
-            if (v != 0.0) d32[(size_t)d * N + r] = (float)(v * dis[r] * dis[r + offs[d]]);
+            const double v = d64[(size_t)d * R + r];
+            if (v != 0.0) d32[(size_t)d * R + r] = (float)(v * dis[r] * dis[wrap_idx(r + offs[d])]);
           }
         }
-        TRY(dalloc(c, &c->dia.dis, N));
-        CK(cudaMemcpyAsync(c->dia.dis, dis.data(), sizeof(double) * N, cudaMemcpyHostToDevice, c->stream));
+        TRY(dalloc(c, &c->dia.dis, R));
+        CK(cudaMemcpyAsync(c->dia.dis, dis.data(), sizeof(double) * R, cudaMemcpyHostToDevice, c->stream));
         CK(cudaMemcpyAsync(c->dia.val32, d32.data(), sizeof(float) * d32.size(), cudaMemcpyHostToDevice,
                            c->stream));
       }
@@ -934,7 +992,7 @@ int mpg_configure(mpg_ctx *c, const mpg_config *cfg) {
 int mpg_csr_sizes(mpg_ctx *c, int64_t *rows, int64_t *nnz) {
   if (!c) return MPG_ERR_ARG;
   if (!c->configured) return fail(c, MPG_ERR_STATE, "not configured");
-  if (rows) *rows = c->hm.N;
+  if (rows) *rows = c->csr_rows;
   if (nnz) *nnz = c->nnz;
   return MPG_OK;
 }
@@ -943,7 +1001,7 @@ int mpg_csr_download(mpg_ctx *c, int32_t *rowptr, int32_t *col, double *val) {
   ENTER(c);
   if (!c->configured) return fail(c, MPG_ERR_STATE, "not configured");
   if (rowptr)
-    CK(cudaMemcpyAsync(rowptr, c->rowptr, sizeof(int32_t) * (c->hm.N + 1), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(rowptr, c->rowptr, sizeof(int32_t) * (c->csr_rows + 1), cudaMemcpyDeviceToHost, c->stream));
   if (col) CK(cudaMemcpyAsync(col, c->col, sizeof(int32_t) * c->nnz, cudaMemcpyDeviceToHost, c->stream));
   if (val) CK(cudaMemcpyAsync(val, c->val, sizeof(double) * c->nnz, cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));

@@ -199,11 +199,18 @@ __global__ void __launch_bounds__(kThreads) k_plain_deposit(PlainParts P, int64_
   }
 }
 
+// Periodic meshes (plane > 0): charge deposited on a ghost node of the x = hi
+// plane belongs to its pair on the x = lo plane (PIC.cpp:132-134); the pair's
+// thread folds it in and clears the ghost plane.
 __global__ void k_rhs_finish(int64_t N, double *__restrict__ rhs, const double *__restrict__ bg,
-                             const uint8_t *__restrict__ bnd) {
+                             const uint8_t *__restrict__ bnd, int64_t nsolve, int64_t plane) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= N) return;
+  if (i >= N || (plane && i >= nsolve)) return;
   double r = rhs[i];
+  if (plane && i < plane) {
+    r += rhs[nsolve + i];
+    rhs[nsolve + i] = 0.0;
+  }
   if (bg) r += bg[i];
   if (bnd[i]) r = 0.0;  // PIC.cpp:155-158
   rhs[i] = r;
@@ -270,6 +277,15 @@ __device__ __forceinline__ double plain_intersect(const DevMesh &M, int &e, doub
     const int4 nb4 = M.nbrs[e];
     const int nb = face == 0 ? nb4.x : face == 1 ? nb4.y : face == 2 ? nb4.z : nb4.w;
     if (nb >= 0) {
+      // a periodic face wraps x to the other side of the box: lo + hi - x on
+      // the reference's mirror-image meshes (particle_move.hpp:190-191 writes
+      // x = -x on its [-1,1] box), a shift by the box length on jittered ones
+      if (M.fper && M.fper[4 * (int64_t)e + face]) {
+        if (M.xshift != 0.0)
+          x[0] = (x[0] + x[0] > M.xflip) ? x[0] - M.xshift : x[0] + M.xshift;
+        else
+          x[0] = M.xflip - x[0];
+      }
       e = nb;
       const int n0 = M.tets[e].x;
       const double delta[3] = {x[0] - M.nodes[3 * n0], x[1] - M.nodes[3 * n0 + 1], x[2] - M.nodes[3 * n0 + 2]};
@@ -504,13 +520,20 @@ __global__ void __launch_bounds__(kThreads) k_mixed_deposit(MixedParts P, int64_
   deposit_fixed_warp(acc, tets, key, b1, b2, b3, Q);
 }
 
+// Periodic meshes (plane > 0): the ghost plane's quanta are folded into
+// their pairs by the pair's thread (integer sums: exact, order free).
 __global__ void k_mixed_convert(int64_t N, unsigned long long *__restrict__ acc, double quantum,
                                 const double *__restrict__ bg, const uint8_t *__restrict__ bnd,
-                                double *__restrict__ rhs) {
+                                double *__restrict__ rhs, int64_t nsolve, int64_t plane) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= N) return;
-  const long long a = (long long)acc[i];
+  if (i >= N || (plane && i >= nsolve)) return;
+  long long a = (long long)acc[i];
   acc[i] = 0ull;
+  if (plane && i < plane) {
+    a += (long long)acc[nsolve + i];
+    acc[nsolve + i] = 0ull;
+    rhs[nsolve + i] = 0.0;
+  }
   double r = -((double)a * quantum);
   if (bg) r += bg[i];
   if (bnd[i]) r = 0.0;
@@ -936,8 +959,15 @@ void launch_plain_deposit(cudaStream_t s, const PlainParts &P, int64_t n, const 
   if (n <= 0) return;
   k_plain_deposit<<<grid_for(n), kThreads, 0, s>>>(P, n, M.tets, M.detj, S, mode, rhs);
 }
-void launch_rhs_finish(cudaStream_t s, int64_t N, double *rhs, const double *bg, const uint8_t *bnd) {
-  k_rhs_finish<<<grid_for(N), kThreads, 0, s>>>(N, rhs, bg, bnd);
+void launch_rhs_finish(cudaStream_t s, const DevMesh &M, double *rhs, const double *bg) {
+  k_rhs_finish<<<grid_for(M.N), kThreads, 0, s>>>(M.N, rhs, bg, M.bnd, M.nsolve, M.fper ? M.plane : 0);
+}
+__global__ void k_periodic_copy(double *__restrict__ phi, int64_t nsolve, int64_t plane) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < plane) phi[nsolve + i] = phi[i];
+}
+void launch_periodic_copy(cudaStream_t s, const DevMesh &M, double *phi) {
+  if (M.fper && M.plane > 0) k_periodic_copy<<<grid_for(M.plane), kThreads, 0, s>>>(phi, M.nsolve, M.plane);
 }
 void launch_efield_plain(cudaStream_t s, const DevMesh &M, const double *phi, double *Etet) {
   k_efield_plain<<<grid_for(M.T), kThreads, 0, s>>>(M.T, M.tets, M.grad, phi, Etet);
@@ -960,9 +990,10 @@ void launch_mixed_deposit(cudaStream_t s, const MixedParts &P, int64_t n, const 
   if (n <= 0) return;
   k_mixed_deposit<<<grid_for(n), kThreads, 0, s>>>(P, n, M.tets, S, acc);
 }
-void launch_mixed_convert(cudaStream_t s, int64_t N, unsigned long long *acc, double quantum, const double *bg,
-                          const uint8_t *bnd, double *rhs) {
-  k_mixed_convert<<<grid_for(N), kThreads, 0, s>>>(N, acc, quantum, bg, bnd, rhs);
+void launch_mixed_convert(cudaStream_t s, const DevMesh &M, unsigned long long *acc, double quantum, const double *bg,
+                          double *rhs) {
+  k_mixed_convert<<<grid_for(M.N), kThreads, 0, s>>>(M.N, acc, quantum, bg, M.bnd, rhs, M.nsolve,
+                                                     M.fper ? M.plane : 0);
 }
 void launch_efield_mixed(cudaStream_t s, const DevMesh &M, const double *phi) {
   k_efield_mixed<<<grid_for(M.T), kThreads, 0, s>>>(M.T, M.tets, M.mrec, phi);

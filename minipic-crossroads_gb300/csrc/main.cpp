@@ -49,7 +49,7 @@ int main(int argc, char **argv) {
     else if (!strcmp(argv[i], "--help") || !strcmp(argv[i], "-h")) {
       std::cout << "usage: " << argv[0]
                 << " [--nparts=N] [--mesh=file] [--dt=x] [--tfinal=x] [--output=k] [--kill-particles=0|1]"
-                   " [--problem=none] [--density=x] [--dump_mesh=0|1] [--steps=N] [--precision=plain|mixed]"
+                   " [--problem=none|two-stream] [--density=x] [--dump_mesh=0|1] [--steps=N] [--precision=plain|mixed]"
                    " [--solver=bicgstab|cg] [--deposit=quarter|linear] [--tol=x]\n";
       return 0;
     } else {
@@ -57,13 +57,10 @@ int main(int argc, char **argv) {
       return 2;
     }
   }
-  if (problem == "two-stream") {
-    std::cerr << "the periodic two-stream problem is not supported by this build\n";
-    return 2;
-  }
+  const bool two_stream = problem == "two-stream";
   try {
     DataWarehouse data;
-    data.create_mesh(meshfile, false);
+    data.create_mesh(meshfile, two_stream);  // main.cpp:89-92: periodic for the two-stream problem
     mpg_config &cfg = data.config();
     cfg.precision = precision == "mixed" ? MPG_MIXED : MPG_PLAIN;
     cfg.solver = solver == "cg" ? MPG_SOLVER_CG : MPG_SOLVER_BICGSTAB;
@@ -75,7 +72,16 @@ int main(int argc, char **argv) {
     data.create_ES();
     data.set_kill_particles_on_wall_impact(part_kill == 1);
     auto t0 = std::chrono::steady_clock::now();
-    {
+    if (two_stream) {
+      // main.cpp:98-106: two counter-streaming electron beams with a sinusoidal
+      // velocity perturbation (temp < 0, particle_fill.hpp:106-110) over ions at rest
+      VECTOR v{0.5, 0.0, 0.0};
+      const FLOAT temp = -.05;
+      ParticleFill fill1a(data, num_particles_per_element / 2, 0, density / 2, v, temp);
+      v[0] *= -1;
+      ParticleFill fill1b(data, num_particles_per_element / 2, 0, density / 2, v, temp);
+      ParticleFill fill2(data, num_particles_per_element, 2, density, VECTOR{0, 0, 0}, 0);
+    } else {
       ParticleFill fill1(data, num_particles_per_element, 0, density);
       ParticleFill fill2(data, num_particles_per_element, 1, density);
     }

@@ -65,6 +65,15 @@ int host_mesh_generate(const mpg_mesh_desc &d, HostMesh &m, std::string &err) {
     err = "mesh: hi must exceed lo";
     return MPG_ERR_ARG;
   }
+  if (d.periodic && d.nx < 2) {
+    err = "mesh: a periodic mesh needs nx >= 2";
+    return MPG_ERR_ARG;
+  }
+  if (d.periodic && d.split == MPG_SPLIT_REF5 && d.nx % 2 == 1) {
+    // mesh.cpp:91-94: the alternating five-tet split only matches across x for even nx
+    err = "mesh: a periodic five-tet mesh needs an even nx";
+    return MPG_ERR_ARG;
+  }
   const int64_t nx = d.nx, ny = d.ny, nz = d.nz, per = d.split;
   const int64_t N = (nx + 1) * (ny + 1) * (nz + 1), T = per * nx * ny * nz;
   if (N >= (1LL << 31) || T >= (1LL << 31)) {
@@ -87,11 +96,18 @@ int host_mesh_generate(const mpg_mesh_desc &d, HostMesh &m, std::string &err) {
         m.nodes[3 * g + 0] = d.lo + i * dx;
         m.nodes[3 * g + 1] = d.lo + j * dy;
         m.nodes[3 * g + 2] = d.lo + k * dz;
-        m.bnd[g] = (i == 0 || i == nx || j == 0 || j == ny || k == 0 || k == nz) ? 1 : 0;
+        // a periodic mesh has no x walls (mesh.cpp:407-412)
+        m.bnd[g] = ((!d.periodic && (i == 0 || i == nx)) || j == 0 || j == ny || k == 0 || k == nz) ? 1 : 0;
       }
   int64_t nb = 0;
   for (int64_t g = 0; g < N; ++g) nb += m.bnd[g];
   m.n_bnodes = nb;
+  // periodic node pairs (mesh.cpp:178-189): interior nodes of the x = hi plane
+  m.pair.assign(N, -1);
+  if (d.periodic)
+    for (int64_t j = 1; j < ny; ++j)
+      for (int64_t k = 1; k < nz; ++k) m.pair[nx * si + j * sj + k] = (int32_t)(j * sj + k);
+  m.nsolve = d.periodic ? N - si : N;
 
   // ---- tets, hex by hex in (i, j, k) order
   m.tets.resize(T * 4);
@@ -114,8 +130,18 @@ int host_mesh_generate(const mpg_mesh_desc &d, HostMesh &m, std::string &err) {
           for (int q = 0; q < 4; ++q) m.tets[4 * (h * per + t) + q] = c[tab[t][q]];
       }
 
-  // ---- face neighbours, per hex
+  // ---- face neighbours, per hex.  On a periodic mesh a face on the x = hi
+  // plane is renamed onto the x = lo plane (Mesh::periodic_face,
+  // mesh.cpp:61-76), so the hexes at the two ends of x are neighbours.
   m.nbrs.assign(T * 4, -1);
+  m.fper.assign(T * 4, 0);
+  const int32_t ghost_shift = (int32_t)(nx * si);
+  auto face_key = [&](const int32_t *g3, int32_t key[3]) {
+    bool hi_plane = d.periodic != 0;
+    for (int q = 0; q < 3; ++q) hi_plane = hi_plane && g3[q] / si == nx;
+    for (int q = 0; q < 3; ++q) key[q] = hi_plane ? g3[q] - ghost_shift : g3[q];
+    std::sort(key, key + 3);
+  };
   int bad = 0;
 #pragma omp parallel for schedule(static) reduction(+ : bad)
   for (int64_t t = 0; t < T; ++t) {
@@ -123,11 +149,11 @@ int host_mesh_generate(const mpg_mesh_desc &d, HostMesh &m, std::string &err) {
     const int64_t hi_ = h / (ny * nz), hj = (h / nz) % ny, hk = h % nz;
     const int64_t corner = hi_ * si + hj * sj + hk;
     for (int f = 0; f < 4; ++f) {
-      int32_t key[3];
+      int32_t key[3], g3[3];
       int all[3][2] = {{1, 1}, {1, 1}, {1, 1}};  // [axis][offset 0/1] all nodes share it
       for (int q = 0; q < 3; ++q) {
         int32_t g = m.tets[4 * t + kFaceNodes[f][q]];
-        key[q] = g;
+        g3[q] = g;
         int64_t r = g - corner;
         int di = (int)(r / si), dj = (int)((r % si) / sj), dk = (int)(r % sj);
         int off[3] = {di, dj, dk};
@@ -136,17 +162,34 @@ int host_mesh_generate(const mpg_mesh_desc &d, HostMesh &m, std::string &err) {
           all[a][1] &= (off[a] == 1);
         }
       }
-      std::sort(key, key + 3);
+      face_key(g3, key);
       int64_t nh[3] = {hi_, hj, hk};
       const int64_t lim[3] = {nx, ny, nz};
       bool wall = false;
       for (int a = 0; a < 3; ++a) {
+        const bool wrap = a == 0 && d.periodic;
         if (all[a][0]) {
-          if (nh[a] == 0) wall = true;
-          else nh[a] -= 1;
+          if (nh[a] == 0) {
+            if (wrap) {
+              nh[a] = lim[a] - 1;
+              m.fper[4 * t + f] = 1;  // mesh.cpp:369-378
+            } else {
+              wall = true;
+            }
+          } else {
+            nh[a] -= 1;
+          }
         } else if (all[a][1]) {
-          if (nh[a] == lim[a] - 1) wall = true;
-          else nh[a] += 1;
+          if (nh[a] == lim[a] - 1) {
+            if (wrap) {
+              nh[a] = 0;
+              m.fper[4 * t + f] = 1;
+            } else {
+              wall = true;
+            }
+          } else {
+            nh[a] += 1;
+          }
         }
       }
       if (wall) {
@@ -158,9 +201,10 @@ int host_mesh_generate(const mpg_mesh_desc &d, HostMesh &m, std::string &err) {
       for (int64_t t2 = h2 * per; t2 < (h2 + 1) * per && found < 0; ++t2) {
         if (t2 == t) continue;
         for (int f2 = 0; f2 < 4; ++f2) {
-          int32_t k2[3] = {m.tets[4 * t2 + kFaceNodes[f2][0]], m.tets[4 * t2 + kFaceNodes[f2][1]],
-                           m.tets[4 * t2 + kFaceNodes[f2][2]]};
-          std::sort(k2, k2 + 3);
+          const int32_t c3[3] = {m.tets[4 * t2 + kFaceNodes[f2][0]], m.tets[4 * t2 + kFaceNodes[f2][1]],
+                                 m.tets[4 * t2 + kFaceNodes[f2][2]]};
+          int32_t k2[3];
+          face_key(c3, k2);
           if (k2[0] == key[0] && k2[1] == key[1] && k2[2] == key[2]) {
             found = (int32_t)t2;
             break;
@@ -185,8 +229,11 @@ int host_mesh_generate(const mpg_mesh_desc &d, HostMesh &m, std::string &err) {
 #pragma omp parallel for schedule(static)
     for (int64_t g = 0; g < N; ++g) {
       if (m.bnd[g]) continue;
+      // a ghost node moves with its pair: the x = hi face is the x = lo face
+      // translated by the box length (the periodic crossing is a translation)
+      const uint64_t src = (uint64_t)host_pmap(m, (int32_t)g);
       for (int q = 0; q < 3; ++q) {
-        double u = unit53(mpg_mix64(base + mpg_mix64(3 * (uint64_t)g + q)));
+        double u = unit53(mpg_mix64(base + mpg_mix64(3 * src + q)));
         m.nodes[3 * g + q] += (2.0 * u - 1.0) * d.jitter * h3[q];
       }
     }
@@ -246,6 +293,7 @@ int host_mesh_generate(const mpg_mesh_desc &d, HostMesh &m, std::string &err) {
   }
 
   // ---- neighbour + vertex permutation per face, indexed by opposite vertex
+  auto xmap = [&](int32_t g) -> int32_t { return (d.periodic && g / si == nx) ? g - ghost_shift : g; };
   m.nbr_opp.resize(T * 4);
 #pragma omp parallel for schedule(static)
   for (int64_t t = 0; t < T; ++t)
@@ -259,9 +307,13 @@ int host_mesh_generate(const mpg_mesh_desc &d, HostMesh &m, std::string &err) {
       int used = 0;
       for (int j = 0; j < 4; ++j) {
         if (j == k) continue;
-        int32_t g = m.tets[4 * t + j];
+        // across a periodic face a vertex of the x = hi plane is the vertex
+        // with the same (j, k) on the x = lo plane -- every such vertex, the
+        // ones on the y/z walls included (Mesh::periodic_face, mesh.cpp:61-76),
+        // not only the ES node pairs
+        const int32_t g = xmap(m.tets[4 * t + j]);
         int pos = 0;
-        while (m.tets[4 * (int64_t)b + pos] != g) ++pos;
+        while (pos < 3 && xmap(m.tets[4 * (int64_t)b + pos]) != g) ++pos;
         perm |= (uint32_t)pos << (2 * j);
         used |= 1 << pos;
       }
@@ -273,8 +325,73 @@ int host_mesh_generate(const mpg_mesh_desc &d, HostMesh &m, std::string &err) {
   return MPG_OK;
 }
 
+// Periodic meshes: rows and columns go through the node pairs (ES.cpp:93-95,
+// 168-176).  Mode 0 keeps all N rows, a ghost row being -phi_ghost + phi_pair
+// = 0 (ES.cpp:183-189); mode 1 keeps the nsolve rows of the x < hi planes.
+// Columns sorted per row, element-order sums, as the oracle.
+static void csr_assemble_periodic(const HostMesh &m, int mode, std::vector<int32_t> &rowptr,
+                                  std::vector<int32_t> &col, std::vector<double> &val) {
+  const int64_t T = m.T;
+  const int64_t R = mode == 1 ? m.nsolve : m.N;
+  std::vector<std::vector<int32_t>> cols(R);
+  for (int64_t t = 0; t < T; ++t)
+    for (int a = 0; a < 4; ++a) {
+      const int32_t r = host_pmap(m, m.tets[4 * t + a]);
+      if (m.bnd[r]) continue;
+      for (int b = 0; b < 4; ++b) {
+        const int32_t c = host_pmap(m, m.tets[4 * t + b]);
+        if (mode == 1 && m.bnd[c]) continue;
+        cols[r].push_back(c);
+      }
+    }
+  rowptr.assign(R + 1, 0);
+  for (int64_t r = 0; r < R; ++r) {
+    if (m.bnd[r]) {
+      cols[r].assign(1, (int32_t)r);
+    } else if (m.pair[r] >= 0) {
+      cols[r] = {m.pair[r], (int32_t)r};
+    } else {
+      std::sort(cols[r].begin(), cols[r].end());
+      cols[r].erase(std::unique(cols[r].begin(), cols[r].end()), cols[r].end());
+    }
+    rowptr[r + 1] = rowptr[r] + (int32_t)cols[r].size();
+  }
+  col.resize(rowptr[R]);
+  val.assign(rowptr[R], 0.0);
+  for (int64_t r = 0; r < R; ++r) std::copy(cols[r].begin(), cols[r].end(), col.begin() + rowptr[r]);
+  const double wcub = 1.0 / 24.0;
+  for (int64_t t = 0; t < T; ++t) {
+    const double *G = &m.grad[12 * t];
+    const double wm = m.detj[t] * wcub;
+    for (int a = 0; a < 4; ++a) {
+      const int32_t r = host_pmap(m, m.tets[4 * t + a]);
+      if (m.bnd[r]) continue;
+      for (int b = 0; b < 4; ++b) {
+        const int32_t c = host_pmap(m, m.tets[4 * t + b]);
+        if (mode == 1 && m.bnd[c]) continue;
+        double k = 0.0;
+        for (int cub = 0; cub < 4; ++cub)
+          for (int dd = 0; dd < 3; ++dd) k += G[3 * a + dd] * (wm * G[3 * b + dd]);
+        const int32_t *p = std::lower_bound(&col[rowptr[r]], &col[0] + rowptr[r + 1], c);
+        val[p - col.data()] += k;
+      }
+    }
+  }
+  for (int64_t r = 0; r < R; ++r) {
+    if (m.bnd[r]) val[rowptr[r]] = 1.0;
+    if (m.pair[r] >= 0) {
+      val[rowptr[r]] = 1.0;
+      val[rowptr[r] + 1] = -1.0;
+    }
+  }
+}
+
 void host_csr_assemble(const HostMesh &m, int mode, std::vector<int32_t> &rowptr, std::vector<int32_t> &col,
                        std::vector<double> &val) {
+  if (m.d.periodic) {
+    csr_assemble_periodic(m, mode, rowptr, col, val);
+    return;
+  }
   const int64_t N = m.N, T = m.T;
   const int64_t nz = m.d.nz, ny = m.d.ny;
   const int64_t sj = nz + 1, si = (ny + 1) * (nz + 1);
@@ -334,7 +451,7 @@ void host_background(const HostMesh &m, double rho_bg, std::vector<double> &bg) 
   bg.assign(m.N, 0.0);
   for (int64_t t = 0; t < m.T; ++t) {
     const double q = -(rho_bg * (m.detj[t] / 6.0)) * 0.25;
-    for (int a = 0; a < 4; ++a) bg[m.tets[4 * t + a]] += q;
+    for (int a = 0; a < 4; ++a) bg[host_pmap(m, m.tets[4 * t + a])] += q;
   }
   for (int64_t i = 0; i < m.N; ++i)
     if (m.bnd[i]) bg[i] = 0.0;

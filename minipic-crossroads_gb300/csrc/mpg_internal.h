@@ -21,12 +21,19 @@ struct HostMesh {
   std::vector<double> normals;  // T*12
   std::vector<double> grad;     // T*12, grad N_i (x,y,z) per local node
   std::vector<uint8_t> bnd;     // N
+  std::vector<int8_t> fper;     // T*4, reference face order: +1 on both sides of an x = lo/hi face (periodic)
+  std::vector<int32_t> pair;    // N: the x = lo node a periodic ghost node stands for, -1 otherwise
+  int64_t nsolve = 0;           // unknowns of the symmetric system (N, or N minus the ghost plane)
 };
+// a periodic ghost node stands for its pair (ES.cpp:93-95, PIC.cpp:132-134)
+static inline int32_t host_pmap(const HostMesh &m, int32_t g) { return m.pair[g] >= 0 ? m.pair[g] : g; }
 
 // Returns 0 or an MPG_ERR_* code with err filled.
 int host_mesh_generate(const mpg_mesh_desc &d, HostMesh &m, std::string &err);
 // mode 0 = reference (identity Dirichlet rows, boundary columns kept),
 // mode 1 = symmetric (boundary columns dropped).
+// mode 1 on a periodic mesh assembles the nsolve rows of the x < hi planes (the
+// ghost plane is the last plane in node order and is copied after a solve)
 void host_csr_assemble(const HostMesh &m, int mode, std::vector<int32_t> &rowptr, std::vector<int32_t> &col,
                        std::vector<double> &val);
 void host_background(const HostMesh &m, double rho_bg, std::vector<double> &bg);

@@ -34,6 +34,11 @@ struct DevMesh {
   double *grad = nullptr;    // T*12
   double *nodes = nullptr;   // N*3
   uint8_t *bnd = nullptr;    // N
+  int8_t *fper = nullptr;    // T*4: periodic face flags (reference face order), null if not periodic
+  double xflip = 0.0;        // lo + hi: a periodic crossing maps x to xflip - x (mirror-image x faces)
+  double xshift = 0.0;       // > 0 (jittered periodic mesh, translated x faces): x moves by -+xshift
+  int64_t nsolve = 0;        // unknowns of the symmetric system; < N on a periodic mesh
+  int64_t plane = 0;         // nodes per x plane ((ny+1)(nz+1)); the ghost plane starts at nsolve
   float4 *mrec = nullptr;    // T*3: J^-1 (9 floats) then E (3 floats)
   uint4 *mnbr = nullptr;     // T: neighbour + permutation per face (indexed by opposite vertex)
   float *fill_ratio = nullptr;  // T: vol/vol_max
@@ -42,7 +47,10 @@ struct DevMesh {
 // ---- plain FP64 path ------------------------------------------------------
 void launch_plain_deposit(cudaStream_t s, const PlainParts &P, int64_t n, const DevMesh &M, const SpeciesTable &S,
                           int mode, double *rhs);
-void launch_rhs_finish(cudaStream_t s, int64_t N, double *rhs, const double *bg, const uint8_t *bnd);
+// rhs += background, Dirichlet rows zeroed; periodic ghost-plane charge folded into the pairs
+void launch_rhs_finish(cudaStream_t s, const DevMesh &M, double *rhs, const double *bg);
+// periodic meshes: the ghost plane of phi takes the values of the x = lo plane
+void launch_periodic_copy(cudaStream_t s, const DevMesh &M, double *phi);
 void launch_efield_plain(cudaStream_t s, const DevMesh &M, const double *phi, double *Etet);
 void launch_plain_move(cudaStream_t s, const PlainParts &P, int64_t n, const DevMesh &M, const double *Etet,
                        const SpeciesTable &S, double dt, int kill, int max_cross, DevStats *st);
@@ -53,8 +61,8 @@ void launch_compact_plain(cudaStream_t s, const PlainParts &P, int64_t n, const 
 // ---- mixed path -----------------------------------------------------------
 void launch_mixed_deposit(cudaStream_t s, const MixedParts &P, int64_t n, const DevMesh &M, const SpeciesTable &S,
                           unsigned long long *acc);
-void launch_mixed_convert(cudaStream_t s, int64_t N, unsigned long long *acc, double quantum, const double *bg,
-                          const uint8_t *bnd, double *rhs);
+void launch_mixed_convert(cudaStream_t s, const DevMesh &M, unsigned long long *acc, double quantum, const double *bg,
+                          double *rhs);
 void launch_efield_mixed(cudaStream_t s, const DevMesh &M, const double *phi);
 void launch_mixed_move(cudaStream_t s, const MixedParts &P, int64_t n, const DevMesh &M, const SpeciesTable &S,
                        float dt, int kill, int max_cross, unsigned long long *acc, DevStats *st);
@@ -94,6 +102,7 @@ int64_t scan_scratch_len(int64_t n);
 // rows are identity rows and are flagged in bnd.
 struct DiaMatrix {
   int64_t n = 0;
+  int64_t nwrap = 0;  // periodic mesh: neighbour indices are taken modulo nwrap (= n); 0 otherwise
   int ndiag = 0;
   int off[27] = {};
   double *val64 = nullptr;  // ndiag * n

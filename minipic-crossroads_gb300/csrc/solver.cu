@@ -46,6 +46,19 @@ namespace {
 
 constexpr int kSlots = 4;  // partial sums per phase
 
+// neighbour row of row i along a stencil offset; on a periodic mesh the rows
+// are the x < hi planes and x wraps around, i.e. the index is taken modulo nwrap
+__device__ __forceinline__ int64_t dia_nb(int64_t i, int off, int64_t nwrap) {
+  int64_t j = i + off;
+  if (nwrap) {
+    if (j < 0)
+      j += nwrap;
+    else if (j >= nwrap)
+      j -= nwrap;
+  }
+  return j;
+}
+
 // sum of partials[0..nb): every thread loads at most one partial (one L2
 // round trip), then a fixed block reduction; all blocks compute the same
 // value bit for bit.
@@ -207,7 +220,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg64_dia(Cg64DiaArgs a) {
     } else {
 #pragma unroll
       for (int d = 0; d < ND; ++d) {
-        s += val[d * n + i] * a.x[i + a.A.off[d]];
+        s += val[d * n + i] * a.x[dia_nb(i, a.A.off[d], a.A.nwrap)];
       }
     }
     const double ri = -1.0 * s + 1.0 * a.b[i];
@@ -245,7 +258,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg64_dia(Cg64DiaArgs a) {
         } else {
 #pragma unroll
           for (int d = 0; d < ND; ++d) {
-                const int64_t j = i + a.A.off[d];
+                const int64_t j = dia_nb(i, a.A.off[d], a.A.nwrap);
             const double pj = first ? a.r[j] : beta * pp[j] + 1.0 * a.r[j];
             s += val[d * n + i] * pj;
           }
@@ -376,7 +389,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
         s = a.x[i];
       } else {
 #pragma unroll
-        for (int d = 0; d < ND; ++d) s += v64[d * n + i] * a.x[i + a.A.off[d]];
+        for (int d = 0; d < ND; ++d) s += v64[d * n + i] * a.x[dia_nb(i, a.A.off[d], a.A.nwrap)];
       }
       const double ri = a.b[i] - s;
       a.r64[i] = ri;
@@ -427,7 +440,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
           s = 0.f;
 #pragma unroll
           for (int d = 0; d < ND; ++d)
-            s = __fmaf_rn(CST ? a.A.cst[d] : v32[d * n + i], v0[i + a.A.off[d]].y, s);
+            s = __fmaf_rn(CST ? a.A.cst[d] : v32[d * n + i], v0[dia_nb(i, a.A.off[d], a.A.nwrap)].y, s);
         }
         // only q is written: other blocks read this node's p concurrently
         reinterpret_cast<float *>(v0 + i)[2] = s;
@@ -472,7 +485,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
           s = 0.f;
 #pragma unroll
           for (int d = 0; d < ND; ++d) {
-            const float4 u = vk[i + a.A.off[d]];
+            const float4 u = vk[dia_nb(i, a.A.off[d], a.A.nwrap)];
             const float rj = __fmaf_rn(-af, u.z, u.x);
             s = __fmaf_rn(CST ? a.A.cst[d] : v32[d * n + i], __fmaf_rn(bf, u.y, rj), s);
           }

@@ -32,7 +32,10 @@ struct orc_mesh {
   std::vector<double> normals;  // T*12
   std::vector<double> grad;     // T*12
   std::vector<uint8_t> bnd;     // N
+  std::vector<int8_t> fper;     // T*4, elem_face_periodic (mesh.cpp:369-392)
+  std::vector<int32_t> pair;    // N, node_pairs (mesh.cpp:178-189), -1 = none
   int csr_mode = -1;
+  int64_t nsolve = 0;           // rows of the assembled system
   std::vector<int32_t> rowptr, col;
   std::vector<double> val;
 };
@@ -119,6 +122,9 @@ extern "C" orc_mesh *orc_mesh_create(const orc_mesh_desc *d, char *err, int errl
   };
   if (d->nx < 1 || d->ny < 1 || d->nz < 1) return fail("mesh size must be >= 1");
   if (d->split != 5 && d->split != 6) return fail("split must be 5 or 6");
+  if (d->periodic && d->nx < 2) return fail("periodic mesh needs nx >= 2");
+  // mesh.cpp:91-94: the alternating five-tet split only matches across x when nx is even
+  if (d->periodic && d->split == 5 && d->nx % 2 == 1) return fail("periodic five-tet mesh needs an even nx");
   orc_mesh *m = new orc_mesh();
   m->d = *d;
   const int64_t nx = d->nx, ny = d->ny, nz = d->nz;
@@ -139,9 +145,15 @@ extern "C" orc_mesh *orc_mesh_create(const orc_mesh_desc *d, char *err, int errl
         m->nodes[3 * g + 0] = d->lo + i * dx;
         m->nodes[3 * g + 1] = d->lo + j * dy;
         m->nodes[3 * g + 2] = d->lo + k * dz;
-        // boundary nodeset (mesh.cpp:407-412), by grid index
-        if (i == 0 || i == nx || j == 0 || j == ny || k == 0 || k == nz) m->bnd[g] = 1;
+        // boundary nodeset (mesh.cpp:407-412), by grid index; a periodic
+        // mesh has no x walls
+        if ((!d->periodic && (i == 0 || i == nx)) || j == 0 || j == ny || k == 0 || k == nz) m->bnd[g] = 1;
       }
+  // periodic node pairs (mesh.cpp:178-189): interior nodes of the x = hi plane
+  m->pair.assign(m->N, -1);
+  if (d->periodic)
+    for (int64_t j = 1; j < ny; ++j)
+      for (int64_t k = 1; k < nz; ++k) m->pair[gid(nx, j, k)] = gid(0, j, k);
   for (int64_t g = 0; g < m->N; ++g) m->n_bnodes += m->bnd[g];
   // tets: mesh.cpp:195-224 (5-split) or Kuhn 6-split
   m->tets.resize(m->T * 4);
@@ -181,13 +193,19 @@ extern "C" orc_mesh *orc_mesh_create(const orc_mesh_desc *d, char *err, int errl
   // face matching (mesh.cpp:233-405): faces (0,1,3),(1,2,3),(0,3,2),(0,2,1)
   static const int fnodes[4][3] = {{0, 1, 3}, {1, 2, 3}, {0, 3, 2}, {0, 2, 1}};
   std::map<std::array<int32_t, 3>, std::vector<std::pair<int32_t, int>>> faces;
+  const int64_t plane = (ny + 1) * (nz + 1);
   for (int64_t t = 0; t < m->T; ++t)
     for (int f = 0; f < 4; ++f) {
       std::array<int32_t, 3> key = {m->tets[4 * t + fnodes[f][0]], m->tets[4 * t + fnodes[f][1]],
                                     m->tets[4 * t + fnodes[f][2]]};
+      // Mesh::periodic_face (mesh.cpp:61-76): a face with every node on the
+      // x = hi plane is renamed onto the x = lo plane
+      if (d->periodic && key[0] / plane == nx && key[1] / plane == nx && key[2] / plane == nx)
+        for (int q = 0; q < 3; ++q) key[q] -= (int32_t)(nx * plane);
       std::sort(key.begin(), key.end());
       faces[key].push_back({(int32_t)t, f});
     }
+  m->fper.assign(m->T * 4, 0);
   m->nbrs.assign(m->T * 4, INT32_MIN);
   auto tuple = [&](int32_t g, int64_t &i, int64_t &j, int64_t &k) {
     i = g / ((ny + 1) * (nz + 1));
@@ -197,6 +215,13 @@ extern "C" orc_mesh *orc_mesh_create(const orc_mesh_desc *d, char *err, int errl
   m->n_faces = (int64_t)faces.size();
   for (auto &kv : faces) {
     auto &v = kv.second;
+    if (d->periodic) {
+      // mesh.cpp:369-378: a (renamed) face on the x = lo plane is periodic on both sides
+      int64_t I[3], J[3], K[3];
+      for (int q = 0; q < 3; ++q) tuple(kv.first[q], I[q], J[q], K[q]);
+      if (I[0] == 0 && I[1] == 0 && I[2] == 0)
+        for (auto &e : v) m->fper[4 * e.first + e.second] = +1;
+    }
     if (v.size() == 2) {
       m->nbrs[4 * v[0].first + v[0].second] = v[1].first;
       m->nbrs[4 * v[1].first + v[1].second] = v[0].first;
@@ -204,7 +229,7 @@ extern "C" orc_mesh *orc_mesh_create(const orc_mesh_desc *d, char *err, int errl
       // must lie on a wall: all three nodes on one boundary plane (mesh.cpp:367-394)
       int64_t I[3], J[3], K[3];
       for (int q = 0; q < 3; ++q) tuple(kv.first[q], I[q], J[q], K[q]);
-      bool wall = (I[0] == 0 && I[1] == 0 && I[2] == 0) || (I[0] == nx && I[1] == nx && I[2] == nx) ||
+      bool wall = (!d->periodic && ((I[0] == 0 && I[1] == 0 && I[2] == 0) || (I[0] == nx && I[1] == nx && I[2] == nx))) ||
                   (J[0] == 0 && J[1] == 0 && J[2] == 0) || (J[0] == ny && J[1] == ny && J[2] == ny) ||
                   (K[0] == 0 && K[1] == 0 && K[2] == 0) || (K[0] == nz && K[1] == nz && K[2] == nz);
       if (!wall) {
@@ -227,8 +252,11 @@ extern "C" orc_mesh *orc_mesh_create(const orc_mesh_desc *d, char *err, int errl
     const double h[3] = {dx, dy, dz};
     for (int64_t g = 0; g < m->N; ++g) {
       if (m->bnd[g]) continue;
+      // a ghost node moves with its pair: the x = hi face is the x = lo face
+      // translated by the box length (the periodic crossing is a translation)
+      const int64_t src = m->pair[g] >= 0 ? m->pair[g] : g;
       for (int q = 0; q < 3; ++q) {
-        double u = unit53(orc_draw(base, 3 * (uint64_t)g + q));
+        double u = unit53(orc_draw(base, 3 * (uint64_t)src + q));
         m->nodes[3 * g + q] += (2.0 * u - 1.0) * d->jitter * h[q];
       }
     }
@@ -284,6 +312,11 @@ extern "C" orc_mesh *orc_mesh_create(const orc_mesh_desc *d, char *err, int errl
 
 extern "C" void orc_mesh_destroy(orc_mesh *m) { delete m; }
 
+extern "C" void orc_mesh_export_periodic(const orc_mesh *m, int8_t *face_periodic, int32_t *node_pairs) {
+  if (face_periodic) memcpy(face_periodic, m->fper.data(), m->fper.size());
+  if (node_pairs) memcpy(node_pairs, m->pair.data(), sizeof(int32_t) * m->pair.size());
+}
+
 extern "C" void orc_mesh_sizes(const orc_mesh *m, int64_t *T, int64_t *N, int64_t *n_faces, int64_t *n_bfaces,
                                int64_t *n_bnodes) {
   if (T) *T = m->T;
@@ -308,42 +341,52 @@ extern "C" void orc_mesh_export(const orc_mesh *m, double *nodes, int32_t *tets,
 /* ------------------------------------------------------------------------ */
 /* P1 stiffness assembly: ES.cpp:83-205.  K_e(i,j) = sum_c sum_d G_i[d] *
  * (wm_c * G_j[d]) with wm_c = detJ * (1/24) for the 4-point degree-2 rule.  */
+// a periodic ghost node stands for its pair (ES.cpp:93-95,168-176; PIC.cpp:132-134)
+static inline int32_t pmap(const orc_mesh *m, int32_t g) { return m->pair[g] >= 0 ? m->pair[g] : g; }
+
 extern "C" int64_t orc_assemble(orc_mesh *m, int mode) {
   const int64_t N = m->N, T = m->T;
-  std::vector<std::vector<int32_t>> cols(N);
+  // mode 1 on a periodic mesh solves for the nodes of the x < hi planes only;
+  // the ghost plane (the last plane in gid order) is copied afterwards
+  const int64_t plane = (int64_t)(m->d.ny + 1) * (m->d.nz + 1);
+  const int64_t R = (mode == 1 && m->d.periodic) ? N - plane : N;
+  std::vector<std::vector<int32_t>> cols(R);
   for (int64_t t = 0; t < T; ++t)
     for (int a = 0; a < 4; ++a) {
-      int32_t r = m->tets[4 * t + a];
+      int32_t r = pmap(m, m->tets[4 * t + a]);
       if (m->bnd[r]) continue;
       for (int b = 0; b < 4; ++b) {
-        int32_t c = m->tets[4 * t + b];
+        int32_t c = pmap(m, m->tets[4 * t + b]);
         if (mode == 1 && m->bnd[c]) continue;
         cols[r].push_back(c);
       }
     }
-  m->rowptr.assign(N + 1, 0);
-  for (int64_t r = 0; r < N; ++r) {
+  m->rowptr.assign(R + 1, 0);
+  for (int64_t r = 0; r < R; ++r) {
     if (m->bnd[r]) {
       cols[r].assign(1, (int32_t)r);
+    } else if (m->pair[r] >= 0) {
+      // ghost row of the reference system: -phi_ghost + phi_pair = 0 (ES.cpp:183-189)
+      cols[r] = {m->pair[r], (int32_t)r};
     } else {
       std::sort(cols[r].begin(), cols[r].end());
       cols[r].erase(std::unique(cols[r].begin(), cols[r].end()), cols[r].end());
     }
     m->rowptr[r + 1] = m->rowptr[r] + (int32_t)cols[r].size();
   }
-  const int64_t nnz = m->rowptr[N];
+  const int64_t nnz = m->rowptr[R];
   m->col.resize(nnz);
   m->val.assign(nnz, 0.0);
-  for (int64_t r = 0; r < N; ++r) std::copy(cols[r].begin(), cols[r].end(), m->col.begin() + m->rowptr[r]);
+  for (int64_t r = 0; r < R; ++r) std::copy(cols[r].begin(), cols[r].end(), m->col.begin() + m->rowptr[r]);
   const double wcub = 1.0 / 24.0;
   for (int64_t t = 0; t < T; ++t) {
     const double *G = &m->grad[12 * t];
     const double wm = m->detj[t] * wcub;
     for (int a = 0; a < 4; ++a) {
-      int32_t r = m->tets[4 * t + a];
+      int32_t r = pmap(m, m->tets[4 * t + a]);
       if (m->bnd[r]) continue;
       for (int b = 0; b < 4; ++b) {
-        int32_t c = m->tets[4 * t + b];
+        int32_t c = pmap(m, m->tets[4 * t + b]);
         if (mode == 1 && m->bnd[c]) continue;
         double k = 0.0;
         for (int cub = 0; cub < 4; ++cub)
@@ -353,11 +396,26 @@ extern "C" int64_t orc_assemble(orc_mesh *m, int mode) {
       }
     }
   }
-  for (int64_t r = 0; r < N; ++r)
+  for (int64_t r = 0; r < R; ++r) {
     if (m->bnd[r]) m->val[m->rowptr[r]] = 1.0;  // ES.cpp:198-204
+    if (m->pair[r] >= 0) {
+      m->val[m->rowptr[r]] = 1.0;
+      m->val[m->rowptr[r] + 1] = -1.0;
+    }
+  }
   m->csr_mode = mode;
+  m->nsolve = R;
   return nnz;
 }
+
+// ghost nodes take their pair's value (the solve of mode 1 leaves them out)
+static void periodic_copy(const orc_mesh *m, double *x) {
+  if (!m->d.periodic) return;
+  for (int64_t g = 0; g < m->N; ++g)
+    if (m->pair[g] >= 0) x[g] = x[m->pair[g]];
+}
+
+extern "C" int64_t orc_csr_rows(const orc_mesh *m) { return m->nsolve; }
 
 extern "C" void orc_csr_export(const orc_mesh *m, int32_t *rowptr, int32_t *col, double *val) {
   if (rowptr) memcpy(rowptr, m->rowptr.data(), m->rowptr.size() * sizeof(int32_t));
@@ -366,7 +424,7 @@ extern "C" void orc_csr_export(const orc_mesh *m, int32_t *rowptr, int32_t *col,
 }
 
 extern "C" void orc_spmv(const orc_mesh *m, const double *x, double *y, int nthreads) {
-  const int64_t N = m->N;
+  const int64_t N = m->nsolve;
 #pragma omp parallel for num_threads(nthr(nthreads)) schedule(static)
   for (int64_t r = 0; r < N; ++r) {
     double s = 0.0;
@@ -405,7 +463,7 @@ extern "C" void orc_background(const orc_mesh *m, double rho_bg, double *bg) {
   std::fill(bg, bg + m->N, 0.0);
   for (int64_t t = 0; t < m->T; ++t) {
     double q = -(rho_bg * (m->detj[t] / 6.0)) * 0.25;
-    for (int a = 0; a < 4; ++a) bg[m->tets[4 * t + a]] += q;
+    for (int a = 0; a < 4; ++a) bg[pmap(m, m->tets[4 * t + a])] += q;
   }
   for (int64_t i = 0; i < m->N; ++i)
     if (m->bnd[i]) bg[i] = 0.0;
@@ -435,12 +493,12 @@ static inline void deposit_one(const orc_mesh *m, int mode, int32_t e, const dou
     for (int i = 0; i < 4; ++i) {
       double val = 0;
       for (int c = 0; c < 4; ++c) val += -tot_q * (wm * Nc[i][c]);
-      rhs[m->tets[4 * e + i]] += val;
+      rhs[pmap(m, m->tets[4 * e + i])] += val;
     }
   } else {
     const double wq = w * q;
     const double lam[4] = {1 - xr[0] - xr[1] - xr[2], xr[0], xr[1], xr[2]};
-    for (int i = 0; i < 4; ++i) rhs[m->tets[4 * e + i]] += -(wq * lam[i]);
+    for (int i = 0; i < 4; ++i) rhs[pmap(m, m->tets[4 * e + i])] += -(wq * lam[i]);
   }
 }
 
@@ -506,10 +564,10 @@ extern "C" void orc_deposit_fixed(const orc_mesh *m, int64_t n, const uint32_t *
 
 /* ------------------------------------------------------------------------ */
 /* solvers                                                                   */
-extern "C" int orc_bicgstab(const orc_mesh *m, const double *rhs, double *x, double tol, int max_iter, double *resid_out,
-                            int nthreads) {
-  // CG_solve.hpp:115-206, operation for operation
-  const int64_t N = m->N;
+static int bicgstab_impl(const orc_mesh *m, const double *rhs, double *x, double tol, int max_iter, double *resid_out,
+                         int nthreads) {
+  // CG_solve.hpp:115-206, operation for operation, over the rows of the assembled system
+  const int64_t N = m->nsolve;
   double rho0, rho, rho_old = 0.0, beta = 0.0, alpha = 0.0, omega = 0.0, resid = 0.0;
   rho0 = dot(rhs, rhs, N, nthreads);
   std::vector<double> r(N), rt(N), p(N), v(N), t(N);
@@ -554,10 +612,17 @@ extern "C" int orc_bicgstab(const orc_mesh *m, const double *rhs, double *x, dou
   return iter;
 }
 
-extern "C" int orc_cg(const orc_mesh *m, const double *rhs, double *x, double tol, int max_iter, double *resid_out,
-                      int nthreads) {
-  // CG_solve.hpp:54-114
-  const int64_t N = m->N;
+extern "C" int orc_bicgstab(const orc_mesh *m, const double *rhs, double *x, double tol, int max_iter, double *resid_out,
+                            int nthreads) {
+  const int it = bicgstab_impl(m, rhs, x, tol, max_iter, resid_out, nthreads);
+  periodic_copy(m, x);
+  return it;
+}
+
+static int cg_impl(const orc_mesh *m, const double *rhs, double *x, double tol, int max_iter, double *resid_out,
+                   int nthreads) {
+  // CG_solve.hpp:54-114, over the rows of the assembled system
+  const int64_t N = m->nsolve;
   double rho0, rho, rho_old = 0.0, beta, alpha;
   rho0 = dot(rhs, rhs, N, nthreads);
   std::vector<double> p(N), q(N), r(N);
@@ -586,6 +651,13 @@ extern "C" int orc_cg(const orc_mesh *m, const double *rhs, double *x, double to
   if (resid_out) *resid_out = sqrt(rho / rho0);
   // number of iterations performed (the loop index at the break, plus one)
   return iter < max_iter ? iter + 1 : iter;
+}
+
+extern "C" int orc_cg(const orc_mesh *m, const double *rhs, double *x, double tol, int max_iter, double *resid_out,
+                      int nthreads) {
+  const int it = cg_impl(m, rhs, x, tol, max_iter, resid_out, nthreads);
+  periodic_copy(m, x);
+  return it;
 }
 
 /* ------------------------------------------------------------------------ */
@@ -715,6 +787,17 @@ static inline double find_intersection(const orc_mesh *m, int32_t &e, double *x,
   if (scale_fact < 1) {
     int32_t nb = m->nbrs[4 * e + face];
     if (nb >= 0) {
+      // a periodic face wraps x to the other side of the box.  The reference's
+      // meshes have mirror-image x faces and it writes x = -x on its [-1,1]
+      // box (particle_move.hpp:190-191), i.e. x -> lo + hi - x; a jittered
+      // mesh has translated x faces, so x moves by the box length instead.
+      if (m->fper[4 * e + face] != 0) {
+        const double L = m->d.hi - m->d.lo;
+        if (m->d.mapping == 4)
+          x[0] = (x[0] + x[0] > m->d.lo + m->d.hi) ? x[0] - L : x[0] + L;
+        else
+          x[0] = (m->d.lo + m->d.hi) - x[0];
+      }
       e = nb;
       // physToReference (mesh.hpp:196-211): ref = 0 + J^-1 (x - x0)
       const double *X0 = &m->nodes[3 * m->tets[4 * e]];

@@ -42,6 +42,7 @@ typedef struct {
   int mapping;
   double jitter;
   uint64_t seed;
+  int periodic; /* periodic in x (mesh.cpp:61-76,178-189,369-392) */
 } orc_mesh_desc;
 
 orc_mesh *orc_mesh_create(const orc_mesh_desc *d, char *err, int errlen);
@@ -52,11 +53,15 @@ void orc_mesh_sizes(const orc_mesh *m, int64_t *T, int64_t *N, int64_t *n_faces,
 void orc_mesh_export(const orc_mesh *m, double *nodes, int32_t *tets, int32_t *nbrs,
                      double *jinv, double *detj, double *normals, double *grad,
                      uint8_t *boundary);
+/* elem_face_periodic T*4 and node_pairs N (mesh.cpp:178-189,369-392) */
+void orc_mesh_export_periodic(const orc_mesh *m, int8_t *face_periodic, int32_t *node_pairs);
 
 /* CSR of the P1 stiffness matrix.  mode 0 = reference assembly (Dirichlet
  * rows are identity rows, interior rows keep boundary columns, ES.cpp:83-213);
  * mode 1 = symmetric form (boundary columns dropped from interior rows). */
 int64_t orc_assemble(orc_mesh *m, int mode);
+/* rows of the assembled system: N, or N minus the ghost plane for mode 1 on a periodic mesh */
+int64_t orc_csr_rows(const orc_mesh *m);
 void orc_csr_export(const orc_mesh *m, int32_t *rowptr, int32_t *col, double *val);
 /* y = A x with the assembled matrix */
 void orc_spmv(const orc_mesh *m, const double *x, double *y, int nthreads);

@@ -24,7 +24,7 @@ def build(force=False):
 class MeshDesc(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("split", C.c_int),
                 ("lo", C.c_double), ("hi", C.c_double), ("mapping", C.c_int),
-                ("jitter", C.c_double), ("seed", C.c_uint64)]
+                ("jitter", C.c_double), ("seed", C.c_uint64), ("periodic", C.c_int)]
 
 
 class StepCfg(C.Structure):
@@ -55,6 +55,9 @@ def lib():
         L.orc_mesh_destroy.argtypes = [P]
         L.orc_mesh_sizes.argtypes = [P] + [C.POINTER(I64)] * 5
         L.orc_mesh_export.argtypes = [P] * 9
+        L.orc_mesh_export_periodic.argtypes = [P] * 3
+        L.orc_csr_rows.restype = I64
+        L.orc_csr_rows.argtypes = [P]
         L.orc_assemble.restype = I64
         L.orc_assemble.argtypes = [P, I32]
         L.orc_csr_export.argtypes = [P, P, P, P]
@@ -96,9 +99,10 @@ def ptr(a):
 class Mesh:
     """Oracle mesh (mesh.cpp:78-714 restated)."""
 
-    def __init__(self, n, split=6, lo=0.0, hi=1.0, mapping=0, jitter=0.0, seed=0):
+    def __init__(self, n, split=6, lo=0.0, hi=1.0, mapping=0, jitter=0.0, seed=0, periodic=0):
         nx, ny, nz = (n, n, n) if np.isscalar(n) else n
-        self.desc = MeshDesc(nx, ny, nz, split, lo, hi, mapping, jitter, seed)
+        self.desc = MeshDesc(nx, ny, nz, split, lo, hi, mapping, jitter, seed, int(periodic))
+        self.periodic = int(periodic)
         err = C.create_string_buffer(256)
         self.h = lib().orc_mesh_create(C.byref(self.desc), err, 256)
         if not self.h:
@@ -117,6 +121,9 @@ class Mesh:
         self.boundary = np.zeros(N, np.uint8)
         lib().orc_mesh_export(self.h, *[ptr(a) for a in (self.nodes, self.tets, self.nbrs, self.jinv, self.detj,
                                                           self.normals, self.grad, self.boundary)])
+        self.face_periodic = np.zeros((T, 4), np.int8)
+        self.node_pairs = np.zeros(N, np.int32)
+        lib().orc_mesh_export_periodic(self.h, ptr(self.face_periodic), ptr(self.node_pairs))
         self.csr = None
 
     def __del__(self):
@@ -126,7 +133,7 @@ class Mesh:
 
     def assemble(self, mode=1):
         nnz = lib().orc_assemble(self.h, mode)
-        rp = np.zeros(self.N + 1, np.int32)
+        rp = np.zeros(lib().orc_csr_rows(self.h) + 1, np.int32)
         col = np.zeros(nnz, np.int32)
         val = np.zeros(nnz)
         lib().orc_csr_export(self.h, ptr(rp), ptr(col), ptr(val))

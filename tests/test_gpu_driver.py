@@ -31,3 +31,22 @@ def test_driver_mixed_linear_cg(mpg, tmp_path):
                        cwd=tmp_path, capture_output=True, text=True, timeout=120)
     assert p.returncode == 0, p.stderr
     assert p.stdout.count("Total KE is") == 4
+
+
+@pytest.mark.parametrize("precision", ["plain", "mixed"])
+def test_driver_two_stream_periodic(mpg, tmp_path, precision):
+    # main.cpp:89-106: --problem two-stream builds the periodic mesh and the
+    # two counter-streaming beams; nothing leaves through x, so the only
+    # losses are at the y/z walls
+    drv = os.path.join(os.path.dirname(mpg.lib_path()), "minipic_gb300")
+    (tmp_path / "brick.txt").write_text("4 4 4 0\n")
+    args = [drv, "--nparts=8", "--dt=0.05", "--steps=4", "--problem=two-stream", "--kill-particles=1",
+            "--precision=" + precision]
+    if precision == "mixed":
+        args += ["--solver=cg", "--deposit=linear", "--tol=1e-10"]
+    p = subprocess.run(args, cwd=tmp_path, capture_output=True, text=True, timeout=120)
+    assert p.returncode == 0, p.stderr
+    out = p.stdout
+    # 5 * 4^3 tets, 4 + 4 beam electrons and 8 ions per tet
+    assert "for 5120 particles" in out
+    assert out.count("Total KE is") == 4

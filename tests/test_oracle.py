@@ -272,3 +272,95 @@ def test_full_step_runs_and_conserves(orc):
         assert rc == 0 and st.solver_resid < 1e-10
     assert P.n == st.n_alive and P.n <= n
     assert 0.5 * ke0 < st.ke < 2 * ke0
+
+
+# ---------------------------------------------------------------------------
+# periodic-in-x meshes (the reference's --problem two-stream set-up)
+@pytest.mark.parametrize("split,n,lo,hi", [(5, 4, -1.0, 1.0), (6, 3, 0.0, 1.0), (6, (4, 3, 5), 0.0, 1.0)])
+def test_periodic_mesh_invariants(orc, split, n, lo, hi):
+    nx, ny, nz = (n, n, n) if np.isscalar(n) else n
+    m = orc.Mesh(n, split=split, lo=lo, hi=hi, periodic=1)
+    per_hex = 4 if split == 5 else 6
+    # mesh.cpp:119-120: the x = hi faces are merged with the x = lo faces
+    total = per_hex * nx * ny * nz + 2 * (nx * ny * (nz + 1) + nx * (ny + 1) * nz + (nx + 1) * ny * nz) - 2 * ny * nz
+    assert m.n_faces == total
+    assert m.n_bfaces == 4 * nx * (ny + nz)          # only the y and z walls
+    g = np.arange(m.N)
+    i, j, k = g // ((ny + 1) * (nz + 1)), (g // (nz + 1)) % (ny + 1), g % (nz + 1)
+    bnd = (j == 0) | (j == ny) | (k == 0) | (k == nz)
+    assert (m.boundary == bnd).all()
+    ghost = (i == nx) & ~bnd
+    assert (m.node_pairs[ghost] == g[ghost] - nx * (ny + 1) * (nz + 1)).all()
+    assert (m.node_pairs[~ghost] == -1).all()
+    # neighbours are mutual, including across the periodic faces
+    for t in range(m.T):
+        for f in range(4):
+            b = m.nbrs[t, f]
+            if b >= 0:
+                assert t in m.nbrs[b]
+    # both sides of every x-plane triangle are flagged (mesh.cpp:369-392)
+    assert (m.face_periodic != 0).sum() == 2 * 2 * ny * nz
+    assert (m.nbrs[m.face_periodic != 0] >= 0).all()
+
+
+def test_periodic_five_tet_needs_even_nx(orc):
+    with pytest.raises(ValueError):
+        orc.Mesh(3, split=5, lo=-1.0, hi=1.0, periodic=1)
+
+
+def test_periodic_walk_wraps_known_answer(orc):
+    # crossing x = hi reappears at x = lo (particle_move.hpp:190-191)
+    m = orc.Mesh(4, split=6, periodic=1)
+    x0 = np.array([0.97, 0.41, 0.57])
+    for t in range(m.T):
+        X = m.nodes[m.tets[t]]
+        xr = np.linalg.solve((X[1:] - X[0]).T, x0 - X[0])
+        if (xr >= 0).all() and xr.sum() <= 1:
+            break
+    P = _single(orc, m, t, xr, np.array([0.1, 0.0, 0.0]))
+    orc.push(m, P, np.zeros((1, 3)), [-1.0], 1.0)
+    r = orc.walk(m, P, 1.0, kill=1)
+    assert r["killed"] == 0 and r["limit"] == 0
+    assert np.allclose(P.x[0], [0.07, 0.41, 0.57], atol=1e-13)
+    X = m.nodes[m.tets[P.cell[0]]]
+    lam = np.array([1 - P.xref[0].sum(), *P.xref[0]])
+    assert np.allclose(lam @ X, P.x[0], atol=1e-13)
+    # and back across x = lo
+    P.v[0] = [-0.2, 0.0, 0.0]
+    orc.push(m, P, np.zeros((1, 3)), [-1.0], 1.0)
+    P.vref[0] = np.linalg.solve((m.nodes[m.tets[P.cell[0]]][1:] - m.nodes[m.tets[P.cell[0]]][0]).T, P.v[0])
+    r = orc.walk(m, P, 1.0, kill=1)
+    assert r["killed"] == 0
+    assert np.allclose(P.x[0], [0.87, 0.41, 0.57], atol=1e-13)
+
+
+def test_periodic_assembly_and_solves_agree(orc):
+    # mode 1 (symmetric, ghost plane left out) is symmetric with zero row sums
+    # away from the walls; mode 0 BiCGStab (reference ghost rows) and mode 1
+    # CG give the same phi
+    import scipy.sparse as sp
+    n = 6
+    m = orc.Mesh(n, split=6, mapping=4, jitter=0.2, seed=5, periodic=1)
+    plane = (n + 1) ** 2
+    rp, col, val = m.assemble(1)
+    R = len(rp) - 1
+    assert R == m.N - plane
+    A = sp.csr_matrix((val, col, rp), shape=(R, R))
+    assert abs(A - A.T).max() < 1e-15
+    # rows two or more cells away from the y and z walls (all x planes,
+    # including the two coupled through the periodic faces)
+    r = np.arange(R)
+    j, k = (r // (n + 1)) % (n + 1), r % (n + 1)
+    inner = (j >= 2) & (j <= n - 2) & (k >= 2) & (k <= n - 2)
+    rs = np.asarray(A.sum(axis=1)).ravel()
+    assert np.abs(rs[inner]).max() < 1e-12 * np.abs(val).max()
+    rng = np.random.default_rng(3)
+    b = rng.standard_normal(m.N)
+    b[m.boundary == 1] = 0
+    b[m.node_pairs >= 0] = 0          # ghost rows carry no charge (PIC.cpp:132-134)
+    x1, it1, _ = orc.cg(m, b, tol=1e-12, max_iter=2000)
+    m.assemble(0)
+    x0, it0, _ = orc.bicgstab(m, b, tol=1e-12, max_iter=2000)
+    assert np.abs(x0 - x1).max() <= 1e-8 * np.abs(x1).max()
+    g = m.node_pairs >= 0
+    assert (x1[g] == x1[m.node_pairs[g]]).all() and (x0[g] == x0[m.node_pairs[g]]).all()
