@@ -38,6 +38,8 @@ import sys
 import threading
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 METRIC = "particle-steps/s (push+deposit+CG) mixed vs FP64 plain; ensemble p50/p99 ms"
 UNIT = "particle-steps/s"
@@ -53,6 +55,17 @@ WORKLOADS = {
                   species=[dict(q=-1.0, m=1.0, n=64 << 20, vth=0.02, drift=(0.2, 0, 0), seed=1),
                            dict(q=-1.0, m=1.0, n=64 << 20, vth=0.02, drift=(-0.2, 0, 0), seed=2, same=0)],
                   rho_background=1.0),
+    # the reference's two-stream problem (main.cpp:89-106) at GPU scale: 48^3
+    # Kuhn mesh of [-1,1]^3 periodic in x, its ParticleFill set-up per tet
+    # (two electron beams v_x = +-0.5 (1 - 0.05 sin(pi x)), H+ at rest),
+    # density 2/3 pi^2, absorbing y/z walls, mixed precision
+    "two-stream": dict(name="kuhn48-periodic-twostream-e8M-H8M-mixed", n_side=48, jitter=0.0, dt=0.01,
+                       sort_interval=10, periodic=1, lo=-1.0, hi=1.0, rho_background=0.0,
+                       ref_fills=[dict(nppe=6, type=0, density=np.pi ** 2 / 3.0, vel=(0.5, 0.0, 0.0), temp=-0.05),
+                                  dict(nppe=6, type=0, density=np.pi ** 2 / 3.0, vel=(-0.5, 0.0, 0.0), temp=-0.05),
+                                  dict(nppe=12, type=2, density=2.0 * np.pi ** 2 / 3.0, vel=(0.0, 0.0, 0.0),
+                                       temp=0.0)],
+                       species=[dict(q=-1.0, m=1.0, n=12 * 6 * 48 ** 3), dict(q=1.0, m=1837.0, n=12 * 6 * 48 ** 3)]),
     # 10^3 Kuhn, 1e5 electrons over a uniform background, plain FP64
     "small": dict(name="kuhn10-e100k-plain", n_side=10, jitter=0.0, dt=0.01, sort_interval=0,
                   species=[dict(q=-1.0, m=1.0, n=100000, vth=0.05, drift=(0, 0, 0), seed=1)],
@@ -82,12 +95,22 @@ WARM_START = 2
 
 def make_ctx(mpg, w, precision, device=0, seed_offset=0):
     ctx = mpg.Ctx(device)
-    ctx.mesh(w["n_side"], split=mpg.SPLIT_KUHN6, lo=0.0, hi=1.0,
-             mapping=mpg.MAP_JITTER if w["jitter"] else mpg.MAP_NONE, jitter=w["jitter"], seed=7)
+    ctx.mesh(w["n_side"], split=mpg.SPLIT_KUHN6, lo=w.get("lo", 0.0), hi=w.get("hi", 1.0),
+             mapping=mpg.MAP_JITTER if w["jitter"] else mpg.MAP_NONE, jitter=w["jitter"], seed=7,
+             periodic=w.get("periodic", 0))
     ctx.configure(precision=precision, deposit=mpg.DEPOSIT_LINEAR, solver=mpg.SOLVER_CG, tol=1e-10, max_iter=5000,
                   warm_start=WARM_START, kill_on_wall=1, max_crossings=1000,
                   sort_interval=w["sort_interval"] if precision == mpg.MIXED else 0,
                   rho_background=w["rho_background"])
+    if "ref_fills" in w:
+        # the reference's per-tet fill (particle_fill.hpp:129-164); species
+        # 0 = e- (-1, 1) and 2 = H+ (1, 1837) as in particle_type.hpp
+        ctx.reserve(total_particles(w))
+        ctx.species(0, -1.0, 1.0)
+        ctx.species(2, 1.0, 1837.0)
+        for f in w["ref_fills"]:
+            ctx.fill_ref(f["nppe"], f["type"], f["density"], vel=f["vel"], temp=f["temp"])
+        return ctx
     # weights: each species carries a total charge of magnitude 1 in the unit cube
     by_charge = {}
     for s in w["species"]:
@@ -425,19 +448,25 @@ def cpu_baseline(w, budget_s=20.0, max_steps=3):
     import numpy as np
     O.build()
     cores = os.cpu_count() or 1
-    m = O.Mesh(w["n_side"], split=6, mapping=4 if w["jitter"] else 0, jitter=w["jitter"], seed=7)
+    m = O.Mesh(w["n_side"], split=6, lo=w.get("lo", 0.0), hi=w.get("hi", 1.0), mapping=4 if w["jitter"] else 0,
+               jitter=w["jitter"], seed=7, periodic=w.get("periodic", 0))
     m.assemble(1)
     P = total_particles(w)
     parts = O.Particles(P)
-    by_charge = {}
-    for s in w["species"]:
-        by_charge[s["q"]] = by_charge.get(s["q"], 0) + s["n"]
     qs, ms = [0.0] * 16, [1.0] * 16
-    for i, s in enumerate(w["species"]):
-        sp = s.get("same", i)
-        qs[sp], ms[sp] = s["q"], s["m"]
-        parts.fill_uniform(m, s["n"], s["seed"], sp, 1.0 / by_charge[s["q"]], drift=s["drift"], vth=s["vth"],
-                           nthreads=cores)
+    if "ref_fills" in w:
+        qs[0], ms[0], qs[2], ms[2] = -1.0, 1.0, 1.0, 1837.0
+        for f in w["ref_fills"]:
+            parts.fill_ref(m, f["nppe"], f["type"], f["density"], vel=f["vel"], temp=f["temp"], mass=ms[f["type"]])
+    else:
+        by_charge = {}
+        for s in w["species"]:
+            by_charge[s["q"]] = by_charge.get(s["q"], 0) + s["n"]
+        for i, s in enumerate(w["species"]):
+            sp = s.get("same", i)
+            qs[sp], ms[sp] = s["q"], s["m"]
+            parts.fill_uniform(m, s["n"], s["seed"], sp, 1.0 / by_charge[s["q"]], drift=s["drift"], vth=s["vth"],
+                               nthreads=cores)
     bg = m.background(w["rho_background"]) if w["rho_background"] else None
     phi = np.zeros(m.N)
     cfg = O.StepCfg(1, 1, 1e-10, 5000, 1, 1, 1, 1000, 1, cores)
