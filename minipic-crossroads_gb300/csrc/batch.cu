@@ -53,7 +53,9 @@ struct SlotDev {
   unsigned long long *acc;
   double *rhs, *phi, *bg, *r64;
   float *r[2], *p[2], *q[2], *z;
-  double *partials;  // 8 * kMaxParts slots
+  double *partials;  // 8 * kMaxParts slots (outer phases); inner phases: one 32-byte record per part
+  double *phi_prev;  // previous solution (initial guess 2 phi[n-1] - phi[n-2])
+  int *hist;         // solutions held in phi / phi_prev (0, 1, 2), kept on the device
   int64_t T, N;
   int off[kND];
   double s64[kND];
@@ -78,11 +80,21 @@ struct SlotStat {
 };
 
 // ---------------------------------------------------------------------------
+// also forms the solver's initial guess: 2 phi[n-1] - phi[n-2] once two
+// solutions exist (the count is advanced by the solver after it finishes)
 __global__ void k_batch_convert(const SlotDev *__restrict__ slots, const int2 *__restrict__ plan) {
   const int2 pl = plan[blockIdx.x];
   const SlotDev &S = slots[pl.x];
   const int64_t i = (int64_t)pl.y * blockDim.x + threadIdx.x;
   if (i >= S.N) return;
+  const int h = *S.hist;
+  if (h >= 2) {
+    const double a = S.phi[i];
+    S.phi[i] = 2.0 * a - S.phi_prev[i];
+    S.phi_prev[i] = a;
+  } else if (h == 1) {
+    S.phi_prev[i] = S.phi[i];
+  }
   const long long a = (long long)S.acc[i];
   S.acc[i] = 0ull;
   double r = -((double)a * S.quantum);
@@ -126,6 +138,22 @@ __device__ __forceinline__ void batch_deposit_warp(const SlotDev *__restrict__ s
   const uint32_t prev = __shfl_up_sync(FULL, key, 1);
   const bool head = lane == 0 || prev != key;
   const unsigned heads = __ballot_sync(FULL, head);
+  if (heads == 1u) {
+    // the whole warp holds one cell (typical after a sort): plain reductions
+    c0 = __reduce_add_sync(FULL, c0);
+    c1 = __reduce_add_sync(FULL, c1);
+    c2 = __reduce_add_sync(FULL, c2);
+    c3 = __reduce_add_sync(FULL, c3);
+    if (lane == 0 && valid) {
+      const SlotDev &S = slots[key >> 24];
+      const int4 nd = S.tets[key & 0xFFFFFFu];
+      atomicAdd(S.acc + nd.x, (unsigned long long)(long long)c0);
+      atomicAdd(S.acc + nd.y, (unsigned long long)(long long)c1);
+      atomicAdd(S.acc + nd.z, (unsigned long long)(long long)c2);
+      atomicAdd(S.acc + nd.w, (unsigned long long)(long long)c3);
+    }
+    return;
+  }
   const int seg = 31 - __clz(heads & (FULL >> (31 - lane)));
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
@@ -155,43 +183,87 @@ __device__ __forceinline__ void batch_deposit_warp(const SlotDev *__restrict__ s
 
 constexpr int kMoveThreads = 256;
 
+// Persistent: one wave of resident blocks; each warp walks a contiguous range
+// of 32-particle chunks and loads the next chunk's records before it
+// processes the current one.  After the (run, cell) sort a run's particles are
+// contiguous, so a lane's particles mostly belong to one run: the lane keeps
+// that run's statistics in registers (kinetic energy per unit mass in
+// float-float) and adds them to the run's counters when its run changes.
 __global__ void __launch_bounds__(kMoveThreads) k_batch_move(MixedParts P, int64_t n, const SlotDev *__restrict__ slots,
                                                              SlotStat *stats, int kill) {
-  __shared__ float ske[256];
-  __shared__ unsigned sk[256], scr[256], sl[256];
-  for (int i = threadIdx.x; i < 256; i += blockDim.x) {
-    ske[i] = 0.f;
-    sk[i] = scr[i] = sl[i] = 0u;
+  const int lane = threadIdx.x & 31;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nchunks = (n + 31) >> 5;
+  const int64_t per = (nchunks + nw - 1) / nw;
+  int64_t c = w * per;
+  const int64_t cend = c + per < nchunks ? c + per : nchunks;
+  int cur = -1;
+  ff ke = {0.f, 0.f};
+  unsigned kl = 0, cr = 0, lm = 0;
+  auto flush = [&]() {
+    if (cur >= 0) {
+      const double e = (double)ke.hi + (double)ke.lo;
+      if (e != 0.0) atomicAdd(&stats[cur].ke, e);
+      if (kl) atomicAdd(&stats[cur].killed, (unsigned long long)kl);
+      if (cr) atomicAdd(&stats[cur].cross, (unsigned long long)cr);
+      if (lm) atomicAdd(&stats[cur].limit, (unsigned long long)lm);
+    }
+    ke = ff{0.f, 0.f};
+    kl = cr = lm = 0;
+  };
+  uint32_t cs_n = MPG_DEAD;
+  float4 bv_n = make_float4(0.f, 0.f, 0.f, 0.f);
+  float2 vv_n = make_float2(0.f, 0.f);
+  if (c < cend) {
+    const int64_t p = c * 32 + lane;
+    if (p < n) {
+      cs_n = P.c[p];
+      bv_n = P.b[p];
+      vv_n = P.v[p];
+    }
   }
-  __syncthreads();
-  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  uint32_t key = MPG_DEAD;
-  float d1 = 0.f, d2 = 0.f, d3 = 0.f;
-  int dq = 0;
-  if (p < n) {
-    const uint32_t cs = P.c[p];
-    if (cs != MPG_DEAD) {
+  for (; c < cend; ++c) {
+    const int64_t p = c * 32 + lane;
+    const uint32_t cs = cs_n;
+    const float4 bv = bv_n;
+    const float2 vv = vv_n;
+    cs_n = MPG_DEAD;
+    if (c + 1 < cend) {
+      const int64_t q = p + 32;
+      if (q < n) {
+        cs_n = P.c[q];
+        bv_n = P.b[q];
+        vv_n = P.v[q];
+      }
+    }
+    uint32_t key = MPG_DEAD;
+    float d1 = 0.f, d2 = 0.f, d3 = 0.f;
+    int dq = 0;
+    if (p < n && cs != MPG_DEAD) {
       const int slot = (int)(cs >> 24);
       const SlotDev &S = slots[slot];
       if (S.active) {
+        if (slot != cur) {
+          flush();
+          cur = slot;
+        }
         uint32_t e = cs & 0xFFFFFFu;
-        const float4 bv = P.b[p];
-        const float2 vv = P.v[p];
         float l1 = bv.x, l2 = bv.y, l3 = bv.z;
         float vx = bv.w, vy = vv.x, vz = vv.y;
         bool dead, lim;
         const int it = mixed_walk(S.rec, S.nbr, e, l1, l2, l3, vx, vy, vz, S.hk, S.dt, kill, S.max_cross, dead, lim);
-        atomicAdd(&scr[slot], (unsigned)it);
-        if (lim) atomicAdd(&sl[slot], 1u);
+        cr += (unsigned)it;
+        lm += lim ? 1u : 0u;
         if (dead) {
-          atomicAdd(&sk[slot], 1u);
+          kl += 1;
           P.c[p] = MPG_DEAD;
         } else {
           if (e != (cs & 0xFFFFFFu)) P.c[p] = ((uint32_t)slot << 24) | e;
           P.b[p] = make_float4(l1, l2, l3, vx);
           P.v[p] = make_float2(vy, vz);
           // kinetic energy per unit mass; scaled by w m / 2 on the host
-          atomicAdd(&ske[slot], __fmaf_rn(vz, vz, __fmaf_rn(vy, vy, vx * vx)));
+          ke = ff_add(ke, ff{__fmaf_rn(vz, vz, __fmaf_rn(vy, vy, vx * vx)), 0.f});
           key = ((uint32_t)slot << 24) | e;
           d1 = l1;
           d2 = l2;
@@ -200,15 +272,23 @@ __global__ void __launch_bounds__(kMoveThreads) k_batch_move(MixedParts P, int64
         }
       }
     }
+    // every lane of the warp is here (c is uniform across the warp)
+    batch_deposit_warp(slots, key, d1, d2, d3, dq);
   }
-  batch_deposit_warp(slots, key, d1, d2, d3, dq);
-  __syncthreads();
-  for (int i = threadIdx.x; i < 256; i += blockDim.x) {
-    if (ske[i] != 0.f) atomicAdd(&stats[i].ke, (double)ske[i]);
-    if (sk[i]) atomicAdd(&stats[i].killed, (unsigned long long)sk[i]);
-    if (scr[i]) atomicAdd(&stats[i].cross, (unsigned long long)scr[i]);
-    if (sl[i]) atomicAdd(&stats[i].limit, (unsigned long long)sl[i]);
+  flush();
+}
+
+// resident blocks of the persistent batch move on the current device (one wave)
+unsigned batch_move_blocks(int device) {
+  static int cached[64] = {0};
+  if (device < 0 || device >= 64) device = 0;
+  if (!cached[device]) {
+    int sms = 0, occ = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batch_move, kMoveThreads, 0);
+    cached[device] = (sms > 0 ? sms : 1) * (occ > 0 ? occ : 1);
   }
+  return (unsigned)cached[device];
 }
 
 // initial deposit of newly admitted particles [n0, n1)
@@ -311,6 +391,8 @@ template <int TH>
 __device__ void solve_run(const SlotDev &S, SlotStat *st, const int part, const int nparts) {
   __shared__ double red[32];
   __shared__ ff smf[4 * 32];
+  __shared__ float smw[4 * 32];
+  __shared__ ff smt[4];
   __shared__ double bc;
   unsigned epoch = 0;
   const int64_t n = S.N;
@@ -433,6 +515,9 @@ __device__ void solve_run(const SlotDev &S, SlotStat *st, const int part, const 
       ff rn = ff_add(rho, ff_mulf(rq, -2.f * af));
       rn = ff_add(rn, ff_mulf(ff_mulf(qq, af), af));
       const float bf = rn.hi > 0.f ? rn.hi / rho.hi : 0.f;
+      // separate r, p, q arrays here (not one float4 per node as in the
+      // single-run solver): a batch CTA holds many rows per thread, where the
+      // row loop is bound by L1 bytes rather than load latency
       const float *rk = S.r[cur], *pk = S.p[cur], *qk = S.q[cur];
       float *rnx = S.r[cur ^ 1], *pnx = S.p[cur ^ 1], *qnx = S.q[cur ^ 1];
       ff dpq = {0.f, 0.f}, drq = {0.f, 0.f}, dqq = {0.f, 0.f}, drr = {0.f, 0.f};
@@ -461,15 +546,65 @@ __device__ void solve_run(const SlotDev &S, SlotStat *st, const int part, const 
         drr = ff_add(drr, ff_prod(ri, ri));
       }
       set = phase & 1;
-      ff v4[4] = {dpq, drq, dqq, drr};
-      block_sum_ff<4>(v4, smf);
-      put_ff(set, v4, 4);
-      if (!group_barrier(st, nparts, epoch)) return;
-      total_ff(set, tot, 4);
-      pq = tot[0];
-      rq = tot[1];
-      qq = tot[2];
-      rho = tot[3];
+      {
+        // block partials: FP32 warp trees, one float-float pass over the warp sums
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        float w4[4] = {dpq.hi + dpq.lo, drq.hi + drq.lo, dqq.hi + dqq.lo, drr.hi + drr.lo};
+        for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+          for (int k = 0; k < 4; ++k) w4[k] += __shfl_down_sync(0xffffffffu, w4[k], o);
+        if (lane == 0)
+#pragma unroll
+          for (int k = 0; k < 4; ++k) smw[k * 32 + wid] = w4[k];
+        __syncthreads();
+        if (wid == 0) {
+          ff tt[4];
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            tt[k] = ff{lane < TH / 32 ? smw[k * 32 + lane] : 0.f, 0.f};
+            for (int o = 16; o > 0; o >>= 1) tt[k] = ff_add(tt[k], ff_shfl_down(tt[k], o));
+          }
+          if (lane == 0) {
+            if (nparts == 1) {
+#pragma unroll
+              for (int k = 0; k < 4; ++k) smt[k] = tt[k];
+            } else {
+              float4 *rec = reinterpret_cast<float4 *>(slot64(set, 0)) + 2 * part;
+              rec[0] = make_float4(tt[0].hi, tt[0].lo, tt[1].hi, tt[1].lo);
+              rec[1] = make_float4(tt[2].hi, tt[2].lo, tt[3].hi, tt[3].lo);
+            }
+          }
+        }
+        if (nparts > 1) {
+          if (!group_barrier(st, nparts, epoch)) return;
+          // run totals: warp 0 sums the part records (at most 64) in part order
+          if (wid == 0) {
+            const float4 *rec = reinterpret_cast<const float4 *>(slot64(set, 0));
+            ff tt[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+              const int q = lane + 32 * j;
+              if (q < nparts) {
+                const float4 x = rec[2 * q], y = rec[2 * q + 1];
+                tt[0] = ff_add(tt[0], ff{x.x, x.y});
+                tt[1] = ff_add(tt[1], ff{x.z, x.w});
+                tt[2] = ff_add(tt[2], ff{y.x, y.y});
+                tt[3] = ff_add(tt[3], ff{y.z, y.w});
+              }
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              for (int o = 16; o > 0; o >>= 1) tt[k] = ff_add(tt[k], ff_shfl_down(tt[k], o));
+              if (lane == 0) smt[k] = tt[k];
+            }
+          }
+        }
+        __syncthreads();
+      }
+      pq = smt[0];
+      rq = smt[1];
+      qq = smt[2];
+      rho = smt[3];
       ++phase;
       cur ^= 1;
       ++total_inner;
@@ -482,6 +617,7 @@ __device__ void solve_run(const SlotDev &S, SlotStat *st, const int part, const 
     st->iters = total_inner;
     st->status = status;
     st->resid = rho0 > 0.0 ? sqrt(rho64 / rho0) : 0.0;
+    if (*S.hist < 2) ++*S.hist;
   }
 }
 
@@ -527,6 +663,7 @@ struct mpg_batch {
   Run runs[kMaxSlots];
   SlotDev *d_slots = nullptr;
   SlotStat *d_stats = nullptr, *h_stats = nullptr;
+  int *d_hist = nullptr;  // per slot: solutions in the extrapolation history
   // plans
   int2 *d_conv_plan = nullptr, *d_ef_plan = nullptr, *d_block_items = nullptr;
   int4 *d_items = nullptr;
@@ -539,6 +676,7 @@ struct mpg_batch {
   uint32_t *d_cnt = nullptr, *d_start = nullptr, *d_scan = nullptr, *d_count = nullptr, *h_count = nullptr;
   int64_t keys_cap = 0, start_cap = 0, scan_cap = 0;
   int64_t steps_since_sort = 0;
+  int64_t admitted_since_sort = 0;  // particles admitted since the last (run, cell) sort
   // graph
   cudaGraphExec_t gexec = nullptr;
   int64_t graph_n = -1;
@@ -719,6 +857,7 @@ int batch_sort(mpg_batch *b) {
   b->cur = other;
   b->n = *b->h_count;
   b->steps_since_sort = 0;
+  b->admitted_since_sort = 0;
   return MPG_OK;
 }
 
@@ -733,10 +872,10 @@ int enqueue_step(mpg_batch *b) {
                                     0, s));
   }
   if (b->n_ef_blocks) k_batch_efield<<<b->n_ef_blocks, 256, 0, s>>>(b->d_slots, b->d_ef_plan);
-  if (b->n > 0)
-    k_batch_move<<<(unsigned)((b->n + kMoveThreads - 1) / kMoveThreads), kMoveThreads, 0, s>>>(b->mp[b->cur], b->n,
-                                                                                               b->d_slots, b->d_stats,
-                                                                                               1);
+  if (b->n > 0) {
+    const unsigned want = (unsigned)((b->n + kMoveThreads - 1) / kMoveThreads), wave = batch_move_blocks(b->device);
+    k_batch_move<<<want < wave ? want : wave, kMoveThreads, 0, s>>>(b->mp[b->cur], b->n, b->d_slots, b->d_stats, 1);
+  }
   BCK(cudaGetLastError());
   return MPG_OK;
 }
@@ -828,7 +967,8 @@ int mpg_batch_create(int device, int64_t budget_bytes, int max_runs, int64_t par
   b->cap = particle_capacity;
   b->used = particle_capacity * 56;
   if (balloc(b, nullptr, &b->d_slots, kMaxSlots) || balloc(b, nullptr, &b->d_stats, kMaxSlots) ||
-      balloc(b, nullptr, &b->d_base, kMaxSlots) || balloc(b, nullptr, &b->d_count, 1))
+      balloc(b, nullptr, &b->d_base, kMaxSlots) || balloc(b, nullptr, &b->d_count, 1) ||
+      balloc(b, nullptr, &b->d_hist, kMaxSlots))
     return bail(MPG_ERR_CUDA);
   if (cudaMallocHost(&b->h_stats, sizeof(SlotStat) * kMaxSlots) != cudaSuccess ||
       cudaMallocHost(&b->h_count, sizeof(uint32_t)) != cudaSuccess)
@@ -852,8 +992,8 @@ int mpg_batch_destroy(mpg_batch *b) {
     cudaFree(b->mp[k].b);
     cudaFree(b->mp[k].v);
   }
-  void *ps[] = {b->d_slots, b->d_stats, b->d_base, b->d_count, b->d_conv_plan, b->d_ef_plan, b->d_block_items,
-                b->d_items, b->d_cnt, b->d_start, b->d_scan};
+  void *ps[] = {b->d_slots, b->d_stats, b->d_base, b->d_count, b->d_hist, b->d_conv_plan, b->d_ef_plan,
+                b->d_block_items, b->d_items, b->d_cnt, b->d_start, b->d_scan};
   for (void *p : ps)
     if (p) cudaFree(p);
   if (b->h_stats) cudaFreeHost(b->h_stats);
@@ -979,6 +1119,8 @@ int mpg_batch_admit(mpg_batch *b, const mpg_run_desc *d, int *slot) {
   BTRY(balloc(b, &r, &r64, hm.N));
   for (int k = 0; k < 7; ++k) BTRY(balloc(b, &r, &f[k], hm.N));
   BTRY(balloc(b, &r, &parts, 8 * kMaxParts));
+  double *phi_prev;
+  BTRY(balloc(b, &r, &phi_prev, hm.N));
   std::vector<float> recv(12 * hm.T), ratio_h;
   for (int64_t t = 0; t < hm.T; ++t) {
     for (int q = 0; q < 9; ++q) recv[12 * t + q] = (float)hm.jinv[9 * t + q];
@@ -1014,6 +1156,9 @@ int mpg_batch_admit(mpg_batch *b, const mpg_run_desc *d, int *slot) {
   v.q[1] = f[5];
   v.z = f[6];
   v.partials = parts;
+  v.phi_prev = phi_prev;
+  v.hist = b->d_hist + s;
+  BCK(cudaMemsetAsync(v.hist, 0, sizeof(int), st));
   // fill: append the run's particles, species field = slot
   DevMesh dm;
   dm.T = hm.T;
@@ -1032,6 +1177,7 @@ int mpg_batch_admit(mpg_batch *b, const mpg_run_desc *d, int *slot) {
     k_batch_deposit<<<(unsigned)((d->n_particles + 255) / 256), 256, 0, st>>>(b->mp[b->cur], n0, b->n, b->d_slots);
   BCK(cudaGetLastError());
   BCK(cudaStreamSynchronize(st));
+  b->admitted_since_sort += d->n_particles;
   b->plan_dirty = true;
   r.last.active = r.active;
   r.last.n_alive = r.n_alive;
@@ -1054,7 +1200,11 @@ int mpg_batch_step(mpg_batch *b, int n_steps, mpg_batch_stats *st) {
         parts += b->runs[s].n_alive;
       }
     if (nact == 0) break;
-    if (b->sort_interval > 0 && b->steps_since_sort >= b->sort_interval) BTRY(batch_sort(b));
+    // sort every sort_interval steps, and before a step when the particles
+    // admitted since the last sort (in fill order) are a tenth of the batch
+    if (b->sort_interval > 0 &&
+        (b->steps_since_sort >= b->sort_interval || b->admitted_since_sort * 10 >= b->n))
+      BTRY(batch_sort(b));
     double ms = 0.0;
     BTRY(step_once(b, ms));
     b->steps_since_sort++;
