@@ -63,12 +63,14 @@ def test_fixed_point_deposit_bit_exact_and_exact_charge(mpg, orc):
     assert (acc2 == acc).all()
 
 
+@pytest.mark.parametrize("n_side", [10, 56])
 @pytest.mark.parametrize("jitter", [0.2, 0.0])
-def test_mixed_solve_reaches_fp64_tolerance(mpg, orc, jitter):
+def test_mixed_solve_reaches_fp64_tolerance(mpg, orc, jitter, n_side):
     # jitter 0.2: stored FP32 operator with Jacobi scaling; jitter 0: uniform
-    # mesh, constant-stencil FP32 operator
-    ctx = _ctx(mpg, n_side=10, warm_start=0, jitter=jitter)
-    m = orc.Mesh(10, split=6, mapping=4 if jitter else 0, jitter=jitter, seed=4)
+    # mesh, constant-stencil FP32 operator.  56^3 has more rows than solver
+    # threads, so the rows are walked along j with the register window.
+    ctx = _ctx(mpg, n_side=n_side, warm_start=0, jitter=jitter)
+    m = orc.Mesh(n_side, split=6, mapping=4 if jitter else 0, jitter=jitter, seed=4)
     m.assemble(1)
     rng = np.random.default_rng(7)
     b = rng.standard_normal(m.N)
@@ -78,7 +80,7 @@ def test_mixed_solve_reaches_fp64_tolerance(mpg, orc, jitter):
     x = ctx.get_field(mpg.FIELD_PHI)
     r = b - m.spmv(x)
     assert np.linalg.norm(r) / np.linalg.norm(b) < 1e-10
-    ox, _, _ = orc.cg(m, b, tol=1e-12)
+    ox, _, _ = orc.cg(m, b, tol=1e-12, max_iter=5000, nthreads=8)
     assert np.abs(x - ox).max() <= 1e-8 * np.abs(ox).max()
 
 
