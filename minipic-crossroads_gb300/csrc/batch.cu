@@ -318,27 +318,43 @@ __global__ void k_batch_kill_slot(uint32_t *c, int64_t n, int slot) {
 
 // counting sort by (run, cell): key = base[slot] + cell; particles of
 // non-resident runs and dead particles are dropped
+// Runs of equal (run, cell) words in a warp (particles stay nearly sorted
+// between sorts): the run's first lane and the lane's rank within its run.
+__device__ __forceinline__ void key_run(uint32_t key, int &first, int &rank, int &len) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const uint32_t prev = __shfl_up_sync(FULL, key, 1);
+  const unsigned heads = __ballot_sync(FULL, lane == 0 || prev != key);
+  first = 31 - __clz(heads & (FULL >> (31 - lane)));
+  rank = lane - first;
+  const unsigned after = heads & ~(FULL >> (31 - lane));
+  len = (after ? __ffs(after) - 1 : 32) - first;
+}
+
 __global__ void k_batch_hist(const uint32_t *__restrict__ c, int64_t n, const int64_t *__restrict__ base,
                              uint32_t *__restrict__ cnt) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n) return;
-  const uint32_t cs = c[p];
-  if (cs == MPG_DEAD) return;
-  const int64_t b = base[cs >> 24];
-  if (b < 0) return;
-  atomicAdd(&cnt[b + (cs & 0xFFFFFFu)], 1u);
+  uint32_t cs = p < n ? c[p] : MPG_DEAD;
+  if (cs != MPG_DEAD && base[cs >> 24] < 0) cs = MPG_DEAD;
+  int first, rank, len;
+  key_run(cs, first, rank, len);
+  if (rank == 0 && cs != MPG_DEAD) atomicAdd(&cnt[base[cs >> 24] + (cs & 0xFFFFFFu)], (unsigned)len);
 }
 
+// one atomic per run of equal keys; lanes of a run keep their order
 __global__ void k_batch_scatter(MixedParts P, int64_t n, MixedParts Q, const int64_t *__restrict__ base,
                                 const uint32_t *__restrict__ start, uint32_t *__restrict__ fill) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n) return;
-  const uint32_t cs = P.c[p];
+  uint32_t cs = p < n ? P.c[p] : MPG_DEAD;
+  if (cs != MPG_DEAD && base[cs >> 24] < 0) cs = MPG_DEAD;
+  int first, rank, len;
+  key_run(cs, first, rank, len);
+  const int64_t k = cs != MPG_DEAD ? base[cs >> 24] + (cs & 0xFFFFFFu) : 0;
+  uint32_t off = 0;
+  if (rank == 0 && cs != MPG_DEAD) off = atomicAdd(&fill[k], (unsigned)len);
+  off = __shfl_sync(0xffffffffu, off, first);
   if (cs == MPG_DEAD) return;
-  const int64_t b = base[cs >> 24];
-  if (b < 0) return;
-  const int64_t k = b + (cs & 0xFFFFFFu);
-  const uint32_t dst = start[k] + atomicAdd(&fill[k], 1u);
+  const uint32_t dst = start[k] + off + (uint32_t)rank;
   Q.c[dst] = cs;
   Q.b[dst] = P.b[p];
   Q.v[dst] = P.v[p];

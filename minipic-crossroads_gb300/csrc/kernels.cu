@@ -687,21 +687,42 @@ __global__ void __launch_bounds__(kThreads) k_mixed_move_persistent(MixedParts P
   block_totals_push(&bt, ke, killed, cross, limit, st);
 }
 
-__global__ void k_cell_hist(const uint32_t *__restrict__ c, int64_t n, uint32_t *__restrict__ cnt) {
-  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n) return;
-  const uint32_t cs = c[p];
-  if (cs != MPG_DEAD) atomicAdd(&cnt[cs & 0xFFFFFFu], 1u);
+// Runs of equal cells in a warp (particles stay nearly sorted between sorts):
+// the run's first lane and the lane's rank within its run.
+__device__ __forceinline__ void cell_run(uint32_t key, int &first, int &rank, int &len) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const uint32_t prev = __shfl_up_sync(FULL, key, 1);
+  const unsigned heads = __ballot_sync(FULL, lane == 0 || prev != key);
+  first = 31 - __clz(heads & (FULL >> (31 - lane)));
+  rank = lane - first;
+  const unsigned after = heads & ~(FULL >> (31 - lane));  // heads above this lane
+  const int next = after ? __ffs(after) - 1 : 32;
+  len = next - first;
 }
 
+__global__ void k_cell_hist(const uint32_t *__restrict__ c, int64_t n, uint32_t *__restrict__ cnt) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t cs = p < n ? c[p] : MPG_DEAD;
+  const uint32_t key = cs == MPG_DEAD ? MPG_DEAD : (cs & 0xFFFFFFu);
+  int first, rank, len;
+  cell_run(key, first, rank, len);
+  if (rank == 0 && key != MPG_DEAD) atomicAdd(&cnt[key], (unsigned)len);
+}
+
+// one atomic per run of equal cells; lanes of a run keep their order
 __global__ void k_cell_scatter(MixedParts P, int64_t n, MixedParts Q, const uint32_t *__restrict__ start,
                                uint32_t *__restrict__ fill) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n) return;
-  const uint32_t cs = P.c[p];
-  if (cs == MPG_DEAD) return;
-  const uint32_t e = cs & 0xFFFFFFu;
-  const uint32_t dst = start[e] + atomicAdd(&fill[e], 1u);
+  const uint32_t cs = p < n ? P.c[p] : MPG_DEAD;
+  const uint32_t key = cs == MPG_DEAD ? MPG_DEAD : (cs & 0xFFFFFFu);
+  int first, rank, len;
+  cell_run(key, first, rank, len);
+  uint32_t base = 0;
+  if (rank == 0 && key != MPG_DEAD) base = atomicAdd(&fill[key], (unsigned)len);
+  base = __shfl_sync(0xffffffffu, base, first);
+  if (key == MPG_DEAD) return;
+  const uint32_t dst = start[key] + base + (uint32_t)rank;
   Q.c[dst] = cs;
   Q.b[dst] = P.b[p];
   Q.v[dst] = P.v[p];
