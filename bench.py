@@ -91,6 +91,9 @@ def total_particles(w):
 # CG initial guess of the single-run workloads (both forms): 2 = linear
 # extrapolation from the last two solutions, 1 = the previous solution
 WARM_START = 2
+# inner solver of the mixed form: "cg" plain FP32 CG, "mg" CG preconditioned
+# by the geometric multigrid V-cycle (falls back to "cg" on periodic meshes)
+MIXED_SOLVER = "mg"
 
 
 def make_ctx(mpg, w, precision, device=0, seed_offset=0):
@@ -98,7 +101,8 @@ def make_ctx(mpg, w, precision, device=0, seed_offset=0):
     ctx.mesh(w["n_side"], split=mpg.SPLIT_KUHN6, lo=w.get("lo", 0.0), hi=w.get("hi", 1.0),
              mapping=mpg.MAP_JITTER if w["jitter"] else mpg.MAP_NONE, jitter=w["jitter"], seed=7,
              periodic=w.get("periodic", 0))
-    ctx.configure(precision=precision, deposit=mpg.DEPOSIT_LINEAR, solver=mpg.SOLVER_CG, tol=1e-10, max_iter=5000,
+    kind = mpg.SOLVER_CG_MG if precision == mpg.MIXED and MIXED_SOLVER == "mg" else mpg.SOLVER_CG
+    ctx.configure(precision=precision, deposit=mpg.DEPOSIT_LINEAR, solver=kind, tol=1e-10, max_iter=5000,
                   warm_start=WARM_START, kill_on_wall=1, max_crossings=1000,
                   sort_interval=w["sort_interval"] if precision == mpg.MIXED else 0,
                   rho_background=w["rho_background"])
@@ -512,9 +516,12 @@ def main():
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--warm-start", type=int, default=2, choices=[0, 1, 2, 3],
                     help="CG initial guess: 0 zero, 1 previous phi, 2/3 linear/quadratic extrapolation")
+    ap.add_argument("--mixed-solver", default="mg", choices=["cg", "mg"],
+                    help="inner solver of the mixed form: plain CG or multigrid-preconditioned CG")
     args = ap.parse_args()
-    global WARM_START
+    global WARM_START, MIXED_SOLVER
     WARM_START = args.warm_start
+    MIXED_SOLVER = args.mixed_solver
     if args.workload in ("ensemble", "serving"):
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the reference has no batched or serving mode; "
@@ -615,6 +622,8 @@ def main():
                            "particles": total_particles(w), "dt": w["dt"], "cg_tol": 1e-10,
                            "cg_initial_guess": ["zero", "previous phi", "extrapolated 2*phi[n-1]-phi[n-2]",
                                                 "extrapolated 3*phi[n-1]-3*phi[n-2]+phi[n-3]"][WARM_START],
+                           "cg_preconditioner": ("geometric multigrid V(1,1)" if precision == mpg.MIXED
+                                                 and MIXED_SOLVER == "mg" and not w.get("periodic", 0) else "none"),
                            "parallelism": "replicas" if world > 1 else "single",
                            "l2": "inputs larger than L2 (particle state > 129 MB), no flush"},
                 "phases_ms_per_step": {k: round(v, 4) for k, v in phases.items()},

@@ -17,7 +17,7 @@ ERR_ARG, ERR_CUDA, ERR_CAPACITY, ERR_WALK_LIMIT, ERR_NAN, ERR_NOT_CONVERGED, ERR
     -1, -2, -3, -4, -5, -6, -7, -8, -9
 PLAIN, MIXED = 0, 1
 DEPOSIT_REF_QUARTER, DEPOSIT_LINEAR = 0, 1
-SOLVER_BICGSTAB, SOLVER_CG = 0, 1
+SOLVER_BICGSTAB, SOLVER_CG, SOLVER_CG_MG = 0, 1, 2
 SPLIT_REF5, SPLIT_KUHN6 = 5, 6
 MAP_NONE, MAP_JITTER = 0, 4
 FIELD_RHS, FIELD_PHI, FIELD_E_TET, FIELD_BACKGROUND = 0, 1, 2, 3

@@ -24,8 +24,8 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler", "-
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-Wall",
              "-I" + INCLUDE, "-I" + CSRC]
 
-CU_SOURCES = ["kernels.cu", "solver.cu", "api.cu", "batch.cu"]
-CXX_SOURCES = ["mesh_host.cpp"]
+CU_SOURCES = ["kernels.cu", "solver.cu", "mg.cu", "api.cu", "batch.cu"]
+CXX_SOURCES = ["mesh_host.cpp", "mg_host.cpp"]
 HEADERS = ["mpg_internal.h", "mpg_kernels.h", "mpg_device.cuh", "mpg_walk.cuh"]
 
 

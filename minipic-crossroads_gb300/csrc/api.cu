@@ -40,6 +40,11 @@ struct mpg_ctx {
   bool configured = false;
   mpg_config cfg{};
   int csr_mode = -1;
+  int csr_mg = 0;              // the multigrid hierarchy was built with the current CSR
+  MgDev mg;                    // multigrid preconditioner of the mixed solver (MPG_SOLVER_CG_MG)
+  bool mg_ok = false;
+  std::vector<void *> mg_bufs;  // its device arrays
+  int mg_max_blocks = 0;
   int64_t nnz = 0;
   int32_t *rowptr = nullptr, *col = nullptr;
   double *val = nullptr;
@@ -311,13 +316,14 @@ int ensure_cg_work(mpg_ctx *c, int64_t n) {
   if (const char *e = getenv("MPG_CG_BLOCKS")) c->cg.block_cap = atoi(e);
   if (const char *e = getenv("MPG_CG_INNER_TOL")) c->inner_tol = atof(e);
   c->cg.max_blocks = cg_max_blocks(c->device, c->cg.threads == 256 || c->cg.threads == 1024 ? c->cg.threads : 512);
+  c->mg_max_blocks = mg_max_blocks(c->device, c->cg.threads == 256 || c->cg.threads == 1024 ? c->cg.threads : 512);
   TRY(dalloc(c, &c->cg.r, n));
   TRY(dalloc(c, &c->cg.p0, n));
   TRY(dalloc(c, &c->cg.p1, n));
   TRY(dalloc(c, &c->cg.q, n));
-  TRY(dalloc(c, &c->cg.v4, 2 * n));
+  TRY(dalloc(c, &c->cg.v4, 3 * n));  // 8n floats for the mixed CG, 9n for the multigrid PCG
   if (c->cg.max_blocks < 1) return fail(c, MPG_ERR_CUDA, "solver kernels cannot be resident (occupancy 0)");
-  TRY(dalloc(c, &c->cg.partials, 8 * (int64_t)c->cg.max_blocks));
+  TRY(dalloc(c, &c->cg.partials, 8 * (int64_t)std::max(c->cg.max_blocks, c->mg_max_blocks)));
   c->cg_n = n;
   return MPG_OK;
 }
@@ -399,13 +405,18 @@ int initial_guess(mpg_ctx *c, int64_t N) {
 
 int phase_solve(mpg_ctx *c) {
   const int64_t N = c->dm.N;
-  if (c->cfg.precision == MPG_MIXED || c->cfg.solver == MPG_SOLVER_CG) {
+  if (c->cfg.precision == MPG_MIXED || c->cfg.solver != MPG_SOLVER_BICGSTAB) {
     TRY(ensure_cg_work(c, N));
     TRY(initial_guess(c, N));
-    int rc = c->cfg.precision == MPG_MIXED
-                 ? run_cg_mixed(c->stream, c->dia, c->rhs, c->phi, c->cfg.tol, c->inner_tol, c->cfg.max_iter, c->cg,
-                                c->d_stats)
-                 : run_cg64_dia(c->stream, c->dia, c->rhs, c->phi, c->cfg.tol, c->cfg.max_iter, c->cg, c->d_stats);
+    int rc;
+    if (c->cfg.precision == MPG_MIXED && c->mg_ok)
+      rc = run_cg_mg(c->stream, c->dia, c->mg, c->rhs, c->phi, c->cfg.tol, c->inner_tol, c->cfg.max_iter, c->cg,
+                     c->mg_max_blocks, c->d_stats);
+    else if (c->cfg.precision == MPG_MIXED)
+      rc = run_cg_mixed(c->stream, c->dia, c->rhs, c->phi, c->cfg.tol, c->inner_tol, c->cfg.max_iter, c->cg,
+                        c->d_stats);
+    else
+      rc = run_cg64_dia(c->stream, c->dia, c->rhs, c->phi, c->cfg.tol, c->cfg.max_iter, c->cg, c->d_stats);
     c->launches += 1;
     if (rc) return fail(c, rc, "CG launch failed: %s", cudaGetErrorString(cudaGetLastError()));
     if (c->dm.fper) {
@@ -608,6 +619,76 @@ void free_mesh(mpg_ctx *c) {
   d = DevMesh();
 }
 
+void free_mg(mpg_ctx *c) {
+  for (void *p : c->mg_bufs) dfree(c, p);
+  c->mg_bufs.clear();
+  c->mg = MgDev();
+  c->mg_ok = false;
+}
+
+// upload a host multigrid hierarchy; levels with more than kMgBlockRows rows
+// (and always the fine one) are processed by the whole grid
+int upload_mg(mpg_ctx *c, const MgHostHierarchy &H) {
+  int64_t kMgBlockRows = 4096;
+  if (const char *e = getenv("MPG_MG_BLOCK_ROWS")) kMgBlockRows = atoll(e);
+  free_mg(c);
+  MgDev &m = c->mg;
+  m.nlev = (int)H.lev.size();
+  for (int l = 0; l < m.nlev; ++l) {
+    const MgHostLevel &h = H.lev[l];
+    MgLevelDev &L = m.lev[l];
+    L.gx = h.gx;
+    L.gy = h.gy;
+    L.gz = h.gz;
+    L.sj = h.gz;
+    L.si = h.gy * h.gz;
+    L.n = (int64_t)h.gx * h.gy * h.gz;
+    float *dinv;
+    uint8_t *bnd;
+    TRY(dalloc(c, &dinv, L.n));
+    TRY(dalloc(c, &bnd, L.n));
+    c->mg_bufs.push_back(dinv);
+    c->mg_bufs.push_back(bnd);
+    CK(cudaMemcpyAsync(dinv, h.dinv.data(), sizeof(float) * L.n, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(bnd, h.bnd.data(), L.n, cudaMemcpyHostToDevice, c->stream));
+    L.dinv = dinv;
+    L.bnd = bnd;
+    if (l > 0) {
+      float *val, *r, *e, *t;
+      TRY(dalloc(c, &val, 27 * L.n));
+      TRY(dalloc(c, &r, L.n));
+      TRY(dalloc(c, &e, L.n));
+      TRY(dalloc(c, &t, L.n));
+      for (void *p : {(void *)val, (void *)r, (void *)e, (void *)t}) c->mg_bufs.push_back(p);
+      CK(cudaMemcpyAsync(val, h.val.data(), sizeof(float) * 27 * L.n, cudaMemcpyHostToDevice, c->stream));
+      CK(cudaMemsetAsync(e, 0, sizeof(float) * L.n, c->stream));
+      CK(cudaMemsetAsync(t, 0, sizeof(float) * L.n, c->stream));
+      L.val = val;
+      L.r = r;
+      L.e = e;
+      L.t = t;
+    }
+  }
+  m.ngrid = 1;
+  while (m.ngrid < m.nlev - 1 && m.lev[m.ngrid].n > kMgBlockRows) ++m.ngrid;
+  int32_t *idx;
+  float *inv;
+  m.dense_m = (int)H.dense_idx.size();
+  TRY(dalloc(c, &idx, m.dense_m));
+  TRY(dalloc(c, &inv, (int64_t)m.dense_m * m.dense_m));
+  c->mg_bufs.push_back(idx);
+  c->mg_bufs.push_back(inv);
+  CK(cudaMemcpyAsync(idx, H.dense_idx.data(), sizeof(int32_t) * m.dense_m, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(inv, H.dense_inv.data(), sizeof(float) * H.dense_inv.size(), cudaMemcpyHostToDevice,
+                     c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  m.dense_idx = idx;
+  m.dense_inv = inv;
+  if (const char *e = getenv("MPG_MG_OMEGA")) m.omega = (float)atof(e);
+  c->mg_ok = true;
+  return MPG_OK;
+}
+
 void free_field(mpg_ctx *c) {
   dfree(c, c->rowptr);
   dfree(c, c->col);
@@ -630,6 +711,7 @@ void free_field(mpg_ctx *c) {
   dfree(c, c->scan_scratch);
   c->scan_len = 0;
   dfree(c, c->bicg_work);
+  free_mg(c);
   c->configured = false;
   c->csr_mode = -1;
 }
@@ -822,7 +904,8 @@ int mpg_configure(mpg_ctx *c, const mpg_config *cfg) {
   if (cfg->precision != MPG_PLAIN && cfg->precision != MPG_MIXED) return fail(c, MPG_ERR_ARG, "bad precision");
   if (cfg->deposit != MPG_DEPOSIT_REF_QUARTER && cfg->deposit != MPG_DEPOSIT_LINEAR)
     return fail(c, MPG_ERR_ARG, "bad deposit mode");
-  if (cfg->solver != MPG_SOLVER_BICGSTAB && cfg->solver != MPG_SOLVER_CG) return fail(c, MPG_ERR_ARG, "bad solver");
+  if (cfg->solver != MPG_SOLVER_BICGSTAB && cfg->solver != MPG_SOLVER_CG && cfg->solver != MPG_SOLVER_CG_MG)
+    return fail(c, MPG_ERR_ARG, "bad solver");
   if (!(cfg->tol > 0) || cfg->max_iter < 1 || cfg->max_crossings < 1)
     return fail(c, MPG_ERR_ARG, "tol, max_iter and max_crossings must be positive");
   if (cfg->precision == MPG_MIXED && c->hm.T >= (int64_t)MPG_WALL)
@@ -833,7 +916,7 @@ int mpg_configure(mpg_ctx *c, const mpg_config *cfg) {
   if (realloc_parts) free_particles(c);
   c->cfg = *cfg;
   // the mixed form always solves the symmetric system with refined CG
-  const int mode = (cfg->precision == MPG_MIXED || cfg->solver == MPG_SOLVER_CG) ? 1 : 0;
+  const int mode = (cfg->precision == MPG_MIXED || cfg->solver != MPG_SOLVER_BICGSTAB) ? 1 : 0;
   const int64_t N = c->hm.N, T = c->hm.T;
   // rows of the assembled system: all nodes, or (symmetric form of a periodic
   // mesh) the nodes of the x < hi planes, the ghost plane being last in order
@@ -854,7 +937,8 @@ int mpg_configure(mpg_ctx *c, const mpg_config *cfg) {
     }
     return j;
   };
-  if (c->csr_mode != mode) {
+  const int want_mg = (cfg->precision == MPG_MIXED && cfg->solver == MPG_SOLVER_CG_MG) ? 1 : 0;
+  if (c->csr_mode != mode || c->csr_mg != want_mg) {
     dfree(c, c->rowptr);
     dfree(c, c->col);
     dfree(c, c->val);
@@ -944,7 +1028,16 @@ int mpg_configure(mpg_ctx *c, const mpg_config *cfg) {
       // FP64 outer residual keeps A itself).  MPG_CG_JACOBI=0 turns it off.
       const char *jenv = getenv("MPG_CG_JACOBI");
       const int center = (int)(std::lower_bound(offs.begin(), offs.end(), (int64_t)0) - offs.begin());
-      if (!c->dia.constant && !(jenv && atoi(jenv) == 0) && center < (int)offs.size() && offs[center] == 0) {
+      // with the multigrid preconditioner the inner operator stays A itself
+      // (the V-cycle smooths with its own D^-1)
+      free_mg(c);
+      if (want_mg) {
+        MgHostHierarchy H;
+        std::string why;
+        if (host_mg_build(c->hm, rp, col, val, H, why)) TRY(upload_mg(c, H));
+      }
+      if (!c->mg_ok && !c->dia.constant && !(jenv && atoi(jenv) == 0) && center < (int)offs.size() &&
+          offs[center] == 0) {
         std::vector<double> dis(R, 1.0);
         for (int64_t r = 0; r < R; ++r) {
           const double dr = d64[(size_t)center * R + r];
@@ -965,6 +1058,7 @@ int mpg_configure(mpg_ctx *c, const mpg_config *cfg) {
       CK(cudaStreamSynchronize(c->stream));
     }
     c->csr_mode = mode;
+    c->csr_mg = want_mg;
   }
   if (!c->rhs) {
     TRY(dalloc(c, &c->rhs, N));

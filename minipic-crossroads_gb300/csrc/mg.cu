@@ -1,0 +1,479 @@
+// mg.cu -- mixed-precision CG preconditioned by a geometric multigrid V-cycle.
+//
+// One cooperative launch per field solve, like k_cg_mixed: FP64 outer
+// refinement (r64 = b - A64 x, stop at |r64| <= tol |b|) around an FP32 inner
+// solve of A z = r64 / |r64|.  The inner solve is preconditioned CG in the
+// single-reduction form of Chronopoulos and Gear (one grid-wide all-reduce
+// of (r, u) and (A u, u) per iteration), with u = M r one multigrid V(1,1)
+// cycle: damped Jacobi smoothing, restriction P^T, Galerkin coarse operators
+// (mg_host.cpp) and a dense solve on the coarsest level.  Levels with many
+// rows are processed by the whole grid (a grid barrier between dependent
+// steps); the small ones and the dense solve by block 0 alone (block
+// barriers), while the other blocks wait at the next grid barrier.
+// Not part of the reference, whose CG (CG_solve.hpp:54-114) is
+// unpreconditioned; the converged phi meets the same FP64 tolerance.
+#include <cuda_runtime.h>
+
+#include "minipic_gb300.h"
+#include "mpg_device.cuh"
+#include "mpg_kernels.h"
+
+namespace {
+
+constexpr int kRecMg = 5;  // block records each of the first 128 threads gathers (grids up to 640 blocks)
+
+struct CgMgArgs {
+  DiaMatrix A;
+  MgDev mg;
+  const double *__restrict__ b;
+  double *x, *r64;
+  float *r[2], *s[2];  // fine-level PCG residual and A p, double-buffered by iteration parity
+  float *u, *w, *p, *z;  // u = M r is the V-cycle's output (mg.lev[0].t), w = A u
+  double *partials;              // outer phases: [2 sets][4][nb]; inner: one 32-byte record per block
+  double tol2, inner_tol2;
+  int max_iter;
+  DevStats *st;
+};
+
+// row range of this block on a level processed by the whole grid
+__device__ __forceinline__ void grid_rows(int64_t n, int64_t &lo, int64_t &hi) {
+  lo = n * blockIdx.x / gridDim.x;
+  hi = n * (blockIdx.x + 1) / gridDim.x;
+}
+
+// (A_l x)_i on level l, x given by the loader xv(j): the solver's
+// 15/27-diagonal operator on level 0, the Galerkin 27-point stencil on the
+// coarser levels; Dirichlet rows are identity rows
+template <int ND, bool CST, typename X>
+__device__ __forceinline__ float level_apply(const CgMgArgs &a, int l, X xv, int64_t i) {
+  const MgLevelDev &L = a.mg.lev[l];
+  if (L.bnd[i]) return xv(i);
+  float s = 0.f;
+  if (l == 0) {
+    const int64_t n = a.A.n;
+#pragma unroll
+    for (int d = 0; d < ND; ++d) s = __fmaf_rn(CST ? a.A.cst[d] : a.A.val32[d * n + i], xv(i + a.A.off[d]), s);
+  } else {
+    const int64_t n = L.n;
+#pragma unroll
+    for (int d = 0; d < 27; ++d) {
+      const int64_t off = (d / 9 - 1) * (int64_t)L.si + ((d / 3) % 3 - 1) * (int64_t)L.sj + (d % 3 - 1);
+      s = __fmaf_rn(L.val[d * n + i], xv(i + off), s);
+    }
+  }
+  return s;
+}
+
+// row index -> (i, j, k) on a level (row counts stay below 2^32)
+__device__ __forceinline__ void level_ijk(const MgLevelDev &L, int64_t r, unsigned &i, unsigned &j, unsigned &k) {
+  const unsigned rr = (unsigned)r, sj = (unsigned)L.sj, si = (unsigned)L.si;
+  i = rr / si;
+  const unsigned rem = rr - i * si;
+  j = rem / sj;
+  k = rem - j * sj;
+}
+
+// restriction r_{l+1}[C] = sum_delta w(delta) t_l[2C + delta] over the 27 fine
+// nodes around 2C (w = 1/2 per non-zero component); zero on Dirichlet rows
+__device__ __forceinline__ float restrict_at(const MgLevelDev &F, const MgLevelDev &Cl, int64_t C) {
+  if (Cl.bnd[C]) return 0.f;
+  unsigned I, J, K;
+  level_ijk(Cl, C, I, J, K);
+  const int64_t f0 = 2 * (int64_t)I * F.si + 2 * (int64_t)J * F.sj + 2 * (int64_t)K;
+  float s = 0.f;
+#pragma unroll
+  for (int di = -1; di <= 1; ++di)
+#pragma unroll
+    for (int dj = -1; dj <= 1; ++dj) {
+      const float wij = (di ? 0.5f : 1.f) * (dj ? 0.5f : 1.f);
+      const float *row = F.t + f0 + di * (int64_t)F.si + dj * (int64_t)F.sj;
+      s = __fmaf_rn(wij * 0.5f, row[-1], s);
+      s = __fmaf_rn(wij, row[0], s);
+      s = __fmaf_rn(wij * 0.5f, row[1], s);
+    }
+  return s;
+}
+
+// prolongation (P c)_i: trilinear interpolation of the coarse result c, as
+// the mean of the 8 corners (fi >> 1, (fi + 1) >> 1) x ... (a corner repeats
+// along a direction where the fine index is even)
+__device__ __forceinline__ float prolong_at(const MgLevelDev &F, const MgLevelDev &Cl, const float *__restrict__ c,
+                                            int64_t i) {
+  unsigned fi, fj, fk;
+  level_ijk(F, i, fi, fj, fk);
+  const int64_t i0 = (int64_t)(fi >> 1) * Cl.si, i1 = (int64_t)((fi + 1) >> 1) * Cl.si;
+  const int64_t j0 = (int64_t)(fj >> 1) * Cl.sj, j1 = (int64_t)((fj + 1) >> 1) * Cl.sj;
+  const int64_t k0 = fk >> 1, k1 = (fk + 1) >> 1;
+  const float s = ((c[i0 + j0 + k0] + c[i0 + j0 + k1]) + (c[i0 + j1 + k0] + c[i0 + j1 + k1])) +
+                  ((c[i1 + j0 + k0] + c[i1 + j0 + k1]) + (c[i1 + j1 + k0] + c[i1 + j1 + k1]));
+  return 0.125f * s;
+}
+
+// pre-smoothing residual on rows [lo, hi) of level l: t = r - A e with
+// e = omega D^-1 r (one Jacobi sweep from zero).  e is not stored: A e reads
+// it through a loader (rv(j) gives r at row j), and the ascending steps
+// recompute it.
+template <int ND, bool CST, typename R>
+__device__ __forceinline__ void presmooth_residual(const CgMgArgs &a, int l, int64_t lo, int64_t hi, R rv) {
+  const MgLevelDev &L = a.mg.lev[l];
+  const float om = a.mg.omega;
+  const float *__restrict__ dinv = L.dinv;
+  auto e0 = [&](int64_t j) { return om * dinv[j] * rv(j); };
+  for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) L.t[i] = rv(i) - level_apply<ND, CST>(a, l, e0, i);
+}
+
+// restriction of level l's t onto the coarse rows [clo, chi) of level l + 1
+__device__ __forceinline__ void restrict_rows(const CgMgArgs &a, int l, int64_t clo, int64_t chi) {
+  const MgLevelDev &L = a.mg.lev[l], &C = a.mg.lev[l + 1];
+  for (int64_t i = clo + threadIdx.x; i < chi; i += blockDim.x) C.r[i] = restrict_at(L, C, i);
+}
+
+// one coarse level's descending steps on rows [lo, hi) (coarse rows
+// [clo, chi)), `sync` between dependent steps
+template <int ND, bool CST, typename Sync>
+__device__ __forceinline__ bool level_down(const CgMgArgs &a, int l, int64_t lo, int64_t hi, int64_t clo, int64_t chi,
+                                           Sync sync) {
+  const float *__restrict__ r = a.mg.lev[l].r;
+  presmooth_residual<ND, CST>(a, l, lo, hi, [&](int64_t j) { return r[j]; });
+  if (!sync()) return false;
+  restrict_rows(a, l, clo, chi);
+  return sync();
+}
+
+// ascending steps: e = omega D^-1 r + P c, then t = e + omega D^-1 (r - A e)
+// (the level's result); r is the level's right-hand side
+template <int ND, bool CST, typename Sync>
+__device__ __forceinline__ bool level_up(const CgMgArgs &a, int l, int64_t lo, int64_t hi, const float *r,
+                                         const float *c, Sync sync) {
+  const MgLevelDev &L = a.mg.lev[l];
+  const MgLevelDev &C = a.mg.lev[l + 1];
+  const float om = a.mg.omega;
+  for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+    float e = om * L.dinv[i] * r[i];
+    if (!L.bnd[i]) e += prolong_at(L, C, c, i);
+    L.e[i] = e;
+  }
+  if (!sync()) return false;
+  const float *__restrict__ ev = L.e;
+  auto ld = [&](int64_t j) { return ev[j]; };
+  for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x)
+    L.t[i] = ev[i] + om * L.dinv[i] * (r[i] - level_apply<ND, CST>(a, l, ld, i));
+  return sync();
+}
+
+// coarsest level: t = A_c^-1 r over its interior rows, one warp per row of
+// the dense inverse across the whole grid (lanes over the row, fixed shuffle
+// tree); the Dirichlet rows of t stay zero
+__device__ __forceinline__ void dense_solve(const MgDev &mg) {
+  const MgLevelDev &Lc = mg.lev[mg.nlev - 1];
+  const int m = mg.dense_m, lane = threadIdx.x & 31;
+  const int nw = (blockDim.x >> 5) * gridDim.x;
+  for (int q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); q < m; q += nw) {
+    const float *__restrict__ row = mg.dense_inv + (int64_t)q * m;
+    float s = 0.f;
+    for (int k = lane; k < m; k += 32) s = __fmaf_rn(row[k], Lc.r[mg.dense_idx[k]], s);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) Lc.t[mg.dense_idx[q]] = s;
+  }
+}
+
+// rest of u = M r after level 0's pre-smoothing residual lev[0].t has been
+// written on this block's rows; rf is level 0's right-hand side r and the
+// result u is lev[0].t.  Levels [0, ngrid) run on the whole grid, levels
+// [ngrid, nlev - 1) on block 0 alone, the dense coarsest solve on the whole
+// grid again.
+template <int ND, bool CST>
+__device__ bool vcycle_rest(const CgMgArgs &a, const float *rf, unsigned &epoch) {
+  const int nl = a.mg.nlev, ng = a.mg.ngrid;
+  auto gsync = [&]() { return grid_barrier(a.st, gridDim.x, epoch); };
+  auto bsync = [&]() {
+    __syncthreads();
+    return true;
+  };
+  int64_t clo, chi;
+  if (!gsync()) return false;
+  grid_rows(a.mg.lev[1].n, clo, chi);
+  restrict_rows(a, 0, clo, chi);
+  if (!gsync()) return false;
+  for (int l = 1; l < ng; ++l) {
+    int64_t lo, hi;
+    grid_rows(a.mg.lev[l].n, lo, hi);
+    grid_rows(a.mg.lev[l + 1].n, clo, chi);
+    if (!level_down<ND, CST>(a, l, lo, hi, clo, chi, gsync)) return false;
+  }
+  const bool blk = ng < nl - 1;
+  if (blk) {
+    if (blockIdx.x == 0)
+      for (int l = ng; l < nl - 1; ++l) level_down<ND, CST>(a, l, 0, a.mg.lev[l].n, 0, a.mg.lev[l + 1].n, bsync);
+    if (!gsync()) return false;
+  }
+  dense_solve(a.mg);
+  if (!gsync()) return false;
+  if (blk) {
+    if (blockIdx.x == 0)
+      for (int l = nl - 2; l >= ng; --l)
+        level_up<ND, CST>(a, l, 0, a.mg.lev[l].n, a.mg.lev[l].r, a.mg.lev[l + 1].t, bsync);
+    if (!gsync()) return false;
+  }
+  for (int l = ng - 1; l >= 0; --l) {
+    int64_t lo, hi;
+    grid_rows(a.mg.lev[l].n, lo, hi);
+    if (!level_up<ND, CST>(a, l, lo, hi, l == 0 ? rf : a.mg.lev[l].r, a.mg.lev[l + 1].t, gsync)) return false;
+  }
+  return true;
+}
+
+template <int ND, int TH, bool CST>
+__global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mg(CgMgArgs a) {
+  __shared__ double red[32];
+  __shared__ float smw[4 * 32];
+  __shared__ ff smf[4 * 32];
+  __shared__ ff smt[4];
+  __shared__ double bcast;
+  unsigned epoch = 0;
+  const int nb = gridDim.x, bid = blockIdx.x;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t n = a.A.n;
+  const int64_t lo = n * bid / nb, hi = n * (bid + 1) / nb;
+  const uint8_t *__restrict__ bnd = a.A.bnd;
+  const double *__restrict__ v64 = a.A.val64;
+  auto slot64 = [&](int set, int k) { return a.partials + ((size_t)(set * 4 + k)) * nb; };
+  // all-reduce of two float-float values per block (block record, grid
+  // barrier, four warps gather every record in block order)
+  auto allreduce2 = [&](int set, ff g, ff d, ff &G, ff &D) -> bool {
+    float w2[2] = {g.hi + g.lo, d.hi + d.lo};
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+      for (int k = 0; k < 2; ++k) w2[k] += __shfl_down_sync(0xffffffffu, w2[k], o);
+    if (lane == 0)
+#pragma unroll
+      for (int k = 0; k < 2; ++k) smw[k * 32 + wid] = w2[k];
+    __syncthreads();
+    if (wid == 0) {
+      ff t[2];
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        t[k] = ff{lane < TH / 32 ? smw[k * 32 + lane] : 0.f, 0.f};
+        for (int o = 16; o > 0; o >>= 1) t[k] = ff_add(t[k], ff_shfl_down(t[k], o));
+      }
+      if (lane == 0) reinterpret_cast<float4 *>(slot64(set, 0))[bid] = make_float4(t[0].hi, t[0].lo, t[1].hi, t[1].lo);
+    }
+    if (!grid_barrier(a.st, nb, epoch)) return false;
+    if (wid < 4) {
+      const float4 *rec = reinterpret_cast<const float4 *>(slot64(set, 0));
+      float4 x[kRecMg];
+#pragma unroll
+      for (int j = 0; j < kRecMg; ++j) {
+        const int i = threadIdx.x + 128 * j;
+        x[j] = i < nb ? rec[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      ff t[2] = {{0.f, 0.f}, {0.f, 0.f}};
+#pragma unroll
+      for (int j = 0; j < kRecMg; ++j) {
+        t[0] = ff_add(t[0], ff{x[j].x, x[j].y});
+        t[1] = ff_add(t[1], ff{x[j].z, x[j].w});
+      }
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        for (int o = 16; o > 0; o >>= 1) t[k] = ff_add(t[k], ff_shfl_down(t[k], o));
+        if (lane == 0) smf[k * 32 + wid] = t[k];
+      }
+    }
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        ff u = lane < 4 ? smf[k * 32 + lane] : ff{0.f, 0.f};
+        for (int o = 2; o > 0; o >>= 1) u = ff_add(u, ff_shfl_down(u, o));
+        if (lane == 0) smt[k] = u;
+      }
+    }
+    __syncthreads();
+    G = smt[0];
+    D = smt[1];
+    __syncthreads();
+    return true;
+  };
+  double bb = 0.0;
+  for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) bb += a.b[i] * a.b[i];
+  double t = block_sum(bb, red);
+  if (threadIdx.x == 0) slot64(1, 3)[bid] = t;  // read after the first barrier
+  int total_inner = 0, status = 0, sweeps = 0, phase = 0;
+  double rho64 = 0.0, rho0 = 0.0;
+  for (;; ++sweeps) {
+    // ---- FP64 residual with the FP64 matrix (identity rows: x = b there)
+    double rr = 0.0;
+    for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+      double s = 0.0;
+      if (bnd[i]) {
+        a.x[i] = a.b[i];
+        s = a.x[i];
+      } else {
+#pragma unroll
+        for (int d = 0; d < ND; ++d) s += v64[d * n + i] * a.x[i + a.A.off[d]];
+      }
+      const double ri = a.b[i] - s;
+      a.r64[i] = ri;
+      rr += ri * ri;
+    }
+    int set = phase & 1;
+    t = block_sum(rr, red);
+    if (threadIdx.x == 0) slot64(set, 0)[bid] = t;
+    if (!grid_barrier(a.st, nb, epoch)) return;
+    if (sweeps == 0) rho0 = grid_total(slot64(1, 3), nb, &bcast);
+    rho64 = grid_total(slot64(set, 0), nb, &bcast);
+    ++phase;
+    if (rho0 == 0.0) {
+      for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) a.x[i] = 0.0;
+      rho64 = 0.0;
+      break;
+    }
+    if (rho64 <= a.tol2 * rho0) break;
+    if (total_inner >= a.max_iter) {
+      status = 1;
+      break;
+    }
+    // ---- inner PCG on A z = r64 / |r64| (FP32), z = 0
+    const double scale = 1.0 / sqrt(rho64);
+    int cur = 0;
+    for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+      a.r[0][i] = (float)(a.r64[i] * scale);
+      a.z[i] = 0.f;
+      a.p[i] = 0.f;
+      a.s[0][i] = 0.f;
+    }
+    if (!grid_barrier(a.st, nb, epoch)) return;
+    {
+      const float *__restrict__ r0 = a.r[0];
+      presmooth_residual<ND, CST>(a, 0, lo, hi, [&](int64_t j) { return r0[j]; });
+    }
+    ff gam0 = {0.f, 0.f}, gam_prev = {0.f, 0.f};
+    float alpha_prev = 1.f;
+    for (int k = 0;; ++k) {
+      if (!vcycle_rest<ND, CST>(a, a.r[cur], epoch)) return;  // u = M r, visible everywhere
+      const float *__restrict__ rc = a.r[cur];
+      ff g = {0.f, 0.f}, dl = {0.f, 0.f};
+      for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+        const float ui = a.u[i];
+        const float wi = level_apply<ND, CST>(a, 0, [&](int64_t j) { return a.u[j]; }, i);
+        a.w[i] = wi;
+        g = ff_add(g, ff_prod(rc[i], ui));
+        dl = ff_add(dl, ff_prod(wi, ui));
+      }
+      set = phase & 1;
+      ff G, D;
+      if (!allreduce2(set, g, dl, G, D)) return;
+      ++phase;
+      if (k == 0) gam0 = G;
+      if (!(G.hi > 0.f) || G.hi <= (float)a.inner_tol2 * gam0.hi || total_inner >= a.max_iter) break;
+      float alpha, beta;
+      if (k == 0) {
+        beta = 0.f;
+        alpha = G.hi / D.hi;
+      } else {
+        beta = G.hi / gam_prev.hi;
+        alpha = G.hi / (D.hi - beta * G.hi / alpha_prev);
+      }
+      // update into the other buffers, fused with the next V-cycle's first
+      // step: that step reads the new residual at neighbour rows, which it
+      // recomputes from the old buffers bit for bit as their owners write it
+      const int nx = cur ^ 1;
+      const float *__restrict__ ro = a.r[cur];
+      const float *__restrict__ so = a.s[cur];
+      const float *__restrict__ wv = a.w;
+      float *__restrict__ rn = a.r[nx];
+      float *__restrict__ sn = a.s[nx];
+      for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+        const float pi = __fmaf_rn(beta, a.p[i], a.u[i]);
+        const float si = __fmaf_rn(beta, so[i], wv[i]);
+        a.p[i] = pi;
+        sn[i] = si;
+        a.z[i] = __fmaf_rn(alpha, pi, a.z[i]);
+        rn[i] = __fmaf_rn(-alpha, si, ro[i]);
+      }
+      presmooth_residual<ND, CST>(a, 0, lo, hi,
+                                  [&](int64_t j) { return __fmaf_rn(-alpha, __fmaf_rn(beta, so[j], wv[j]), ro[j]); });
+      cur = nx;
+      gam_prev = G;
+      alpha_prev = alpha;
+      ++total_inner;
+    }
+    // ---- x += |r64| z  (FP64)
+    const double back = sqrt(rho64);
+    for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) a.x[i] += (double)a.z[i] * back;
+    if (!grid_barrier(a.st, nb, epoch)) return;
+  }
+  if (bid == 0 && threadIdx.x == 0) {
+    a.st->solver_iters = total_inner;
+    a.st->solver_status = status;
+    a.st->iters_total += total_inner;
+    if (status) a.st->solver_fail = 1;
+    a.st->solver_resid = rho0 > 0.0 ? sqrt(rho64 / rho0) : 0.0;
+  }
+}
+
+void *mg_kernel_of(int nd, bool cst, int th) {
+  static void *tab[2][2][3] = {
+      {{(void *)k_cg_mg<15, 256, false>, (void *)k_cg_mg<15, 512, false>, (void *)k_cg_mg<15, 1024, false>},
+       {(void *)k_cg_mg<15, 256, true>, (void *)k_cg_mg<15, 512, true>, (void *)k_cg_mg<15, 1024, true>}},
+      {{(void *)k_cg_mg<27, 256, false>, (void *)k_cg_mg<27, 512, false>, (void *)k_cg_mg<27, 1024, false>},
+       {(void *)k_cg_mg<27, 256, true>, (void *)k_cg_mg<27, 512, true>, (void *)k_cg_mg<27, 1024, true>}}};
+  return tab[nd > 15 ? 1 : 0][cst ? 1 : 0][th <= 256 ? 0 : th <= 512 ? 1 : 2];
+}
+
+}  // namespace
+
+int mg_max_blocks(int device, int threads) {
+  int sms = 0, occ = 1 << 30, o = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  for (int nd : {15, 27})
+    for (int cst = 0; cst < 2; ++cst) {
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, mg_kernel_of(nd, cst != 0, threads), threads, 0);
+      occ = o < occ ? o : occ;
+    }
+  int nbmax = sms * occ;
+  return nbmax < 128 * kRecMg ? nbmax : 128 * kRecMg;
+}
+
+int run_cg_mg(cudaStream_t s, const DiaMatrix &A, const MgDev &mg, const double *b, double *x, double tol,
+              double inner_tol, int max_iter, CgWork &w, int max_blocks, DevStats *st) {
+  CgMgArgs a;
+  a.A = A;
+  a.mg = mg;
+  a.b = b;
+  a.x = x;
+  a.r64 = w.r;
+  // fine-level PCG vectors over the first 9n floats of the work buffer (12n)
+  float *f = reinterpret_cast<float *>(w.v4);
+  const int64_t n = A.n;
+  a.w = f + 0 * n;
+  a.p = f + 1 * n;
+  a.z = f + 2 * n;
+  a.r[0] = f + 3 * n;
+  a.r[1] = f + 4 * n;
+  a.s[0] = f + 5 * n;
+  a.s[1] = f + 6 * n;
+  a.mg.lev[0].r = nullptr;  // level 0's right-hand side is r[cur]
+  a.mg.lev[0].e = f + 7 * n;
+  a.mg.lev[0].t = f + 8 * n;
+  a.u = a.mg.lev[0].t;
+  a.partials = w.partials;
+  a.tol2 = tol * tol;
+  a.inner_tol2 = inner_tol * inner_tol;
+  a.max_iter = max_iter;
+  a.st = st;
+  const int th = w.threads == 256 || w.threads == 1024 ? w.threads : 512;
+  int64_t want = (n + th - 1) / th;
+  if (want < 1) want = 1;
+  int cap = max_blocks;
+  if (w.block_cap > 0 && w.block_cap < cap) cap = w.block_cap;
+  const int nb = (int)(want < cap ? want : cap);
+  if (cudaMemsetAsync(&st->bar_count, 0, sizeof(unsigned), s) != cudaSuccess) return MPG_ERR_CUDA;
+  static const int mode0 = 0;
+  if (cudaMemcpyAsync(&st->bar_mode, &mode0, sizeof(int), cudaMemcpyHostToDevice, s) != cudaSuccess)
+    return MPG_ERR_CUDA;
+  void *args[] = {&a};
+  cudaError_t e = cudaLaunchCooperativeKernel(mg_kernel_of(A.ndiag, A.constant != 0, th), dim3(nb), dim3(th), args, 0, s);
+  return e == cudaSuccess ? MPG_OK : MPG_ERR_CUDA;
+}

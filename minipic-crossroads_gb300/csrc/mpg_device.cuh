@@ -113,6 +113,21 @@ __device__ __forceinline__ double block_sum(double v, double *smem32) {
   return s;
 }
 
+// sum of partials[0..nb): every thread loads at most one partial (one L2
+// round trip), then a fixed block reduction; all blocks compute the same
+// value bit for bit.
+__device__ __forceinline__ double grid_total(const double *partials, int nb, double *sh) {
+  double s = 0.0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) s += partials[i];
+  __shared__ double red2[32];
+  s = block_sum(s, red2);
+  if (threadIdx.x == 0) *sh = s;
+  __syncthreads();
+  const double v = *sh;
+  __syncthreads();
+  return v;
+}
+
 // ---------------------------------------------------------------------------
 // float-float ("double-single") arithmetic: a value is hi + lo with |lo| <=
 // ulp(hi)/2, about 44 significant bits, built from FP32 operations only

@@ -40,6 +40,25 @@ void host_background(const HostMesh &m, double rho_bg, std::vector<double> &bg);
 // acceptance ratio vol/vol_max per tet for the volume-uniform fill
 void host_fill_ratio(const HostMesh &m, std::vector<float> &ratio);
 
+// Geometric multigrid hierarchy of the structured node grid (mg_host.cpp):
+// level 0 is the fine grid (its operator is the solver's own), levels >= 1
+// hold Galerkin 27-point stencils [d][n], d = 9 (di+1) + 3 (dj+1) + (dk+1);
+// the coarsest level is solved with a dense inverse over its interior nodes.
+struct MgHostLevel {
+  int gx = 0, gy = 0, gz = 0;   // nodes per axis (x slowest)
+  std::vector<float> val;       // 27 * n, levels >= 1
+  std::vector<float> dinv;      // n: 1 / diagonal (1 on Dirichlet rows)
+  std::vector<uint8_t> bnd;     // n
+};
+struct MgHostHierarchy {
+  std::vector<MgHostLevel> lev;
+  std::vector<int32_t> dense_idx;  // interior rows of the coarsest level
+  std::vector<float> dense_inv;    // row-major inverse over them
+};
+// from the symmetric (mode 1) CSR of a non-periodic mesh; false with a reason otherwise
+bool host_mg_build(const HostMesh &m, const std::vector<int32_t> &rp, const std::vector<int32_t> &col,
+                   const std::vector<double> &val, MgHostHierarchy &H, std::string &why);
+
 // counter-based generator shared by the jitter and the fills (splitmix64 finaliser)
 static inline uint64_t mpg_mix64(uint64_t z) {
   z += 0x9E3779B97F4A7C15ULL;

@@ -120,13 +120,42 @@ struct DiaMatrix {
 
 struct CgWork {
   double *r = nullptr, *p0 = nullptr, *p1 = nullptr, *q = nullptr;  // FP64 vectors, n each
-  float4 *v4 = nullptr;  // mixed inner vectors {r, p, q, z} per node, two copies (2n)
+  float4 *v4 = nullptr;  // mixed inner vectors {r, p, q, z} per node, two copies (3n allocated; the
+                         // multigrid PCG uses 9n floats of it)
   double *partials = nullptr;  // 8 * max_blocks
   int max_blocks = 0;
   int threads = 512;  // block size of the cooperative solver kernels (256, 512 or 1024)
   int bar_mode = 0;   // grid barrier flavour (0: fence + volatile polling, 1: release/acquire)
   int block_cap = 0;  // > 0: at most this many blocks in the mixed solver's grid
 };
+// Geometric multigrid preconditioner of the mixed solver (mg.cu, mg_host.cpp):
+// device view of the levels.  Level 0 is the fine grid (operator: the solver's
+// DiaMatrix; vectors r/e/t inside the solver's work buffer), levels >= 1 hold
+// Galerkin 27-point stencils; levels [0, ngrid) are processed by the whole
+// grid, the others and the dense coarsest solve by one block.
+struct MgLevelDev {
+  int64_t n = 0;
+  int si = 0, sj = 0, gx = 0, gy = 0, gz = 0;  // strides and nodes per axis (x slowest)
+  const float *val = nullptr;                  // 27 * n (levels >= 1)
+  const float *dinv = nullptr;                 // n
+  const uint8_t *bnd = nullptr;                // n
+  float *r = nullptr, *e = nullptr, *t = nullptr;
+};
+constexpr int kMgMaxLevels = 8;
+struct MgDev {
+  int nlev = 0, ngrid = 0;
+  MgLevelDev lev[kMgMaxLevels];
+  const int32_t *dense_idx = nullptr;
+  const float *dense_inv = nullptr;
+  int dense_m = 0;
+  float omega = 0.8f;
+};
+// mixed CG preconditioned by one V(1,1) cycle per iteration, one cooperative
+// launch; `max_blocks` from mg_max_blocks
+int run_cg_mg(cudaStream_t s, const DiaMatrix &A, const MgDev &mg, const double *b, double *x, double tol,
+              double inner_tol, int max_iter, CgWork &w, int max_blocks, DevStats *st);
+int mg_max_blocks(int device, int threads);
+
 // plain FP64 CG on CSR (CG_solve.hpp:54-114), one cooperative launch; returns 0 or an MPG_ERR_*
 int run_cg64(cudaStream_t s, int device, int64_t n, const int32_t *rowptr, const int32_t *col, const double *val,
              const double *b, double *x, double tol, int max_iter, CgWork &w, DevStats *st);

@@ -59,20 +59,6 @@ __device__ __forceinline__ int64_t dia_nb(int64_t i, int off, int64_t nwrap) {
   return j;
 }
 
-// sum of partials[0..nb): every thread loads at most one partial (one L2
-// round trip), then a fixed block reduction; all blocks compute the same
-// value bit for bit.
-__device__ __forceinline__ double grid_total(const double *partials, int nb, double *sh) {
-  double s = 0.0;
-  for (int i = threadIdx.x; i < nb; i += blockDim.x) s += partials[i];
-  __shared__ double red2[32];
-  s = block_sum(s, red2);
-  if (threadIdx.x == 0) *sh = s;
-  __syncthreads();
-  const double v = *sh;
-  __syncthreads();
-  return v;
-}
 
 // ---------------------------------------------------------------------------
 // plain FP64 CG on CSR (used by mpg_cg_csr for caller-owned matrices)

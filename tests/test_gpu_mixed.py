@@ -84,6 +84,58 @@ def test_mixed_solve_reaches_fp64_tolerance(mpg, orc, jitter, n_side):
     assert np.abs(x - ox).max() <= 1e-8 * np.abs(ox).max()
 
 
+@pytest.mark.parametrize("n_side,split", [(16, 6), (24, 5), (56, 6), (9, 6)])
+@pytest.mark.parametrize("jitter", [0.2, 0.0])
+def test_mg_preconditioned_solve_reaches_fp64_tolerance(mpg, orc, jitter, n_side, split):
+    # the multigrid-preconditioned inner CG reaches the same FP64 tolerance
+    # in far fewer iterations; 9 cells per side cannot be coarsened (odd), so
+    # that mesh runs the unpreconditioned mixed CG
+    def solve(kind):
+        ctx = mpg.Ctx(0)
+        ctx.mesh(n_side, split=split, lo=0.0, hi=1.0, mapping=mpg.MAP_JITTER if jitter else 0, jitter=jitter,
+                 seed=4)
+        ctx.configure(precision=mpg.MIXED, deposit=mpg.DEPOSIT_LINEAR, solver=kind, tol=1e-10, warm_start=0)
+        ctx.set_field(mpg.FIELD_RHS, b)
+        it, _ = ctx.solve()
+        return ctx.get_field(mpg.FIELD_PHI), it
+    m = orc.Mesh(n_side, split=split, mapping=4 if jitter else 0, jitter=jitter, seed=4)
+    m.assemble(1)
+    rng = np.random.default_rng(7)
+    b = rng.standard_normal(m.N)
+    b[m.boundary == 1] = 0
+    x, it_mg = solve(mpg.SOLVER_CG_MG)
+    x2, it2 = solve(mpg.SOLVER_CG_MG)
+    assert it2 == it_mg and (x2.view(np.uint64) == x.view(np.uint64)).all()  # deterministic
+    r = b - m.spmv(x)
+    assert np.linalg.norm(r) / np.linalg.norm(b) < 1e-10
+    ox, _, _ = orc.cg(m, b, tol=1e-12, max_iter=5000, nthreads=8)
+    assert np.abs(x - ox).max() <= 1e-8 * np.abs(ox).max()
+    _, it_cg = solve(mpg.SOLVER_CG)
+    if n_side % 2 == 0:
+        assert 2 * it_mg < it_cg, (it_mg, it_cg)
+    else:
+        assert it_mg == it_cg
+
+
+def test_mg_steps_track_plain_form(mpg):
+    n = 40000
+    mixed = _ctx(mpg, n_side=16, solver=mpg.SOLVER_CG_MG, warm_start=2)
+    plain = _ctx(mpg, n_side=16, precision=mpg.PLAIN, warm_start=2)
+    for c in (mixed, plain):
+        _two_species(c, n)
+    phis = []
+    for s in range(5):
+        sm = mixed.step(0.01, 1)
+        sp = plain.step(0.01, 1)
+        pm = mixed.get_field(mpg.FIELD_PHI)
+        pp = plain.get_field(mpg.FIELD_PHI)
+        phis.append(np.abs(pm - pp).max() / np.abs(pp).max())
+        assert abs(sm.ke - sp.ke) <= 1e-5 * sp.ke
+        assert abs(sm.n_alive - sp.n_alive) <= max(3, 1e-3 * n)
+        assert sm.solver_iters < sp.solver_iters
+    assert max(phis) <= 1e-6, phis
+
+
 def test_mixed_steps_track_plain_form(mpg):
     n = 40000
     mixed = _ctx(mpg, n_side=8)
