@@ -191,14 +191,49 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def uses_mg(w):
+    return MIXED_SOLVER == "mg" and not w.get("periodic", 0) and mg_levels(w["n_side"])
+
+
+def mg_levels(n_side, dense_max=1400):
+    """Node extents of the multigrid levels: halve while the interior has more
+    than dense_max nodes and the cell count is even (the host hierarchy's rule)."""
+    g = [n_side + 1]
+    while len(g) < 8 and (g[-1] - 2) ** 3 > dense_max:
+        if (g[-1] - 1) % 2 or g[-1] < 5:
+            break
+        g.append((g[-1] - 1) // 2 + 1)
+    if len(g) < 2 or (g[-1] - 2) ** 3 > dense_max:
+        return []
+    return g
+
+
+def mg_iter_bytes(n_side, N, coef):
+    """Algorithmic bytes of one multigrid-preconditioned inner iteration.
+
+    Fine level, per row: fused update + pre-smoothing reads p, u, s, w, z, r,
+    D^-1 and writes p, s, z, r, t (44 B); restriction reads t (4 B); the two
+    ascending steps read D^-1, r, e and write e, t (28 B); w = A u reads u, r and
+    writes w (12 B); three stencil passes read the FP32 coefficients (3 coef).
+    Coarse levels, per row: 27 FP32 coefficients in two passes plus about 80 B
+    of vectors.  Coarsest level: its dense inverse (m^2 FP32)."""
+    g = mg_levels(n_side)
+    b = (44 + 4 + 28 + 12 + 3 * coef) * N
+    for gl in g[1:-1]:
+        b += (2 * 27 * 4 + 80) * gl ** 3
+    m = (g[-1] - 2) ** 3
+    return b + 4 * m * m + 40 * g[-1] ** 3
+
+
 def phase_bytes(w, ctx, stats, steps, mpg):
     """Algorithmic bytes per launch of each phase of the mixed step.
 
-    Solver (structured diagonal operator, nd = 15 diagonals on the Kuhn grid):
-    per inner iteration 4*nd bytes of FP32 coefficients per row (none with the
+    Solver (structured diagonal operator, nd = 15 diagonals on the Kuhn grid),
+    plain inner CG: per inner iteration 4*nd bytes of FP32 coefficients per row (none with the
     constant stencil of an unjittered mesh) + 16 B of vector reads (r, q, p, z)
     + 16 B of vector writes; per refinement sweep (about 3 per solve) the FP64
     residual reads 8*nd + 16 B and writes 8 B per row, the restart 20 B.
+    Multigrid-preconditioned inner CG: mg_iter_bytes per inner iteration.
     """
     T, N = ctx.T, ctx.N
     P = total_particles(w)
@@ -207,6 +242,8 @@ def phase_bytes(w, ctx, stats, steps, mpg):
     coef = 0 if w["jitter"] == 0 else 4 * nd
     cg_iter = (coef + 32) * N
     sweep = (8 * nd + 24 + 20) * N
+    if uses_mg(w):
+        cg_iter = mg_iter_bytes(w["n_side"], N, coef)
     return {
         # 28 B read + 28 B write per particle, 16 B of node ids, 4 x 8 B accumulator RMW,
         # per-tet walk record (48 B) + neighbour table (16 B) read once
@@ -597,7 +634,8 @@ def main():
         hbm, kind = peaks()
         pb = phase_bytes(w, ctx, ph, k_ph, mpg) if precision == mpg.MIXED else None
         dominant = max(("solve", "move", "efield", "deposit"), key=lambda k: phases[k])
-        kern = {"solve": "k_cg_mixed", "move": "k_mixed_move_persistent", "efield": "k_efield_mixed",
+        kern = {"solve": "k_cg_mg" if uses_mg(w) else "k_cg_mixed", "move": "k_mixed_move_persistent",
+                "efield": "k_efield_mixed",
                 "deposit": "k_mixed_convert"}[dominant]
         roof = None
         if pb is not None:

@@ -315,6 +315,7 @@ int ensure_cg_work(mpg_ctx *c, int64_t n) {
   if (const char *e = getenv("MPG_CG_BARRIER")) c->cg.bar_mode = atoi(e);
   if (const char *e = getenv("MPG_CG_BLOCKS")) c->cg.block_cap = atoi(e);
   if (const char *e = getenv("MPG_CG_INNER_TOL")) c->inner_tol = atof(e);
+  if (const char *e = getenv("MPG_CG_INNER_SAFETY")) c->cg.inner_safety = atof(e);
   c->cg.max_blocks = cg_max_blocks(c->device, c->cg.threads == 256 || c->cg.threads == 1024 ? c->cg.threads : 512);
   c->mg_max_blocks = mg_max_blocks(c->device, c->cg.threads == 256 || c->cg.threads == 1024 ? c->cg.threads : 512);
   TRY(dalloc(c, &c->cg.r, n));

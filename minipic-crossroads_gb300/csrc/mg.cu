@@ -18,7 +18,49 @@
 #include "mpg_device.cuh"
 #include "mpg_kernels.h"
 
+#ifdef MPG_CG_PROFILE
+// optional phase timing (compile with -DMPG_CG_PROFILE), SM cycles of block 0:
+// [2 q] work before the q-th grid barrier of an inner iteration, [2 q + 1]
+// the wait in it; [63] inner iterations
+__device__ unsigned long long g_mg_prof[64];
+extern "C" int mpg_probe_mg_profile(unsigned long long *out) {
+  return cudaMemcpyFromSymbol(out, g_mg_prof, sizeof(g_mg_prof)) == cudaSuccess ? 0 : -2;
+}
+#endif
+
 namespace {
+
+// grid barrier with the optional per-barrier timing
+struct MgSync {
+  DevStats *st;
+  unsigned epoch = 0;
+#ifdef MPG_CG_PROFILE
+  int q = 0;
+  unsigned long long last = 0;
+#endif
+  __device__ bool operator()() {
+#ifdef MPG_CG_PROFILE
+    const bool rec = blockIdx.x == 0 && threadIdx.x == 0 && q < 31;
+    unsigned long long t0 = clock64();
+    if (rec && last) g_mg_prof[2 * q] += t0 - last;
+    const bool ok = grid_barrier(st, gridDim.x, epoch);
+    const unsigned long long t1 = clock64();
+    if (rec && last) g_mg_prof[2 * q + 1] += t1 - t0;
+    last = t1;
+    ++q;
+    return ok;
+#else
+    return grid_barrier(st, gridDim.x, epoch);
+#endif
+  }
+  // start of an inner iteration's barrier numbering
+  __device__ void iteration() {
+#ifdef MPG_CG_PROFILE
+    if (blockIdx.x == 0 && threadIdx.x == 0 && last) g_mg_prof[63] += 1;
+    q = 0;
+#endif
+  }
+};
 
 constexpr int kRecMg = 5;  // block records each of the first 128 threads gathers (grids up to 640 blocks)
 
@@ -30,7 +72,7 @@ struct CgMgArgs {
   float *r[2], *s[2];  // fine-level PCG residual and A p, double-buffered by iteration parity
   float *u, *w, *p, *z;  // u = M r is the V-cycle's output (mg.lev[0].t), w = A u
   double *partials;              // outer phases: [2 sets][4][nb]; inner: one 32-byte record per block
-  double tol2, inner_tol2;
+  double tol2, inner_tol2, safety2;
   int max_iter;
   DevStats *st;
 };
@@ -184,9 +226,9 @@ __device__ __forceinline__ void dense_solve(const MgDev &mg) {
 // [ngrid, nlev - 1) on block 0 alone, the dense coarsest solve on the whole
 // grid again.
 template <int ND, bool CST>
-__device__ bool vcycle_rest(const CgMgArgs &a, const float *rf, unsigned &epoch) {
+__device__ bool vcycle_rest(const CgMgArgs &a, const float *rf, MgSync &bar) {
   const int nl = a.mg.nlev, ng = a.mg.ngrid;
-  auto gsync = [&]() { return grid_barrier(a.st, gridDim.x, epoch); };
+  auto gsync = [&]() { return bar(); };
   auto bsync = [&]() {
     __syncthreads();
     return true;
@@ -231,7 +273,8 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mg(CgMgArgs a) {
   __shared__ ff smf[4 * 32];
   __shared__ ff smt[4];
   __shared__ double bcast;
-  unsigned epoch = 0;
+  MgSync bar;
+  bar.st = a.st;
   const int nb = gridDim.x, bid = blockIdx.x;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int64_t n = a.A.n;
@@ -259,7 +302,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mg(CgMgArgs a) {
       }
       if (lane == 0) reinterpret_cast<float4 *>(slot64(set, 0))[bid] = make_float4(t[0].hi, t[0].lo, t[1].hi, t[1].lo);
     }
-    if (!grid_barrier(a.st, nb, epoch)) return false;
+    if (!bar()) return false;
     if (wid < 4) {
       const float4 *rec = reinterpret_cast<const float4 *>(slot64(set, 0));
       float4 x[kRecMg];
@@ -320,7 +363,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mg(CgMgArgs a) {
     int set = phase & 1;
     t = block_sum(rr, red);
     if (threadIdx.x == 0) slot64(set, 0)[bid] = t;
-    if (!grid_barrier(a.st, nb, epoch)) return;
+    if (!bar()) return;
     if (sweeps == 0) rho0 = grid_total(slot64(1, 3), nb, &bcast);
     rho64 = grid_total(slot64(set, 0), nb, &bcast);
     ++phase;
@@ -343,15 +386,17 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mg(CgMgArgs a) {
       a.p[i] = 0.f;
       a.s[0][i] = 0.f;
     }
-    if (!grid_barrier(a.st, nb, epoch)) return;
+    if (!bar()) return;
     {
       const float *__restrict__ r0 = a.r[0];
       presmooth_residual<ND, CST>(a, 0, lo, hi, [&](int64_t j) { return r0[j]; });
     }
     ff gam0 = {0.f, 0.f}, gam_prev = {0.f, 0.f};
     float alpha_prev = 1.f;
+    const float stop_rel = (float)fmax(a.inner_tol2, a.safety2 * a.tol2 * rho0 / rho64);
     for (int k = 0;; ++k) {
-      if (!vcycle_rest<ND, CST>(a, a.r[cur], epoch)) return;  // u = M r, visible everywhere
+      bar.iteration();
+      if (!vcycle_rest<ND, CST>(a, a.r[cur], bar)) return;  // u = M r, visible everywhere
       const float *__restrict__ rc = a.r[cur];
       ff g = {0.f, 0.f}, dl = {0.f, 0.f};
       for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
@@ -366,7 +411,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mg(CgMgArgs a) {
       if (!allreduce2(set, g, dl, G, D)) return;
       ++phase;
       if (k == 0) gam0 = G;
-      if (!(G.hi > 0.f) || G.hi <= (float)a.inner_tol2 * gam0.hi || total_inner >= a.max_iter) break;
+      if (!(G.hi > 0.f) || G.hi <= stop_rel * gam0.hi || total_inner >= a.max_iter) break;
       float alpha, beta;
       if (k == 0) {
         beta = 0.f;
@@ -402,7 +447,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mg(CgMgArgs a) {
     // ---- x += |r64| z  (FP64)
     const double back = sqrt(rho64);
     for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) a.x[i] += (double)a.z[i] * back;
-    if (!grid_barrier(a.st, nb, epoch)) return;
+    if (!bar()) return;
   }
   if (bid == 0 && threadIdx.x == 0) {
     a.st->solver_iters = total_inner;
@@ -461,6 +506,7 @@ int run_cg_mg(cudaStream_t s, const DiaMatrix &A, const MgDev &mg, const double 
   a.partials = w.partials;
   a.tol2 = tol * tol;
   a.inner_tol2 = inner_tol * inner_tol;
+  a.safety2 = w.inner_safety * w.inner_safety;
   a.max_iter = max_iter;
   a.st = st;
   const int th = w.threads == 256 || w.threads == 1024 ? w.threads : 512;

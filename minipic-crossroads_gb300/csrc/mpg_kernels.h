@@ -124,6 +124,10 @@ struct CgWork {
                          // multigrid PCG uses 9n floats of it)
   double *partials = nullptr;  // 8 * max_blocks
   int max_blocks = 0;
+  // inner stop of the mixed solvers: the FP32 residual reduction also ends
+  // once it is below inner_safety^2 * (tol^2 |b|^2 / |r64|^2), the reduction
+  // the outer FP64 test needs (0: fixed inner_tol only)
+  double inner_safety = 0.5;
   int threads = 512;  // block size of the cooperative solver kernels (256, 512 or 1024)
   int bar_mode = 0;   // grid barrier flavour (0: fence + volatile polling, 1: release/acquire)
   int block_cap = 0;  // > 0: at most this many blocks in the mixed solver's grid

@@ -308,7 +308,7 @@ struct CgMixedArgs {
   float4 *v[2];  // inner vectors per node {r, p, q, z}, double-buffered
   double *partials;  // [2 sets][kSlots][nb]
   double tol2;
-  double inner_tol2;
+  double inner_tol2, safety2;
   int max_iter;
   DevStats *st;
 };
@@ -444,7 +444,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
     ff pq = tot[0], rq = tot[1], qq = tot[2], rho = rin0;
     ++phase;
     int cur = 0;
-    const float stop = (float)a.inner_tol2 * rin0.hi;
+    const float stop = (float)fmax(a.inner_tol2, a.safety2 * a.tol2 * rho0 / rho64) * rin0.hi;
     for (;;) {
       if (rho.hi <= stop || total_inner >= a.max_iter || !(pq.hi > 0.f)) break;
       // scalars in float / float-float (identical in every thread)
@@ -742,6 +742,7 @@ int run_cg_mixed(cudaStream_t s, const DiaMatrix &A, const double *b, double *x,
   a.partials = w.partials;
   a.tol2 = tol * tol;
   a.inner_tol2 = inner_tol * inner_tol;
+  a.safety2 = w.inner_safety * w.inner_safety;
   a.max_iter = max_iter;
   a.st = st;
   const int th = threads_of(w);
