@@ -686,6 +686,7 @@ int upload_mg(mpg_ctx *c, const MgHostHierarchy &H) {
   m.dense_idx = idx;
   m.dense_inv = inv;
   if (const char *e = getenv("MPG_MG_OMEGA")) m.omega = (float)atof(e);
+  if (const char *e = getenv("MPG_MG_RELIABLE")) m.reliable = atoi(e);
   c->mg_ok = true;
   return MPG_OK;
 }

@@ -282,43 +282,50 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mg(CgMgArgs a) {
   const uint8_t *__restrict__ bnd = a.A.bnd;
   const double *__restrict__ v64 = a.A.val64;
   auto slot64 = [&](int set, int k) { return a.partials + ((size_t)(set * 4 + k)) * nb; };
-  // all-reduce of two float-float values per block (block record, grid
-  // barrier, four warps gather every record in block order)
-  auto allreduce2 = [&](int set, ff g, ff d, ff &G, ff &D) -> bool {
-    float w2[2] = {g.hi + g.lo, d.hi + d.lo};
+  // all-reduce of four float-float values per block (block record of two
+  // float4, grid barrier, four warps gather every record in block order)
+  auto allreduce4 = [&](int set, const ff (&v)[4], ff (&out)[4]) -> bool {
+    float w4[4] = {v[0].hi + v[0].lo, v[1].hi + v[1].lo, v[2].hi + v[2].lo, v[3].hi + v[3].lo};
     for (int o = 16; o > 0; o >>= 1)
 #pragma unroll
-      for (int k = 0; k < 2; ++k) w2[k] += __shfl_down_sync(0xffffffffu, w2[k], o);
+      for (int k = 0; k < 4; ++k) w4[k] += __shfl_down_sync(0xffffffffu, w4[k], o);
     if (lane == 0)
 #pragma unroll
-      for (int k = 0; k < 2; ++k) smw[k * 32 + wid] = w2[k];
+      for (int k = 0; k < 4; ++k) smw[k * 32 + wid] = w4[k];
     __syncthreads();
     if (wid == 0) {
-      ff t[2];
+      ff t[4];
 #pragma unroll
-      for (int k = 0; k < 2; ++k) {
+      for (int k = 0; k < 4; ++k) {
         t[k] = ff{lane < TH / 32 ? smw[k * 32 + lane] : 0.f, 0.f};
         for (int o = 16; o > 0; o >>= 1) t[k] = ff_add(t[k], ff_shfl_down(t[k], o));
       }
-      if (lane == 0) reinterpret_cast<float4 *>(slot64(set, 0))[bid] = make_float4(t[0].hi, t[0].lo, t[1].hi, t[1].lo);
+      if (lane == 0) {
+        float4 *rec = reinterpret_cast<float4 *>(slot64(set, 0)) + 2 * bid;
+        rec[0] = make_float4(t[0].hi, t[0].lo, t[1].hi, t[1].lo);
+        rec[1] = make_float4(t[2].hi, t[2].lo, t[3].hi, t[3].lo);
+      }
     }
     if (!bar()) return false;
     if (wid < 4) {
       const float4 *rec = reinterpret_cast<const float4 *>(slot64(set, 0));
-      float4 x[kRecMg];
+      float4 x[kRecMg], y[kRecMg];
 #pragma unroll
       for (int j = 0; j < kRecMg; ++j) {
         const int i = threadIdx.x + 128 * j;
-        x[j] = i < nb ? rec[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        x[j] = i < nb ? rec[2 * i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        y[j] = i < nb ? rec[2 * i + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
       }
-      ff t[2] = {{0.f, 0.f}, {0.f, 0.f}};
+      ff t[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
 #pragma unroll
       for (int j = 0; j < kRecMg; ++j) {
         t[0] = ff_add(t[0], ff{x[j].x, x[j].y});
         t[1] = ff_add(t[1], ff{x[j].z, x[j].w});
+        t[2] = ff_add(t[2], ff{y[j].x, y[j].y});
+        t[3] = ff_add(t[3], ff{y[j].z, y[j].w});
       }
 #pragma unroll
-      for (int k = 0; k < 2; ++k) {
+      for (int k = 0; k < 4; ++k) {
         for (int o = 16; o > 0; o >>= 1) t[k] = ff_add(t[k], ff_shfl_down(t[k], o));
         if (lane == 0) smf[k * 32 + wid] = t[k];
       }
@@ -326,15 +333,15 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mg(CgMgArgs a) {
     __syncthreads();
     if (wid == 0) {
 #pragma unroll
-      for (int k = 0; k < 2; ++k) {
+      for (int k = 0; k < 4; ++k) {
         ff u = lane < 4 ? smf[k * 32 + lane] : ff{0.f, 0.f};
         for (int o = 2; o > 0; o >>= 1) u = ff_add(u, ff_shfl_down(u, o));
         if (lane == 0) smt[k] = u;
       }
     }
     __syncthreads();
-    G = smt[0];
-    D = smt[1];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) out[k] = smt[k];
     __syncthreads();
     return true;
   };
@@ -343,7 +350,13 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mg(CgMgArgs a) {
   double t = block_sum(bb, red);
   if (threadIdx.x == 0) slot64(1, 3)[bid] = t;  // read after the first barrier
   int total_inner = 0, status = 0, sweeps = 0, phase = 0;
-  double rho64 = 0.0, rho0 = 0.0;
+  double rho64 = 0.0, rho0 = 0.0, rho_prev64 = 0.0;
+  // PCG state kept across refinement sweeps when reliable updates are on:
+  // the search direction p (and s = A p) continues, rescaled to the new
+  // right-hand side, instead of restarting from z = 0, p = 0
+  ff gam_prev = {0.f, 0.f};
+  int cur = 0;
+  bool have_dir = false;
   for (;; ++sweeps) {
     // ---- FP64 residual with the FP64 matrix (identity rows: x = b there)
     double rr = 0.0;
@@ -379,47 +392,62 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mg(CgMgArgs a) {
     }
     // ---- inner PCG on A z = r64 / |r64| (FP32), z = 0
     const double scale = 1.0 / sqrt(rho64);
-    int cur = 0;
-    for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-      a.r[0][i] = (float)(a.r64[i] * scale);
-      a.z[i] = 0.f;
-      a.p[i] = 0.f;
-      a.s[0][i] = 0.f;
+    const bool carry = have_dir && a.mg.reliable;
+    // the old system's vectors in the new scale: r_new = r64_new / |r64_new|
+    // is the old recursive residual times f = |r64_old| / |r64_new|
+    const float f = carry ? (float)sqrt(rho_prev64 / rho64) : 0.f;
+    if (carry) {
+      gam_prev = ff_mulf(ff_mulf(gam_prev, f), f);
+    } else {
+      have_dir = false;
+      cur = 0;
+    }
+    {
+      float *__restrict__ rc = a.r[cur];
+      float *__restrict__ sc = a.s[cur];
+      for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+        rc[i] = (float)(a.r64[i] * scale);
+        a.z[i] = 0.f;
+        a.p[i] = carry ? a.p[i] * f : 0.f;
+        sc[i] = carry ? sc[i] * f : 0.f;
+      }
     }
     if (!bar()) return;
     {
-      const float *__restrict__ r0 = a.r[0];
+      const float *__restrict__ r0 = a.r[cur];
       presmooth_residual<ND, CST>(a, 0, lo, hi, [&](int64_t j) { return r0[j]; });
     }
-    ff gam0 = {0.f, 0.f}, gam_prev = {0.f, 0.f};
-    float alpha_prev = 1.f;
+    ff gam0 = {0.f, 0.f};
     const float stop_rel = (float)fmax(a.inner_tol2, a.safety2 * a.tol2 * rho0 / rho64);
     for (int k = 0;; ++k) {
       bar.iteration();
       if (!vcycle_rest<ND, CST>(a, a.r[cur], bar)) return;  // u = M r, visible everywhere
       const float *__restrict__ rc = a.r[cur];
-      ff g = {0.f, 0.f}, dl = {0.f, 0.f};
+      const float *__restrict__ sc = a.s[cur];
+      // (r, u), (w, u), (u, s) and (p, s) with w = A u: the last two give the
+      // exact (p_new, A p_new) = (w, u) + 2 beta (u, s) + beta^2 (p, s), which
+      // stays valid when the residual was replaced by the true one
+      ff v[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
       for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
         const float ui = a.u[i];
         const float wi = level_apply<ND, CST>(a, 0, [&](int64_t j) { return a.u[j]; }, i);
+        const float si = sc[i];
         a.w[i] = wi;
-        g = ff_add(g, ff_prod(rc[i], ui));
-        dl = ff_add(dl, ff_prod(wi, ui));
+        v[0] = ff_add(v[0], ff_prod(rc[i], ui));
+        v[1] = ff_add(v[1], ff_prod(wi, ui));
+        v[2] = ff_add(v[2], ff_prod(ui, si));
+        v[3] = ff_add(v[3], ff_prod(a.p[i], si));
       }
       set = phase & 1;
-      ff G, D;
-      if (!allreduce2(set, g, dl, G, D)) return;
+      ff tot[4];
+      if (!allreduce4(set, v, tot)) return;
       ++phase;
+      const ff G = tot[0];
       if (k == 0) gam0 = G;
       if (!(G.hi > 0.f) || G.hi <= stop_rel * gam0.hi || total_inner >= a.max_iter) break;
-      float alpha, beta;
-      if (k == 0) {
-        beta = 0.f;
-        alpha = G.hi / D.hi;
-      } else {
-        beta = G.hi / gam_prev.hi;
-        alpha = G.hi / (D.hi - beta * G.hi / alpha_prev);
-      }
+      const float beta = have_dir ? G.hi / gam_prev.hi : 0.f;
+      const ff den = ff_add(ff_add(tot[1], ff_mulf(tot[2], 2.f * beta)), ff_mulf(ff_mulf(tot[3], beta), beta));
+      const float alpha = G.hi / den.hi;
       // update into the other buffers, fused with the next V-cycle's first
       // step: that step reads the new residual at neighbour rows, which it
       // recomputes from the old buffers bit for bit as their owners write it
@@ -441,9 +469,10 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mg(CgMgArgs a) {
                                   [&](int64_t j) { return __fmaf_rn(-alpha, __fmaf_rn(beta, so[j], wv[j]), ro[j]); });
       cur = nx;
       gam_prev = G;
-      alpha_prev = alpha;
+      have_dir = true;
       ++total_inner;
     }
+    rho_prev64 = rho64;
     // ---- x += |r64| z  (FP64)
     const double back = sqrt(rho64);
     for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) a.x[i] += (double)a.z[i] * back;

@@ -153,6 +153,7 @@ struct MgDev {
   const float *dense_inv = nullptr;
   int dense_m = 0;
   float omega = 0.8f;
+  int reliable = 1;  // keep the search direction across refinement sweeps (reliable updates)
 };
 // mixed CG preconditioned by one V(1,1) cycle per iteration, one cooperative
 // launch; `max_blocks` from mg_max_blocks
