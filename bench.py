@@ -653,7 +653,8 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32" if precision == mpg.MIXED else "f64",
-                "precision": ("mixed: f32 push/walk, i64 fixed-point deposit, f32 CG inside f64 refinement"
+                "precision": (("mixed: f32 push/walk, i64 fixed-point deposit, f32 "
+                               + ("multigrid-preconditioned CG" if uses_mg(w) else "CG") + " inside f64 refinement")
                               if precision == mpg.MIXED else "plain f64"),
                 "data": "synthetic",
                 "config": {"workload": w["name"], "n_side": w["n_side"], "tets": ctx.T, "nodes": ctx.N,
