@@ -316,11 +316,22 @@ class Ctx:
         del cap
         return n.value
 
-    def mixed_download(self):
-        cap = max(self.slots(), 1)
-        cs = np.zeros(cap, np.uint32)
-        b = np.zeros((cap, 3), np.float32)
-        v = np.zeros((cap, 3), np.float32)
+    def mixed_download(self, out=None):
+        """(cellsp, barycentrics, velocities) of the live slots; `out` = three
+        caller arrays (uint32 [cap], float32 [cap, 3] x 2, e.g. pinned host
+        memory) to download into instead of fresh ones."""
+        if out is None:
+            cap = max(self.slots(), 1)
+            cs = np.zeros(cap, np.uint32)
+            b = np.zeros((cap, 3), np.float32)
+            v = np.zeros((cap, 3), np.float32)
+        else:
+            cs, b, v = out
+            if cs.dtype != np.uint32 or b.dtype != np.float32 or v.dtype != np.float32 or b.shape[1:] != (3,) \
+                    or v.shape[1:] != (3,) or not (len(cs) == len(b) == len(v)) or not all(
+                        a.flags.c_contiguous for a in (cs, b, v)):
+                raise ValueError("out must be contiguous uint32 [cap] and float32 [cap, 3] arrays")
+            cap = len(cs)
         n = C.c_int64()
         self._ck(self.L.mpg_mixed_download(self.h, cap, C.byref(n), ptr(cs), ptr(b), ptr(v)))
         return cs[: n.value], b[: n.value], v[: n.value]

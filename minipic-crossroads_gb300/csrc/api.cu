@@ -1340,30 +1340,51 @@ int mpg_mixed_upload(mpg_ctx *c, int64_t n, const uint32_t *cellsp, const float 
   TRY(ensure_particles(c));
   if (c->precision != MPG_MIXED) return fail(c, MPG_ERR_STATE, "context is not in mixed precision");
   if (n < 0 || n > c->cap) return fail(c, MPG_ERR_CAPACITY, "upload exceeds capacity");
-  for (int64_t i = 0; i < n; ++i) {
-    if (cellsp[i] == MPG_DEAD) continue;
-    if ((int64_t)(cellsp[i] & 0xFFFFFFu) >= c->hm.T || (cellsp[i] >> 24) >= MPG_MAX_SPECIES)
-      return fail(c, MPG_ERR_ARG, "cellsp[%lld] out of range", (long long)i);
-    if (!c->weight_set[cellsp[i] >> 24])
-      return fail(c, MPG_ERR_STATE, "species %u has no weight (fill or upload it first)", cellsp[i] >> 24);
-  }
+  // staged upload: the words are validated on the device before they replace
+  // the resident state, so a rejected upload leaves the context unchanged
   cudaStream_t s = c->stream;
+  const int64_t nn = n > 0 ? n : 1;
+  uint32_t *sc;
   float *sb, *sv;
-  CK(cudaMallocAsync((void **)&sb, sizeof(float) * 3 * (n > 0 ? n : 1), s));
-  CK(cudaMallocAsync((void **)&sv, sizeof(float) * 3 * (n > 0 ? n : 1), s));
+  unsigned long long *chk;
+  CK(cudaMallocAsync((void **)&sc, sizeof(uint32_t) * nn, s));
+  CK(cudaMallocAsync((void **)&sb, sizeof(float) * 3 * nn, s));
+  CK(cudaMallocAsync((void **)&sv, sizeof(float) * 3 * nn, s));
+  CK(cudaMallocAsync((void **)&chk, 2 * sizeof(unsigned long long), s));
+  uint32_t wmask = 0;
+  for (int k = 0; k < MPG_MAX_SPECIES; ++k)
+    if (c->weight_set[k]) wmask |= 1u << k;
+  unsigned long long h_chk[2] = {~0ull, 0ull};
+  CK(cudaMemcpyAsync(chk, h_chk, sizeof(h_chk), cudaMemcpyHostToDevice, s));
   if (n > 0) {
-    CK(cudaMemcpyAsync(c->mp[c->cur].c, cellsp, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(sc, cellsp, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(sb, b, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(sv, v, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, s));
+    launch_mixed_check(s, sc, n, c->hm.T, wmask, chk);
+    CKL();
+  }
+  CK(cudaMemcpyAsync(h_chk, chk, sizeof(h_chk), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  int rc = MPG_OK;
+  if (h_chk[0] != ~0ull) {
+    const int64_t i = (int64_t)h_chk[0];
+    if ((int64_t)(cellsp[i] & 0xFFFFFFu) >= c->hm.T || (cellsp[i] >> 24) >= MPG_MAX_SPECIES)
+      rc = fail(c, MPG_ERR_ARG, "cellsp[%lld] out of range", (long long)i);
+    else
+      rc = fail(c, MPG_ERR_STATE, "species %u has no weight (fill or upload it first)", cellsp[i] >> 24);
+  } else if (n > 0) {
+    CK(cudaMemcpyAsync(c->mp[c->cur].c, sc, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s));
     launch_mixed_pack(s, sb, sv, c->mp[c->cur], n);
     CKL();
   }
+  CK(cudaFreeAsync(sc, s));
   CK(cudaFreeAsync(sb, s));
   CK(cudaFreeAsync(sv, s));
+  CK(cudaFreeAsync(chk, s));
   CK(cudaStreamSynchronize(s));
+  if (rc != MPG_OK) return rc;
   c->n = n;
-  c->n_live = 0;
-  for (int64_t i = 0; i < n; ++i) c->n_live += cellsp[i] != MPG_DEAD;
+  c->n_live = (int64_t)h_chk[1];
   c->acc_valid = false;
   c->needs_sort = true;
   return MPG_OK;

@@ -911,6 +911,27 @@ __global__ void k_cols_to_rows(const double *__restrict__ cols, double *__restri
   if (p >= n) return;
   for (int d = 0; d < 3; ++d) rows[3 * p + d] = cols[d * cap + p];
 }
+// validation of uploaded cell/species words: out[0] = lowest index of an
+// entry with a cell out of range, a species out of range or a species without
+// weight (initialised to all ones), out[1] += live entries
+__global__ void k_mixed_check(const uint32_t *__restrict__ cs, int64_t n, int64_t T, uint32_t weight_mask,
+                              unsigned long long *__restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned live = 0;
+  if (i < n) {
+    const uint32_t w = cs[i];
+    if (w != MPG_DEAD) {
+      const uint32_t sp = w >> 24;
+      if ((int64_t)(w & 0xFFFFFFu) >= T || sp >= MPG_MAX_SPECIES || !((weight_mask >> sp) & 1u))
+        atomicMin(&out[0], (unsigned long long)i);
+      else
+        live = 1;
+    }
+  }
+  live = __reduce_add_sync(0xffffffffu, live);
+  if ((threadIdx.x & 31) == 0 && live) atomicAdd(&out[1], (unsigned long long)live);
+}
+
 __global__ void k_mixed_pack(const float *__restrict__ b, const float *__restrict__ v, MixedParts X, int64_t n) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
@@ -1084,6 +1105,10 @@ void launch_cols_to_rows(cudaStream_t s, const double *cols, double *rows, int64
 }
 void launch_mixed_pack(cudaStream_t s, const float *b, const float *v, MixedParts X, int64_t n) {
   if (n > 0) k_mixed_pack<<<grid_for(n), kThreads, 0, s>>>(b, v, X, n);
+}
+void launch_mixed_check(cudaStream_t s, const uint32_t *cs, int64_t n, int64_t T, uint32_t weight_mask,
+                        unsigned long long *out) {
+  if (n > 0) k_mixed_check<<<grid_for(n), kThreads, 0, s>>>(cs, n, T, weight_mask, out);
 }
 void launch_mixed_unpack(cudaStream_t s, const MixedParts X, int64_t n, float *b, float *v) {
   if (n > 0) k_mixed_unpack<<<grid_for(n), kThreads, 0, s>>>(X, n, b, v);

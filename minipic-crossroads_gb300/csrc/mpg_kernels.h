@@ -86,6 +86,9 @@ void launch_rows_to_cols(cudaStream_t s, const double *rows, double *cols, int64
 void launch_cols_to_rows(cudaStream_t s, const double *cols, double *rows, int64_t n, int64_t cap);
 void launch_mixed_pack(cudaStream_t s, const float *b, const float *v, MixedParts X, int64_t n);
 void launch_mixed_unpack(cudaStream_t s, const MixedParts X, int64_t n, float *b, float *v);
+// out[0] = lowest invalid index (caller sets it to all ones), out[1] += live entries
+void launch_mixed_check(cudaStream_t s, const uint32_t *cs, int64_t n, int64_t T, uint32_t weight_mask,
+                        unsigned long long *out);
 // plain -> mixed conversion of a state (b = float(xref), v = float(v))
 void launch_plain_to_mixed(cudaStream_t s, const PlainParts &P, int64_t n0, int64_t n, const MixedParts &X);
 // mixed -> plain (x = ref_to_phys(cell, b), xref = b, w = species weight)

@@ -193,6 +193,39 @@ def test_mixed_walk_known_answer(mpg):
         assert st.n_killed == 1
 
 
+def test_mixed_upload_rejects_bad_words_and_keeps_state(mpg):
+    # the upload is validated on the device before it replaces the resident
+    # state: a cell out of range is an argument error, a species without a
+    # weight a state error, and a rejected upload changes nothing
+    ctx = _ctx(mpg, n_side=4)
+    ctx.reserve(1000)
+    ctx.fill_uniform(1000, 3, 0, 1e-3, vth=0.05)
+    cs, b, v = ctx.mixed_download()
+    n0 = ctx.count()
+    bad = cs.copy()
+    bad[777] = (bad[777] & 0xFF000000) | ctx.T  # cell index = T
+    with pytest.raises(mpg.MpgError) as e:
+        ctx.mixed_upload(bad, b, v)
+    assert e.value.code == mpg.ERR_ARG and "777" in str(e.value)
+    bad = cs.copy()
+    bad[5] = (5 << 24) | (bad[5] & 0xFFFFFF)  # species 5 has no weight
+    bad[9] = (bad[9] & 0xFF000000) | ctx.T
+    with pytest.raises(mpg.MpgError) as e:
+        ctx.mixed_upload(bad, b, v)
+    assert e.value.code == mpg.ERR_STATE  # lowest bad index (5) is reported
+    assert ctx.count() == n0
+    cs2, b2, v2 = ctx.mixed_download()
+    assert (cs2 == cs).all() and (b2.view(np.uint32) == b.view(np.uint32)).all()
+    dead = cs.copy()
+    dead[::3] = mpg.DEAD
+    ctx.mixed_upload(dead, b, v)
+    assert ctx.count() == int((dead != mpg.DEAD).sum())
+    out = (np.empty_like(cs), np.empty_like(b), np.empty_like(v))
+    cs3, b3, v3 = ctx.mixed_download(out=out)
+    assert cs3.base is out[0] or cs3 is out[0]
+    assert (cs3 == dead).all() and (b3.view(np.uint32) == b.view(np.uint32)).all()
+
+
 @pytest.mark.parametrize("ws", [2, 3])
 @pytest.mark.parametrize("form", ["mixed", "plain"])
 def test_extrapolated_initial_guess_same_solution(mpg, form, ws):
