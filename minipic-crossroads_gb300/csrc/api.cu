@@ -54,7 +54,8 @@ struct mpg_ctx {
   double *phi_prev = nullptr;   // previous solution (warm_start 2, 3)
   double *phi_prev2 = nullptr;  // the one before (warm_start 3)
   int phi_hist = 0;             // solutions held in phi / phi_prev / phi_prev2 (0 .. 3)
-  unsigned long long *acc = nullptr;
+  unsigned long long *acc = nullptr;  // fixed-point charge, one slot per (cell, corner), grouped by node (4T)
+  long long *acc_node = nullptr;      // per-node quanta for downloads (N)
   bool acc_valid = false;
   bool needs_sort = false;  // particles added or replaced since the last cell sort
   double inner_tol = 1e-5;  // relative residual target of the mixed solver's FP32 inner CG
@@ -363,7 +364,7 @@ int phase_deposit_plain(mpg_ctx *c) {
 int phase_deposit_mixed(mpg_ctx *c) {
   if (!c->acc_valid) {
     ensure_qfix(c);
-    CK(cudaMemsetAsync(c->acc, 0, sizeof(unsigned long long) * c->dm.N, c->stream));
+    CK(cudaMemsetAsync(c->acc, 0, sizeof(unsigned long long) * 4 * c->dm.T, c->stream));
     launch_mixed_deposit(c->stream, c->mp[c->cur], c->n, c->dm, c->sp, c->acc);
     c->acc_valid = true;
     c->launches += 1;
@@ -520,6 +521,8 @@ int one_step(mpg_ctx *c, double dt, mpg_step_stats *acc_st, bool &sorted) {
   ev_record(c, 3);
   CK(cudaMemsetAsync(&c->d_stats->ke, 0, sizeof(double), c->stream));
   if (mixed) {
+    // the move deposits the new positions' charge into zeroed slots
+    CK(cudaMemsetAsync(c->acc, 0, sizeof(unsigned long long) * 4 * c->dm.T, c->stream));
     launch_mixed_move(c->stream, c->mp[c->cur], c->n, c->dm, c->sp, (float)dt, c->cfg.kill_on_wall,
                       c->cfg.max_crossings, c->acc, c->d_stats);
   } else {
@@ -599,6 +602,21 @@ int upload_mesh(mpg_ctx *c) {
   CK(cudaMemcpyAsync(d.mrec, rec.data(), sizeof(float) * 12 * h.T, cudaMemcpyHostToDevice, s));
   host_fill_ratio(h, ratio);
   CK(cudaMemcpyAsync(d.fill_ratio, ratio.data(), sizeof(float) * h.T, cudaMemcpyHostToDevice, s));
+  // charge slots grouped by node: node i owns [off[i], off[i+1]), one slot per
+  // (tet, corner) that uses it, in tet order; c2n[t] = the slots of t's corners
+  std::vector<int32_t> off(h.N + 1, 0), c2n(4 * h.T);
+  for (int64_t t = 0; t < h.T; ++t)
+    for (int k = 0; k < 4; ++k) ++off[h.tets[4 * t + k] + 1];
+  for (int64_t i = 0; i < h.N; ++i) off[i + 1] += off[i];
+  {
+    std::vector<int32_t> fill(off.begin(), off.end() - 1);
+    for (int64_t t = 0; t < h.T; ++t)
+      for (int k = 0; k < 4; ++k) c2n[4 * t + k] = fill[h.tets[4 * t + k]]++;
+  }
+  TRY(dalloc(c, &d.n2c_off, h.N + 1));
+  TRY(dalloc(c, &d.c2n, h.T));
+  CK(cudaMemcpyAsync(d.n2c_off, off.data(), sizeof(int32_t) * (h.N + 1), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d.c2n, c2n.data(), sizeof(int32_t) * 4 * h.T, cudaMemcpyHostToDevice, s));
   CK(cudaStreamSynchronize(s));
   return MPG_OK;
 }
@@ -617,6 +635,8 @@ void free_mesh(mpg_ctx *c) {
   dfree(c, d.mrec);
   dfree(c, d.mnbr);
   dfree(c, d.fill_ratio);
+  dfree(c, d.n2c_off);
+  dfree(c, d.c2n);
   d = DevMesh();
 }
 
@@ -708,6 +728,7 @@ void free_field(mpg_ctx *c) {
   dfree(c, c->bg);
   dfree(c, c->Etet);
   dfree(c, c->acc);
+  dfree(c, c->acc_node);
   dfree(c, c->sort_cnt);
   dfree(c, c->sort_start);
   dfree(c, c->scan_scratch);
@@ -1066,7 +1087,9 @@ int mpg_configure(mpg_ctx *c, const mpg_config *cfg) {
     TRY(dalloc(c, &c->rhs, N));
     TRY(dalloc(c, &c->phi, N));
     TRY(dalloc(c, &c->Etet, 3 * T));
-    TRY(dalloc(c, &c->acc, N));
+    TRY(dalloc(c, &c->acc, 4 * T));
+    TRY(dalloc(c, &c->acc_node, N));
+    CK(cudaMemsetAsync(c->acc, 0, sizeof(unsigned long long) * 4 * T, c->stream));
     TRY(dalloc(c, &c->sort_cnt, T + 1));
     TRY(dalloc(c, &c->sort_start, T + 1));
     CK(cudaMemsetAsync(c->phi, 0, sizeof(double) * N, c->stream));
@@ -1396,12 +1419,16 @@ int mpg_charge_download(mpg_ctx *c, int64_t *acc, double *quantum, int64_t *qfix
   if (c->cfg.precision != MPG_MIXED) return fail(c, MPG_ERR_STATE, "charge accumulator exists in the mixed form only");
   ensure_qfix(c);
   if (!c->acc_valid && c->parts_alloc) {
-    CK(cudaMemsetAsync(c->acc, 0, sizeof(unsigned long long) * c->dm.N, c->stream));
+    CK(cudaMemsetAsync(c->acc, 0, sizeof(unsigned long long) * 4 * c->dm.T, c->stream));
     launch_mixed_deposit(c->stream, c->mp[c->cur], c->n, c->dm, c->sp, c->acc);
     CKL();
     c->acc_valid = true;
   }
-  if (acc) CK(cudaMemcpyAsync(acc, c->acc, sizeof(int64_t) * c->dm.N, cudaMemcpyDeviceToHost, c->stream));
+  if (acc) {
+    launch_node_quanta(c->stream, c->dm, c->acc, c->acc_node);
+    CKL();
+    CK(cudaMemcpyAsync(acc, c->acc_node, sizeof(int64_t) * c->dm.N, cudaMemcpyDeviceToHost, c->stream));
+  }
   CK(cudaStreamSynchronize(c->stream));
   if (quantum) *quantum = c->quantum;
   if (qfix)
@@ -1415,7 +1442,6 @@ int mpg_weight_charge(mpg_ctx *c) {
   if (c->cfg.precision == MPG_MIXED) {
     c->acc_valid = false;
     TRY(phase_deposit_mixed(c));
-    c->acc_valid = false;  // the conversion consumed (zeroed) the accumulator
   } else {
     TRY(phase_deposit_plain(c));
   }
@@ -1450,7 +1476,7 @@ int mpg_move(mpg_ctx *c, double dt, mpg_step_stats *st) {
   TRY(zero_stats(c));
   if (c->cfg.precision == MPG_MIXED) {
     // the fused kernel also deposits; keep the accumulator consistent
-    CK(cudaMemsetAsync(c->acc, 0, sizeof(unsigned long long) * c->dm.N, c->stream));
+    CK(cudaMemsetAsync(c->acc, 0, sizeof(unsigned long long) * 4 * c->dm.T, c->stream));
     ensure_qfix(c);
     launch_mixed_move(c->stream, c->mp[c->cur], c->n, c->dm, c->sp, (float)dt, c->cfg.kill_on_wall,
                       c->cfg.max_crossings, c->acc, c->d_stats);

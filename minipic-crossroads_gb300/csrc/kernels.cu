@@ -438,12 +438,14 @@ __global__ void __launch_bounds__(kScanThreads) k_compact_plain(PlainParts P, in
 // usual case after a cell sort) add their contributions with a segmented warp
 // scan, and the last lane of each run issues the four atomics.  Without this,
 // a sorted warp sends 32 same-address atomics to one L2 slice, which
-// serialise.  Integer addition is associative, so the result does not depend
-// on the grouping.  Every lane of the warp must call this; lanes with
-// key < 0 contribute nothing.
-__device__ __forceinline__ void deposit_fixed_warp(unsigned long long *__restrict__ acc,
-                                                   const int4 *__restrict__ tets, int key, float b1, float b2,
-                                                   float b3, int Q) {
+// serialise.  The atomics go to the cell's own four corner slots (not to
+// the nodes, which 24 tets share), so distinct cells never contend: slot
+// (t, k) sits at acc[c2n[t].k], inside node tets[t][k]'s contiguous slot
+// range, and k_mixed_convert sums each node's range.  Integer addition is
+// associative, so the result does not depend on the grouping.  Every lane of
+// the warp must call this; lanes with key < 0 contribute nothing.
+__device__ __forceinline__ void deposit_fixed_warp(unsigned long long *__restrict__ acc, const int4 *__restrict__ c2n,
+                                                   int key, float b1, float b2, float b3, int Q) {
   // |Q| <= 2^25 quanta, so a run of up to 32 lanes sums to < 2^30 in int32
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -465,11 +467,11 @@ __device__ __forceinline__ void deposit_fixed_warp(unsigned long long *__restric
     c2 = __reduce_add_sync(FULL, c2);
     c3 = __reduce_add_sync(FULL, c3);
     if (lane == 0 && key >= 0) {
-      const int4 nd = tets[key];
-      atomicAdd(acc + nd.x, (unsigned long long)(long long)c0);
-      atomicAdd(acc + nd.y, (unsigned long long)(long long)c1);
-      atomicAdd(acc + nd.z, (unsigned long long)(long long)c2);
-      atomicAdd(acc + nd.w, (unsigned long long)(long long)c3);
+      const int4 q = c2n[key];
+      atomicAdd(acc + q.x, (unsigned long long)(long long)c0);
+      atomicAdd(acc + q.y, (unsigned long long)(long long)c1);
+      atomicAdd(acc + q.z, (unsigned long long)(long long)c2);
+      atomicAdd(acc + q.w, (unsigned long long)(long long)c3);
     }
     return;
   }
@@ -491,15 +493,15 @@ __device__ __forceinline__ void deposit_fixed_warp(unsigned long long *__restric
   const int sn = __shfl_down_sync(FULL, seg, 1);
   const bool tail = lane == 31 || sn != seg;
   if (tail && key >= 0) {
-    const int4 nd = tets[key];
-    atomicAdd(acc + nd.x, (unsigned long long)(long long)c0);
-    atomicAdd(acc + nd.y, (unsigned long long)(long long)c1);
-    atomicAdd(acc + nd.z, (unsigned long long)(long long)c2);
-    atomicAdd(acc + nd.w, (unsigned long long)(long long)c3);
+    const int4 q = c2n[key];
+    atomicAdd(acc + q.x, (unsigned long long)(long long)c0);
+    atomicAdd(acc + q.y, (unsigned long long)(long long)c1);
+    atomicAdd(acc + q.z, (unsigned long long)(long long)c2);
+    atomicAdd(acc + q.w, (unsigned long long)(long long)c3);
   }
 }
 
-__global__ void __launch_bounds__(kThreads) k_mixed_deposit(MixedParts P, int64_t n, const int4 *__restrict__ tets,
+__global__ void __launch_bounds__(kThreads) k_mixed_deposit(MixedParts P, int64_t n, const int4 *__restrict__ c2n,
                                                             SpeciesTable S, unsigned long long *__restrict__ acc) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int key = -1;
@@ -517,27 +519,42 @@ __global__ void __launch_bounds__(kThreads) k_mixed_deposit(MixedParts P, int64_
     }
   }
   // each lane converts its own charge Q, so runs may mix species
-  deposit_fixed_warp(acc, tets, key, b1, b2, b3, Q);
+  deposit_fixed_warp(acc, c2n, key, b1, b2, b3, Q);
+}
+
+// charge quanta of node i: the sum of its slot range acc[off[i] .. off[i+1])
+// (one thread per node; the slots are zeroed by a memset before the next
+// deposit, which is cheaper than zeroing them here, behind the reads)
+__device__ __forceinline__ long long node_quanta(int64_t i, const int32_t *__restrict__ off,
+                                                 const unsigned long long *__restrict__ acc) {
+  long long a = 0;
+  for (int32_t q = off[i]; q < off[i + 1]; ++q) a += (long long)acc[q];
+  return a;
 }
 
 // Periodic meshes (plane > 0): the ghost plane's quanta are folded into
 // their pairs by the pair's thread (integer sums: exact, order free).
-__global__ void k_mixed_convert(int64_t N, unsigned long long *__restrict__ acc, double quantum,
-                                const double *__restrict__ bg, const uint8_t *__restrict__ bnd,
+__global__ void k_mixed_convert(int64_t N, const int32_t *__restrict__ off, const unsigned long long *__restrict__ acc,
+                                double quantum, const double *__restrict__ bg, const uint8_t *__restrict__ bnd,
                                 double *__restrict__ rhs, int64_t nsolve, int64_t plane) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N || (plane && i >= nsolve)) return;
-  long long a = (long long)acc[i];
-  acc[i] = 0ull;
+  long long a = node_quanta(i, off, acc);
   if (plane && i < plane) {
-    a += (long long)acc[nsolve + i];
-    acc[nsolve + i] = 0ull;
+    a += node_quanta(nsolve + i, off, acc);
     rhs[nsolve + i] = 0.0;
   }
   double r = -((double)a * quantum);
   if (bg) r += bg[i];
   if (bnd[i]) r = 0.0;
   rhs[i] = r;
+}
+
+// per-node quanta, for downloads
+__global__ void k_node_quanta(int64_t N, const int32_t *__restrict__ off, const unsigned long long *__restrict__ acc,
+                              long long *__restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < N) out[i] = node_quanta(i, off, acc);
 }
 
 // E per tet from phi: E = sum_k (phi_k - phi_0) * row_{k-1}(J^-1); the phi
@@ -560,7 +577,7 @@ __global__ void k_efield_mixed(int64_t T, const int4 *__restrict__ tets, float4 
 
 __global__ void __launch_bounds__(kThreads) k_mixed_move(MixedParts P, int64_t n, const float4 *__restrict__ rec,
                                                          const uint4 *__restrict__ nbr,
-                                                         const int4 *__restrict__ tets, SpeciesTable S, float dt,
+                                                         const int4 *__restrict__ c2n, SpeciesTable S, float dt,
                                                          int kill, int max_cross, unsigned long long *__restrict__ acc,
                                                          DevStats *st) {
   __shared__ BlockTotals bt;
@@ -602,7 +619,7 @@ __global__ void __launch_bounds__(kThreads) k_mixed_move(MixedParts P, int64_t n
     }
   }
   // deposit of the new position for the next step's field solve
-  deposit_fixed_warp(acc, tets, dep_key, d1, d2, d3, dq);
+  deposit_fixed_warp(acc, c2n, dep_key, d1, d2, d3, dq);
   block_totals_push(&bt, ff{ke, 0.f}, killed, cross, limit, st);
 }
 
@@ -615,7 +632,7 @@ __global__ void __launch_bounds__(kThreads) k_mixed_move(MixedParts P, int64_t n
 __global__ void __launch_bounds__(kThreads) k_mixed_move_persistent(MixedParts P, int64_t n,
                                                                     const float4 *__restrict__ rec,
                                                                     const uint4 *__restrict__ nbr,
-                                                                    const int4 *__restrict__ tets, SpeciesTable S,
+                                                                    const int4 *__restrict__ c2n, SpeciesTable S,
                                                                     float dt, int kill, int max_cross,
                                                                     unsigned long long *__restrict__ acc,
                                                                     DevStats *st) {
@@ -682,7 +699,7 @@ __global__ void __launch_bounds__(kThreads) k_mixed_move_persistent(MixedParts P
       }
     }
     // every lane of the warp is here (c is uniform across the warp)
-    deposit_fixed_warp(acc, tets, dep_key, d1, d2, d3, dq);
+    deposit_fixed_warp(acc, c2n, dep_key, d1, d2, d3, dq);
   }
   block_totals_push(&bt, ke, killed, cross, limit, st);
 }
@@ -1030,12 +1047,15 @@ void launch_compact_plain(cudaStream_t s, const PlainParts &P, int64_t n, const 
 void launch_mixed_deposit(cudaStream_t s, const MixedParts &P, int64_t n, const DevMesh &M, const SpeciesTable &S,
                           unsigned long long *acc) {
   if (n <= 0) return;
-  k_mixed_deposit<<<grid_for(n), kThreads, 0, s>>>(P, n, M.tets, S, acc);
+  k_mixed_deposit<<<grid_for(n), kThreads, 0, s>>>(P, n, M.c2n, S, acc);
 }
 void launch_mixed_convert(cudaStream_t s, const DevMesh &M, unsigned long long *acc, double quantum, const double *bg,
                           double *rhs) {
-  k_mixed_convert<<<grid_for(M.N), kThreads, 0, s>>>(M.N, acc, quantum, bg, M.bnd, rhs, M.nsolve,
+  k_mixed_convert<<<grid_for(M.N), kThreads, 0, s>>>(M.N, M.n2c_off, acc, quantum, bg, M.bnd, rhs, M.nsolve,
                                                      M.fper ? M.plane : 0);
+}
+void launch_node_quanta(cudaStream_t s, const DevMesh &M, const unsigned long long *acc, long long *out) {
+  k_node_quanta<<<grid_for(M.N), kThreads, 0, s>>>(M.N, M.n2c_off, acc, out);
 }
 void launch_efield_mixed(cudaStream_t s, const DevMesh &M, const double *phi) {
   k_efield_mixed<<<grid_for(M.T), kThreads, 0, s>>>(M.T, M.tets, M.mrec, phi);
@@ -1059,12 +1079,12 @@ void launch_mixed_move(cudaStream_t s, const MixedParts &P, int64_t n, const Dev
   if (n <= 0) return;
   static const char *env = getenv("MPG_MOVE_KERNEL");
   if (env && atoi(env) == 0) {
-    k_mixed_move<<<grid_for(n), kThreads, 0, s>>>(P, n, M.mrec, M.mnbr, M.tets, S, dt, kill, max_cross, acc, st);
+    k_mixed_move<<<grid_for(n), kThreads, 0, s>>>(P, n, M.mrec, M.mnbr, M.c2n, S, dt, kill, max_cross, acc, st);
     return;
   }
   const unsigned wave = move_wave_blocks();
   const unsigned want = grid_for(n);
-  k_mixed_move_persistent<<<want < wave ? want : wave, kThreads, 0, s>>>(P, n, M.mrec, M.mnbr, M.tets, S, dt, kill,
+  k_mixed_move_persistent<<<want < wave ? want : wave, kThreads, 0, s>>>(P, n, M.mrec, M.mnbr, M.c2n, S, dt, kill,
                                                                          max_cross, acc, st);
 }
 void launch_mixed_sort(cudaStream_t s, const MixedParts &P, int64_t n, const MixedParts &Q, int64_t T, uint32_t *cnt,

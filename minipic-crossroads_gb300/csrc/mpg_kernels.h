@@ -42,6 +42,11 @@ struct DevMesh {
   float4 *mrec = nullptr;    // T*3: J^-1 (9 floats) then E (3 floats)
   uint4 *mnbr = nullptr;     // T: neighbour + permutation per face (indexed by opposite vertex)
   float *fill_ratio = nullptr;  // T: vol/vol_max
+  // fixed-point charge slots of the mixed form, grouped by node: node i owns
+  // slots [n2c_off[i], n2c_off[i+1]), one per (tet, corner) that uses it;
+  // c2n[t] holds the slots of tet t's four corners
+  int32_t *n2c_off = nullptr;   // N+1
+  int4 *c2n = nullptr;          // T
 };
 
 // ---- plain FP64 path ------------------------------------------------------
@@ -59,10 +64,17 @@ void launch_compact_plain(cudaStream_t s, const PlainParts &P, int64_t n, const 
                           int64_t scratch_len, uint32_t *d_count);
 
 // ---- mixed path -----------------------------------------------------------
+// The fixed-point charge accumulator holds one slot per (cell, corner), 4T
+// entries grouped by node (DevMesh::n2c_off, c2n); node i's quanta are the
+// sum of its slot range.
 void launch_mixed_deposit(cudaStream_t s, const MixedParts &P, int64_t n, const DevMesh &M, const SpeciesTable &S,
                           unsigned long long *acc);
+// rhs from the slots (gathered per node; the slots stay unchanged, the
+// caller zeroes them before the next deposit)
 void launch_mixed_convert(cudaStream_t s, const DevMesh &M, unsigned long long *acc, double quantum, const double *bg,
                           double *rhs);
+// per-node quanta (N) from the slots
+void launch_node_quanta(cudaStream_t s, const DevMesh &M, const unsigned long long *acc, long long *out);
 void launch_efield_mixed(cudaStream_t s, const DevMesh &M, const double *phi);
 void launch_mixed_move(cudaStream_t s, const MixedParts &P, int64_t n, const DevMesh &M, const SpeciesTable &S,
                        float dt, int kill, int max_cross, unsigned long long *acc, DevStats *st);
