@@ -245,12 +245,14 @@ def phase_bytes(w, ctx, stats, steps, mpg):
     if uses_mg(w):
         cg_iter = mg_iter_bytes(w["n_side"], N, coef)
     return {
-        # 28 B read + 28 B write per particle, 16 B of node ids, 4 x 8 B accumulator RMW,
-        # per-tet walk record (48 B) + neighbour table (16 B) read once
-        "move": P * (56 + 16) + N * 16 + T * 64,
+        # 28 B read + 28 B write per particle; per tet the walk record (48 B), the
+        # neighbour table (16 B) and the charge-slot indices (16 B) read once and
+        # its four 8-byte charge slots written once
+        "move": P * 56 + T * (48 + 16 + 16 + 32),
         "solve": iters * cg_iter + 3 * sweep,
         "efield": T * (16 + 48 + 12) + N * 8,
-        "deposit": N * (8 + 8 + 8 + 8),
+        # per node: slot offsets, background, flag, rhs; the 4T charge slots read
+        "deposit": N * (4 + 8 + 1 + 8) + T * 32,
         "cg_iter_bytes": cg_iter, "iters_per_step": iters,
     }
 
