@@ -707,6 +707,12 @@ int upload_mg(mpg_ctx *c, const MgHostHierarchy &H) {
   m.dense_inv = inv;
   if (const char *e = getenv("MPG_MG_OMEGA")) m.omega = (float)atof(e);
   if (const char *e = getenv("MPG_MG_RELIABLE")) m.reliable = atoi(e);
+  int64_t fuse_rows = 1 << 20;
+  if (const char *e = getenv("MPG_MG_FUSE_UPDATE_ROWS")) fuse_rows = atoll(e);
+  m.fuse_update = m.lev[0].n <= fuse_rows ? 1 : 0;
+  if (c->dia.constant)
+    for (int d = 0; d < c->dia.ndiag; ++d)
+      if (c->dia.off[d] == 0 && c->dia.cst[d] != 0.f) m.dinv0 = (float)(1.0 / (double)c->dia.cst[d]);
   c->mg_ok = true;
   return MPG_OK;
 }

@@ -155,12 +155,19 @@ __device__ __forceinline__ float prolong_at(const MgLevelDev &F, const MgLevelDe
 // e = omega D^-1 r (one Jacobi sweep from zero).  e is not stored: A e reads
 // it through a loader (rv(j) gives r at row j), and the ascending steps
 // recompute it.
+// D^-1 of row j on level l: one constant on level 0 of a uniform mesh (its
+// Dirichlet rows carry r = 0, so their own D^-1 = 1 never matters)
+template <bool CST>
+__device__ __forceinline__ float dinv_at(const CgMgArgs &a, int l, const float *__restrict__ dinv, int64_t j) {
+  return (CST && l == 0) ? a.mg.dinv0 : dinv[j];
+}
+
 template <int ND, bool CST, typename R>
 __device__ __forceinline__ void presmooth_residual(const CgMgArgs &a, int l, int64_t lo, int64_t hi, R rv) {
   const MgLevelDev &L = a.mg.lev[l];
   const float om = a.mg.omega;
   const float *__restrict__ dinv = L.dinv;
-  auto e0 = [&](int64_t j) { return om * dinv[j] * rv(j); };
+  auto e0 = [&](int64_t j) { return om * dinv_at<CST>(a, l, dinv, j) * rv(j); };
   for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) L.t[i] = rv(i) - level_apply<ND, CST>(a, l, e0, i);
 }
 
@@ -191,7 +198,7 @@ __device__ __forceinline__ bool level_up(const CgMgArgs &a, int l, int64_t lo, i
   const MgLevelDev &C = a.mg.lev[l + 1];
   const float om = a.mg.omega;
   for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-    float e = om * L.dinv[i] * r[i];
+    float e = om * dinv_at<CST>(a, l, L.dinv, i) * r[i];
     if (!L.bnd[i]) e += prolong_at(L, C, c, i);
     L.e[i] = e;
   }
@@ -199,7 +206,7 @@ __device__ __forceinline__ bool level_up(const CgMgArgs &a, int l, int64_t lo, i
   const float *__restrict__ ev = L.e;
   auto ld = [&](int64_t j) { return ev[j]; };
   for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x)
-    L.t[i] = ev[i] + om * L.dinv[i] * (r[i] - level_apply<ND, CST>(a, l, ld, i));
+    L.t[i] = ev[i] + om * dinv_at<CST>(a, l, L.dinv, i) * (r[i] - level_apply<ND, CST>(a, l, ld, i));
   return sync();
 }
 
@@ -448,9 +455,10 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mg(CgMgArgs a) {
       const float beta = have_dir ? G.hi / gam_prev.hi : 0.f;
       const ff den = ff_add(ff_add(tot[1], ff_mulf(tot[2], 2.f * beta)), ff_mulf(ff_mulf(tot[3], beta), beta));
       const float alpha = G.hi / den.hi;
-      // update into the other buffers, fused with the next V-cycle's first
-      // step: that step reads the new residual at neighbour rows, which it
-      // recomputes from the old buffers bit for bit as their owners write it
+      // update into the other buffers, fused (levels up to fuse_update rows)
+      // with the next V-cycle's first step: that step reads the new residual
+      // at neighbour rows, which it recomputes from the old buffers bit for
+      // bit as their owners write it
       const int nx = cur ^ 1;
       const float *__restrict__ ro = a.r[cur];
       const float *__restrict__ so = a.s[cur];
@@ -465,8 +473,15 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mg(CgMgArgs a) {
         a.z[i] = __fmaf_rn(alpha, pi, a.z[i]);
         rn[i] = __fmaf_rn(-alpha, si, ro[i]);
       }
-      presmooth_residual<ND, CST>(a, 0, lo, hi,
-                                  [&](int64_t j) { return __fmaf_rn(-alpha, __fmaf_rn(beta, so[j], wv[j]), ro[j]); });
+      if (a.mg.fuse_update) {
+        presmooth_residual<ND, CST>(
+            a, 0, lo, hi, [&](int64_t j) { return __fmaf_rn(-alpha, __fmaf_rn(beta, so[j], wv[j]), ro[j]); });
+      } else {
+        // large levels: one barrier more, but the pre-smoothing then reads
+        // one vector per neighbour instead of three
+        if (!bar()) return;
+        presmooth_residual<ND, CST>(a, 0, lo, hi, [&](int64_t j) { return rn[j]; });
+      }
       cur = nx;
       gam_prev = G;
       have_dir = true;

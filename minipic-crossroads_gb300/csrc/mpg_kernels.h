@@ -169,6 +169,8 @@ struct MgDev {
   int dense_m = 0;
   float omega = 0.8f;
   int reliable = 1;  // keep the search direction across refinement sweeps (reliable updates)
+  int fuse_update = 1;  // fuse the PCG update with the next pre-smoothing (level 0 up to ~1M rows)
+  float dinv0 = 1.f;    // level 0's D^-1 on a uniform mesh (constant stencil)
 };
 // mixed CG preconditioned by one V(1,1) cycle per iteration, one cooperative
 // launch; `max_blocks` from mg_max_blocks
