@@ -5,7 +5,7 @@
 //
 //   minipic_gb300 --mesh=brick.txt --nparts=10 --dt=0.1 --tfinal=2.0
 //                 [--kill-particles=1] [--density=...] [--output=k] [--dump_mesh=1]
-//                 [--steps=N] [--precision=plain|mixed] [--solver=bicgstab|cg]
+//                 [--steps=N] [--precision=plain|mixed] [--solver=bicgstab|cg|cg-mg]
 //                 [--deposit=quarter|linear] [--tol=1e-6]
 #include <cmath>
 #include <cstdio>
@@ -50,7 +50,7 @@ int main(int argc, char **argv) {
       std::cout << "usage: " << argv[0]
                 << " [--nparts=N] [--mesh=file] [--dt=x] [--tfinal=x] [--output=k] [--kill-particles=0|1]"
                    " [--problem=none|two-stream] [--density=x] [--dump_mesh=0|1] [--steps=N] [--precision=plain|mixed]"
-                   " [--solver=bicgstab|cg] [--deposit=quarter|linear] [--tol=x]\n";
+                   " [--solver=bicgstab|cg|cg-mg] [--deposit=quarter|linear] [--tol=x]\n";
       return 0;
     } else {
       std::cerr << "unknown option " << argv[i] << "\n";
@@ -63,7 +63,7 @@ int main(int argc, char **argv) {
     data.create_mesh(meshfile, two_stream);  // main.cpp:89-92: periodic for the two-stream problem
     mpg_config &cfg = data.config();
     cfg.precision = precision == "mixed" ? MPG_MIXED : MPG_PLAIN;
-    cfg.solver = solver == "cg" ? MPG_SOLVER_CG : MPG_SOLVER_BICGSTAB;
+    cfg.solver = solver == "cg" ? MPG_SOLVER_CG : solver == "cg-mg" ? MPG_SOLVER_CG_MG : MPG_SOLVER_BICGSTAB;
     cfg.deposit = deposit == "linear" ? MPG_DEPOSIT_LINEAR : MPG_DEPOSIT_REF_QUARTER;
     cfg.tol = tol;
     cfg.kill_on_wall = part_kill == 1;
