@@ -192,23 +192,29 @@ def peaks():
 
 
 def uses_mg(w):
-    return MIXED_SOLVER == "mg" and not w.get("periodic", 0) and mg_levels(w["n_side"])
+    return MIXED_SOLVER == "mg" and bool(mg_levels(w["n_side"], w.get("periodic", 0)))
 
 
-def mg_levels(n_side, dense_max=1400):
-    """Node extents of the multigrid levels: halve while the interior has more
-    than dense_max nodes and the cell count is even (the host hierarchy's rule)."""
-    g = [n_side + 1]
-    while len(g) < 8 and (g[-1] - 2) ** 3 > dense_max:
-        if (g[-1] - 1) % 2 or g[-1] < 5:
+def mg_levels(n_side, periodic=0, dense_max=1500):
+    """(x, y/z) node extents of the multigrid levels: halve while the interior
+    has more than dense_max unknowns and the counts allow it (the host
+    hierarchy's rule; a periodic x axis holds n planes and halves while even
+    and the result stays >= 4)."""
+    def interior(x, g):
+        return (x if periodic else x - 2) * (g - 2) ** 2
+    lev = [(n_side if periodic else n_side + 1, n_side + 1)]
+    while len(lev) < 8 and interior(*lev[-1]) > dense_max:
+        x, g = lev[-1]
+        okx = (x % 2 == 0 and x // 2 >= 4) if periodic else ((x - 1) % 2 == 0 and x >= 5)
+        if not okx or (g - 1) % 2 or g < 5:
             break
-        g.append((g[-1] - 1) // 2 + 1)
-    if len(g) < 2 or (g[-1] - 2) ** 3 > dense_max:
+        lev.append((x // 2 if periodic else (x - 1) // 2 + 1, (g - 1) // 2 + 1))
+    if len(lev) < 2 or interior(*lev[-1]) > dense_max:
         return []
-    return g
+    return [(x, g, interior(x, g)) for x, g in lev]
 
 
-def mg_iter_bytes(n_side, N, coef):
+def mg_iter_bytes(n_side, N, coef, periodic=0):
     """Algorithmic bytes of one multigrid-preconditioned inner iteration.
 
     Fine level, per row: fused update + pre-smoothing reads p, u, s, w, z, r,
@@ -217,12 +223,12 @@ def mg_iter_bytes(n_side, N, coef):
     writes w (12 B); three stencil passes read the FP32 coefficients (3 coef).
     Coarse levels, per row: 27 FP32 coefficients in two passes plus about 80 B
     of vectors.  Coarsest level: its dense inverse (m^2 FP32)."""
-    g = mg_levels(n_side)
+    lev = mg_levels(n_side, periodic)
     b = (44 + 4 + 28 + 12 + 3 * coef) * N
-    for gl in g[1:-1]:
-        b += (2 * 27 * 4 + 80) * gl ** 3
-    m = (g[-1] - 2) ** 3
-    return b + 4 * m * m + 40 * g[-1] ** 3
+    for x, g, _ in lev[1:-1]:
+        b += (2 * 27 * 4 + 80) * x * g * g
+    x, g, m = lev[-1]
+    return b + 4 * m * m + 40 * x * g * g
 
 
 def phase_bytes(w, ctx, stats, steps, mpg):
@@ -243,7 +249,7 @@ def phase_bytes(w, ctx, stats, steps, mpg):
     cg_iter = (coef + 32) * N
     sweep = (8 * nd + 24 + 20) * N
     if uses_mg(w):
-        cg_iter = mg_iter_bytes(w["n_side"], N, coef)
+        cg_iter = mg_iter_bytes(w["n_side"], N, coef, w.get("periodic", 0))
     return {
         # 28 B read + 28 B write per particle; per tet the walk record (48 B), the
         # neighbour table (16 B) and the charge-slot indices (16 B) read once and
@@ -664,7 +670,7 @@ def main():
                            "cg_initial_guess": ["zero", "previous phi", "extrapolated 2*phi[n-1]-phi[n-2]",
                                                 "extrapolated 3*phi[n-1]-3*phi[n-2]+phi[n-3]"][WARM_START],
                            "cg_preconditioner": ("geometric multigrid V(1,1)" if precision == mpg.MIXED
-                                                 and MIXED_SOLVER == "mg" and not w.get("periodic", 0) else "none"),
+                                                 and uses_mg(w) else "none"),
                            "parallelism": "replicas" if world > 1 else "single",
                            "l2": "inputs larger than L2 (particle state > 129 MB), no flush"},
                 "phases_ms_per_step": {k: round(v, 4) for k, v in phases.items()},

@@ -661,6 +661,7 @@ int upload_mg(mpg_ctx *c, const MgHostHierarchy &H) {
     L.gx = h.gx;
     L.gy = h.gy;
     L.gz = h.gz;
+    L.px = h.px ? 1 : 0;
     L.sj = h.gz;
     L.si = h.gy * h.gz;
     L.n = (int64_t)h.gx * h.gy * h.gz;

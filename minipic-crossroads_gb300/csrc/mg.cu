@@ -92,14 +92,22 @@ __device__ __forceinline__ float level_apply(const CgMgArgs &a, int l, X xv, int
   if (L.bnd[i]) return xv(i);
   float s = 0.f;
   if (l == 0) {
-    const int64_t n = a.A.n;
+    const int64_t n = a.A.n, nwrap = a.A.nwrap;
 #pragma unroll
-    for (int d = 0; d < ND; ++d) s = __fmaf_rn(CST ? a.A.cst[d] : a.A.val32[d * n + i], xv(i + a.A.off[d]), s);
+    for (int d = 0; d < ND; ++d)
+      s = __fmaf_rn(CST ? a.A.cst[d] : a.A.val32[d * n + i], xv(dia_nb(i, a.A.off[d], nwrap)), s);
   } else {
     const int64_t n = L.n;
+    // x-plane offsets of the -1 / +1 neighbours (wrapping on a periodic level)
+    int64_t xm = -(int64_t)L.si, xp = L.si;
+    if (L.px) {
+      const int64_t I = i / L.si;
+      if (I == 0) xm += (int64_t)L.gx * L.si;
+      if (I == L.gx - 1) xp -= (int64_t)L.gx * L.si;
+    }
 #pragma unroll
     for (int d = 0; d < 27; ++d) {
-      const int64_t off = (d / 9 - 1) * (int64_t)L.si + ((d / 3) % 3 - 1) * (int64_t)L.sj + (d % 3 - 1);
+      const int64_t off = (d / 9 == 0 ? xm : d / 9 == 2 ? xp : 0) + ((d / 3) % 3 - 1) * (int64_t)L.sj + (d % 3 - 1);
       s = __fmaf_rn(L.val[d * n + i], xv(i + off), s);
     }
   }
@@ -121,14 +129,16 @@ __device__ __forceinline__ float restrict_at(const MgLevelDev &F, const MgLevelD
   if (Cl.bnd[C]) return 0.f;
   unsigned I, J, K;
   level_ijk(Cl, C, I, J, K);
-  const int64_t f0 = 2 * (int64_t)I * F.si + 2 * (int64_t)J * F.sj + 2 * (int64_t)K;
+  const int64_t f0 = 2 * (int64_t)J * F.sj + 2 * (int64_t)K;
   float s = 0.f;
 #pragma unroll
   for (int di = -1; di <= 1; ++di)
 #pragma unroll
     for (int dj = -1; dj <= 1; ++dj) {
       const float wij = (di ? 0.5f : 1.f) * (dj ? 0.5f : 1.f);
-      const float *row = F.t + f0 + di * (int64_t)F.si + dj * (int64_t)F.sj;
+      int64_t fi = 2 * (int64_t)I + di;  // fine x-plane, wrapping on a periodic level
+      if (F.px) fi = fi < 0 ? fi + F.gx : fi >= F.gx ? fi - F.gx : fi;
+      const float *row = F.t + fi * F.si + f0 + dj * (int64_t)F.sj;
       s = __fmaf_rn(wij * 0.5f, row[-1], s);
       s = __fmaf_rn(wij, row[0], s);
       s = __fmaf_rn(wij * 0.5f, row[1], s);
@@ -143,7 +153,9 @@ __device__ __forceinline__ float prolong_at(const MgLevelDev &F, const MgLevelDe
                                             int64_t i) {
   unsigned fi, fj, fk;
   level_ijk(F, i, fi, fj, fk);
-  const int64_t i0 = (int64_t)(fi >> 1) * Cl.si, i1 = (int64_t)((fi + 1) >> 1) * Cl.si;
+  unsigned ci1 = (fi + 1) >> 1;
+  if (Cl.px && ci1 == (unsigned)Cl.gx) ci1 = 0;  // the last fine plane sits between the last and first coarse ones
+  const int64_t i0 = (int64_t)(fi >> 1) * Cl.si, i1 = (int64_t)ci1 * Cl.si;
   const int64_t j0 = (int64_t)(fj >> 1) * Cl.sj, j1 = (int64_t)((fj + 1) >> 1) * Cl.sj;
   const int64_t k0 = fk >> 1, k1 = (fk + 1) >> 1;
   const float s = ((c[i0 + j0 + k0] + c[i0 + j0 + k1]) + (c[i0 + j1 + k0] + c[i0 + j1 + k1])) +
@@ -374,7 +386,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mg(CgMgArgs a) {
         s = a.x[i];
       } else {
 #pragma unroll
-        for (int d = 0; d < ND; ++d) s += v64[d * n + i] * a.x[i + a.A.off[d]];
+        for (int d = 0; d < ND; ++d) s += v64[d * n + i] * a.x[dia_nb(i, a.A.off[d], a.A.nwrap)];
       }
       const double ri = a.b[i] - s;
       a.r64[i] = ri;

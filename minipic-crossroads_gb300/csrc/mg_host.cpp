@@ -24,21 +24,26 @@
 
 namespace {
 
-constexpr int kDenseMaxDefault = 1400;  // interior unknowns of the coarsest level (11^3 = 1331)
+constexpr int kDenseMaxDefault = 1500;  // interior unknowns of the coarsest level (11^3 = 1331, 12 x 11^2 = 1452)
 constexpr int kMaxLevels = 8;
 
-inline bool is_bnd(int64_t i, int64_t j, int64_t k, int gx, int gy, int gz) {
-  return i == 0 || j == 0 || k == 0 || i == gx - 1 || j == gy - 1 || k == gz - 1;
-}
-
 // row access to a level's FP64 operator: level 0 is the assembled CSR, the
-// coarser ones are 27-point stencils [d][n] with d = 9 (di+1) + 3 (dj+1) + (dk+1)
+// coarser ones are 27-point stencils [d][n] with d = 9 (di+1) + 3 (dj+1) + (dk+1).
+// On a mesh periodic in x the levels hold the gx x-planes without the ghost
+// plane, x indices wrap around and only the y/z walls are Dirichlet rows.
 struct LevelOp {
   int gx, gy, gz;
+  bool px = false;  // periodic in x
   const std::vector<int32_t> *rp = nullptr, *col = nullptr;
   const std::vector<double> *val = nullptr;
   std::vector<double> dia;  // 27 * n (coarse levels)
   int64_t n() const { return (int64_t)gx * gy * gz; }
+  bool bnd(int64_t i, int64_t j, int64_t k) const {
+    return (!px && (i == 0 || i == gx - 1)) || j == 0 || k == 0 || j == gy - 1 || k == gz - 1;
+  }
+  int64_t wrapx(int64_t i) const { return px ? (i % gx + gx) % gx : i; }
+  // interior unknowns (rows that are not Dirichlet rows)
+  int64_t interior() const { return (int64_t)(px ? gx : gx - 2) * (gy - 2) * (gz - 2); }
 };
 
 }  // namespace
@@ -46,26 +51,32 @@ struct LevelOp {
 bool host_mg_build(const HostMesh &m, const std::vector<int32_t> &rp, const std::vector<int32_t> &col,
                    const std::vector<double> &val, MgHostHierarchy &H, std::string &why) {
   H = MgHostHierarchy();
-  if (m.d.periodic) {
-    why = "periodic meshes are not coarsened";
-    return false;
-  }
-  const int gx0 = m.d.nx + 1, gy0 = m.d.ny + 1, gz0 = m.d.nz + 1;
+  const bool px = m.d.periodic != 0;
   std::vector<LevelOp> ops(1);
-  ops[0].gx = gx0;
-  ops[0].gy = gy0;
-  ops[0].gz = gz0;
+  // level 0: the solver's rows (a periodic mesh solves the nx planes x < hi)
+  ops[0].gx = px ? m.d.nx : m.d.nx + 1;
+  ops[0].gy = m.d.ny + 1;
+  ops[0].gz = m.d.nz + 1;
+  ops[0].px = px;
   ops[0].rp = &rp;
   ops[0].col = &col;
   ops[0].val = &val;
+  if ((int64_t)rp.size() != ops[0].n() + 1) {
+    why = "system rows do not match the node grid";
+    return false;
+  }
   int64_t kDenseMax = kDenseMaxDefault;
   if (const char *e = getenv("MPG_MG_DENSE_MAX")) kDenseMax = atoll(e);
-  auto interior = [](const LevelOp &o) { return (int64_t)(o.gx - 2) * (o.gy - 2) * (o.gz - 2); };
-  while ((int)ops.size() < kMaxLevels && interior(ops.back()) > kDenseMax) {
+  while ((int)ops.size() < kMaxLevels && ops.back().interior() > kDenseMax) {
     const LevelOp &f = ops.back();
-    if ((f.gx - 1) % 2 || (f.gy - 1) % 2 || (f.gz - 1) % 2 || f.gx < 5 || f.gy < 5 || f.gz < 5) break;
+    // y, z: node extents 2m+1 -> m+1 (Dirichlet ends stay on the grid);
+    // x: the same, or on a periodic level an even plane count 2m -> m (m >= 4,
+    // so that the 27-point stencil's x-1 and x+1 planes stay distinct)
+    const bool okx = f.px ? (f.gx % 2 == 0 && f.gx / 2 >= 4) : ((f.gx - 1) % 2 == 0 && f.gx >= 5);
+    if (!okx || (f.gy - 1) % 2 || (f.gz - 1) % 2 || f.gy < 5 || f.gz < 5) break;
     LevelOp c;
-    c.gx = (f.gx - 1) / 2 + 1;
+    c.px = f.px;
+    c.gx = f.px ? f.gx / 2 : (f.gx - 1) / 2 + 1;
     c.gy = (f.gy - 1) / 2 + 1;
     c.gz = (f.gz - 1) / 2 + 1;
     const int64_t nc = c.n();
@@ -76,31 +87,36 @@ bool host_mg_build(const HostMesh &m, const std::vector<int32_t> &rp, const std:
     for (int64_t C = 0; C < nc; ++C) {
       const int64_t I = C / csi, J = (C / csj) % c.gy, K = C % csj;
       double acc[27] = {0};
-      if (is_bnd(I, J, K, c.gx, c.gy, c.gz)) {
+      if (c.bnd(I, J, K)) {
         c.dia[13 * nc + C] = 1.0;  // identity row
         continue;
       }
       for (int di = -1; di <= 1; ++di)
         for (int dj = -1; dj <= 1; ++dj)
           for (int dk = -1; dk <= 1; ++dk) {
-            const int64_t fi = 2 * I + di, fj = 2 * J + dj, fk = 2 * K + dk;
-            if (is_bnd(fi, fj, fk, f.gx, f.gy, f.gz)) continue;
+            const int64_t fi = f.wrapx(2 * I + di), fj = 2 * J + dj, fk = 2 * K + dk;
+            if (f.bnd(fi, fj, fk)) continue;
             const double wf = (di ? 0.5 : 1.0) * (dj ? 0.5 : 1.0) * (dk ? 0.5 : 1.0);
             const int64_t frow = fi * fsi + fj * fsj + fk;
             auto visit = [&](int64_t fcol, double a) {
               const int64_t gi = fcol / fsi, gj = (fcol / fsj) % f.gy, gk = fcol % fsj;
-              if (is_bnd(gi, gj, gk, f.gx, f.gy, f.gz)) return;
+              if (f.bnd(gi, gj, gk)) return;
               // coarse nodes interpolating fine node (gi, gj, gk)
-              const int64_t ci0 = gi / 2, ci1 = (gi + 1) / 2, cj0 = gj / 2, cj1 = (gj + 1) / 2, ck0 = gk / 2,
-                            ck1 = (gk + 1) / 2;
+              const int64_t ci0 = gi / 2, ci1 = c.wrapx((gi + 1) / 2), cj0 = gj / 2, cj1 = (gj + 1) / 2,
+                            ck0 = gk / 2, ck1 = (gk + 1) / 2;
               const int ni = gi % 2 ? 2 : 1, nj = gj % 2 ? 2 : 1, nk = gk % 2 ? 2 : 1;
               const double wi = gi % 2 ? 0.5 : 1.0, wj = gj % 2 ? 0.5 : 1.0, wk = gk % 2 ? 0.5 : 1.0;
               for (int a1 = 0; a1 < ni; ++a1)
                 for (int a2 = 0; a2 < nj; ++a2)
                   for (int a3 = 0; a3 < nk; ++a3) {
                     const int64_t CI = a1 ? ci1 : ci0, CJ = a2 ? cj1 : cj0, CK = a3 ? ck1 : ck0;
-                    if (is_bnd(CI, CJ, CK, c.gx, c.gy, c.gz)) continue;
-                    const int d = 9 * (int)(CI - I + 1) + 3 * (int)(CJ - J + 1) + (int)(CK - K + 1);
+                    if (c.bnd(CI, CJ, CK)) continue;
+                    int64_t dI = CI - I;
+                    if (c.px) {
+                      if (dI > 1) dI -= c.gx;
+                      if (dI < -1) dI += c.gx;
+                    }
+                    const int d = 9 * (int)(dI + 1) + 3 * (int)(CJ - J + 1) + (int)(CK - K + 1);
                     acc[d] += wf * a * (wi * wj * wk);
                   }
             };
@@ -111,8 +127,8 @@ bool host_mg_build(const HostMesh &m, const std::vector<int32_t> &rp, const std:
               for (int d = 0; d < 27; ++d) {
                 const double a = f.dia[d * nf + frow];
                 if (a == 0.0) continue;
-                const int64_t off = (d / 9 - 1) * fsi + ((d / 3) % 3 - 1) * fsj + (d % 3 - 1);
-                visit(frow + off, a);
+                const int64_t gi = f.wrapx(fi + d / 9 - 1), gj = fj + (d / 3) % 3 - 1, gk = fk + d % 3 - 1;
+                visit(gi * fsi + gj * fsj + gk, a);
               }
             }
           }
@@ -120,7 +136,7 @@ bool host_mg_build(const HostMesh &m, const std::vector<int32_t> &rp, const std:
     }
     ops.push_back(std::move(c));
   }
-  if (ops.size() < 2 || interior(ops.back()) > kDenseMax) {
+  if (ops.size() < 2 || ops.back().interior() > kDenseMax) {
     why = "grid cannot be coarsened to a small enough level";
     return false;
   }
@@ -132,12 +148,13 @@ bool host_mg_build(const HostMesh &m, const std::vector<int32_t> &rp, const std:
     L.gx = o.gx;
     L.gy = o.gy;
     L.gz = o.gz;
+    L.px = o.px;
     const int64_t n = o.n();
     L.dinv.assign(n, 1.0f);
     L.bnd.assign(n, 1);
     for (int64_t r = 0; r < n; ++r) {
       const int64_t i = r / ((int64_t)o.gy * o.gz), j = (r / o.gz) % o.gy, k = r % o.gz;
-      L.bnd[r] = is_bnd(i, j, k, o.gx, o.gy, o.gz) ? 1 : 0;
+      L.bnd[r] = o.bnd(i, j, k) ? 1 : 0;
     }
     if (l == 0) {
       for (int64_t r = 0; r < n; ++r)
@@ -161,9 +178,12 @@ bool host_mg_build(const HostMesh &m, const std::vector<int32_t> &rp, const std:
   const int64_t sj = o.gz, si = (int64_t)o.gy * o.gz;
   for (int a = 0; a < mm; ++a) {
     const int64_t r = H.dense_idx[a];
+    const int64_t ri = r / si, rj = (r / sj) % o.gy, rk = r % sj;
     for (int d = 0; d < 27; ++d) {
-      const int64_t c = r + (d / 9 - 1) * si + ((d / 3) % 3 - 1) * sj + (d % 3 - 1);
-      if (c < 0 || c >= n || pos[c] < 0) continue;
+      const int64_t ci = o.wrapx(ri + d / 9 - 1), cj = rj + (d / 3) % 3 - 1, ck = rk + d % 3 - 1;
+      if (ci < 0 || ci >= o.gx || cj < 0 || cj >= o.gy || ck < 0 || ck >= o.gz) continue;
+      const int64_t c = ci * si + cj * sj + ck;
+      if (pos[c] < 0) continue;
       M[(size_t)a * mm + pos[c]] += o.dia[d * n + r];
     }
     Inv[(size_t)a * mm + a] = 1.0;

@@ -113,6 +113,19 @@ __device__ __forceinline__ double block_sum(double v, double *smem32) {
   return s;
 }
 
+// neighbour row of row i along a stencil offset; on a periodic mesh the rows
+// are the x < hi planes and x wraps around, i.e. the index is taken modulo nwrap
+__device__ __forceinline__ int64_t dia_nb(int64_t i, int off, int64_t nwrap) {
+  int64_t j = i + off;
+  if (nwrap) {
+    if (j < 0)
+      j += nwrap;
+    else if (j >= nwrap)
+      j -= nwrap;
+  }
+  return j;
+}
+
 // sum of partials[0..nb): every thread loads at most one partial (one L2
 // round trip), then a fixed block reduction; all blocks compute the same
 // value bit for bit.

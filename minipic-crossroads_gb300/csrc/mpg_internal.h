@@ -45,7 +45,8 @@ void host_fill_ratio(const HostMesh &m, std::vector<float> &ratio);
 // hold Galerkin 27-point stencils [d][n], d = 9 (di+1) + 3 (dj+1) + (dk+1);
 // the coarsest level is solved with a dense inverse over its interior nodes.
 struct MgHostLevel {
-  int gx = 0, gy = 0, gz = 0;   // nodes per axis (x slowest)
+  int gx = 0, gy = 0, gz = 0;   // nodes per axis (x slowest); x-planes on a periodic level
+  bool px = false;              // periodic in x (indices wrap, no x walls)
   std::vector<float> val;       // 27 * n, levels >= 1
   std::vector<float> dinv;      // n: 1 / diagonal (1 on Dirichlet rows)
   std::vector<uint8_t> bnd;     // n

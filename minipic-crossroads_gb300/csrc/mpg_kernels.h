@@ -155,6 +155,7 @@ struct CgWork {
 struct MgLevelDev {
   int64_t n = 0;
   int si = 0, sj = 0, gx = 0, gy = 0, gz = 0;  // strides and nodes per axis (x slowest)
+  int px = 0;                                  // periodic in x: gx planes, x indices wrap
   const float *val = nullptr;                  // 27 * n (levels >= 1)
   const float *dinv = nullptr;                 // n
   const uint8_t *bnd = nullptr;                // n

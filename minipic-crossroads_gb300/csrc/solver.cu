@@ -46,18 +46,6 @@ namespace {
 
 constexpr int kSlots = 4;  // partial sums per phase
 
-// neighbour row of row i along a stencil offset; on a periodic mesh the rows
-// are the x < hi planes and x wraps around, i.e. the index is taken modulo nwrap
-__device__ __forceinline__ int64_t dia_nb(int64_t i, int off, int64_t nwrap) {
-  int64_t j = i + off;
-  if (nwrap) {
-    if (j < 0)
-      j += nwrap;
-    else if (j >= nwrap)
-      j -= nwrap;
-  }
-  return j;
-}
 
 
 // ---------------------------------------------------------------------------

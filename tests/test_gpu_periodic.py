@@ -70,6 +70,65 @@ def test_periodic_solves_match_oracle(mpg, orc, solver):
     assert (x[g] == x[m.node_pairs[g]]).all()
 
 
+@pytest.mark.parametrize("jit", [0.2, 0.0])
+def test_periodic_mg_solve_matches_oracle(mpg, orc, jit):
+    # multigrid-preconditioned mixed solve on a 16^3 mesh periodic in x
+    # (x coarsens plane by plane with wrap-around): the oracle's solution to
+    # 1e-8, the ghost plane equal to its pair, far fewer iterations than the
+    # plain inner CG, and bit-identical repeats
+    n = 16
+    m = orc.Mesh(n, split=6, lo=0.0, hi=1.0, mapping=4 if jit else 0, jitter=jit, seed=5, periodic=1)
+    rng = np.random.default_rng(13)
+    b = rng.standard_normal(m.N)
+    b[m.boundary == 1] = 0
+    b[m.node_pairs >= 0] = 0
+
+    def solve(kind):
+        ctx = mpg.Ctx(0)
+        ctx.mesh(n, split=6, lo=0.0, hi=1.0, mapping=4 if jit else 0, jitter=jit, seed=5, periodic=1)
+        ctx.configure(precision=mpg.MIXED, solver=kind, tol=1e-11, max_iter=3000, warm_start=0)
+        ctx.set_field(mpg.FIELD_RHS, b)
+        it, _ = ctx.solve()
+        return ctx.get_field(mpg.FIELD_PHI), it
+
+    x, it_mg = solve(mpg.SOLVER_CG_MG)
+    x2, it2 = solve(mpg.SOLVER_CG_MG)
+    assert it2 == it_mg and (x2.view(np.uint64) == x.view(np.uint64)).all()
+    m.assemble(1)
+    ox, _, _ = orc.cg(m, b, tol=1e-13, max_iter=3000)
+    assert np.abs(x - ox).max() <= 1e-8 * np.abs(ox).max()
+    g = m.node_pairs >= 0
+    assert (x[g] == x[m.node_pairs[g]]).all()
+    _, it_cg = solve(mpg.SOLVER_CG)
+    assert 2 * it_mg < it_cg, (it_mg, it_cg)
+
+
+def test_periodic_mg_steps_track_plain(mpg):
+    # the two counter-streaming beams of test_periodic_mixed_tracks_plain on a
+    # 16^3 mesh, mixed form with the multigrid-preconditioned solver
+    def make(prec, kind):
+        ctx = mpg.Ctx(0)
+        ctx.mesh(16, split=mpg.SPLIT_KUHN6, mapping=mpg.MAP_JITTER, jitter=0.2, seed=3, periodic=1)
+        ctx.configure(precision=prec, deposit=mpg.DEPOSIT_LINEAR, solver=kind, tol=1e-10, warm_start=2,
+                      kill_on_wall=1, rho_background=1.0)
+        n = 60000
+        ctx.reserve(n)
+        ctx.fill_uniform(n // 2, 1, 0, 1.0 / n, drift=(0.3, 0.0, 0.0), vth=0.02)
+        ctx.fill_uniform(n // 2, 2, 0, 1.0 / n, drift=(-0.3, 0.0, 0.0), vth=0.02)
+        return ctx
+    mixed, plain = make(mpg.MIXED, mpg.SOLVER_CG_MG), make(mpg.PLAIN, mpg.SOLVER_CG)
+    errs = []
+    for s in range(5):
+        sm = mixed.step(0.02, 1)
+        sp = plain.step(0.02, 1)
+        pm = mixed.get_field(mpg.FIELD_PHI)
+        pp = plain.get_field(mpg.FIELD_PHI)
+        errs.append(np.abs(pm - pp).max() / np.abs(pp).max())
+        assert abs(sm.n_alive - sp.n_alive) <= 3
+        assert sm.solver_iters < sp.solver_iters
+    assert max(errs) <= 1e-6, errs
+
+
 @pytest.mark.parametrize("mesh", [(4, 5, -1.0, 1.0, 0, 0.0), (6, 6, 0.0, 1.0, 4, 0.2)])
 @pytest.mark.parametrize("kill", [1, 0])
 def test_periodic_push_walk_resynced_bit_exact(mpg, orc, mesh, kill):
