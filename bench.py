@@ -92,7 +92,7 @@ def total_particles(w):
 # extrapolation from the last two solutions, 1 = the previous solution
 WARM_START = 2
 # inner solver of the mixed form: "cg" plain FP32 CG, "mg" CG preconditioned
-# by the geometric multigrid V-cycle (falls back to "cg" on periodic meshes)
+# by the geometric multigrid V-cycle (falls back to "cg" on odd cell counts)
 MIXED_SOLVER = "mg"
 
 
