@@ -602,17 +602,8 @@ int upload_mesh(mpg_ctx *c) {
   CK(cudaMemcpyAsync(d.mrec, rec.data(), sizeof(float) * 12 * h.T, cudaMemcpyHostToDevice, s));
   host_fill_ratio(h, ratio);
   CK(cudaMemcpyAsync(d.fill_ratio, ratio.data(), sizeof(float) * h.T, cudaMemcpyHostToDevice, s));
-  // charge slots grouped by node: node i owns [off[i], off[i+1]), one slot per
-  // (tet, corner) that uses it, in tet order; c2n[t] = the slots of t's corners
-  std::vector<int32_t> off(h.N + 1, 0), c2n(4 * h.T);
-  for (int64_t t = 0; t < h.T; ++t)
-    for (int k = 0; k < 4; ++k) ++off[h.tets[4 * t + k] + 1];
-  for (int64_t i = 0; i < h.N; ++i) off[i + 1] += off[i];
-  {
-    std::vector<int32_t> fill(off.begin(), off.end() - 1);
-    for (int64_t t = 0; t < h.T; ++t)
-      for (int k = 0; k < 4; ++k) c2n[4 * t + k] = fill[h.tets[4 * t + k]]++;
-  }
+  std::vector<int32_t> off, c2n;
+  host_charge_slots(h, off, c2n);
   TRY(dalloc(c, &d.n2c_off, h.N + 1));
   TRY(dalloc(c, &d.c2n, h.T));
   CK(cudaMemcpyAsync(d.n2c_off, off.data(), sizeof(int32_t) * (h.N + 1), cudaMemcpyHostToDevice, s));

@@ -50,7 +50,9 @@ struct SlotDev {
   const int4 *tets;
   const uint8_t *bnd;
   const float *fill_ratio;
-  unsigned long long *acc;
+  unsigned long long *acc;   // fixed-point charge slots, one per (tet, corner), grouped by node (4T)
+  const int32_t *n2c_off;    // N+1: node i's slots are acc[n2c_off[i] .. n2c_off[i+1])
+  const int4 *c2n;           // T: the slots of tet t's four corners
   double *rhs, *phi, *bg, *r64;
   float *r[2], *p[2], *q[2], *z;
   double *partials;  // 8 * kMaxParts slots (outer phases); inner phases: one 32-byte record per part
@@ -63,7 +65,7 @@ struct SlotDev {
   double quantum;
   int Q;
   float hk, dt;
-  double tol2, inner_tol2;
+  double tol2, inner_tol2, safety2;  // safety2: inner stop at safety2 * tol2 |b|^2 / |r64|^2 as well
   int max_iter, max_cross;
   int active;    // stepped
   int resident;  // particles kept
@@ -95,8 +97,8 @@ __global__ void k_batch_convert(const SlotDev *__restrict__ slots, const int2 *_
   } else if (h == 1) {
     S.phi_prev[i] = S.phi[i];
   }
-  const long long a = (long long)S.acc[i];
-  S.acc[i] = 0ull;
+  long long a = 0;
+  for (int32_t q = S.n2c_off[i]; q < S.n2c_off[i + 1]; ++q) a += (long long)S.acc[q];
   double r = -((double)a * S.quantum);
   if (S.bg) r += S.bg[i];
   if (S.bnd[i]) r = 0.0;
@@ -118,6 +120,10 @@ __global__ void k_batch_efield(const SlotDev *__restrict__ slots, const int2 *__
   r2.z = __fmaf_rn(d3, r1.w, __fmaf_rn(d2, r1.x, d1 * r0.y));
   r2.w = __fmaf_rn(d3, r2.x, __fmaf_rn(d2, r1.y, d1 * r0.z));
   rec[3 * t + 2] = r2;
+  // the charge slots were read by k_batch_convert; zero them for the move
+  ulonglong2 *a2 = reinterpret_cast<ulonglong2 *>(S.acc + 4 * t);
+  a2[0] = make_ulonglong2(0ull, 0ull);
+  a2[1] = make_ulonglong2(0ull, 0ull);
 }
 
 // warp-aggregated fixed-point deposit keyed by the full cellsp word (runs
@@ -146,11 +152,11 @@ __device__ __forceinline__ void batch_deposit_warp(const SlotDev *__restrict__ s
     c3 = __reduce_add_sync(FULL, c3);
     if (lane == 0 && valid) {
       const SlotDev &S = slots[key >> 24];
-      const int4 nd = S.tets[key & 0xFFFFFFu];
-      atomicAdd(S.acc + nd.x, (unsigned long long)(long long)c0);
-      atomicAdd(S.acc + nd.y, (unsigned long long)(long long)c1);
-      atomicAdd(S.acc + nd.z, (unsigned long long)(long long)c2);
-      atomicAdd(S.acc + nd.w, (unsigned long long)(long long)c3);
+      const int4 q = S.c2n[key & 0xFFFFFFu];
+      atomicAdd(S.acc + q.x, (unsigned long long)(long long)c0);
+      atomicAdd(S.acc + q.y, (unsigned long long)(long long)c1);
+      atomicAdd(S.acc + q.z, (unsigned long long)(long long)c2);
+      atomicAdd(S.acc + q.w, (unsigned long long)(long long)c3);
     }
     return;
   }
@@ -173,11 +179,11 @@ __device__ __forceinline__ void batch_deposit_warp(const SlotDev *__restrict__ s
   const bool tail = lane == 31 || sn != seg;
   if (tail && valid) {
     const SlotDev &S = slots[key >> 24];
-    const int4 nd = S.tets[key & 0xFFFFFFu];
-    atomicAdd(S.acc + nd.x, (unsigned long long)(long long)c0);
-    atomicAdd(S.acc + nd.y, (unsigned long long)(long long)c1);
-    atomicAdd(S.acc + nd.z, (unsigned long long)(long long)c2);
-    atomicAdd(S.acc + nd.w, (unsigned long long)(long long)c3);
+    const int4 q = S.c2n[key & 0xFFFFFFu];
+    atomicAdd(S.acc + q.x, (unsigned long long)(long long)c0);
+    atomicAdd(S.acc + q.y, (unsigned long long)(long long)c1);
+    atomicAdd(S.acc + q.z, (unsigned long long)(long long)c2);
+    atomicAdd(S.acc + q.w, (unsigned long long)(long long)c3);
   }
 }
 
@@ -524,7 +530,7 @@ __device__ void solve_run(const SlotDev &S, SlotStat *st, const int part, const 
     ff pq = tot[0], rq = tot[1], qq = tot[2], rho = rin0;
     ++phase;
     int cur = 0;
-    const float stop = (float)S.inner_tol2 * rin0.hi;
+    const float stop = (float)fmax(S.inner_tol2, S.safety2 * S.tol2 * rho0 / rho64) * rin0.hi;
     for (;;) {
       if (rho.hi <= stop || total_inner >= S.max_iter || !(pq.hi > 0.f)) break;
       const float af = rho.hi / pq.hi;
@@ -747,7 +753,10 @@ void free_run(Run &r) {
 int64_t run_bytes_estimate(const mpg_run_desc &d) {
   const int64_t n = d.n_side;
   const int64_t T = 6 * n * n * n, N = (n + 1) * (n + 1) * (n + 1);
-  return T * (48 + 16 + 16 + 4) + N * (1 + 8 + 8 * 4 + 4 * 7) + 8 * kMaxParts * 8 + d.n_particles * 56;
+  // per tet: walk record, neighbours, node ids, fill ratio, 4 charge slots, slot
+  // indices; per node: flag, slot offset, rhs, phi, background, r64, previous
+  // phi, 7 FP32 solver vectors
+  return T * (48 + 16 + 16 + 4 + 32 + 16) + N * (1 + 4 + 8 * 5 + 4 * 7) + 8 * kMaxParts * 8 + d.n_particles * 56;
 }
 
 int upload_slots(mpg_batch *b) {
@@ -1105,6 +1114,8 @@ int mpg_batch_admit(mpg_batch *b, const mpg_run_desc *d, int *slot) {
   v.N = hm.N;
   v.tol2 = d->tol * d->tol;
   v.inner_tol2 = 1e-10;
+  v.safety2 = 0.25;  // the reduction the outer test needs, halved (as the single-run solvers)
+  if (const char *e = getenv("MPG_CG_INNER_SAFETY")) v.safety2 = atof(e) * atof(e);
   v.max_iter = d->max_iter;
   v.max_cross = 1000;
   v.dt = (float)d->dt;
@@ -1128,7 +1139,11 @@ int mpg_batch_admit(mpg_batch *b, const mpg_run_desc *d, int *slot) {
   BTRY(balloc(b, &r, &tets, hm.T));
   BTRY(balloc(b, &r, &bnd, hm.N));
   BTRY(balloc(b, &r, &ratio, hm.T));
-  BTRY(balloc(b, &r, &acc, hm.N));
+  BTRY(balloc(b, &r, &acc, 4 * hm.T));
+  int32_t *n2c_off;
+  int4 *c2n;
+  BTRY(balloc(b, &r, &n2c_off, hm.N + 1));
+  BTRY(balloc(b, &r, &c2n, hm.T));
   BTRY(balloc(b, &r, &rhs, hm.N));
   BTRY(balloc(b, &r, &phi, hm.N));
   BTRY(balloc(b, &r, &bg, hm.N));
@@ -1152,7 +1167,11 @@ int mpg_batch_admit(mpg_batch *b, const mpg_run_desc *d, int *slot) {
   BCK(cudaMemcpyAsync(bnd, hm.bnd.data(), hm.N, cudaMemcpyHostToDevice, st));
   BCK(cudaMemcpyAsync(ratio, ratio_h.data(), sizeof(float) * hm.T, cudaMemcpyHostToDevice, st));
   BCK(cudaMemcpyAsync(bg, bgh.data(), sizeof(double) * hm.N, cudaMemcpyHostToDevice, st));
-  BCK(cudaMemsetAsync(acc, 0, sizeof(unsigned long long) * hm.N, st));
+  BCK(cudaMemsetAsync(acc, 0, sizeof(unsigned long long) * 4 * hm.T, st));
+  std::vector<int32_t> offh, c2nh;
+  host_charge_slots(hm, offh, c2nh);
+  BCK(cudaMemcpyAsync(n2c_off, offh.data(), sizeof(int32_t) * (hm.N + 1), cudaMemcpyHostToDevice, st));
+  BCK(cudaMemcpyAsync(c2n, c2nh.data(), sizeof(int32_t) * 4 * hm.T, cudaMemcpyHostToDevice, st));
   BCK(cudaMemsetAsync(phi, 0, sizeof(double) * hm.N, st));
   v.rec = rec;
   v.nbr = nbr;
@@ -1160,6 +1179,8 @@ int mpg_batch_admit(mpg_batch *b, const mpg_run_desc *d, int *slot) {
   v.bnd = bnd;
   v.fill_ratio = ratio;
   v.acc = acc;
+  v.n2c_off = n2c_off;
+  v.c2n = c2n;
   v.rhs = rhs;
   v.phi = phi;
   v.bg = bg;

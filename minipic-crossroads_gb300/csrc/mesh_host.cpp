@@ -463,3 +463,14 @@ void host_fill_ratio(const HostMesh &m, std::vector<float> &ratio) {
   ratio.resize(m.T);
   for (int64_t t = 0; t < m.T; ++t) ratio[t] = (float)(m.detj[t] / dmax);
 }
+
+void host_charge_slots(const HostMesh &m, std::vector<int32_t> &off, std::vector<int32_t> &c2n) {
+  off.assign(m.N + 1, 0);
+  c2n.resize(4 * m.T);
+  for (int64_t t = 0; t < m.T; ++t)
+    for (int k = 0; k < 4; ++k) ++off[m.tets[4 * t + k] + 1];
+  for (int64_t i = 0; i < m.N; ++i) off[i + 1] += off[i];
+  std::vector<int32_t> fill(off.begin(), off.end() - 1);
+  for (int64_t t = 0; t < m.T; ++t)
+    for (int k = 0; k < 4; ++k) c2n[4 * t + k] = fill[m.tets[4 * t + k]]++;
+}

@@ -39,6 +39,10 @@ void host_csr_assemble(const HostMesh &m, int mode, std::vector<int32_t> &rowptr
 void host_background(const HostMesh &m, double rho_bg, std::vector<double> &bg);
 // acceptance ratio vol/vol_max per tet for the volume-uniform fill
 void host_fill_ratio(const HostMesh &m, std::vector<float> &ratio);
+// fixed-point charge slots grouped by node: node i owns [off[i], off[i+1]),
+// one slot per (tet, corner) that uses it, in tet order; c2n[4 t + k] is the
+// slot of tet t's corner k
+void host_charge_slots(const HostMesh &m, std::vector<int32_t> &off, std::vector<int32_t> &c2n);
 
 // Geometric multigrid hierarchy of the structured node grid (mg_host.cpp):
 // level 0 is the fine grid (its operator is the solver's own), levels >= 1
