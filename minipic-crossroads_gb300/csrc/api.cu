@@ -323,7 +323,7 @@ int ensure_cg_work(mpg_ctx *c, int64_t n) {
   TRY(dalloc(c, &c->cg.p0, n));
   TRY(dalloc(c, &c->cg.p1, n));
   TRY(dalloc(c, &c->cg.q, n));
-  TRY(dalloc(c, &c->cg.v4, 3 * n));  // 8n floats for the mixed CG, 9n for the multigrid PCG
+  TRY(dalloc(c, &c->cg.v4, 3 * n));  // 8n floats for the mixed CG, 10n for the multigrid PCG
   if (c->cg.max_blocks < 1) return fail(c, MPG_ERR_CUDA, "solver kernels cannot be resident (occupancy 0)");
   TRY(dalloc(c, &c->cg.partials, 8 * (int64_t)std::max(c->cg.max_blocks, c->mg_max_blocks)));
   c->cg_n = n;
@@ -699,6 +699,7 @@ int upload_mg(mpg_ctx *c, const MgHostHierarchy &H) {
   m.dense_inv = inv;
   if (const char *e = getenv("MPG_MG_OMEGA")) m.omega = (float)atof(e);
   if (const char *e = getenv("MPG_MG_RELIABLE")) m.reliable = atoi(e);
+  if (const char *e = getenv("MPG_MG_NU0")) m.nu0 = atoi(e) == 2 ? 2 : 1;
   int64_t fuse_rows = 1 << 20;
   if (const char *e = getenv("MPG_MG_FUSE_UPDATE_ROWS")) fuse_rows = atoll(e);
   m.fuse_update = m.lev[0].n <= fuse_rows ? 1 : 0;

@@ -175,12 +175,19 @@ __device__ __forceinline__ float dinv_at(const CgMgArgs &a, int l, const float *
 }
 
 template <int ND, bool CST, typename R>
-__device__ __forceinline__ void presmooth_residual(const CgMgArgs &a, int l, int64_t lo, int64_t hi, R rv) {
+__device__ __forceinline__ void presmooth_residual(const CgMgArgs &a, int l, int64_t lo, int64_t hi, R rv,
+                                                   float *__restrict__ out) {
   const MgLevelDev &L = a.mg.lev[l];
   const float om = a.mg.omega;
   const float *__restrict__ dinv = L.dinv;
   auto e0 = [&](int64_t j) { return om * dinv_at<CST>(a, l, dinv, j) * rv(j); };
-  for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) L.t[i] = rv(i) - level_apply<ND, CST>(a, l, e0, i);
+  for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) out[i] = rv(i) - level_apply<ND, CST>(a, l, e0, i);
+}
+
+// where level 0's first pre-smoothing residual goes: t (one sweep), or t2
+// when level 0 smooths twice (the second sweep then writes t)
+__device__ __forceinline__ float *first_residual(const CgMgArgs &a) {
+  return a.mg.nu0 == 2 ? a.mg.lev[0].t2 : a.mg.lev[0].t;
 }
 
 // restriction of level l's t onto the coarse rows [clo, chi) of level l + 1
@@ -195,7 +202,7 @@ template <int ND, bool CST, typename Sync>
 __device__ __forceinline__ bool level_down(const CgMgArgs &a, int l, int64_t lo, int64_t hi, int64_t clo, int64_t chi,
                                            Sync sync) {
   const float *__restrict__ r = a.mg.lev[l].r;
-  presmooth_residual<ND, CST>(a, l, lo, hi, [&](int64_t j) { return r[j]; });
+  presmooth_residual<ND, CST>(a, l, lo, hi, [&](int64_t j) { return r[j]; }, a.mg.lev[l].t);
   if (!sync()) return false;
   restrict_rows(a, l, clo, chi);
   return sync();
@@ -219,6 +226,35 @@ __device__ __forceinline__ bool level_up(const CgMgArgs &a, int l, int64_t lo, i
   auto ld = [&](int64_t j) { return ev[j]; };
   for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x)
     L.t[i] = ev[i] + om * dinv_at<CST>(a, l, L.dinv, i) * (r[i] - level_apply<ND, CST>(a, l, ld, i));
+  return sync();
+}
+
+// level 0 with two Jacobi sweeps on each side (V(2,2) there): the
+// pre-smoothed error was e2 = omega D^-1 (r + t1) with t1 = r - A omega D^-1 r
+// (in t2); e3 = e2 + P c, then two post-smoothing sweeps; the result is t
+template <int ND, bool CST, typename Sync>
+__device__ __forceinline__ bool level0_up_twice(const CgMgArgs &a, int64_t lo, int64_t hi, const float *r,
+                                                const float *c, Sync sync) {
+  const MgLevelDev &L = a.mg.lev[0];
+  const MgLevelDev &C = a.mg.lev[1];
+  const float om = a.mg.omega;
+  for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+    float e = om * dinv_at<CST>(a, 0, L.dinv, i) * (r[i] + L.t2[i]);
+    if (!L.bnd[i]) e += prolong_at(L, C, c, i);
+    L.e[i] = e;
+  }
+  if (!sync()) return false;
+  {
+    const float *__restrict__ ev = L.e;
+    auto ld = [&](int64_t j) { return ev[j]; };
+    for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x)
+      L.t2[i] = ev[i] + om * dinv_at<CST>(a, 0, L.dinv, i) * (r[i] - level_apply<ND, CST>(a, 0, ld, i));
+  }
+  if (!sync()) return false;
+  const float *__restrict__ ev = L.t2;
+  auto ld = [&](int64_t j) { return ev[j]; };
+  for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x)
+    L.t[i] = ev[i] + om * dinv_at<CST>(a, 0, L.dinv, i) * (r[i] - level_apply<ND, CST>(a, 0, ld, i));
   return sync();
 }
 
@@ -254,6 +290,14 @@ __device__ bool vcycle_rest(const CgMgArgs &a, const float *rf, MgSync &bar) {
   };
   int64_t clo, chi;
   if (!gsync()) return false;
+  if (a.mg.nu0 == 2) {
+    // second pre-smoothing sweep on level 0: t = t1 - A omega D^-1 t1
+    int64_t lo, hi;
+    grid_rows(a.mg.lev[0].n, lo, hi);
+    const float *__restrict__ t1 = a.mg.lev[0].t2;
+    presmooth_residual<ND, CST>(a, 0, lo, hi, [&](int64_t j) { return t1[j]; }, a.mg.lev[0].t);
+    if (!gsync()) return false;
+  }
   grid_rows(a.mg.lev[1].n, clo, chi);
   restrict_rows(a, 0, clo, chi);
   if (!gsync()) return false;
@@ -280,7 +324,11 @@ __device__ bool vcycle_rest(const CgMgArgs &a, const float *rf, MgSync &bar) {
   for (int l = ng - 1; l >= 0; --l) {
     int64_t lo, hi;
     grid_rows(a.mg.lev[l].n, lo, hi);
-    if (!level_up<ND, CST>(a, l, lo, hi, l == 0 ? rf : a.mg.lev[l].r, a.mg.lev[l + 1].t, gsync)) return false;
+    if (l == 0 && a.mg.nu0 == 2) {
+      if (!level0_up_twice<ND, CST>(a, lo, hi, rf, a.mg.lev[1].t, gsync)) return false;
+    } else if (!level_up<ND, CST>(a, l, lo, hi, l == 0 ? rf : a.mg.lev[l].r, a.mg.lev[l + 1].t, gsync)) {
+      return false;
+    }
   }
   return true;
 }
@@ -434,7 +482,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mg(CgMgArgs a) {
     if (!bar()) return;
     {
       const float *__restrict__ r0 = a.r[cur];
-      presmooth_residual<ND, CST>(a, 0, lo, hi, [&](int64_t j) { return r0[j]; });
+      presmooth_residual<ND, CST>(a, 0, lo, hi, [&](int64_t j) { return r0[j]; }, first_residual(a));
     }
     ff gam0 = {0.f, 0.f};
     const float stop_rel = (float)fmax(a.inner_tol2, a.safety2 * a.tol2 * rho0 / rho64);
@@ -487,12 +535,13 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mg(CgMgArgs a) {
       }
       if (a.mg.fuse_update) {
         presmooth_residual<ND, CST>(
-            a, 0, lo, hi, [&](int64_t j) { return __fmaf_rn(-alpha, __fmaf_rn(beta, so[j], wv[j]), ro[j]); });
+            a, 0, lo, hi, [&](int64_t j) { return __fmaf_rn(-alpha, __fmaf_rn(beta, so[j], wv[j]), ro[j]); },
+            first_residual(a));
       } else {
         // large levels: one barrier more, but the pre-smoothing then reads
         // one vector per neighbour instead of three
         if (!bar()) return;
-        presmooth_residual<ND, CST>(a, 0, lo, hi, [&](int64_t j) { return rn[j]; });
+        presmooth_residual<ND, CST>(a, 0, lo, hi, [&](int64_t j) { return rn[j]; }, first_residual(a));
       }
       cur = nx;
       gam_prev = G;
@@ -545,7 +594,7 @@ int run_cg_mg(cudaStream_t s, const DiaMatrix &A, const MgDev &mg, const double 
   a.b = b;
   a.x = x;
   a.r64 = w.r;
-  // fine-level PCG vectors over the first 9n floats of the work buffer (12n)
+  // fine-level PCG vectors over the first 10n floats of the work buffer (12n)
   float *f = reinterpret_cast<float *>(w.v4);
   const int64_t n = A.n;
   a.w = f + 0 * n;
@@ -558,6 +607,7 @@ int run_cg_mg(cudaStream_t s, const DiaMatrix &A, const MgDev &mg, const double 
   a.mg.lev[0].r = nullptr;  // level 0's right-hand side is r[cur]
   a.mg.lev[0].e = f + 7 * n;
   a.mg.lev[0].t = f + 8 * n;
+  a.mg.lev[0].t2 = f + 9 * n;
   a.u = a.mg.lev[0].t;
   a.partials = w.partials;
   a.tol2 = tol * tol;

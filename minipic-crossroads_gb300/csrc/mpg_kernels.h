@@ -136,7 +136,7 @@ struct DiaMatrix {
 struct CgWork {
   double *r = nullptr, *p0 = nullptr, *p1 = nullptr, *q = nullptr;  // FP64 vectors, n each
   float4 *v4 = nullptr;  // mixed inner vectors {r, p, q, z} per node, two copies (3n allocated; the
-                         // multigrid PCG uses 9n floats of it)
+                         // multigrid PCG uses 10n floats of it)
   double *partials = nullptr;  // 8 * max_blocks
   int max_blocks = 0;
   // inner stop of the mixed solvers: the FP32 residual reduction also ends
@@ -160,6 +160,7 @@ struct MgLevelDev {
   const float *dinv = nullptr;                 // n
   const uint8_t *bnd = nullptr;                // n
   float *r = nullptr, *e = nullptr, *t = nullptr;
+  float *t2 = nullptr;  // level 0 with two smoothing sweeps: the first residual, then the second iterate
 };
 constexpr int kMgMaxLevels = 8;
 struct MgDev {
@@ -171,6 +172,7 @@ struct MgDev {
   float omega = 0.8f;
   int reliable = 1;  // keep the search direction across refinement sweeps (reliable updates)
   int fuse_update = 1;  // fuse the PCG update with the next pre-smoothing (level 0 up to ~1M rows)
+  int nu0 = 2;          // Jacobi sweeps before and after the coarse correction on level 0 (1 or 2)
   float dinv0 = 1.f;    // level 0's D^-1 on a uniform mesh (constant stencil)
 };
 // mixed CG preconditioned by one V(1,1) cycle per iteration, one cooperative
