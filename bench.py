@@ -217,14 +217,16 @@ def mg_levels(n_side, periodic=0, dense_max=1500):
 def mg_iter_bytes(n_side, N, coef, periodic=0):
     """Algorithmic bytes of one multigrid-preconditioned inner iteration.
 
-    Fine level, per row: fused update + pre-smoothing reads p, u, s, w, z, r,
-    D^-1 and writes p, s, z, r, t (44 B); restriction reads t (4 B); the two
-    ascending steps read D^-1, r, e and write e, t (28 B); w = A u reads u, r and
-    writes w (12 B); three stencil passes read the FP32 coefficients (3 coef).
+    Fine level (two Jacobi sweeps on each side), per row: fused update +
+    first pre-smoothing reads p, u, s, w, z, r, D^-1 and writes p, s, z, r, t1
+    (44 B); the second reads t1, D^-1 and writes t (12 B); restriction reads t
+    (4 B); the three ascending passes read D^-1, r, t1 / e / e2 and write e /
+    e2 / u (48 B); w = A u and the four dots read u, r, s, p and write w (20 B);
+    five stencil passes read the FP32 coefficients (5 coef).
     Coarse levels, per row: 27 FP32 coefficients in two passes plus about 80 B
     of vectors.  Coarsest level: its dense inverse (m^2 FP32)."""
     lev = mg_levels(n_side, periodic)
-    b = (44 + 4 + 28 + 12 + 3 * coef) * N
+    b = (44 + 12 + 4 + 48 + 20 + 5 * coef) * N
     for x, g, _ in lev[1:-1]:
         b += (2 * 27 * 4 + 80) * x * g * g
     x, g, m = lev[-1]
