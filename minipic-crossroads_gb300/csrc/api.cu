@@ -687,10 +687,14 @@ int upload_mg(mpg_ctx *c, const MgHostHierarchy &H) {
   int32_t *idx;
   float *inv;
   m.dense_m = (int)H.dense_idx.size();
+  float *dr;
   TRY(dalloc(c, &idx, m.dense_m));
   TRY(dalloc(c, &inv, (int64_t)m.dense_m * m.dense_m));
+  TRY(dalloc(c, &dr, m.dense_m));
   c->mg_bufs.push_back(idx);
   c->mg_bufs.push_back(inv);
+  c->mg_bufs.push_back(dr);
+  m.dense_r = dr;
   CK(cudaMemcpyAsync(idx, H.dense_idx.data(), sizeof(int32_t) * m.dense_m, cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemcpyAsync(inv, H.dense_inv.data(), sizeof(float) * H.dense_inv.size(), cudaMemcpyHostToDevice,
                      c->stream));

@@ -190,10 +190,22 @@ __device__ __forceinline__ float *first_residual(const CgMgArgs &a) {
   return a.mg.nu0 == 2 ? a.mg.lev[0].t2 : a.mg.lev[0].t;
 }
 
-// restriction of level l's t onto the coarse rows [clo, chi) of level l + 1
+// restriction of level l's t onto the coarse rows [clo, chi) of level l + 1;
+// the coarsest level keeps only its interior rows, in order (the dense
+// solve's right-hand side)
 __device__ __forceinline__ void restrict_rows(const CgMgArgs &a, int l, int64_t clo, int64_t chi) {
   const MgLevelDev &L = a.mg.lev[l], &C = a.mg.lev[l + 1];
-  for (int64_t i = clo + threadIdx.x; i < chi; i += blockDim.x) C.r[i] = restrict_at(L, C, i);
+  if (l + 1 < a.mg.nlev - 1) {
+    for (int64_t i = clo + threadIdx.x; i < chi; i += blockDim.x) C.r[i] = restrict_at(L, C, i);
+    return;
+  }
+  const int x0 = C.px ? 0 : 1, ny = C.gy - 2, nz = C.gz - 2;
+  for (int64_t i = clo + threadIdx.x; i < chi; i += blockDim.x) {
+    if (C.bnd[i]) continue;
+    unsigned I, J, K;
+    level_ijk(C, i, I, J, K);
+    a.mg.dense_r[((int64_t)(I - x0) * ny + (J - 1)) * nz + (K - 1)] = restrict_at(L, C, i);
+  }
 }
 
 // one coarse level's descending steps on rows [lo, hi) (coarse rows
@@ -258,17 +270,27 @@ __device__ __forceinline__ bool level0_up_twice(const CgMgArgs &a, int64_t lo, i
   return sync();
 }
 
-// coarsest level: t = A_c^-1 r over its interior rows, one warp per row of
-// the dense inverse across the whole grid (lanes over the row, fixed shuffle
-// tree); the Dirichlet rows of t stay zero
+// coarsest level: t = A_c^-1 r over its interior rows (r compact in
+// dense_r), one warp per row of the dense inverse across the whole grid
+// (lanes over the row, four chains, fixed shuffle tree); the Dirichlet rows
+// of t stay zero
 __device__ __forceinline__ void dense_solve(const MgDev &mg) {
   const MgLevelDev &Lc = mg.lev[mg.nlev - 1];
   const int m = mg.dense_m, lane = threadIdx.x & 31;
   const int nw = (blockDim.x >> 5) * gridDim.x;
   for (int q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); q < m; q += nw) {
     const float *__restrict__ row = mg.dense_inv + (int64_t)q * m;
-    float s = 0.f;
-    for (int k = lane; k < m; k += 32) s = __fmaf_rn(row[k], Lc.r[mg.dense_idx[k]], s);
+    const float *__restrict__ rc = mg.dense_r;
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;  // four independent chains
+    int k = lane;
+    for (; k + 96 < m; k += 128) {
+      s0 = __fmaf_rn(row[k], rc[k], s0);
+      s1 = __fmaf_rn(row[k + 32], rc[k + 32], s1);
+      s2 = __fmaf_rn(row[k + 64], rc[k + 64], s2);
+      s3 = __fmaf_rn(row[k + 96], rc[k + 96], s3);
+    }
+    for (; k < m; k += 32) s0 = __fmaf_rn(row[k], rc[k], s0);
+    float s = (s0 + s1) + (s2 + s3);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     if (lane == 0) Lc.t[mg.dense_idx[q]] = s;

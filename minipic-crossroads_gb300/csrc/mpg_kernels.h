@@ -168,6 +168,7 @@ struct MgDev {
   MgLevelDev lev[kMgMaxLevels];
   const int32_t *dense_idx = nullptr;
   const float *dense_inv = nullptr;
+  float *dense_r = nullptr;  // the coarsest level's right-hand side over its interior rows (dense_m)
   int dense_m = 0;
   float omega = 0.8f;
   int reliable = 1;  // keep the search direction across refinement sweeps (reliable updates)
