@@ -563,12 +563,18 @@ def main():
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--warm-start", type=int, default=2, choices=[0, 1, 2, 3],
                     help="CG initial guess: 0 zero, 1 previous phi, 2/3 linear/quadratic extrapolation")
+    ap.add_argument("--sort-interval", type=int, default=None,
+                    help="cell sort every K steps in the mixed form (default: the workload's, 10)")
     ap.add_argument("--mixed-solver", default="mg", choices=["cg", "mg"],
                     help="inner solver of the mixed form: plain CG or multigrid-preconditioned CG")
     args = ap.parse_args()
     global WARM_START, MIXED_SOLVER
     WARM_START = args.warm_start
     MIXED_SOLVER = args.mixed_solver
+    if args.sort_interval is not None:
+        for wl in WORKLOADS.values():
+            if wl["sort_interval"]:
+                wl["sort_interval"] = args.sort_interval
     if args.workload in ("ensemble", "serving"):
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the reference has no batched or serving mode; "
@@ -668,6 +674,7 @@ def main():
                               if precision == mpg.MIXED else "plain f64"),
                 "data": "synthetic",
                 "config": {"workload": w["name"], "n_side": w["n_side"], "tets": ctx.T, "nodes": ctx.N,
+                           "sort_interval": w["sort_interval"],
                            "particles": total_particles(w), "dt": w["dt"], "cg_tol": 1e-10,
                            "cg_initial_guess": ["zero", "previous phi", "extrapolated 2*phi[n-1]-phi[n-2]",
                                                 "extrapolated 3*phi[n-1]-3*phi[n-2]+phi[n-3]"][WARM_START],
