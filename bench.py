@@ -678,7 +678,9 @@ def main():
                            "particles": total_particles(w), "dt": w["dt"], "cg_tol": 1e-10,
                            "cg_initial_guess": ["zero", "previous phi", "extrapolated 2*phi[n-1]-phi[n-2]",
                                                 "extrapolated 3*phi[n-1]-3*phi[n-2]+phi[n-3]"][WARM_START],
-                           "cg_preconditioner": ("geometric multigrid V(1,1)" if precision == mpg.MIXED
+                           "cg_preconditioner": ("geometric multigrid V-cycle (2 Jacobi sweeps per side on "
+                                                 "the fine level, 1 on coarser levels, dense coarsest solve)"
+                                                 if precision == mpg.MIXED
                                                  and uses_mg(w) else "none"),
                            "parallelism": "replicas" if world > 1 else "single",
                            "l2": "inputs larger than L2 (particle state > 129 MB), no flush"},
