@@ -715,31 +715,39 @@ def main():
         for _ in range(2):
             ctx.step(w["dt"], 1)
         cs, b, v = ctx.mixed_download()
+        pinned = False
         try:
             import torch
-            pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
+
+            def pin(a):
+                t = torch.empty(a.nbytes, dtype=torch.uint8, pin_memory=True).numpy().view(a.dtype).reshape(a.shape)
+                np.copyto(t, a)
+                return t
             cs, b, v = pin(cs), pin(b), pin(v)
-        except Exception:
-            pass
-        try:
             out = tuple(pin(np.empty_like(a)) for a in (cs, b, v))
+            pinned = True
         except Exception:
             out = None
         ke = args.steps
-        t0 = time.perf_counter()
-        ctx.mixed_upload(cs, b, v)
-        n_e = ctx.count()
-        for _ in range(ke):
-            ctx.step(w["dt"], 1)
-        cs2, b2, v2 = ctx.mixed_download(out=out)
-        t1 = time.perf_counter()
-        eps = barrier_sum(n_e * ke) / barrier_max(t1 - t0)
+        # three end-to-end passes (upload, K steps, download); the median is reported
+        reps = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            ctx.mixed_upload(cs, b, v)
+            n_e = ctx.count()
+            for _ in range(ke):
+                ctx.step(w["dt"], 1)
+            cs2, b2, v2 = ctx.mixed_download(out=out)
+            t1 = time.perf_counter()
+            reps.append(barrier_sum(n_e * ke) / barrier_max(t1 - t0))
+        eps = sorted(reps)[1]
         if rank == 0:
             nbytes = cs.nbytes + b.nbytes + v.nbytes
             line["e2e"] = {"value": eps, "unit": UNIT, "h2d_bytes_per_step": int(nbytes / ke),
                            "d2h_bytes_per_step": int((cs2.nbytes + b2.nbytes + v2.nbytes) / ke + 136),
-                           "how": "mpg_mixed_upload from pinned host buffers, mpg_step x K with stats read back "
-                                  "each step, mpg_mixed_download into pinned host buffers; host wall clock"}
+                           "pinned_host_buffers": pinned, "passes": [round(x, 1) for x in reps],
+                           "how": "mpg_mixed_upload from host buffers, mpg_step x K with stats read back each "
+                                  "step, mpg_mixed_download into host buffers; host wall clock, median of 3 passes"}
     if rank == 0 and not args.no_ensemble and args.workload == "standard" and world == 1:
         # the ensemble part of the metric: 256 runs in the batch engine
         ens = run_ensemble(mpg, args, device=local)
