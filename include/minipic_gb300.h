@@ -250,6 +250,17 @@ int mpg_batch_run_phi(mpg_batch *b, int slot, double *phi);
 int mpg_batch_run_particles(mpg_batch *b, int slot, int64_t cap, int64_t *n, uint32_t *cell, float *b3, float *v3);
 int mpg_batch_retire(mpg_batch *b, int slot);
 
+/* Multigrid hierarchy of MPG_SOLVER_CG_MG for a mesh, built on the host
+ * only (no device; a check of the preconditioner's set-up).  *nlev = number
+ * of levels; for `level`: extent[3] = node extents (x-planes on a periodic
+ * mesh, x slowest) and, where the pointers are non-null, its 27-point FP32
+ * stencil val27[d * n + row] (levels >= 1; d = 9 (dx+1) + 3 (dy+1) + (dz+1)),
+ * D^-1 dinv[n] and Dirichlet flags bnd[n], n = extent product.  dense_max:
+ * interior unknowns allowed on the coarsest level (0: the default).
+ * MPG_ERR_ARG when the grid cannot be coarsened. */
+int mpg_mg_hierarchy(const mpg_mesh_desc *mesh, int64_t dense_max, int level, int *nlev, int *extent, float *val27,
+                     float *dinv, uint8_t *bnd);
+
 /* Allocation-free variant of mpg_cg_csr.  No counterpart in the reference.
  *
  * For callers that cannot allocate device memory at the point of the call:

@@ -32,7 +32,7 @@ EXPORTS = [
     "mpg_csr_download", "mpg_particles_reserve", "mpg_fill_ref", "mpg_fill_uniform", "mpg_particles_upload",
     "mpg_particles_download", "mpg_particles_count", "mpg_mixed_download", "mpg_mixed_upload",
     "mpg_charge_download", "mpg_weight_charge", "mpg_solve", "mpg_weight_efield", "mpg_move", "mpg_step",
-    "mpg_sort", "mpg_get_field", "mpg_set_field", "mpg_cg_csr", "mpg_cg_csr_noalloc",
+    "mpg_sort", "mpg_get_field", "mpg_set_field", "mpg_cg_csr", "mpg_cg_csr_noalloc", "mpg_mg_hierarchy",
     "mpg_batch_create", "mpg_batch_destroy", "mpg_batch_last_error", "mpg_batch_set_tuning", "mpg_batch_admit",
     "mpg_batch_step", "mpg_batch_run_info", "mpg_batch_run_phi", "mpg_batch_run_particles", "mpg_batch_retire",
 ]
@@ -141,6 +141,7 @@ def load():
         "mpg_set_field": ([P, I, P], I),
         "mpg_cg_csr": ([P, I64, P, P, P, P, P, D, I, C.POINTER(I), C.POINTER(D)], I),
         "mpg_cg_csr_noalloc": ([P, I64, P, P, P, P, P, D, I, C.POINTER(I), C.POINTER(D)], I),
+        "mpg_mg_hierarchy": ([C.POINTER(MeshDesc), I64, I, C.POINTER(I), P, P, P, P], I),
         "mpg_batch_create": ([I, I64, I, I64, C.POINTER(P)], I),
         "mpg_batch_destroy": ([P], I),
         "mpg_batch_last_error": ([P, C.c_char_p, I], I),
@@ -168,6 +169,27 @@ class MpgError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__(f"[{code}] {msg}")
         self.code = code
+
+
+def mg_hierarchy(n, split=SPLIT_KUHN6, lo=0.0, hi=1.0, mapping=MAP_NONE, jitter=0.0, seed=0, periodic=0,
+                 dense_max=0, level=0):
+    """Level `level` of the multigrid hierarchy MPG_SOLVER_CG_MG builds for a
+    mesh, computed on the host only (no GPU): dict(nlev, extent, val [27, n]
+    (levels >= 1), dinv [n], bnd [n])."""
+    L = load()
+    nx, ny, nz = (n, n, n) if np.isscalar(n) else n
+    d = MeshDesc(nx, ny, nz, split, lo, hi, mapping, jitter, seed, int(periodic))
+    nlev, ext = C.c_int(), (C.c_int * 3)()
+    rc = L.mpg_mg_hierarchy(C.byref(d), dense_max, level, C.byref(nlev), ext, None, None, None)
+    if rc != OK:
+        raise MpgError(rc, "mpg_mg_hierarchy failed")
+    m = ext[0] * ext[1] * ext[2]
+    val = np.zeros((27, m), np.float32) if level > 0 else None
+    dinv, bnd = np.zeros(m, np.float32), np.zeros(m, np.uint8)
+    rc = L.mpg_mg_hierarchy(C.byref(d), dense_max, level, C.byref(nlev), ext, ptr(val), ptr(dinv), ptr(bnd))
+    if rc != OK:
+        raise MpgError(rc, "mpg_mg_hierarchy failed")
+    return dict(nlev=nlev.value, extent=(ext[0], ext[1], ext[2]), val=val, dinv=dinv, bnd=bnd)
 
 
 class Ctx:

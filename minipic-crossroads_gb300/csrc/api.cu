@@ -851,6 +851,30 @@ int mpg_timer(mpg_ctx *c, int op, double *ms) {
   return MPG_OK;
 }
 
+int mpg_mg_hierarchy(const mpg_mesh_desc *mesh, int64_t dense_max, int level, int *nlev, int *extent, float *val27,
+                     float *dinv, uint8_t *bnd) {
+  if (!mesh || !nlev || !extent) return MPG_ERR_ARG;
+  HostMesh hm;
+  std::string err;
+  int rc = host_mesh_generate(*mesh, hm, err);
+  if (rc) return rc;
+  std::vector<int32_t> rp, col;
+  std::vector<double> val;
+  host_csr_assemble(hm, 1, rp, col, val);
+  MgHostHierarchy H;
+  if (!host_mg_build(hm, rp, col, val, H, err, dense_max)) return MPG_ERR_ARG;
+  *nlev = (int)H.lev.size();
+  if (level < 0 || level >= *nlev) return MPG_ERR_ARG;
+  const MgHostLevel &L = H.lev[level];
+  extent[0] = L.gx;
+  extent[1] = L.gy;
+  extent[2] = L.gz;
+  if (val27 && level > 0) std::copy(L.val.begin(), L.val.end(), val27);
+  if (dinv) std::copy(L.dinv.begin(), L.dinv.end(), dinv);
+  if (bnd) std::copy(L.bnd.begin(), L.bnd.end(), bnd);
+  return MPG_OK;
+}
+
 int mpg_mesh_build(mpg_ctx *c, const mpg_mesh_desc *d) {
   ENTER(c);
   if (!d) return fail(c, MPG_ERR_ARG, "null mesh descriptor");

@@ -49,7 +49,7 @@ struct LevelOp {
 }  // namespace
 
 bool host_mg_build(const HostMesh &m, const std::vector<int32_t> &rp, const std::vector<int32_t> &col,
-                   const std::vector<double> &val, MgHostHierarchy &H, std::string &why) {
+                   const std::vector<double> &val, MgHostHierarchy &H, std::string &why, int64_t dense_max) {
   H = MgHostHierarchy();
   const bool px = m.d.periodic != 0;
   std::vector<LevelOp> ops(1);
@@ -67,6 +67,7 @@ bool host_mg_build(const HostMesh &m, const std::vector<int32_t> &rp, const std:
   }
   int64_t kDenseMax = kDenseMaxDefault;
   if (const char *e = getenv("MPG_MG_DENSE_MAX")) kDenseMax = atoll(e);
+  if (dense_max > 0) kDenseMax = dense_max;
   while ((int)ops.size() < kMaxLevels && ops.back().interior() > kDenseMax) {
     const LevelOp &f = ops.back();
     // y, z: node extents 2m+1 -> m+1 (Dirichlet ends stay on the grid);

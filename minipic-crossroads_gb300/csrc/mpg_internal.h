@@ -60,9 +60,11 @@ struct MgHostHierarchy {
   std::vector<int32_t> dense_idx;  // interior rows of the coarsest level
   std::vector<float> dense_inv;    // row-major inverse over them
 };
-// from the symmetric (mode 1) CSR of a non-periodic mesh; false with a reason otherwise
+// from the symmetric (mode 1) CSR of the mesh (periodic in x or not); false
+// with a reason when the grid cannot be coarsened.  dense_max: interior
+// unknowns of the coarsest level (0: the default, or MPG_MG_DENSE_MAX)
 bool host_mg_build(const HostMesh &m, const std::vector<int32_t> &rp, const std::vector<int32_t> &col,
-                   const std::vector<double> &val, MgHostHierarchy &H, std::string &why);
+                   const std::vector<double> &val, MgHostHierarchy &H, std::string &why, int64_t dense_max = 0);
 
 // counter-based generator shared by the jitter and the fills (splitmix64 finaliser)
 static inline uint64_t mpg_mix64(uint64_t z) {
