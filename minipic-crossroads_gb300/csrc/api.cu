@@ -672,14 +672,18 @@ int upload_mg(mpg_ctx *c, const MgHostHierarchy &H) {
       TRY(dalloc(c, &r, L.n));
       TRY(dalloc(c, &e, L.n));
       TRY(dalloc(c, &t, L.n));
-      for (void *p : {(void *)val, (void *)r, (void *)e, (void *)t}) c->mg_bufs.push_back(p);
+      float *t2;
+      TRY(dalloc(c, &t2, L.n));
+      for (void *p : {(void *)val, (void *)r, (void *)e, (void *)t, (void *)t2}) c->mg_bufs.push_back(p);
       CK(cudaMemcpyAsync(val, h.val.data(), sizeof(float) * 27 * L.n, cudaMemcpyHostToDevice, c->stream));
       CK(cudaMemsetAsync(e, 0, sizeof(float) * L.n, c->stream));
       CK(cudaMemsetAsync(t, 0, sizeof(float) * L.n, c->stream));
+      CK(cudaMemsetAsync(t2, 0, sizeof(float) * L.n, c->stream));
       L.val = val;
       L.r = r;
       L.e = e;
       L.t = t;
+      L.t2 = t2;
     }
   }
   m.ngrid = 1;
@@ -704,6 +708,7 @@ int upload_mg(mpg_ctx *c, const MgHostHierarchy &H) {
   if (const char *e = getenv("MPG_MG_OMEGA")) m.omega = (float)atof(e);
   if (const char *e = getenv("MPG_MG_RELIABLE")) m.reliable = atoi(e);
   if (const char *e = getenv("MPG_MG_NU0")) m.nu0 = atoi(e) == 2 ? 2 : 1;
+  if (const char *e = getenv("MPG_MG_NU1")) m.nu1 = atoi(e) == 2 ? 2 : 1;
   int64_t fuse_rows = 1 << 20;
   if (const char *e = getenv("MPG_MG_FUSE_UPDATE_ROWS")) fuse_rows = atoll(e);
   m.fuse_update = m.lev[0].n <= fuse_rows ? 1 : 0;

@@ -245,13 +245,13 @@ __device__ __forceinline__ bool level_up(const CgMgArgs &a, int l, int64_t lo, i
 // pre-smoothed error was e2 = omega D^-1 (r + t1) with t1 = r - A omega D^-1 r
 // (in t2); e3 = e2 + P c, then two post-smoothing sweeps; the result is t
 template <int ND, bool CST, typename Sync>
-__device__ __forceinline__ bool level0_up_twice(const CgMgArgs &a, int64_t lo, int64_t hi, const float *r,
-                                                const float *c, Sync sync) {
-  const MgLevelDev &L = a.mg.lev[0];
-  const MgLevelDev &C = a.mg.lev[1];
+__device__ __forceinline__ bool level_up_twice(const CgMgArgs &a, int l, int64_t lo, int64_t hi, const float *r,
+                                               const float *c, Sync sync) {
+  const MgLevelDev &L = a.mg.lev[l];
+  const MgLevelDev &C = a.mg.lev[l + 1];
   const float om = a.mg.omega;
   for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-    float e = om * dinv_at<CST>(a, 0, L.dinv, i) * (r[i] + L.t2[i]);
+    float e = om * dinv_at<CST>(a, l, L.dinv, i) * (r[i] + L.t2[i]);
     if (!L.bnd[i]) e += prolong_at(L, C, c, i);
     L.e[i] = e;
   }
@@ -260,13 +260,28 @@ __device__ __forceinline__ bool level0_up_twice(const CgMgArgs &a, int64_t lo, i
     const float *__restrict__ ev = L.e;
     auto ld = [&](int64_t j) { return ev[j]; };
     for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x)
-      L.t2[i] = ev[i] + om * dinv_at<CST>(a, 0, L.dinv, i) * (r[i] - level_apply<ND, CST>(a, 0, ld, i));
+      L.t2[i] = ev[i] + om * dinv_at<CST>(a, l, L.dinv, i) * (r[i] - level_apply<ND, CST>(a, l, ld, i));
   }
   if (!sync()) return false;
   const float *__restrict__ ev = L.t2;
   auto ld = [&](int64_t j) { return ev[j]; };
   for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x)
-    L.t[i] = ev[i] + om * dinv_at<CST>(a, 0, L.dinv, i) * (r[i] - level_apply<ND, CST>(a, 0, ld, i));
+    L.t[i] = ev[i] + om * dinv_at<CST>(a, l, L.dinv, i) * (r[i] - level_apply<ND, CST>(a, l, ld, i));
+  return sync();
+}
+
+// a grid level l >= 1 with two pre-smoothing sweeps: t1 (in t2), then t
+template <int ND, bool CST, typename Sync>
+__device__ __forceinline__ bool level_down_twice(const CgMgArgs &a, int l, int64_t lo, int64_t hi, int64_t clo,
+                                                 int64_t chi, Sync sync) {
+  const MgLevelDev &L = a.mg.lev[l];
+  const float *__restrict__ r = L.r;
+  presmooth_residual<ND, CST>(a, l, lo, hi, [&](int64_t j) { return r[j]; }, L.t2);
+  if (!sync()) return false;
+  const float *__restrict__ t1 = L.t2;
+  presmooth_residual<ND, CST>(a, l, lo, hi, [&](int64_t j) { return t1[j]; }, L.t);
+  if (!sync()) return false;
+  restrict_rows(a, l, clo, chi);
   return sync();
 }
 
@@ -327,7 +342,11 @@ __device__ bool vcycle_rest(const CgMgArgs &a, const float *rf, MgSync &bar) {
     int64_t lo, hi;
     grid_rows(a.mg.lev[l].n, lo, hi);
     grid_rows(a.mg.lev[l + 1].n, clo, chi);
-    if (!level_down<ND, CST>(a, l, lo, hi, clo, chi, gsync)) return false;
+    if (a.mg.nu1 == 2) {
+      if (!level_down_twice<ND, CST>(a, l, lo, hi, clo, chi, gsync)) return false;
+    } else if (!level_down<ND, CST>(a, l, lo, hi, clo, chi, gsync)) {
+      return false;
+    }
   }
   const bool blk = ng < nl - 1;
   if (blk) {
@@ -346,8 +365,10 @@ __device__ bool vcycle_rest(const CgMgArgs &a, const float *rf, MgSync &bar) {
   for (int l = ng - 1; l >= 0; --l) {
     int64_t lo, hi;
     grid_rows(a.mg.lev[l].n, lo, hi);
-    if (l == 0 && a.mg.nu0 == 2) {
-      if (!level0_up_twice<ND, CST>(a, lo, hi, rf, a.mg.lev[1].t, gsync)) return false;
+    if (l > 0 && a.mg.nu1 == 2) {
+      if (!level_up_twice<ND, CST>(a, l, lo, hi, a.mg.lev[l].r, a.mg.lev[l + 1].t, gsync)) return false;
+    } else if (l == 0 && a.mg.nu0 == 2) {
+      if (!level_up_twice<ND, CST>(a, 0, lo, hi, rf, a.mg.lev[1].t, gsync)) return false;
     } else if (!level_up<ND, CST>(a, l, lo, hi, l == 0 ? rf : a.mg.lev[l].r, a.mg.lev[l + 1].t, gsync)) {
       return false;
     }

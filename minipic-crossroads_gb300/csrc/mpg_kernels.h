@@ -160,7 +160,7 @@ struct MgLevelDev {
   const float *dinv = nullptr;                 // n
   const uint8_t *bnd = nullptr;                // n
   float *r = nullptr, *e = nullptr, *t = nullptr;
-  float *t2 = nullptr;  // level 0 with two smoothing sweeps: the first residual, then the second iterate
+  float *t2 = nullptr;  // levels with two smoothing sweeps: the first residual, then the second iterate
 };
 constexpr int kMgMaxLevels = 8;
 struct MgDev {
@@ -174,6 +174,7 @@ struct MgDev {
   int reliable = 1;  // keep the search direction across refinement sweeps (reliable updates)
   int fuse_update = 1;  // fuse the PCG update with the next pre-smoothing (level 0 up to ~1M rows)
   int nu0 = 2;          // Jacobi sweeps before and after the coarse correction on level 0 (1 or 2)
+  int nu1 = 1;          // the same on the other grid-wide levels (1 or 2)
   float dinv0 = 1.f;    // level 0's D^-1 on a uniform mesh (constant stencil)
 };
 // mixed CG preconditioned by one V(1,1) cycle per iteration, one cooperative
