@@ -4,12 +4,14 @@
 // refinement (r64 = b - A64 x, stop at |r64| <= tol |b|) around an FP32 inner
 // solve of A z = r64 / |r64|.  The inner solve is preconditioned CG in the
 // single-reduction form of Chronopoulos and Gear (one grid-wide all-reduce
-// of (r, u) and (A u, u) per iteration), with u = M r one multigrid V(1,1)
-// cycle: damped Jacobi smoothing, restriction P^T, Galerkin coarse operators
-// (mg_host.cpp) and a dense solve on the coarsest level.  Levels with many
-// rows are processed by the whole grid (a grid barrier between dependent
-// steps); the small ones and the dense solve by block 0 alone (block
-// barriers), while the other blocks wait at the next grid barrier.
+// of four dots per iteration), with u = M r one multigrid V-cycle: damped
+// Jacobi smoothing (two sweeps per side on the fine level, one on the
+// others), restriction P^T, Galerkin coarse operators (mg_host.cpp) and a
+// dense solve on the coarsest level.  Levels with many rows are processed by
+// the whole grid (a grid barrier between dependent steps); small ones by
+// block 0 alone (block barriers) while the other blocks wait at the next grid
+// barrier; the dense solve by the whole grid.  The search direction survives
+// the FP64 refinement sweeps (reliable updates).
 // Not part of the reference, whose CG (CG_solve.hpp:54-114) is
 // unpreconditioned; the converged phi meets the same FP64 tolerance.
 #include <cuda_runtime.h>
@@ -71,7 +73,7 @@ struct CgMgArgs {
   double *x, *r64;
   float *r[2], *s[2];  // fine-level PCG residual and A p, double-buffered by iteration parity
   float *u, *w, *p, *z;  // u = M r is the V-cycle's output (mg.lev[0].t), w = A u
-  double *partials;              // outer phases: [2 sets][4][nb]; inner: one 32-byte record per block
+  double *partials;      // outer phases: [2 sets][4][nb]; inner: one 32-byte record per block
   double tol2, inner_tol2, safety2;
   int max_iter;
   DevStats *st;
@@ -312,9 +314,9 @@ __device__ __forceinline__ void dense_solve(const MgDev &mg) {
   }
 }
 
-// rest of u = M r after level 0's pre-smoothing residual lev[0].t has been
-// written on this block's rows; rf is level 0's right-hand side r and the
-// result u is lev[0].t.  Levels [0, ngrid) run on the whole grid, levels
+// rest of u = M r after level 0's first pre-smoothing residual has been
+// written on this block's rows (first_residual); rf is level 0's right-hand
+// side r and the result u is lev[0].t.  Levels [0, ngrid) run on the whole grid, levels
 // [ngrid, nlev - 1) on block 0 alone, the dense coarsest solve on the whole
 // grid again.
 template <int ND, bool CST>
