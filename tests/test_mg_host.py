@@ -118,3 +118,15 @@ def test_coarse_operators_are_galerkin_products(mpg, orc, n, split, mapping, jit
 def test_odd_cell_counts_are_not_coarsened(mpg):
     with pytest.raises(mpg.MpgError):
         mpg.mg_hierarchy(9, level=0)
+
+
+@pytest.mark.parametrize("n,periodic", [(32, 0), (24, 1), (16, 0)])
+def test_bench_level_model_matches_library(mpg, n, periodic):
+    # bench.py's algorithmic-bytes model of the multigrid iteration uses the
+    # same level extents the library builds
+    import bench
+    model = bench.mg_levels(n, periodic)
+    h = mpg.mg_hierarchy(n, periodic=periodic, level=len(model) - 1)
+    assert len(model) == h["nlev"]
+    x, g, _ = model[-1]
+    assert h["extent"] == (x, g, g)
