@@ -92,7 +92,7 @@ def total_particles(w):
 # extrapolation from the last two solutions, 1 = the previous solution
 WARM_START = 2
 # inner solver of the mixed form: "cg" plain FP32 CG, "mg" CG preconditioned
-# by the geometric multigrid V-cycle (falls back to "cg" on odd cell counts)
+# by the geometric multigrid V-cycle (falls back to "cg" on grids too small to coarsen)
 MIXED_SOLVER = "mg"
 
 
@@ -196,19 +196,19 @@ def uses_mg(w):
 
 
 def mg_levels(n_side, periodic=0, dense_max=1500):
-    """(x, y/z) node extents of the multigrid levels: halve while the interior
-    has more than dense_max unknowns and the counts allow it (the host
-    hierarchy's rule; a periodic x axis holds n planes and halves while even
-    and the result stays >= 4)."""
+    """(x, y/z) node extents of the multigrid levels: halve (g -> g // 2 + 1)
+    while the interior has more than dense_max unknowns (the host hierarchy's
+    rule; a periodic x axis holds n planes and halves while even and the
+    result stays >= 4)."""
     def interior(x, g):
         return (x if periodic else x - 2) * (g - 2) ** 2
     lev = [(n_side if periodic else n_side + 1, n_side + 1)]
     while len(lev) < 8 and interior(*lev[-1]) > dense_max:
         x, g = lev[-1]
-        okx = (x % 2 == 0 and x // 2 >= 4) if periodic else ((x - 1) % 2 == 0 and x >= 5)
-        if not okx or (g - 1) % 2 or g < 5:
+        okx = (x % 2 == 0 and x // 2 >= 4) if periodic else x >= 5
+        if not okx or g < 5:
             break
-        lev.append((x // 2 if periodic else (x - 1) // 2 + 1, (g - 1) // 2 + 1))
+        lev.append((x // 2 if periodic else x // 2 + 1, g // 2 + 1))
     if len(lev) < 2 or interior(*lev[-1]) > dense_max:
         return []
     return [(x, g, interior(x, g)) for x, g in lev]

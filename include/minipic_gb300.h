@@ -44,8 +44,8 @@ extern "C" {
 #define MPG_SOLVER_BICGSTAB 0     /* CG_solve.hpp:115-206 (x := 0, reference default)   */
 #define MPG_SOLVER_CG 1           /* CG_solve.hpp:54-114                                 */
 #define MPG_SOLVER_CG_MG 2        /* mixed form: CG preconditioned by a geometric        */
-                                  /* multigrid V-cycle (not in the reference; needs      */
-                                  /* even cell counts, else plain inner CG)              */
+                                  /* multigrid V-cycle (not in the reference; grids of   */
+                                  /* <= 1500 interior nodes: plain inner CG)             */
 
 #define MPG_SPLIT_REF5 5          /* mesh.cpp:195-224 five-tet alternating split         */
 #define MPG_SPLIT_KUHN6 6         /* six Kuhn tets per hex                               */

@@ -2,8 +2,8 @@
 // preconditioner, built once per configure on the host.
 //
 // The node grid of the structured tet mesh (gx * gy * gz nodes, x slowest)
-// is coarsened by two in every direction while every extent is even: coarse
-// node C sits on fine node 2C.  Prolongation P is trilinear interpolation in
+// is coarsened by two in every direction: coarse node C sits on fine node 2C
+// (with an even node extent the last coarse node is the far boundary node).  Prolongation P is trilinear interpolation in
 // index space between interior nodes (Dirichlet nodes carry no error), the
 // restriction is P^T, and the coarse operator is the Galerkin product
 // A_c = P^T A P, a 27-point stencil on the coarse grid (Dirichlet rows are
@@ -70,16 +70,20 @@ bool host_mg_build(const HostMesh &m, const std::vector<int32_t> &rp, const std:
   if (dense_max > 0) kDenseMax = dense_max;
   while ((int)ops.size() < kMaxLevels && ops.back().interior() > kDenseMax) {
     const LevelOp &f = ops.back();
-    // y, z: node extents 2m+1 -> m+1 (Dirichlet ends stay on the grid);
-    // x: the same, or on a periodic level an even plane count 2m -> m (m >= 4,
-    // so that the 27-point stencil's x-1 and x+1 planes stay distinct)
-    const bool okx = f.px ? (f.gx % 2 == 0 && f.gx / 2 >= 4) : ((f.gx - 1) % 2 == 0 && f.gx >= 5);
-    if (!okx || (f.gy - 1) % 2 || (f.gz - 1) % 2 || f.gy < 5 || f.gz < 5) break;
+    // Dirichlet axes: coarse node C sits on fine node 2C; node extents 2m+1 ->
+    // m+1, and an even extent 2m -> m+1 whose last coarse node is the far
+    // boundary node 2m-1 (only that boundary interval is one fine cell long;
+    // interior nodes interpolate as everywhere else).  A periodic x axis
+    // needs an even plane count 2m -> m (m >= 4, so that the 27-point
+    // stencil's x-1 and x+1 planes stay distinct).
+    const bool okx = f.px ? (f.gx % 2 == 0 && f.gx / 2 >= 4) : f.gx >= 5;
+    if (!okx || f.gy < 5 || f.gz < 5) break;
     LevelOp c;
     c.px = f.px;
-    c.gx = f.px ? f.gx / 2 : (f.gx - 1) / 2 + 1;
-    c.gy = (f.gy - 1) / 2 + 1;
-    c.gz = (f.gz - 1) / 2 + 1;
+    auto half = [](int g) { return g / 2 + 1; };  // (2m+1) -> m+1 and 2m -> m+1
+    c.gx = f.px ? f.gx / 2 : half(f.gx);
+    c.gy = half(f.gy);
+    c.gz = half(f.gz);
     const int64_t nc = c.n();
     c.dia.assign(27 * nc, 0.0);
     const int64_t fsj = f.gz, fsi = (int64_t)f.gy * f.gz, csj = c.gz, csi = (int64_t)c.gy * c.gz;

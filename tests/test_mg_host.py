@@ -2,7 +2,8 @@
 only, no GPU): each coarse operator equals the Galerkin product P^T A P of the
 oracle's assembled symmetric system with trilinear interpolation P (to FP32
 rounding of the stored stencil), level 0's D^-1 and Dirichlet flags match the
-system, and meshes periodic in x coarsen plane by plane with wrap-around.
+system, odd cell counts coarsen with a one-cell last interval, and meshes
+periodic in x coarsen plane by plane with wrap-around.
 
 The preconditioner is not part of the reference (its CG is unpreconditioned);
 the converged solution is checked against the oracle CG on the GPU
@@ -17,8 +18,11 @@ MESHES = [
     (8, 6, 0, 0.0, 0, 100),
     ((8, 6, 10), 6, 4, 0.2, 0, 100),
     (8, 5, 0, 0.0, 0, 100),
+    (9, 6, 0, 0.0, 0, 100),             # odd cell counts: the last coarse interval is one fine cell
+    ((9, 7, 12), 6, 4, 0.2, 0, 60),
     (16, 6, 4, 0.2, 1, 0),
     (16, 6, 0, 0.0, 1, 0),
+    ((16, 9, 11), 6, 4, 0.2, 1, 300),
 ]
 
 
@@ -99,9 +103,9 @@ def test_coarse_operators_are_galerkin_products(mpg, orc, n, split, mapping, jit
                              dense_max=dense_max, level=lev)
         ext = h["extent"]
         if periodic:
-            assert ext == (fine[0] // 2, (fine[1] - 1) // 2 + 1, (fine[2] - 1) // 2 + 1)
+            assert ext == (fine[0] // 2, fine[1] // 2 + 1, fine[2] // 2 + 1)
         else:
-            assert ext == tuple((g - 1) // 2 + 1 for g in fine)
+            assert ext == tuple(g // 2 + 1 for g in fine)
         P = _interp(fine, ext, periodic)
         Ac = (P.T @ Af @ P).tocsr()
         Ms = _stencil_matrix(h["val"], ext, h["bnd"], periodic)
@@ -115,12 +119,13 @@ def test_coarse_operators_are_galerkin_products(mpg, orc, n, split, mapping, jit
         Af, fine = Ac, ext
 
 
-def test_odd_cell_counts_are_not_coarsened(mpg):
+def test_too_small_grid_is_not_coarsened(mpg):
+    # 3 cells per side: 4 nodes, fewer than the 5 a halving needs
     with pytest.raises(mpg.MpgError):
-        mpg.mg_hierarchy(9, level=0)
+        mpg.mg_hierarchy(3, dense_max=1, level=0)
 
 
-@pytest.mark.parametrize("n,periodic", [(32, 0), (24, 1), (16, 0)])
+@pytest.mark.parametrize("n,periodic", [(32, 0), (31, 0), (24, 1), (16, 0)])
 def test_bench_level_model_matches_library(mpg, n, periodic):
     # bench.py's algorithmic-bytes model of the multigrid iteration uses the
     # same level extents the library builds
