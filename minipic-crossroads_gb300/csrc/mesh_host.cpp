@@ -402,19 +402,32 @@ void host_csr_assemble(const HostMesh &m, int mode, std::vector<int32_t> &rowptr
     return (int)((ci - ri + 1) * 9 + (cj - rj + 1) * 3 + (ck - rk + 1));
   };
   auto delta = [&](int o) -> int64_t { return (o / 9 - 1) * si + ((o / 3) % 3 - 1) * sj + (o % 3 - 1); };
+  // rows are assembled in parallel, each from the (tet, corner) pairs that
+  // use its node, in tet order: every entry sums its element contributions in
+  // the order of the element loop (ES.cpp:83-213), so the values are those of
+  // the sequential assembly bit for bit
+  std::vector<int32_t> off, c2n;
+  host_charge_slots(m, off, c2n);
+  std::vector<int32_t> inc(4 * T);
+  for (int64_t q = 0; q < 4 * T; ++q) inc[c2n[q]] = (int32_t)q;
   std::vector<uint32_t> mask(N, 0);
-  for (int64_t t = 0; t < T; ++t)
-    for (int a = 0; a < 4; ++a) {
-      int32_t r = m.tets[4 * t + a];
-      if (m.bnd[r]) continue;
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (int64_t r = 0; r < N; ++r) {
+    if (m.bnd[r]) {
+      mask[r] = 1u << 13;
+      continue;
+    }
+    uint32_t mk = 0;
+    for (int32_t q = off[r]; q < off[r + 1]; ++q) {
+      const int64_t t = inc[q] >> 2;
       for (int b = 0; b < 4; ++b) {
         int32_t c = m.tets[4 * t + b];
         if (mode == 1 && m.bnd[c]) continue;
-        mask[r] |= 1u << offset_index(r, c);
+        mk |= 1u << offset_index((int32_t)r, c);
       }
     }
-  for (int64_t r = 0; r < N; ++r)
-    if (m.bnd[r]) mask[r] = 1u << 13;
+    mask[r] = mk;
+  }
   rowptr.assign(N + 1, 0);
   for (int64_t r = 0; r < N; ++r) rowptr[r + 1] = rowptr[r] + __builtin_popcount(mask[r]);
   col.resize(rowptr[N]);
@@ -426,25 +439,28 @@ void host_csr_assemble(const HostMesh &m, int mode, std::vector<int32_t> &rowptr
       if (mask[r] & (1u << o)) col[p++] = (int32_t)(r + delta(o));
   }
   const double wcub = 1.0 / 24.0;
-  for (int64_t t = 0; t < T; ++t) {
-    const double *G = &m.grad[12 * t];
-    const double wm = m.detj[t] * wcub;
-    for (int a = 0; a < 4; ++a) {
-      int32_t r = m.tets[4 * t + a];
-      if (m.bnd[r]) continue;
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (int64_t r = 0; r < N; ++r) {
+    if (m.bnd[r]) {
+      val[rowptr[r]] = 1.0;
+      continue;
+    }
+    for (int32_t q = off[r]; q < off[r + 1]; ++q) {
+      const int64_t t = inc[q] >> 2;
+      const int a = inc[q] & 3;
+      const double *G = &m.grad[12 * t];
+      const double wm = m.detj[t] * wcub;
       for (int b = 0; b < 4; ++b) {
         int32_t c = m.tets[4 * t + b];
         if (mode == 1 && m.bnd[c]) continue;
         double k = 0.0;
         for (int cub = 0; cub < 4; ++cub)
           for (int dd = 0; dd < 3; ++dd) k += G[3 * a + dd] * (wm * G[3 * b + dd]);
-        int o = offset_index(r, c);
+        int o = offset_index((int32_t)r, c);
         val[rowptr[r] + __builtin_popcount(mask[r] & ((1u << o) - 1u))] += k;
       }
     }
   }
-  for (int64_t r = 0; r < N; ++r)
-    if (m.bnd[r]) val[rowptr[r]] = 1.0;
 }
 
 void host_background(const HostMesh &m, double rho_bg, std::vector<double> &bg) {

@@ -207,18 +207,18 @@ bool host_mg_build(const HostMesh &m, const std::vector<int32_t> &rp, const std:
         std::swap(Inv[(size_t)p * mm + q], Inv[(size_t)piv * mm + q]);
       }
     const double inv = 1.0 / M[(size_t)p * mm + p];
-    for (int q = 0; q < mm; ++q) {
-      M[(size_t)p * mm + q] *= inv;
-      Inv[(size_t)p * mm + q] *= inv;
-    }
+    // columns q < p of the pivot row are already exactly zero, so M's updates
+    // start at column p; the rows are eliminated in parallel (each row's
+    // arithmetic, and so the result, is that of the sequential loop)
+    for (int q = p; q < mm; ++q) M[(size_t)p * mm + q] *= inv;
+    for (int q = 0; q < mm; ++q) Inv[(size_t)p * mm + q] *= inv;
+#pragma omp parallel for schedule(static)
     for (int r = 0; r < mm; ++r) {
       if (r == p) continue;
       const double f = M[(size_t)r * mm + p];
       if (f == 0.0) continue;
-      for (int q = 0; q < mm; ++q) {
-        M[(size_t)r * mm + q] -= f * M[(size_t)p * mm + q];
-        Inv[(size_t)r * mm + q] -= f * Inv[(size_t)p * mm + q];
-      }
+      for (int q = p; q < mm; ++q) M[(size_t)r * mm + q] -= f * M[(size_t)p * mm + q];
+      for (int q = 0; q < mm; ++q) Inv[(size_t)r * mm + q] -= f * Inv[(size_t)p * mm + q];
     }
   }
   H.dense_inv.resize((size_t)mm * mm);
