@@ -4,20 +4,30 @@
 One "step" = PIC::time_step (PIC.cpp:245-267) over the whole particle list:
 fixed-point charge -> field solve -> E per tet -> fused push/walk/deposit.
 
-Default workload (N=1): 48^3 Kuhn-split unit cube, interior nodes jittered
-by U(-0.2h, 0.2h), 8M electrons (q/m = -1, v_th = 0.05) + 8M ions
-(q/m = +0.01, v_th = 0.005) uniform in volume, dt = 0.01, mixed precision,
-CG to 1e-10 relative residual.  Particle state (16M x 28 B = 470 MB) is larger
-than L2, so no L2 flush is needed between steps.
+Default workload (N=1, the mixed-precision target configuration): 128^3
+Kuhn-split unit cube (12,582,912 tets, 2,146,689 nodes), 128M electrons
+(q/m = -1) in two counter-streaming Maxwellian beams (drift +-0.2 along x,
+v_th = 0.02, equal halves) over a fixed uniform neutralising background,
+absorbing walls, dt = 0.005, cell sort every 10 steps, mixed precision
+(FP32 push/gather, int64 fixed-point deposit, FP32 multigrid-preconditioned
+CG inside FP64 refinement to 1e-10).  Particle state (128M x 28 B = 3.8 GB)
+is far larger than L2, so no L2 flush is needed between steps.
 
-Printed JSON line (rank 0): metric/value in particle-steps/s, the plain FP64
-form of the same workload, per-phase device times, the roofline of the
-dominant kernel, the CPU baseline (the CPU restatement of the reference's
-algorithm, timed on this host's cores), the end-to-end number through the C
-ABI with host buffers, clocks sampled during the timed region.
+Printed JSON line (rank 0): metric/value in particle-steps/s of the mixed
+form with its state resident in HBM; the mixed form with the plain inner CG
+(the same solver family as the FP64 form) and the plain FP64 form on the
+same fill, each with its ratio; per-phase device times; the roofline of the
+dominant kernel and of the FP64 form's solver; the error of the mixed form
+against the FP64 form over the configuration's 100 steps (phi per step, E,
+particle positions and velocities matched by particle id, survivor counts,
+exact charge); the CPU baseline (the CPU restatement of the reference's
+algorithm, timed on this host's cores); the end-to-end number through the C
+ABI with host buffers; clocks sampled during the timed region; the 256-run
+ensemble (p50/p99 step latency) and the 48^3 two-species configuration as
+extra keys.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                  [--workload standard|large|small|ensemble|serving]
+                  [--workload large|standard|two-stream|small|ensemble|serving]
 
 Ensemble: 256 independent runs (n^3 Kuhn meshes, n uniform in [8,32];
 particle counts log-uniform in [1e4, 2e6]; v_th uniform in [0.02, 0.1]; seeds
@@ -25,8 +35,7 @@ particle counts log-uniform in [1e4, 2e6]; v_th uniform in [0.02, 0.1]; seeds
 solver block size and sort interval picked by a short autotuning pass.
 Serving: Poisson arrivals (20 runs/s for --serve-seconds, default 60) of the
 same run mix, 5% of them 64^3 meshes with 16M particles, 50-500 steps each,
-admitted against a 150 GB device budget; time advances with the measured
-device time of the batch steps (a virtual clock).
+admitted against a 150 GB device budget (see run_serving).
 """
 import argparse
 import importlib.util
@@ -47,11 +56,12 @@ UNIT = "particle-steps/s"
 WORKLOADS = {
     # 48^3 jittered Kuhn, two species (electrons + ions), mixed precision
     "standard": dict(name="kuhn48-jitter0.2-e8M-ion8M-mixed", n_side=48, jitter=0.2, dt=0.01, sort_interval=10,
+                     steps=200,
                      species=[dict(q=-1.0, m=1.0, n=8 << 20, vth=0.05, drift=(0, 0, 0), seed=1),
                               dict(q=1.0, m=100.0, n=8 << 20, vth=0.005, drift=(0, 0, 0), seed=2)],
                      rho_background=0.0),
     # 128^3 Kuhn, 128M electrons in two counter-streaming beams over a fixed background
-    "large": dict(name="kuhn128-2beam-e128M-mixed", n_side=128, jitter=0.0, dt=0.005, sort_interval=10,
+    "large": dict(name="kuhn128-2beam-e128M-mixed", n_side=128, jitter=0.0, dt=0.005, sort_interval=10, steps=100,
                   species=[dict(q=-1.0, m=1.0, n=64 << 20, vth=0.02, drift=(0.2, 0, 0), seed=1),
                            dict(q=-1.0, m=1.0, n=64 << 20, vth=0.02, drift=(-0.2, 0, 0), seed=2, same=0)],
                   rho_background=1.0),
@@ -60,14 +70,14 @@ WORKLOADS = {
     # (two electron beams v_x = +-0.5 (1 - 0.05 sin(pi x)), H+ at rest),
     # density 2/3 pi^2, absorbing y/z walls, mixed precision
     "two-stream": dict(name="kuhn48-periodic-twostream-e8M-H8M-mixed", n_side=48, jitter=0.0, dt=0.01,
-                       sort_interval=10, periodic=1, lo=-1.0, hi=1.0, rho_background=0.0,
+                       sort_interval=10, steps=100, periodic=1, lo=-1.0, hi=1.0, rho_background=0.0,
                        ref_fills=[dict(nppe=6, type=0, density=np.pi ** 2 / 3.0, vel=(0.5, 0.0, 0.0), temp=-0.05),
                                   dict(nppe=6, type=0, density=np.pi ** 2 / 3.0, vel=(-0.5, 0.0, 0.0), temp=-0.05),
                                   dict(nppe=12, type=2, density=2.0 * np.pi ** 2 / 3.0, vel=(0.0, 0.0, 0.0),
                                        temp=0.0)],
                        species=[dict(q=-1.0, m=1.0, n=12 * 6 * 48 ** 3), dict(q=1.0, m=1837.0, n=12 * 6 * 48 ** 3)]),
     # 10^3 Kuhn, 1e5 electrons over a uniform background, plain FP64
-    "small": dict(name="kuhn10-e100k-plain", n_side=10, jitter=0.0, dt=0.01, sort_interval=0,
+    "small": dict(name="kuhn10-e100k-plain", n_side=10, jitter=0.0, dt=0.01, sort_interval=0, steps=100,
                   species=[dict(q=-1.0, m=1.0, n=100000, vth=0.05, drift=(0, 0, 0), seed=1)],
                   rho_background=1.0),
 }
@@ -96,16 +106,19 @@ WARM_START = 2
 MIXED_SOLVER = "mg"
 
 
-def make_ctx(mpg, w, precision, device=0, seed_offset=0):
+def make_ctx(mpg, w, precision, device=0, seed_offset=0, solver=None, track_ids=0):
+    """One run of workload w in the given form; solver "mg" or "cg" picks the
+    mixed form's inner solver (default MIXED_SOLVER)."""
     ctx = mpg.Ctx(device)
     ctx.mesh(w["n_side"], split=mpg.SPLIT_KUHN6, lo=w.get("lo", 0.0), hi=w.get("hi", 1.0),
              mapping=mpg.MAP_JITTER if w["jitter"] else mpg.MAP_NONE, jitter=w["jitter"], seed=7,
              periodic=w.get("periodic", 0))
-    kind = mpg.SOLVER_CG_MG if precision == mpg.MIXED and MIXED_SOLVER == "mg" else mpg.SOLVER_CG
+    solver = solver or MIXED_SOLVER
+    kind = mpg.SOLVER_CG_MG if precision == mpg.MIXED and solver == "mg" else mpg.SOLVER_CG
     ctx.configure(precision=precision, deposit=mpg.DEPOSIT_LINEAR, solver=kind, tol=1e-10, max_iter=5000,
                   warm_start=WARM_START, kill_on_wall=1, max_crossings=1000,
                   sort_interval=w["sort_interval"] if precision == mpg.MIXED else 0,
-                  rho_background=w["rho_background"])
+                  rho_background=w["rho_background"], track_ids=track_ids)
     if "ref_fills" in w:
         # the reference's per-tet fill (particle_fill.hpp:129-164); species
         # 0 = e- (-1, 1) and 2 = H+ (1, 1837) as in particle_type.hpp
@@ -348,34 +361,87 @@ def autotune(mpg, runs, device=0):
                       for v, th, si in results]}
 
 
-def accuracy_vs_plain(mpg, w, device=0, steps=3):
-    """Error of the mixed form against the FP64 plain form on the same fills:
-    max |phi_mixed - phi_plain| / max |phi_plain| after each of `steps` steps,
-    the relative KE difference, and whether the mixed form's fixed-point
-    charge (the accumulator the fused move leaves for the next solve) sums
-    exactly to the particles' quanta."""
-    import numpy as np
-    m = make_ctx(mpg, w, mpg.MIXED, device=device)
-    p = make_ctx(mpg, w, mpg.PLAIN, device=device)
-    errs, ke = [], 0.0
+def _by_id(d, n_ids):
+    """Particle arrays of a download placed at their ids (NaN / -1 where dead)."""
+    live = d["cell"] >= 0
+    ids = d["id"][live]
+    cell = np.full(n_ids, -1, np.int64)
+    x = np.full((n_ids, 3), np.nan)
+    v = np.full((n_ids, 3), np.nan)
+    cell[ids] = d["cell"][live]
+    x[ids] = d["x"][live]
+    v[ids] = d["v"][live]
+    return cell, x, v
+
+
+def accuracy_vs_plain(mpg, w, steps, device=0):
+    """Error of the mixed form against the FP64 plain form over `steps` steps
+    of the same fills (both forms stepped side by side):
+      * phi: max |phi_mixed - phi_plain| / max |phi_plain| after every step;
+      * E per tet after the last step: max |E_mixed - E_plain| / max |E_plain|;
+      * particles after the last step, matched by id: survivors in both forms,
+        in one form only, cell-id disagreements, max and rms |x_mixed -
+        x_plain| (box length 1), max |v_mixed - v_plain| / max |v_plain|;
+      * the kinetic energy per step and the survivor counts per step;
+      * charge_exact: the mixed form's fixed-point charge sums exactly to its
+        particles' quanta.
+    Also returns the plain form's per-phase device times over these steps."""
+    m = make_ctx(mpg, w, mpg.MIXED, device=device, track_ids=1)
+    p = make_ctx(mpg, w, mpg.PLAIN, device=device, track_ids=1)
+    n_ids = total_particles(w) if "ref_fills" not in w else p.count()
+    p.set_timing(True)
+    errs, ke, alive = [], 0.0, []
+    tp = {k: 0.0 for k in ("deposit", "solve", "efield", "move", "sort")}
+    iters_p, iters_m = 0, 0
     for _ in range(steps):
         sm = m.step(w["dt"], 1)
         sp = p.step(w["dt"], 1)
+        for k in tp:
+            tp[k] += getattr(sp, "ms_" + k)
+        iters_p += sp.solver_iters
+        iters_m += sm.solver_iters
         pm = m.get_field(mpg.FIELD_PHI)
         pp = p.get_field(mpg.FIELD_PHI)
         errs.append(float(np.abs(pm - pp).max() / max(np.abs(pp).max(), 1e-300)))
         ke = max(ke, abs(sm.ke - sp.ke) / max(abs(sp.ke), 1e-300))
+        alive.append((int(sm.n_alive), int(sp.n_alive)))
+    p.set_timing(False)
+    Em = m.get_field(mpg.FIELD_E_TET)
+    Ep = p.get_field(mpg.FIELD_E_TET)
+    e_err = float(np.abs(Em - Ep).max() / max(np.abs(Ep).max(), 1e-300))
     acc, _, qfix = m.charge()
     cs, _, _ = m.mixed_download()
     live = cs != mpg.DEAD
     species = (cs[live] >> 24).astype(np.int64)
     expect = int(np.bincount(species, minlength=len(qfix)).astype(object).dot(qfix.astype(object)))
     exact = int(acc.astype(object).sum()) == expect
+    del cs, live, species
+    cm, xm, vm = _by_id(m.download(), n_ids)
     m.close()
+    cp, xp, vp = _by_id(p.download(), n_ids)
     p.close()
-    return {"steps": steps, "phi_rel_err_max": max(errs), "phi_rel_err_per_step": errs, "ke_rel_diff_max": ke,
-            "charge_exact": bool(exact), "how": "same fills, both forms stepped side by side; "
-            "max|phi_mixed-phi_plain|/max|phi_plain|"}
+    both = (cm >= 0) & (cp >= 0)
+    dx = np.abs(xm[both] - xp[both])
+    dv = np.abs(vm[both] - vp[both])
+    vscale = max(float(np.abs(vp[both]).max()) if both.any() else 0.0, 1e-300)
+    parts = {"alive_both": int(both.sum()), "alive_mixed_only": int(((cm >= 0) & (cp < 0)).sum()),
+             "alive_plain_only": int(((cp >= 0) & (cm < 0)).sum()),
+             "cell_mismatch": int((cm[both] != cp[both]).sum()),
+             "x_abs_err_max": float(dx.max()) if dx.size else 0.0,
+             "x_abs_err_rms": float(np.sqrt((dx ** 2).mean())) if dx.size else 0.0,
+             "v_rel_err_max": float(dv.max() / vscale) if dv.size else 0.0,
+             "v_rel_err_rms": float(np.sqrt((dv ** 2).mean()) / vscale) if dv.size else 0.0}
+    plain_phases = {k: round(v / steps, 4) for k, v in tp.items()}
+    out = {"steps": steps, "phi_rel_err_max": max(errs), "phi_rel_err_last": errs[-1],
+           "phi_rel_err_every_10": [errs[i] for i in range(9, steps, 10)],
+           "e_rel_err_last": e_err, "ke_rel_diff_max": ke, "charge_exact": bool(exact),
+           "particles_last_step": parts,
+           "alive_mixed_vs_plain_every_10": [alive[i] for i in range(9, steps, 10)],
+           "alive_max_abs_diff": max(abs(a - b) for a, b in alive),
+           "solver_iters_per_step": {"mixed": iters_m / steps, "plain": iters_p / steps},
+           "how": "same fills, both forms stepped side by side; phi and E: max|mixed-plain|/max|plain|; "
+                  "particles matched by id after the last step (x in units of the box length)"}
+    return out, plain_phases
 
 
 def plain_sequential_rate(mpg, runs, k=6, steps=3, device=0):
@@ -492,75 +558,201 @@ def run_serving(mpg, args, device=0):
                         "speedup_vs_plain_sequential": value / seq}}
 
 
-def cpu_baseline(w, budget_s=20.0, max_steps=3):
-    """The CPU restatement of the reference step (plain FP64, all host cores)."""
-    sys.path.insert(0, ROOT)
-    from oracle import oracle as O
-    import numpy as np
-    O.build()
-    cores = os.cpu_count() or 1
-    m = O.Mesh(w["n_side"], split=6, lo=w.get("lo", 0.0), hi=w.get("hi", 1.0), mapping=4 if w["jitter"] else 0,
-               jitter=w["jitter"], seed=7, periodic=w.get("periodic", 0))
-    m.assemble(1)
-    P = total_particles(w)
-    parts = O.Particles(P)
-    qs, ms = [0.0] * 16, [1.0] * 16
-    if "ref_fills" in w:
-        qs[0], ms[0], qs[2], ms[2] = -1.0, 1.0, 1.0, 1837.0
-        for f in w["ref_fills"]:
-            parts.fill_ref(m, f["nppe"], f["type"], f["density"], vel=f["vel"], temp=f["temp"], mass=ms[f["type"]])
-    else:
-        by_charge = {}
-        for s in w["species"]:
-            by_charge[s["q"]] = by_charge.get(s["q"], 0) + s["n"]
-        for i, s in enumerate(w["species"]):
-            sp = s.get("same", i)
-            qs[sp], ms[sp] = s["q"], s["m"]
-            parts.fill_uniform(m, s["n"], s["seed"], sp, 1.0 / by_charge[s["q"]], drift=s["drift"], vth=s["vth"],
-                               nthreads=cores)
-    bg = m.background(w["rho_background"]) if w["rho_background"] else None
-    phi = np.zeros(m.N)
-    cfg = O.StepCfg(1, 1, 1e-10, 5000, 1, 1, 1, 1000, 1, cores)
-    scratch = np.zeros((P, 3))
+class CpuRun:
+    """The CPU restatement of the reference step (plain FP64, OpenMP on all
+    host cores) set up on workload w: mesh, assembled system, fill."""
+
+    def __init__(self, w):
+        sys.path.insert(0, ROOT)
+        from oracle import oracle as O
+        O.build()
+        self.O, self.w = O, w
+        self.cores = os.cpu_count() or 1
+        m = O.Mesh(w["n_side"], split=6, lo=w.get("lo", 0.0), hi=w.get("hi", 1.0), mapping=4 if w["jitter"] else 0,
+                   jitter=w["jitter"], seed=7, periodic=w.get("periodic", 0))
+        m.assemble(1)
+        P = total_particles(w)
+        parts = O.Particles(P)
+        qs, ms = [0.0] * 16, [1.0] * 16
+        if "ref_fills" in w:
+            qs[0], ms[0], qs[2], ms[2] = -1.0, 1.0, 1.0, 1837.0
+            for f in w["ref_fills"]:
+                parts.fill_ref(m, f["nppe"], f["type"], f["density"], vel=f["vel"], temp=f["temp"],
+                               mass=ms[f["type"]])
+        else:
+            by_charge = {}
+            for sp in w["species"]:
+                by_charge[sp["q"]] = by_charge.get(sp["q"], 0) + sp["n"]
+            for i, sp in enumerate(w["species"]):
+                k = sp.get("same", i)
+                qs[k], ms[k] = sp["q"], sp["m"]
+                parts.fill_uniform(m, sp["n"], sp["seed"], k, 1.0 / by_charge[sp["q"]], drift=sp["drift"],
+                                   vth=sp["vth"], nthreads=self.cores)
+        self.m, self.parts, self.qs, self.ms = m, parts, qs, ms
+        self.bg = m.background(w["rho_background"]) if w["rho_background"] else None
+        self.phi = np.zeros(m.N)
+        self.cfg = O.StepCfg(1, 1, 1e-10, 5000, 1, 1, 1, 1000, 1, self.cores)
+        self.scratch = np.zeros((P, 3))
+
+    def step(self):
+        """One full step; returns (particles at its start, seconds)."""
+        n0 = self.parts.n
+        t0 = time.perf_counter()
+        self.O.step(self.m, self.parts, self.cfg, self.w["dt"], self.qs, self.ms, self.bg, self.phi, self.scratch)
+        return n0, time.perf_counter() - t0
+
+
+def cpu_baseline(w, budget_s=15.0, max_steps=3):
+    """A bounded sample of the workload on the CPU restatement: full steps of
+    the whole workload until budget_s seconds of stepping or max_steps."""
+    run = CpuRun(w)
     done, ps, t_used = 0, 0, 0.0
     while done < max_steps and t_used < budget_s:
-        n0 = parts.n
-        t0 = time.perf_counter()
-        O.step(m, parts, cfg, w["dt"], qs, ms, bg, phi, scratch)
-        t_used += time.perf_counter() - t0
+        n0, dt = run.step()
+        t_used += dt
         ps += n0
         done += 1
-    return {"value": ps / t_used, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{done} full steps of the same workload ({P} particles, plain FP64, OpenMP {cores} threads)",
+    return {"value": ps / t_used, "unit": UNIT, "cores": run.cores, "kind": "port", "steps_timed": done,
+            "sample": f"{done} full steps of the same workload ({total_particles(w)} particles, plain FP64, "
+                      f"OpenMP {run.cores} threads)",
             "seconds": round(t_used, 3)}
 
 
 def run_reference(args, w):
+    """The reference arm: the CPU restatement of the reference's step (the
+    reference itself cannot be built here), W untimed and K timed full steps
+    of the whole workload on all host cores; rank 0 only."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    cb = cpu_baseline(w, budget_s=max(10.0, 6.0 * args.steps), max_steps=max(1, min(args.steps, 3)))
-    line = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_particles(w) / cb["value"] * 1e3,
+    run = CpuRun(w)
+    for _ in range(args.warmup):
+        run.step()
+    ps, t_used = 0, 0.0
+    for _ in range(args.steps):
+        n0, dt = run.step()
+        ps += n0
+        t_used += dt
+    value = ps / t_used
+    cb = {"value": value, "unit": UNIT, "cores": run.cores, "kind": "port", "steps_timed": args.steps,
+          "sample": f"{args.steps} timed full steps after {args.warmup} untimed ones of the whole workload "
+                    f"({total_particles(w)} particles, plain FP64, OpenMP {run.cores} threads)",
+          "seconds": round(t_used, 3)}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_used / max(args.steps, 1) * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": w["name"]}, "cpu_baseline": cb,
-            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def plain_bytes(w, ctx, phases_ms, iters_per_step):
+    """Algorithmic bytes (and FP64 operations) per step of the plain FP64
+    form's phases, for its roofline.
+    move (k_plain_move): per particle 88 B read (cell, x, x_ref, v, weight,
+      species) + 76 B written (cell, x, x_ref, v); per tet the walk tables
+      (neighbours 16 B, J^-1 72 B, E 24 B, first node 16 B) once.
+    solve (k_cg64_dia): per CG iteration and row the FP64 diagonals (8 nd B)
+      and eight 8-byte vector touches (p and r gathered, p and q written, x
+      and r read and written); nd = 15 on the Kuhn split.  FP64 operations
+      per row and iteration: 4 nd (p_j = beta p_j + r_j recomputed per
+      neighbour, then the product and the sum) + 10 (dots and updates).
+    compaction (the plain form's 'sort' phase): per particle 4 B (live count)
+      + 88 B read + 88 B written."""
+    T, N = ctx.T, ctx.N
+    P = total_particles(w)
+    nd = 15
+    return {"move": P * 164 + T * 128, "solve": iters_per_step * (8 * nd + 64) * N,
+            "solve_fp64_ops": iters_per_step * (4 * nd + 10) * N, "sort": P * 180}
+
+
+def time_steps(ctx, w, steps, warmup):
+    """(particle-steps, device ms, stats) of `steps` steps after `warmup`."""
+    for _ in range(warmup):
+        ctx.step(w["dt"], 1)
+    n0 = ctx.count()
+    ctx.timer_start()
+    st = ctx.step(w["dt"], steps)
+    ms = ctx.timer_stop()
+    return 0.5 * (n0 + st.n_alive) * steps, ms, st
+
+
+def phase_times(ctx, w, k):
+    ctx.set_timing(True)
+    ph = ctx.step(w["dt"], k)
+    ctx.set_timing(False)
+    return {n: getattr(ph, "ms_" + n) / k for n in ("deposit", "solve", "efield", "move", "sort")}, ph
+
+
+def e2e_mixed(mpg, ctx, w, steps, barrier_sum, barrier_max):
+    """End to end through the C ABI with host buffers: state upload, K steps
+    with the step statistics read back each step, state download; host wall
+    clock, median of three passes."""
+    for _ in range(2):
+        ctx.step(w["dt"], 1)
+    cs, b, v = ctx.mixed_download()
+    pinned = False
+    try:
+        import torch
+
+        def pin(a):
+            t = torch.empty(a.nbytes, dtype=torch.uint8, pin_memory=True).numpy().view(a.dtype).reshape(a.shape)
+            np.copyto(t, a)
+            return t
+        cs, b, v = pin(cs), pin(b), pin(v)
+        out = tuple(pin(np.empty_like(a)) for a in (cs, b, v))
+        pinned = True
+    except Exception:
+        out = None
+    reps = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        ctx.mixed_upload(cs, b, v)
+        n_e = ctx.count()
+        for _ in range(steps):
+            ctx.step(w["dt"], 1)
+        cs2, b2, v2 = ctx.mixed_download(out=out)
+        t1 = time.perf_counter()
+        reps.append(barrier_sum(n_e * steps) / barrier_max(t1 - t0))
+    nbytes = cs.nbytes + b.nbytes + v.nbytes
+    return {"value": sorted(reps)[1], "unit": UNIT, "h2d_bytes_per_step": int(nbytes / steps),
+            "d2h_bytes_per_step": int((cs2.nbytes + b2.nbytes + v2.nbytes) / steps + 136),
+            "pinned_host_buffers": pinned, "passes": [round(x, 1) for x in reps],
+            "how": "mpg_mixed_upload from host buffers, mpg_step x K with stats read back each "
+                   "step, mpg_mixed_download into host buffers; host wall clock, median of 3 passes"}
+
+
+def standard_summary(mpg, args, device):
+    """The 48^3 two-species configuration, mixed and plain, as an extra key."""
+    w = WORKLOADS["standard"]
+    ctx = make_ctx(mpg, w, mpg.MIXED, device=device)
+    ps, ms, st = time_steps(ctx, w, args.steps, max(args.warmup, 3))
+    ctx.close()
+    pc = make_ctx(mpg, w, mpg.PLAIN, device=device)
+    kp = max(1, min(args.steps, 5))
+    pps, pms, _ = time_steps(pc, w, kp, 2)
+    pc.close()
+    v, pv = ps / (ms * 1e-3), pps / (pms * 1e-3)
+    return {"workload": w["name"], "value": v, "unit": UNIT, "steps": args.steps, "ms_per_step": ms / args.steps,
+            "plain_fp64": {"value": pv, "steps": kp, "ms_per_step": pms / kp}, "mixed_over_plain": v / pv}
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="standard", choices=sorted(WORKLOADS) + ["ensemble", "serving"])
+    ap.add_argument("--workload", default="large", choices=sorted(WORKLOADS) + ["ensemble", "serving"])
     ap.add_argument("--serve-seconds", type=float, default=60.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the 48^3 configuration key")
+    ap.add_argument("--accuracy-steps", type=int, default=None,
+                    help="steps of the mixed-vs-FP64 comparison (default: the configuration's step count)")
     ap.add_argument("--warm-start", type=int, default=2, choices=[0, 1, 2, 3],
                     help="CG initial guess: 0 zero, 1 previous phi, 2/3 linear/quadratic extrapolation")
     ap.add_argument("--sort-interval", type=int, default=None,
@@ -578,7 +770,7 @@ def main():
     if args.workload in ("ensemble", "serving"):
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the reference has no batched or serving mode; "
-                              "its CPU step is timed by the standard workload"}))
+                              "its CPU step is timed by the single-run workloads"}))
             return 0
         mpg = _pkg()
         mpg.build()
@@ -620,6 +812,7 @@ def main():
     mpg.build()
     mpg.load()
     precision = mpg.PLAIN if args.workload == "small" else mpg.MIXED
+    mixed = precision == mpg.MIXED
     ctx = make_ctx(mpg, w, precision, device=local, seed_offset=rank)
     for _ in range(args.warmup):
         ctx.step(w["dt"], 1)
@@ -633,126 +826,111 @@ def main():
     ms = ctx.timer_stop()
     clk = clocks.stop()
     launches = st.n_launches
-    n1 = st.n_alive
-    particle_steps = 0.5 * (n0 + n1) * args.steps
+    particle_steps = 0.5 * (n0 + st.n_alive) * args.steps
     t_max = barrier_max(ms)
     ps_total = barrier_sum(particle_steps)
     value = ps_total / (t_max * 1e-3)
 
     # per-phase device times on a separate timed pass
-    ctx.set_timing(True)
     k_ph = min(args.steps, 10)
-    ph = ctx.step(w["dt"], k_ph)
-    ctx.set_timing(False)
-    phases = {k: getattr(ph, "ms_" + k) / k_ph for k in ("deposit", "solve", "efield", "move", "sort")}
+    phases, ph = phase_times(ctx, w, k_ph)
     line = {}
+    hbm, kind = peaks()
     if rank == 0:
-        hbm, kind = peaks()
-        pb = phase_bytes(w, ctx, ph, k_ph, mpg) if precision == mpg.MIXED else None
-        dominant = max(("solve", "move", "efield", "deposit"), key=lambda k: phases[k])
-        kern = {"solve": "k_cg_mg" if uses_mg(w) else "k_cg_mixed", "move": "k_mixed_move_persistent",
-                "efield": "k_efield_mixed",
-                "deposit": "k_mixed_convert"}[dominant]
+        pb = phase_bytes(w, ctx, ph, k_ph, mpg) if mixed else None
         roof = None
         if pb is not None:
+            dominant = max(("solve", "move", "efield", "deposit"), key=lambda k: phases[k])
+            kern = {"solve": "k_cg_mg" if uses_mg(w) else "k_cg_mixed", "move": "k_mixed_move_persistent",
+                    "efield": "k_efield_mixed", "deposit": "k_mixed_convert"}[dominant]
             bytes_launch = pb[dominant]
             achieved = bytes_launch / (phases[dominant] * 1e-3) / 1e9
-            traffic = read_traffic(kern, w["name"])
             roof = {"bound": "hbm", "kernel": kern, "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-                    "frac": round(achieved / hbm, 4), "peak_kind": kind, "traffic": traffic,
+                    "frac": round(achieved / hbm, 4), "peak_kind": kind, "traffic": read_traffic(kern, w["name"]),
                     "algorithmic_bytes_per_launch": int(bytes_launch), "ms_per_launch": round(phases[dominant], 4)}
-            # the particle kernel alone, for reference
-            mv = pb["move"] / (phases["move"] * 1e-3) / 1e9
-            roof["move_kernel_gbs"] = round(mv, 1)
-            roof["move_kernel_frac"] = round(mv / hbm, 4)
+            # the other large phase for reference
+            other = "solve" if dominant == "move" else "move"
+            ob = pb[other] / (phases[other] * 1e-3) / 1e9
+            roof[other + "_gbs"] = round(ob, 1)
+            roof[other + "_frac"] = round(ob / hbm, 4)
             roof["cg_iters_per_step"] = round(pb["iters_per_step"], 1)
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32" if precision == mpg.MIXED else "f64",
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32" if mixed else "f64",
                 "precision": (("mixed: f32 push/walk, i64 fixed-point deposit, f32 "
                                + ("multigrid-preconditioned CG" if uses_mg(w) else "CG") + " inside f64 refinement")
-                              if precision == mpg.MIXED else "plain f64"),
+                              if mixed else "plain f64"),
                 "data": "synthetic",
                 "config": {"workload": w["name"], "n_side": w["n_side"], "tets": ctx.T, "nodes": ctx.N,
                            "sort_interval": w["sort_interval"],
-                           "particles": total_particles(w), "dt": w["dt"], "cg_tol": 1e-10,
+                           "particles": total_particles(w), "dt": w["dt"], "config_steps": w["steps"],
+                           "cg_tol": 1e-10,
                            "cg_initial_guess": ["zero", "previous phi", "extrapolated 2*phi[n-1]-phi[n-2]",
                                                 "extrapolated 3*phi[n-1]-3*phi[n-2]+phi[n-3]"][WARM_START],
                            "cg_preconditioner": ("geometric multigrid V-cycle (2 Jacobi sweeps per side on "
                                                  "the fine level, 1 on coarser levels, dense coarsest solve)"
-                                                 if precision == mpg.MIXED
-                                                 and uses_mg(w) else "none"),
+                                                 if mixed and uses_mg(w) else "none"),
                            "parallelism": "replicas" if world > 1 else "single",
                            "l2": "inputs larger than L2 (particle state > 129 MB), no flush"},
                 "phases_ms_per_step": {k: round(v, 4) for k, v in phases.items()},
                 "solver_iters_per_step": ph.solver_iters / k_ph,
                 "roofline": roof, "gpu_launches": launches, "clocks": clk}
-    # plain FP64 form of the same workload (the form the mixed target is measured against)
-    if not args.no_plain and precision == mpg.MIXED:
+    if mixed and not args.no_plain:
         ctx.close()
         ctx = None
+        # the mixed form with the plain inner CG: the FP64 form's solver family
+        if uses_mg(w):
+            cc = make_ctx(mpg, w, mpg.MIXED, device=local, seed_offset=rank, solver="cg")
+            kc = max(1, min(args.steps, 10))
+            cps, cms, cst = time_steps(cc, w, kc, 2)
+            cv = barrier_sum(cps) / (barrier_max(cms) * 1e-3)
+            cc.close()
+        else:
+            cv, kc, cms, cst = value, args.steps, ms, st
+        # plain FP64 form of the same workload (the form the mixed target is measured against)
         pc = make_ctx(mpg, w, mpg.PLAIN, device=local, seed_offset=rank)
         kp = max(1, min(args.steps, 5))
-        pc.step(w["dt"], 2)
-        q0 = pc.count()
-        pc.timer_start()
-        pst = pc.step(w["dt"], kp)
-        pms = pc.timer_stop()
-        pv = barrier_sum(0.5 * (q0 + pst.n_alive) * kp) / (barrier_max(pms) * 1e-3)
-        if rank == 0:
-            line["plain_fp64"] = {"value": pv, "unit": UNIT, "steps": kp, "ms_per_step": pms / kp,
-                                  "mixed_over_plain": value / pv}
+        pps, pms, pst = time_steps(pc, w, kp, 2)
+        pv = barrier_sum(pps) / (barrier_max(pms) * 1e-3)
         pc.close()
-        # error of the mixed form against the FP64 plain form on the same inputs
         if rank == 0:
-            line["accuracy_vs_plain_fp64"] = accuracy_vs_plain(mpg, w, device=local)
+            line["mixed_cg"] = {"value": cv, "unit": UNIT, "steps": kc, "ms_per_step": cms / kc,
+                                "solver_iters_per_step": cst.solver_iters / kc,
+                                "how": "mixed form with the unpreconditioned FP32 inner CG (the plain form's "
+                                       "solver family)"}
+            line["plain_fp64"] = {"value": pv, "unit": UNIT, "steps": kp, "ms_per_step": pms / kp,
+                                  "solver_iters_per_step": pst.solver_iters / kp,
+                                  "mixed_over_plain": value / pv, "mixed_cg_over_plain": cv / pv}
+            acc, pphase = accuracy_vs_plain(mpg, w, args.accuracy_steps or w["steps"], device=local)
+            line["accuracy_vs_plain_fp64"] = acc
+            pb = plain_bytes(w, pc, pphase, acc["solver_iters_per_step"]["plain"])
+            pl = line["plain_fp64"]
+            pl["phases_ms_per_step"] = pphase
+            pl["roofline"] = {
+                "bound": "hbm", "kernel": "k_cg64_dia", "unit": "GB/s", "peak": hbm, "peak_kind": kind,
+                "achieved": round(pb["solve"] / (pphase["solve"] * 1e-3) / 1e9, 1),
+                "frac": round(pb["solve"] / (pphase["solve"] * 1e-3) / 1e9 / hbm, 4),
+                "fp64_tflops": round(pb["solve_fp64_ops"] / (pphase["solve"] * 1e-3) / 1e12, 3),
+                "fp64_nominal_tflops": 1.25,
+                "move_gbs": round(pb["move"] / (pphase["move"] * 1e-3) / 1e9, 1),
+                "compaction_gbs": round(pb["sort"] / (max(pphase["sort"], 1e-9) * 1e-3) / 1e9, 1),
+                "how": "algorithmic bytes per step (bench.plain_bytes) / phase device time over the accuracy "
+                       "run's steps; FP64 operations without fused multiply-adds"}
         if not args.no_e2e:
             ctx = make_ctx(mpg, w, precision, device=local, seed_offset=rank)
-    # end to end through the C ABI with host buffers: state upload, K steps with
-    # the step statistics read back each step, state download
-    if not args.no_e2e and ctx is not None and precision == mpg.MIXED:
-        import numpy as np
-        for _ in range(2):
-            ctx.step(w["dt"], 1)
-        cs, b, v = ctx.mixed_download()
-        pinned = False
-        try:
-            import torch
-
-            def pin(a):
-                t = torch.empty(a.nbytes, dtype=torch.uint8, pin_memory=True).numpy().view(a.dtype).reshape(a.shape)
-                np.copyto(t, a)
-                return t
-            cs, b, v = pin(cs), pin(b), pin(v)
-            out = tuple(pin(np.empty_like(a)) for a in (cs, b, v))
-            pinned = True
-        except Exception:
-            out = None
-        ke = args.steps
-        # three end-to-end passes (upload, K steps, download); the median is reported
-        reps = []
-        for _ in range(3):
-            t0 = time.perf_counter()
-            ctx.mixed_upload(cs, b, v)
-            n_e = ctx.count()
-            for _ in range(ke):
-                ctx.step(w["dt"], 1)
-            cs2, b2, v2 = ctx.mixed_download(out=out)
-            t1 = time.perf_counter()
-            reps.append(barrier_sum(n_e * ke) / barrier_max(t1 - t0))
-        eps = sorted(reps)[1]
+    if not args.no_e2e and ctx is not None and mixed:
+        e2e = e2e_mixed(mpg, ctx, w, args.steps, barrier_sum, barrier_max)
         if rank == 0:
-            nbytes = cs.nbytes + b.nbytes + v.nbytes
-            line["e2e"] = {"value": eps, "unit": UNIT, "h2d_bytes_per_step": int(nbytes / ke),
-                           "d2h_bytes_per_step": int((cs2.nbytes + b2.nbytes + v2.nbytes) / ke + 136),
-                           "pinned_host_buffers": pinned, "passes": [round(x, 1) for x in reps],
-                           "how": "mpg_mixed_upload from host buffers, mpg_step x K with stats read back each "
-                                  "step, mpg_mixed_download into host buffers; host wall clock, median of 3 passes"}
-    if rank == 0 and not args.no_ensemble and args.workload == "standard" and world == 1:
+            line["e2e"] = e2e
+    if ctx is not None:
+        ctx.close()
+    if rank == 0 and world == 1 and mixed and not args.no_ensemble:
         # the ensemble part of the metric: 256 runs in the batch engine
         ens = run_ensemble(mpg, args, device=local)
         line["ensemble"] = dict(ens["ensemble"], value=ens["value"], unit=UNIT, workload=ens["config"]["workload"],
                                 particles=ens["config"]["particles"], steps=ens["steps"])
+    if rank == 0 and world == 1 and args.workload == "large" and not args.no_extra:
+        line["standard_48"] = standard_summary(mpg, args, local)
     if rank == 0:
         if not args.no_cpu:
             try:

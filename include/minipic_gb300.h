@@ -172,7 +172,17 @@ int mpg_solve(mpg_ctx *ctx, int *iters, double *resid);         /* ES::solve, ES
 int mpg_weight_efield(mpg_ctx *ctx);                            /* PIC::weight_Efield, PIC.cpp:186-189 */
 int mpg_move(mpg_ctx *ctx, double dt, mpg_step_stats *st);      /* ParticleMove::move, particle_move.hpp:398-404, plus KE */
 int mpg_step(mpg_ctx *ctx, double dt, int n_steps, mpg_step_stats *st); /* PIC::time_step x n_steps */
-int mpg_sort(mpg_ctx *ctx);                                     /* ParticleList::sort, particle_list.cpp:90-146 */
+/* ParticleList::sort (particle_list.cpp:90-116): live particles in cell order;
+ * inside a cell the previous list order is kept (a stable sort, the same on
+ * every run; the reference's BinSort leaves that order open).  Dead particles
+ * are dropped.  The mixed step also sorts every sort_interval steps; the
+ * plain step never does (Serial list order, PIC.cpp:51-53). */
+int mpg_sort(mpg_ctx *ctx);
+/* ParticleList::compute_start_particles_by_element / start_by_element
+ * (particle_list.cpp:118-146): start[e] = first list position of cell e's
+ * particles, start[T] = count (len >= T + 1).  Valid after mpg_sort until
+ * particles move, are added or are replaced (MPG_ERR_STATE otherwise). */
+int mpg_cell_starts(mpg_ctx *ctx, int64_t len, int64_t *start);
 
 /* ES::rhs / ES::phi / set_analytic_RHS-style access (ES.hpp:53-71) */
 int mpg_get_field(mpg_ctx *ctx, int which, double *host);

@@ -244,7 +244,17 @@ class ParticleList {  // particle_list.hpp:54-320
   bool is_dead(std::size_t i) const { return cell_.at(i) < 0; }
   std::size_t snapshot_size() const { return (std::size_t)snap_n_; }
   void sort() { check(ctx_->ctx, mpg_sort(ctx_->ctx), "mpg_sort"); }
-  void compute_start_particles_by_element() { sort(); }
+  // particle_list.cpp:135-146: sort, then the first list position per element
+  void compute_start_particles_by_element() {
+    sort();
+    int64_t T = 0, N = 0, nb = 0;
+    check(ctx_->ctx, mpg_mesh_sizes(ctx_->ctx, &T, &N, &nb), "mpg_mesh_sizes");
+    start_.resize(T + 1);
+    check(ctx_->ctx, mpg_cell_starts(ctx_->ctx, T + 1, start_.data()), "mpg_cell_starts");
+  }
+  // particle_list.hpp:253-257 (start_by_element_ after compute_start_particles_by_element)
+  LO start(LO elem) const { return (LO)start_.at(elem); }
+  LO count_for_element(LO elem) const { return (LO)(start_.at(elem + 1) - start_.at(elem)); }
   void dump_particles(std::ostream &out) const {  // particle_list.hpp:221-226
     refresh();
     for (int64_t i = 0; i < snap_n_; ++i)
@@ -258,6 +268,7 @@ class ParticleList {  // particle_list.hpp:54-320
   mutable std::vector<int32_t> cell_, sp_;
   mutable std::vector<double> x_, xr_, v_, w_;
   mutable int64_t snap_n_ = 0;
+  std::vector<int64_t> start_;
 };
 
 class ES {  // ES.hpp:48-116

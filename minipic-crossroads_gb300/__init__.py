@@ -32,7 +32,7 @@ EXPORTS = [
     "mpg_csr_download", "mpg_particles_reserve", "mpg_fill_ref", "mpg_fill_uniform", "mpg_particles_upload",
     "mpg_particles_download", "mpg_particles_count", "mpg_mixed_download", "mpg_mixed_upload",
     "mpg_charge_download", "mpg_weight_charge", "mpg_solve", "mpg_weight_efield", "mpg_move", "mpg_step",
-    "mpg_sort", "mpg_get_field", "mpg_set_field", "mpg_cg_csr", "mpg_cg_csr_noalloc", "mpg_mg_hierarchy",
+    "mpg_sort", "mpg_cell_starts", "mpg_get_field", "mpg_set_field", "mpg_cg_csr", "mpg_cg_csr_noalloc", "mpg_mg_hierarchy",
     "mpg_batch_create", "mpg_batch_destroy", "mpg_batch_last_error", "mpg_batch_set_tuning", "mpg_batch_admit",
     "mpg_batch_step", "mpg_batch_run_info", "mpg_batch_run_phi", "mpg_batch_run_particles", "mpg_batch_retire",
 ]
@@ -137,6 +137,7 @@ def load():
         "mpg_move": ([P, D, C.POINTER(StepStats)], I),
         "mpg_step": ([P, D, I, C.POINTER(StepStats)], I),
         "mpg_sort": ([P], I),
+        "mpg_cell_starts": ([P, I64, P], I),
         "mpg_get_field": ([P, I, P], I),
         "mpg_set_field": ([P, I, P], I),
         "mpg_cg_csr": ([P, I64, P, P, P, P, P, D, I, C.POINTER(I), C.POINTER(D)], I),
@@ -394,6 +395,12 @@ class Ctx:
 
     def sort(self):
         self._ck(self.L.mpg_sort(self.h))
+
+    def cell_starts(self):
+        """start[e] = first list position of cell e after the last sort (T + 1 entries)."""
+        a = np.zeros(self.T + 1, np.int64)
+        self._ck(self.L.mpg_cell_starts(self.h, len(a), ptr(a)))
+        return a
 
     def get_field(self, which):
         n = 3 * self.T if which == FIELD_E_TET else self.N

@@ -74,6 +74,9 @@ struct mpg_ctx {
   int64_t cg_n = 0;
   double *bicg_work = nullptr, *red_dev = nullptr, *red_host = nullptr;
   uint32_t *sort_cnt = nullptr, *sort_start = nullptr, *scan_scratch = nullptr;
+  uint32_t *sort_perm = nullptr, *sort_long = nullptr;  // stable cell sort: permutation (cap), long-range list
+  int64_t sort_perm_cap = 0;
+  bool starts_valid = false;  // sort_start holds the start offsets of the current particle order
   int64_t scan_len = 0;
   uint32_t *d_count = nullptr, *h_count = nullptr;
   DevStats *d_stats = nullptr, *h_stats = nullptr;
@@ -176,6 +179,10 @@ int ensure_scan_scratch(mpg_ctx *c) {
 }
 
 void free_particles(mpg_ctx *c) {
+  dfree(c, c->sort_perm);
+  dfree(c, c->sort_long);
+  c->sort_perm_cap = 0;
+  c->starts_valid = false;
   for (int k = 0; k < 2; ++k) {
     dfree(c, c->pp[k].cell);
     dfree(c, c->pp[k].x);
@@ -474,25 +481,61 @@ int compact_plain(mpg_ctx *c) {
   CK(cudaStreamSynchronize(c->stream));
   c->cur = other;
   c->n = *c->h_count;
+  c->starts_valid = false;
   return MPG_OK;
 }
 
+// scratch of the stable cell sort for the current particle capacity
+int sort_work(mpg_ctx *c, SortWork &w) {
+  if (c->cap >= (int64_t)1 << 32) return fail(c, MPG_ERR_ARG, "the cell sort needs fewer than 2^32 particle slots");
+  if (!c->sort_perm || c->sort_perm_cap < c->cap) {
+    dfree(c, c->sort_perm);
+    dfree(c, c->sort_long);
+    TRY(dalloc(c, &c->sort_perm, std::max<int64_t>(c->cap, 1)));
+    TRY(dalloc(c, &c->sort_long, c->cap / 32 + 2));
+    c->sort_perm_cap = c->cap;
+  }
+  w.cnt = c->sort_cnt;
+  w.start = c->sort_start;
+  w.perm = c->sort_perm;
+  w.long_count = c->sort_long;
+  w.long_list = c->sort_long + 1;
+  w.scan_scratch = c->scan_scratch;
+  w.scan_len = c->scan_len;
+  w.long_blocks = sort_long_blocks(c->device);
+  return MPG_OK;
+}
+
+// Stable cell sort of the mixed form (drops dead particles).  The new count
+// is read back at the next host sync; the slots [count, n) of the new buffer
+// are dead, so the grid bound n stays valid until then.
 int sort_mixed(mpg_ctx *c) {
   c->needs_sort = false;
+  SortWork w;
+  TRY(sort_work(c, w));
   const int other = 1 - c->cur;
-  launch_mixed_sort(c->stream, c->mp[c->cur], c->n, c->mp[other], c->dm.T, c->sort_cnt, c->sort_start,
-                    c->scan_scratch, c->scan_len, c->d_count);
-  c->launches += 6;
+  launch_mixed_sort(c->stream, c->mp[c->cur], c->n, c->mp[other], c->dm.T, w, c->d_count);
+  c->launches += 9;
   CKL();
   c->cur = other;
-  // the new count is read back at the next host sync; slots [count, n) of the
-  // new buffer are marked dead so that the grid bound n stays valid
-  const int64_t n = c->n;
-  if (n > 0) {
-    launch_mark_tail_dead(c->stream, c->mp[c->cur].c, n, c->d_count);
-    c->launches += 1;
-    CKL();
-  }
+  c->starts_valid = true;
+  return MPG_OK;
+}
+
+// Stable cell sort of the plain form (mpg_sort only: the plain step keeps
+// the reference's Serial list order, PIC.cpp:51-53)
+int sort_plain(mpg_ctx *c) {
+  SortWork w;
+  TRY(sort_work(c, w));
+  const int other = 1 - c->cur;
+  launch_plain_sort(c->stream, c->pp[c->cur], c->n, c->pp[other], c->dm.T, w, c->d_count);
+  c->launches += 9;
+  CKL();
+  CK(cudaMemcpyAsync(c->h_count, c->d_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  c->cur = other;
+  c->n = *c->h_count;
+  c->starts_valid = true;
   return MPG_OK;
 }
 
@@ -518,11 +561,13 @@ int one_step(mpg_ctx *c, double dt, mpg_step_stats *acc_st, bool &sorted) {
   TRY(phase_solve(c));
   ev_record(c, 2);
   TRY(phase_efield(c));
-  ev_record(c, 3);
   CK(cudaMemsetAsync(&c->d_stats->ke, 0, sizeof(double), c->stream));
+  c->starts_valid = false;
+  // the move deposits the new positions' charge into zeroed slots (the
+  // memset is timed with the E-field phase, the move phase is the kernel)
+  if (mixed) CK(cudaMemsetAsync(c->acc, 0, sizeof(unsigned long long) * 4 * c->dm.T, c->stream));
+  ev_record(c, 3);
   if (mixed) {
-    // the move deposits the new positions' charge into zeroed slots
-    CK(cudaMemsetAsync(c->acc, 0, sizeof(unsigned long long) * 4 * c->dm.T, c->stream));
     launch_mixed_move(c->stream, c->mp[c->cur], c->n, c->dm, c->sp, (float)dt, c->cfg.kill_on_wall,
                       c->cfg.max_crossings, c->acc, c->d_stats);
   } else {
@@ -739,6 +784,7 @@ void free_field(mpg_ctx *c) {
   dfree(c, c->acc_node);
   dfree(c, c->sort_cnt);
   dfree(c, c->sort_start);
+  c->starts_valid = false;
   dfree(c, c->scan_scratch);
   c->scan_len = 0;
   dfree(c, c->bicg_work);
@@ -1214,6 +1260,7 @@ int mpg_fill_ref(mpg_ctx *c, int nppe, int type, double density, const double ve
   c->id_next += add;
   c->acc_valid = false;
   c->needs_sort = true;
+  c->starts_valid = false;
   CK(cudaStreamSynchronize(c->stream));
   return MPG_OK;
 }
@@ -1236,6 +1283,7 @@ int mpg_fill_uniform(mpg_ctx *c, int64_t n, uint64_t seed, int type, double weig
   c->id_next += n;
   c->acc_valid = false;
   c->needs_sort = true;
+  c->starts_valid = false;
   CK(cudaStreamSynchronize(c->stream));
   return MPG_OK;
 }
@@ -1320,6 +1368,7 @@ int mpg_particles_upload(mpg_ctx *c, int64_t n, const int32_t *cell, const doubl
   c->id_next = n;
   c->acc_valid = false;
   c->needs_sort = true;
+  c->starts_valid = false;
   return MPG_OK;
 }
 
@@ -1442,6 +1491,7 @@ int mpg_mixed_upload(mpg_ctx *c, int64_t n, const uint32_t *cellsp, const float 
   c->n_live = (int64_t)h_chk[1];
   c->acc_valid = false;
   c->needs_sort = true;
+  c->starts_valid = false;
   return MPG_OK;
 }
 
@@ -1506,6 +1556,7 @@ int mpg_move(mpg_ctx *c, double dt, mpg_step_stats *st) {
   TRY(ensure_particles(c));
   mpg_step_stats acc{};
   TRY(zero_stats(c));
+  c->starts_valid = false;
   if (c->cfg.precision == MPG_MIXED) {
     // the fused kernel also deposits; keep the accumulator consistent
     CK(cudaMemsetAsync(c->acc, 0, sizeof(unsigned long long) * 4 * c->dm.T, c->stream));
@@ -1580,9 +1631,25 @@ int mpg_sort(mpg_ctx *c) {
   if (c->cfg.precision == MPG_MIXED) {
     TRY(sort_mixed(c));
     TRY(finish_counts_mixed(c, true));
+  } else {
+    // on request only: the plain step keeps the reference's Serial list order
+    TRY(sort_plain(c));
   }
-  // the plain form keeps the reference Serial order (no sort, PIC.cpp:51-53)
   CK(cudaStreamSynchronize(c->stream));
+  return MPG_OK;
+}
+
+int mpg_cell_starts(mpg_ctx *c, int64_t len, int64_t *start) {
+  ENTER(c);
+  if (!c->has_mesh) return fail(c, MPG_ERR_STATE, "no mesh");
+  const int64_t T = c->dm.T;
+  if (!start || len < T + 1) return fail(c, MPG_ERR_ARG, "start needs T + 1 = %lld entries", (long long)(T + 1));
+  if (!c->starts_valid || !c->sort_start)
+    return fail(c, MPG_ERR_STATE, "particles changed since the last sort: call mpg_sort first");
+  std::vector<uint32_t> tmp(T + 1);
+  CK(cudaMemcpyAsync(tmp.data(), c->sort_start, sizeof(uint32_t) * (T + 1), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  for (int64_t e = 0; e <= T; ++e) start[e] = tmp[e];
   return MPG_OK;
 }
 

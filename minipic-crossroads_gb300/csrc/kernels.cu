@@ -718,38 +718,200 @@ __device__ __forceinline__ void cell_run(uint32_t key, int &first, int &rank, in
   len = next - first;
 }
 
+// ---- stable cell sort (ParticleList::sort + compute_start_particles_by_element,
+// particle_list.cpp:90-146) --------------------------------------------------
+// 1. k_cell_hist: particles per cell (one atomic per warp run of equal cells);
+// 2. exclusive scan: the first sorted position of every cell (start);
+// 3. k_cell_slots: every live particle's input index goes to a slot of its
+//    cell's range, claimed per warp run with one atomic (the order inside a
+//    range depends on timing here);
+// 4. k_cell_order / k_cell_order_long: each cell's range of input indices is
+//    sorted ascending, so the order inside a cell is the input order: the
+//    permutation is that of a stable sort by cell, the same on every run (the
+//    reference's BinSort leaves it open);
+// 5. k_sort_gather_*: sorted record i = input record perm[i] (coalesced
+//    stores; the loads follow the input order cell by cell).
+// Keys: mixed cellsp words (species << 24 | cell, MPG_DEAD = dead) or plain
+// int32 cells (< 0 = dead); dead particles are dropped.
+template <bool kMixed>
+__device__ __forceinline__ uint32_t sort_key(const uint32_t *__restrict__ c, int64_t p, int64_t n) {
+  if (p >= n) return MPG_DEAD;
+  const uint32_t v = c[p];
+  if (kMixed) return v == MPG_DEAD ? MPG_DEAD : (v & 0xFFFFFFu);
+  return (int32_t)v < 0 ? MPG_DEAD : v;
+}
+
+template <bool kMixed>
 __global__ void k_cell_hist(const uint32_t *__restrict__ c, int64_t n, uint32_t *__restrict__ cnt) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t cs = p < n ? c[p] : MPG_DEAD;
-  const uint32_t key = cs == MPG_DEAD ? MPG_DEAD : (cs & 0xFFFFFFu);
+  const uint32_t key = sort_key<kMixed>(c, p, n);
   int first, rank, len;
   cell_run(key, first, rank, len);
   if (rank == 0 && key != MPG_DEAD) atomicAdd(&cnt[key], (unsigned)len);
 }
 
-// one atomic per run of equal cells; lanes of a run keep their order
-__global__ void k_cell_scatter(MixedParts P, int64_t n, MixedParts Q, const uint32_t *__restrict__ start,
-                               uint32_t *__restrict__ fill) {
+template <bool kMixed>
+__global__ void k_cell_slots(const uint32_t *__restrict__ c, int64_t n, const uint32_t *__restrict__ start,
+                             uint32_t *__restrict__ fill, uint32_t *__restrict__ perm) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t cs = p < n ? P.c[p] : MPG_DEAD;
-  const uint32_t key = cs == MPG_DEAD ? MPG_DEAD : (cs & 0xFFFFFFu);
+  const uint32_t key = sort_key<kMixed>(c, p, n);
   int first, rank, len;
   cell_run(key, first, rank, len);
   uint32_t base = 0;
   if (rank == 0 && key != MPG_DEAD) base = atomicAdd(&fill[key], (unsigned)len);
   base = __shfl_sync(0xffffffffu, base, first);
-  if (key == MPG_DEAD) return;
-  const uint32_t dst = start[key] + base + (uint32_t)rank;
-  Q.c[dst] = cs;
-  Q.b[dst] = P.b[p];
-  Q.v[dst] = P.v[p];
-  if (P.id) Q.id[dst] = P.id[p];
+  if (key != MPG_DEAD) perm[start[key] + base + (uint32_t)rank] = (uint32_t)p;
+}
+
+// ranges of up to kSortLocal entries are sorted by one thread (insertion sort,
+// in registers and L1); longer ones are listed for k_cell_order_long
+constexpr int kSortLocal = 32;
+__global__ void k_cell_order(const uint32_t *__restrict__ start, int64_t T, uint32_t *__restrict__ perm,
+                             uint32_t *__restrict__ long_list, uint32_t *__restrict__ long_count) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= T) return;
+  const uint32_t lo = start[e], m = start[e + 1] - lo;
+  if (m < 2) return;
+  if (m > (uint32_t)kSortLocal) {
+    long_list[atomicAdd(long_count, 1u)] = (uint32_t)e;
+    return;
+  }
+  uint32_t a[kSortLocal];
+  bool sorted = true;
+  for (uint32_t k = 0; k < m; ++k) {
+    a[k] = perm[lo + k];
+    if (k && a[k] < a[k - 1]) sorted = false;
+  }
+  if (sorted) return;
+  for (uint32_t k = 1; k < m; ++k) {
+    const uint32_t x = a[k];
+    int j = (int)k - 1;
+    while (j >= 0 && a[j] > x) {
+      a[j + 1] = a[j];
+      --j;
+    }
+    a[j + 1] = x;
+  }
+  for (uint32_t k = 0; k < m; ++k) perm[lo + k] = a[k];
+}
+
+// number of entries of a taken among the first d outputs of the merge of
+// sorted runs a[0..la) and b[0..lb) (entries are distinct)
+__device__ __forceinline__ uint32_t merge_split(const uint32_t *a, uint32_t la, const uint32_t *b, uint32_t lb,
+                                                uint32_t d) {
+  uint32_t lo = d > lb ? d - lb : 0u, hi = d < la ? d : la;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (a[mid] <= b[d - 1 - mid])
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+// Long ranges, one block each (grid-stride over the list): tiles of
+// kLongTile entries are sorted in shared memory (bitonic), then runs are
+// merged pairwise (merge path split over the block's threads) between the
+// range and the same range of tmp, until one run is left.
+constexpr int kLongThreads = 1024;
+constexpr int kLongTile = 4096;
+__global__ void __launch_bounds__(kLongThreads) k_cell_order_long(const uint32_t *__restrict__ start,
+                                                                  const uint32_t *__restrict__ long_list,
+                                                                  const uint32_t *__restrict__ long_count,
+                                                                  uint32_t *__restrict__ perm,
+                                                                  uint32_t *__restrict__ tmp) {
+  __shared__ uint32_t sm[kLongTile];
+  const uint32_t nl = *long_count;
+  const int tid = threadIdx.x;
+  for (uint32_t li = blockIdx.x; li < nl; li += gridDim.x) {
+    const uint32_t e = long_list[li];
+    const uint32_t lo = start[e], m = start[e + 1] - lo;
+    uint32_t *a = perm + lo;
+    for (uint32_t t0 = 0; t0 < m; t0 += kLongTile) {
+      const uint32_t len = min((uint32_t)kLongTile, m - t0);
+      for (int i = tid; i < kLongTile; i += kLongThreads) sm[i] = (uint32_t)i < len ? a[t0 + i] : 0xFFFFFFFFu;
+      __syncthreads();
+      for (int k = 2; k <= kLongTile; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+          for (int i = tid; i < kLongTile; i += kLongThreads) {
+            const int ixj = i ^ j;
+            if (ixj > i) {
+              const uint32_t x = sm[i], y = sm[ixj];
+              if ((x > y) == ((i & k) == 0)) {
+                sm[i] = y;
+                sm[ixj] = x;
+              }
+            }
+          }
+          __syncthreads();
+        }
+      for (int i = tid; (uint32_t)i < len; i += kLongThreads) a[t0 + i] = sm[i];
+      __syncthreads();
+    }
+    uint32_t *src = a, *dst = tmp + lo;
+    for (uint32_t w = kLongTile; w < m; w <<= 1) {
+      for (uint32_t p0 = 0; p0 < m; p0 += 2 * w) {
+        const uint32_t l1 = min(w, m - p0), l2 = min(w, m - p0 - l1), L = l1 + l2;
+        const uint32_t *A = src + p0, *B = src + p0 + l1;
+        const uint32_t d0 = (uint32_t)(((uint64_t)L * tid) / kLongThreads);
+        const uint32_t d1 = (uint32_t)(((uint64_t)L * (tid + 1)) / kLongThreads);
+        uint32_t i = merge_split(A, l1, B, l2, d0), j = d0 - i;
+        for (uint32_t d = d0; d < d1; ++d) {
+          if (j >= l2 || (i < l1 && A[i] <= B[j]))
+            dst[p0 + d] = A[i++];
+          else
+            dst[p0 + d] = B[j++];
+        }
+      }
+      __syncthreads();
+      uint32_t *t = src;
+      src = dst;
+      dst = t;
+    }
+    if (src != a)
+      for (uint32_t i = tid; i < m; i += kLongThreads) a[i] = src[i];
+    __syncthreads();
+  }
+}
+
+// sorted slot i < count takes input record perm[i]; slots [count, n) are
+// dead (the grid bound n stays the old count until the host reads the new one)
+__global__ void k_sort_gather_mixed(MixedParts P, int64_t n, MixedParts Q, const uint32_t *__restrict__ perm,
+                                    const uint32_t *__restrict__ count) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (i >= (int64_t)*count) {
+    Q.c[i] = MPG_DEAD;
+    return;
+  }
+  const uint32_t p = perm[i];
+  Q.c[i] = P.c[p];
+  Q.b[i] = P.b[p];
+  Q.v[i] = P.v[p];
+  if (P.id) Q.id[i] = P.id[p];
+}
+
+__global__ void k_sort_gather_plain(PlainParts P, PlainParts Q, const uint32_t *__restrict__ perm,
+                                    const uint32_t *__restrict__ count) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)*count) return;
+  const int64_t p = perm[i];
+  Q.cell[i] = P.cell[p];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    Q.x[d * Q.cap + i] = P.x[d * P.cap + p];
+    Q.xr[d * Q.cap + i] = P.xr[d * P.cap + p];
+    Q.v[d * Q.cap + i] = P.v[d * P.cap + p];
+  }
+  Q.w[i] = P.w[p];
+  Q.sp[i] = P.sp[p];
+  if (P.id) Q.id[i] = P.id[p];
 }
 
 __global__ void k_copy_u32(const uint32_t *src, uint32_t *dst) { *dst = *src; }
 
-// slots at or beyond the device count are dead (after a sort the grid bound
-// stays at the old count until the host reads the new one)
+// initial guess of the next solve from the last solutions (see launch_extrapolate)
 __global__ void k_extrapolate(int64_t n, double *__restrict__ phi, double *__restrict__ prev,
                               double *__restrict__ prev2) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -764,10 +926,6 @@ __global__ void k_extrapolate(int64_t n, double *__restrict__ phi, double *__res
   prev[i] = a;
 }
 
-__global__ void k_mark_tail_dead(uint32_t *c, int64_t n, const uint32_t *count) {
-  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p < n && p >= (int64_t)*count) c[p] = MPG_DEAD;
-}
 
 // ---------------------------------------------------------------------------
 // fills
@@ -1087,17 +1245,35 @@ void launch_mixed_move(cudaStream_t s, const MixedParts &P, int64_t n, const Dev
   k_mixed_move_persistent<<<want < wave ? want : wave, kThreads, 0, s>>>(P, n, M.mrec, M.mnbr, M.c2n, S, dt, kill,
                                                                          max_cross, acc, st);
 }
-void launch_mixed_sort(cudaStream_t s, const MixedParts &P, int64_t n, const MixedParts &Q, int64_t T, uint32_t *cnt,
-                       uint32_t *start, uint32_t *scratch, int64_t scratch_len, uint32_t *d_count) {
-  cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * T, s);
-  if (n > 0) k_cell_hist<<<grid_for(n), kThreads, 0, s>>>(P.c, n, cnt);
-  scan_u32(s, cnt, start, T, scratch, scratch_len);
-  cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * T, s);
-  if (n > 0) k_cell_scatter<<<grid_for(n), kThreads, 0, s>>>(P, n, Q, start, cnt);
-  k_copy_u32<<<1, 1, 0, s>>>(start + T, d_count);
+// the five passes of the stable cell sort; leaves perm[0..count) and start
+// (T + 1 entries) behind, and the count in *d_count
+template <bool kMixed>
+static void cell_sort_order(cudaStream_t s, const uint32_t *keys, int64_t n, int64_t T, const SortWork &w,
+                            uint32_t *tmp, uint32_t *d_count) {
+  cudaMemsetAsync(w.cnt, 0, sizeof(uint32_t) * T, s);
+  cudaMemsetAsync(w.long_count, 0, sizeof(uint32_t), s);
+  if (n > 0) k_cell_hist<kMixed><<<grid_for(n), kThreads, 0, s>>>(keys, n, w.cnt);
+  scan_u32(s, w.cnt, w.start, T, w.scan_scratch, w.scan_len);
+  cudaMemsetAsync(w.cnt, 0, sizeof(uint32_t) * T, s);
+  if (n > 0) k_cell_slots<kMixed><<<grid_for(n), kThreads, 0, s>>>(keys, n, w.start, w.cnt, w.perm);
+  k_cell_order<<<grid_for(T), kThreads, 0, s>>>(w.start, T, w.perm, w.long_list, w.long_count);
+  k_cell_order_long<<<w.long_blocks, kLongThreads, 0, s>>>(w.start, w.long_list, w.long_count, w.perm, tmp);
+  k_copy_u32<<<1, 1, 0, s>>>(w.start + T, d_count);
 }
-void launch_mark_tail_dead(cudaStream_t s, uint32_t *c, int64_t n, const uint32_t *count) {
-  if (n > 0) k_mark_tail_dead<<<grid_for(n), kThreads, 0, s>>>(c, n, count);
+void launch_mixed_sort(cudaStream_t s, const MixedParts &P, int64_t n, const MixedParts &Q, int64_t T,
+                       const SortWork &w, uint32_t *d_count) {
+  cell_sort_order<true>(s, P.c, n, T, w, Q.c, d_count);
+  if (n > 0) k_sort_gather_mixed<<<grid_for(n), kThreads, 0, s>>>(P, n, Q, w.perm, d_count);
+}
+void launch_plain_sort(cudaStream_t s, const PlainParts &P, int64_t n, const PlainParts &Q, int64_t T,
+                       const SortWork &w, uint32_t *d_count) {
+  cell_sort_order<false>(s, (const uint32_t *)P.cell, n, T, w, (uint32_t *)Q.cell, d_count);
+  if (n > 0) k_sort_gather_plain<<<grid_for(n), kThreads, 0, s>>>(P, Q, w.perm, d_count);
+}
+int sort_long_blocks(int device) {
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  return 2 * (sms > 0 ? sms : 1);
 }
 void launch_extrapolate(cudaStream_t s, int64_t n, double *phi, double *prev, double *prev2) {
   if (n > 0) k_extrapolate<<<grid_for(n), kThreads, 0, s>>>(n, phi, prev, prev2);

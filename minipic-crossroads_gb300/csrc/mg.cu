@@ -20,48 +20,14 @@
 #include "mpg_device.cuh"
 #include "mpg_kernels.h"
 
-#ifdef MPG_CG_PROFILE
-// optional phase timing (compile with -DMPG_CG_PROFILE), SM cycles of block 0:
-// [2 q] work before the q-th grid barrier of an inner iteration, [2 q + 1]
-// the wait in it; [63] inner iterations
-__device__ unsigned long long g_mg_prof[64];
-extern "C" int mpg_probe_mg_profile(unsigned long long *out) {
-  return cudaMemcpyFromSymbol(out, g_mg_prof, sizeof(g_mg_prof)) == cudaSuccess ? 0 : -2;
-}
-#endif
-
 namespace {
 
-// grid barrier with the optional per-barrier timing
+// grid barrier of the cooperative solve (epoch-counted, bounded wait)
 struct MgSync {
   DevStats *st;
   unsigned epoch = 0;
-#ifdef MPG_CG_PROFILE
-  int q = 0;
-  unsigned long long last = 0;
-#endif
-  __device__ bool operator()() {
-#ifdef MPG_CG_PROFILE
-    const bool rec = blockIdx.x == 0 && threadIdx.x == 0 && q < 31;
-    unsigned long long t0 = clock64();
-    if (rec && last) g_mg_prof[2 * q] += t0 - last;
-    const bool ok = grid_barrier(st, gridDim.x, epoch);
-    const unsigned long long t1 = clock64();
-    if (rec && last) g_mg_prof[2 * q + 1] += t1 - t0;
-    last = t1;
-    ++q;
-    return ok;
-#else
-    return grid_barrier(st, gridDim.x, epoch);
-#endif
-  }
-  // start of an inner iteration's barrier numbering
-  __device__ void iteration() {
-#ifdef MPG_CG_PROFILE
-    if (blockIdx.x == 0 && threadIdx.x == 0 && last) g_mg_prof[63] += 1;
-    q = 0;
-#endif
-  }
+  __device__ bool operator()() { return grid_barrier(st, gridDim.x, epoch); }
+  __device__ void iteration() {}
 };
 
 constexpr int kRecMg = 5;  // block records each of the first 128 threads gathers (grids up to 640 blocks)

@@ -78,11 +78,28 @@ void launch_node_quanta(cudaStream_t s, const DevMesh &M, const unsigned long lo
 void launch_efield_mixed(cudaStream_t s, const DevMesh &M, const double *phi);
 void launch_mixed_move(cudaStream_t s, const MixedParts &P, int64_t n, const DevMesh &M, const SpeciesTable &S,
                        float dt, int kill, int max_cross, unsigned long long *acc, DevStats *st);
-// counting sort by cell: drops dead particles; *d_count receives the new count
+// Scratch of the stable cell sort: per-cell counts and starts (start holds
+// T + 1 entries: the first sorted position of every cell, start[T] = count),
+// the permutation (one uint32 per particle slot), the list of cells with long
+// ranges (cap / 32 + 1 entries) and its counter, the scan scratch.
+struct SortWork {
+  uint32_t *cnt = nullptr, *start = nullptr, *perm = nullptr, *long_list = nullptr, *long_count = nullptr;
+  uint32_t *scan_scratch = nullptr;
+  int64_t scan_len = 0;
+  int long_blocks = 1;
+};
+// Stable counting sort by cell (ParticleList::sort, particle_list.cpp:90-146):
+// live particles of P in cell order, inside a cell in their input order, into
+// Q; dead particles are dropped; *d_count receives the new count.  The mixed
+// form marks the slots [count, n) of Q dead.  Particle slots must number
+// fewer than 2^32.
 void launch_mixed_sort(cudaStream_t s, const MixedParts &P, int64_t n, const MixedParts &Q, int64_t T,
-                       uint32_t *cnt, uint32_t *start, uint32_t *scratch, int64_t scratch_len, uint32_t *d_count);
+                       const SortWork &w, uint32_t *d_count);
+void launch_plain_sort(cudaStream_t s, const PlainParts &P, int64_t n, const PlainParts &Q, int64_t T,
+                       const SortWork &w, uint32_t *d_count);
+// blocks of the long-range pass (two per SM)
+int sort_long_blocks(int device);
 
-void launch_mark_tail_dead(cudaStream_t s, uint32_t *c, int64_t n, const uint32_t *count);
 // initial guess from the last solutions: phi <- 2 phi - prev (prev2 null) or
 // phi <- 3 phi - 3 prev + prev2; the history shifts by one
 void launch_extrapolate(cudaStream_t s, int64_t n, double *phi, double *prev, double *prev2);

@@ -26,22 +26,6 @@
 #include "minipic_gb300.h"
 #include "mpg_kernels.h"
 
-#ifdef MPG_CG_PROFILE
-// optional phase timing of the mixed inner loop (compile with -DMPG_CG_PROFILE),
-// in SM cycles of block 0: [0] compute, [1] barrier wait, [2] grid totals,
-// [3] iterations, [4] row loop only, [5] block reduction + partial store
-__device__ unsigned long long g_cg_prof[8];
-// per block (up to 1024): [0] compute + block reduction, [1] barrier wait, [2] grid totals
-__device__ unsigned long long g_cg_prof_blk[1024 * 3];
-__device__ __forceinline__ unsigned long long gtimer() { return (unsigned long long)clock64(); }
-extern "C" int mpg_probe_cg_profile(unsigned long long *out) {
-  return cudaMemcpyFromSymbol(out, g_cg_prof, sizeof(g_cg_prof)) == cudaSuccess ? 0 : -2;
-}
-extern "C" int mpg_probe_cg_profile_blocks(unsigned long long *out) {
-  return cudaMemcpyFromSymbol(out, g_cg_prof_blk, sizeof(g_cg_prof_blk)) == cudaSuccess ? 0 : -2;
-}
-#endif
-
 namespace {
 
 constexpr int kSlots = 4;  // partial sums per phase
@@ -440,9 +424,6 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
       ff rn = ff_add(rho, ff_mulf(rq, -2.f * af));
       rn = ff_add(rn, ff_mulf(ff_mulf(qq, af), af));
       const float bf = rn.hi > 0.f ? rn.hi / rho.hi : 0.f;
-#ifdef MPG_CG_PROFILE
-      const unsigned long long tA = gtimer();
-#endif
       const float4 *vk = a.v[cur];
       float4 *vnx = a.v[cur ^ 1];
       ff dpq = {0.f, 0.f}, drq = {0.f, 0.f}, dqq = {0.f, 0.f}, drr = {0.f, 0.f};
@@ -470,9 +451,6 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
         dqq = ff_add(dqq, ff_prod(s, s));
         drr = ff_add(drr, ff_prod(ri, ri));
       }
-#ifdef MPG_CG_PROFILE
-      const unsigned long long tL = gtimer();
-#endif
       set = phase & 1;
       {
         // block partials: FP32 warp trees (each thread holds its rows'
@@ -501,13 +479,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
           }
         }
       }
-#ifdef MPG_CG_PROFILE
-      const unsigned long long tB = gtimer();
-#endif
       if (!grid_barrier(a.st, nb, epoch)) return;
-#ifdef MPG_CG_PROFILE
-      const unsigned long long tC = gtimer();
-#endif
       // grid totals: the first four warps load every block record up front
       // (thread t: records t, t + 128, ...; one L2 round trip), add them in
       // float-float, reduce across lanes and across the four warps.  Same
@@ -554,23 +526,6 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
       rq = smt[1];
       qq = smt[2];
       rho = smt[3];
-#ifdef MPG_CG_PROFILE
-      if (threadIdx.x == 0 && bid < 1024) {
-        const unsigned long long tE = gtimer();
-        g_cg_prof_blk[3 * bid + 0] += tB - tA;
-        g_cg_prof_blk[3 * bid + 1] += tC - tB;
-        g_cg_prof_blk[3 * bid + 2] += tE - tC;
-      }
-      if (bid == 0 && threadIdx.x == 0) {
-        const unsigned long long tD = gtimer();
-        g_cg_prof[0] += tB - tA;
-        g_cg_prof[1] += tC - tB;
-        g_cg_prof[2] += tD - tC;
-        g_cg_prof[3] += 1;
-        g_cg_prof[4] += tL - tA;
-        g_cg_prof[5] += tB - tL;
-      }
-#endif
       ++phase;
       cur ^= 1;
       ++total_inner;

@@ -897,6 +897,35 @@ extern "C" int64_t orc_compact(int mode, int64_t n, int32_t *cell, double *x, do
   return nnew;
 }
 
+/* ------------------------------------------------------------------------ */
+/* sort by element                                                           */
+/* ParticleList::sort and compute_start_particles_by_element
+ * (particle_list.cpp:90-146): the particle list ordered by element.  The
+ * reference's Kokkos BinSort is built with sort_within_bins = false
+ * (particle_list.cpp:100), which leaves the order inside an element open; here
+ * it is the input order (std::stable_sort by element).  Entries with cell < 0
+ * (dead) are dropped.  perm[k] = input index of the k-th particle of the
+ * sorted list; start[e] = first sorted position whose element is >= e (the
+ * bisection of particle_list.cpp:118-133, i.e. lower_bound), start[T] =
+ * count.  Returns the count. */
+extern "C" int64_t orc_sort_by_cell(int64_t n, const int32_t *cell, int64_t T, int64_t *perm, int64_t *start) {
+  std::vector<int64_t> idx;
+  idx.reserve(n);
+  for (int64_t p = 0; p < n; ++p)
+    if (cell[p] >= 0) idx.push_back(p);
+  std::stable_sort(idx.begin(), idx.end(), [&](int64_t a, int64_t b) { return cell[a] < cell[b]; });
+  const int64_t m = (int64_t)idx.size();
+  for (int64_t k = 0; k < m; ++k) perm[k] = idx[k];
+  if (start) {
+    int64_t k = 0;
+    for (int64_t e = 0; e <= T; ++e) {
+      while (k < m && cell[idx[k]] < e) ++k;
+      start[e] = k;
+    }
+  }
+  return m;
+}
+
 extern "C" double orc_kinetic(int64_t n, const double *v, const double *w, const int32_t *sp, const double *mass,
                               int nthreads) {
   // PIC.cpp:191-200

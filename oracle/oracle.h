@@ -120,6 +120,13 @@ int64_t orc_walk(const orc_mesh *m, int64_t n, int32_t *cell, double *x,
 int64_t orc_compact(int mode, int64_t n, int32_t *cell, double *x, double *xref,
                     double *v, double *w, int32_t *sp, int64_t *id);
 
+/* ParticleList::sort + compute_start_particles_by_element
+ * (particle_list.cpp:90-146) with the order inside an element fixed to the
+ * input order (stable sort by element), dead (cell < 0) dropped: perm[k] =
+ * input index of sorted position k, start[T+1] = first position of each
+ * element (start may be NULL).  Returns the count. */
+int64_t orc_sort_by_cell(int64_t n, const int32_t *cell, int64_t T, int64_t *perm, int64_t *start);
+
 double orc_kinetic(int64_t n, const double *v, const double *w, const int32_t *sp,
                    const double *m_of_species, int nthreads);
 

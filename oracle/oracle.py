@@ -77,6 +77,8 @@ def lib():
         L.orc_compact.restype = I64
         L.orc_compact.argtypes = [I32, I64, P, P, P, P, P, P, P]
         L.orc_kinetic.restype = D
+        L.orc_sort_by_cell.restype = I64
+        L.orc_sort_by_cell.argtypes = [I64, P, I64, P, P]
         L.orc_kinetic.argtypes = [I64, P, P, P, P, I32]
         L.orc_fill_ref.restype = I64
         L.orc_fill_ref.argtypes = [P, I32, I32, D, P, D, D, I64, P, P, P, P, P, P]
@@ -265,6 +267,17 @@ def compact(parts, mode=1):
     parts.n = lib().orc_compact(mode, parts.n, ptr(parts.cell), ptr(parts.x), ptr(parts.xref), ptr(parts.v),
                                 ptr(parts.w), ptr(parts.sp), ptr(parts.id))
     return parts.n
+
+
+def sort_by_cell(cell, T):
+    """Stable sort by element (ParticleList::sort, particle_list.cpp:90-146):
+    (perm, start) with perm[k] the input index of sorted position k (dead
+    entries, cell < 0, dropped) and start[e] the first position of element e."""
+    cell = np.ascontiguousarray(cell, np.int32)
+    perm = np.zeros(len(cell), np.int64)
+    start = np.zeros(T + 1, np.int64)
+    m = lib().orc_sort_by_cell(len(cell), ptr(cell), T, ptr(perm), ptr(start))
+    return perm[:m], start
 
 
 def kinetic(parts, m_of_species):

@@ -242,6 +242,71 @@ def test_config1_plain_steps_match_oracle(mpg, orc):
     assert np.abs(g["x"][a] - P.x[b]).max() < 1e-8
 
 
+def _by_id(ids, *arrays):
+    order = np.argsort(ids, kind="stable")
+    return (ids[order],) + tuple(a[order] for a in arrays)
+
+
+def test_config1_full_run_matches_oracle(mpg, orc, capsys):
+    """The plain-FP64 configuration as specified: 10^3 Kuhn cube of [0,1]^3,
+    100,000 electrons uniform in volume from seed 1, v_th = 0.05, uniform
+    neutralising background, phi = 0 on the boundary, absorbing walls,
+    dt = 0.01, 100 steps, CG to 1e-10 -- the GPU plain form against the
+    oracle from the same fill, never re-synchronised.
+
+    Per step: survivors, wall exits and face crossings equal the oracle's
+    exactly and the kinetic energy agrees to 1e-10; every 10 steps the
+    surviving particles, matched by id, sit in the same cells with positions
+    within 1e-9 and velocities within 1e-9 relative.  What differs between
+    the two is only floating-point summation order (the GPU deposit's atomic
+    order, the CG dot products' tree order), which moves phi by about the
+    solver tolerance; the test reports the largest position difference and
+    the cell flips it saw."""
+    n_side, n, steps = 10, 100000, 100
+    ctx, m = _mesh_pair(mpg, orc, n_side, 6, 0.0, 1.0)
+    ctx.configure(precision=mpg.PLAIN, deposit=mpg.DEPOSIT_LINEAR, solver=mpg.SOLVER_CG, tol=1e-10, max_iter=5000,
+                  warm_start=1, kill_on_wall=1, rho_background=1.0, track_ids=1)
+    ctx.reserve(n)
+    ctx.fill_uniform(n, 1, 0, 1.0 / n, vth=0.05)
+    P = orc.Particles(n)
+    P.fill_uniform(m, n, 1, 0, 1.0 / n, vth=0.05)
+    d = ctx.download()
+    assert (d["cell"] == P.cell).all() and (d["xref"] == P.xref).all()
+    # single-precision logf/cosf of the velocity draw may differ by an ulp
+    # between CUDA and glibc: both runs start from the GPU's velocities
+    P.v[:] = d["v"]
+    m.assemble(1)
+    bg = m.background(1.0)
+    phi = np.zeros(m.N)
+    cfg = orc.StepCfg(1, 1, 1e-10, 5000, 1, 1, 1, 1000, 1, 1)
+    worst_x, worst_v, flips, exits = 0.0, 0.0, 0, 0
+    for s in range(steps):
+        st = ctx.step(0.01, 1)
+        rc, ost, _ = orc.step(m, P, cfg, 0.01, [-1.0], [1.0], bg, phi)
+        assert rc == 0
+        assert st.n_alive == ost.n_alive, s
+        assert st.n_killed == ost.n_killed, s
+        assert st.n_crossings == ost.n_crossings, s
+        assert abs(st.ke - ost.ke) <= 1e-10 * ost.ke, s
+        exits += st.n_killed
+        if s % 10 == 9:
+            g = ctx.download()
+            gi, gc, gx, gv = _by_id(g["id"], g["cell"], g["x"], g["v"])
+            oi, oc, ox, ov = _by_id(P.id[: P.n].copy(), P.cell[: P.n].copy(), P.x[: P.n].copy(),
+                                    P.v[: P.n].copy())
+            assert (gi == oi).all(), s
+            flips += int((gc != oc).sum())
+            worst_x = max(worst_x, float(np.abs(gx - ox).max()))
+            worst_v = max(worst_v, float(np.abs(gv - ov).max() / np.abs(ov).max()))
+    assert flips == 0
+    assert worst_x <= 1e-9 and worst_v <= 1e-9
+    phi_gpu = ctx.get_field(mpg.FIELD_PHI)
+    assert np.abs(phi_gpu - phi).max() <= 1e-8 * np.abs(phi).max()
+    with capsys.disabled():
+        print(f"\nconfig 1 (100 steps): {exits} wall exits, survivors {st.n_alive}, cell flips {flips}, "
+              f"max |dx| {worst_x:.2e}, max |dv|/|v| {worst_v:.2e}")
+
+
 def test_capacity_and_argument_errors(mpg):
     ctx = mpg.Ctx(0)
     ctx.mesh(2, split=5, lo=-1, hi=1)

@@ -1,0 +1,92 @@
+"""GPU checks of the stable cell sort (ParticleList::sort and
+compute_start_particles_by_element, particle_list.cpp:90-146).
+
+Bit-exact against the oracle's std::stable_sort by cell (dead particles
+dropped): the permutation of the particle list, every record moved with its
+particle, and the start offsets per cell.  Inside a cell the list keeps its
+input order, so on a fill whose list is in id order the result is the
+(cell, id) order, and the same on every run.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _ctx(mpg, precision, n_side=8, jitter=0.0, **cfg):
+    ctx = mpg.Ctx(0)
+    ctx.mesh(n_side, split=mpg.SPLIT_KUHN6, mapping=mpg.MAP_JITTER if jitter else mpg.MAP_NONE, jitter=jitter,
+             seed=3)
+    base = dict(precision=precision, deposit=mpg.DEPOSIT_LINEAR, solver=mpg.SOLVER_CG, tol=1e-10, warm_start=1,
+                kill_on_wall=1, sort_interval=0, track_ids=1, rho_background=1.0)
+    base.update(cfg)
+    ctx.configure(**base)
+    return ctx
+
+
+@pytest.mark.parametrize("form", ["mixed", "plain"])
+def test_sort_permutation_matches_oracle_stable_sort(mpg, orc, form):
+    precision = mpg.MIXED if form == "mixed" else mpg.PLAIN
+    ctx = _ctx(mpg, precision, jitter=0.2)
+    n = 40000
+    ctx.reserve(n)
+    ctx.fill_uniform(n, 21, 0, 1.0 / n, vth=0.3)
+    # after a few steps the list is out of cell order and (mixed) holds dead slots
+    ctx.step(0.02, 3)
+    before = ctx.download()
+    perm, start = orc.sort_by_cell(before["cell"], ctx.T)
+    ctx.sort()
+    after = ctx.download()
+    assert len(after["cell"]) == len(perm) == ctx.count()
+    assert (after["id"] == before["id"][perm]).all()
+    assert (after["cell"] == before["cell"][perm]).all()
+    for k in ("x", "xref", "v", "w", "sp"):
+        assert (after[k] == before[k][perm]).all(), k
+    assert (ctx.cell_starts() == start).all()
+
+
+def test_sort_of_a_fresh_fill_is_cell_then_id_order(mpg, orc):
+    ctx = _ctx(mpg, mpg.MIXED, n_side=6)
+    n = 30000
+    ctx.reserve(n)
+    ctx.fill_uniform(n, 5, 0, 1.0 / n, vth=0.05)
+    ctx.sort()
+    d = ctx.download()
+    order = np.lexsort((d["id"], d["cell"]))
+    assert (order == np.arange(len(order))).all()
+    assert (np.sort(d["id"]) == np.arange(n)).all()
+
+
+def test_sort_long_cell_ranges_and_repeatability(mpg, orc):
+    """Cells holding more particles than one thread sorts (a 9000-particle
+    cell spans three shared-memory tiles and two merge passes) and a
+    shuffled input with dead slots: the mixed form keeps every cell's input
+    order, bit for bit, on two runs."""
+    ctx = _ctx(mpg, mpg.MIXED, n_side=4)
+    T = ctx.T
+    rng = np.random.default_rng(8)
+    n = 20000
+    cells = rng.integers(0, T, n).astype(np.uint32)
+    cells[rng.choice(n, 9000, replace=False)] = 7
+    cells[rng.choice(n, 600, replace=False)] = 11
+    dead = rng.choice(n, 500, replace=False)
+    cs = cells.copy()
+    cs[dead] = mpg.DEAD
+    b = np.full((n, 3), 0.25, np.float32)
+    v = np.zeros((n, 3), np.float32)
+    v[:, 0] = np.arange(n, dtype=np.float32)  # the input index, exact in FP32 below 2^24
+    ctx.species(0, -1.0, 1.0)
+    ctx.reserve(n)
+    ctx.fill_uniform(1, 1, 0, 1.0, vth=0.0)  # gives species 0 its weight
+    cell_oracle = np.where(cs == mpg.DEAD, -1, cs.astype(np.int64)).astype(np.int32)
+    perm, start = orc.sort_by_cell(cell_oracle, T)
+    runs = []
+    for _ in range(2):
+        ctx.mixed_upload(cs, b, v)
+        ctx.sort()
+        cs2, b2, v2 = ctx.mixed_download()
+        runs.append((cs2.copy(), v2.copy()))
+        assert (v2[:, 0].astype(np.int64) == perm).all()
+        assert (cs2 == cs[perm]).all()
+        assert (ctx.cell_starts() == start).all()
+    assert (runs[0][0] == runs[1][0]).all() and (runs[0][1] == runs[1][1]).all()

@@ -243,6 +243,21 @@ def test_compaction_modes(orc):
     assert list(P2.id[: P2.n]) == [0, 8, 2, 7, 4, 5]
 
 
+def test_sort_by_cell_known_answer(orc):
+    # ParticleList::sort + compute_start_particles_by_element: stable by cell,
+    # dead (-1) dropped, start = lower_bound of each element (particle_list.cpp:118-133)
+    cell = np.array([3, 1, -1, 1, 0, 3, 2, -1, 1], np.int32)
+    perm, start = orc.sort_by_cell(cell, 5)
+    assert perm.tolist() == [4, 1, 3, 8, 6, 0, 5]
+    assert start.tolist() == [0, 1, 4, 5, 7, 7]
+    rng = np.random.default_rng(3)
+    cell = rng.integers(-1, 50, 5000).astype(np.int32)
+    perm, start = orc.sort_by_cell(cell, 50)
+    live = np.flatnonzero(cell >= 0)
+    assert (perm == live[np.argsort(cell[live], kind="stable")]).all()
+    assert (start == np.searchsorted(cell[perm], np.arange(51), side="left")).all()
+
+
 def test_gather_ref_vs_per_tet(orc):
     # the reference's 48-term gather equals E_tet * sum(lambda): a few ulp apart
     m = orc.Mesh(6, split=6, mapping=4, jitter=0.2, seed=5)
