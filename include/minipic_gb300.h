@@ -184,6 +184,15 @@ int mpg_sort(mpg_ctx *ctx);
  * particles move, are added or are replaced (MPG_ERR_STATE otherwise). */
 int mpg_cell_starts(mpg_ctx *ctx, int64_t len, int64_t *start);
 
+/* Test of the failure path of the cooperative field solvers (no counterpart
+ * in the reference, whose solves run on the host): in the solves of later
+ * steps, block skip_block of the solver's grid does not arrive at its grid
+ * barriers, and a barrier wait gives up after poll_limit polls (0: the
+ * default of ~2^22, about a second).  The solve then ends without hanging:
+ * every block leaves the kernel, the step returns MPG_ERR_TIMEOUT and the
+ * ctx stays usable.  skip_block < 0 turns the test off. */
+int mpg_set_barrier_test(mpg_ctx *ctx, int skip_block, unsigned poll_limit);
+
 /* ES::rhs / ES::phi / set_analytic_RHS-style access (ES.hpp:53-71) */
 int mpg_get_field(mpg_ctx *ctx, int which, double *host);
 int mpg_set_field(mpg_ctx *ctx, int which, const double *host);
@@ -253,6 +262,18 @@ int mpg_batch_last_error(mpg_batch *b, char *buf, int len);
 int mpg_batch_set_tuning(mpg_batch *b, int cg_threads, int sort_interval);
 /* MPG_ERR_CAPACITY when the budget, the particle capacity or the slots are exhausted */
 int mpg_batch_admit(mpg_batch *b, const mpg_run_desc *desc, int *slot);
+/* mpg_batch_admit in two parts, so that the host work of an admission can
+ * overlap the batch's steps.  mpg_batch_prepare builds the run's mesh, field
+ * stencil and tables on the host: it touches no device and no batch, so any
+ * host thread may call it while another thread steps the batch.
+ * mpg_batch_admit_prepared uploads a prepared run into a free slot and fills
+ * its particles (between steps, on the thread that steps the batch); the prep
+ * stays the caller's (it may be admitted again, e.g. into another batch) until
+ * mpg_run_prep_destroy.  Same results as mpg_batch_admit. */
+typedef struct mpg_run_prep mpg_run_prep;
+int mpg_batch_prepare(const mpg_run_desc *desc, mpg_run_prep **out);
+int mpg_batch_admit_prepared(mpg_batch *b, const mpg_run_prep *prep, int *slot);
+int mpg_run_prep_destroy(mpg_run_prep *prep);
 int mpg_batch_step(mpg_batch *b, int n_steps, mpg_batch_stats *st);
 int mpg_batch_run_info(mpg_batch *b, int slot, mpg_run_info *info);
 int mpg_batch_run_phi(mpg_batch *b, int slot, double *phi);
@@ -286,10 +307,11 @@ int mpg_mg_hierarchy(const mpg_mesh_desc *mesh, int64_t dense_max, int level, in
  *
  * Same arguments and result as mpg_cg_csr, plus the stream to run on
  * (a cudaStream_t passed as void*, NULL = the default stream); the caller
- * owns and passes the CSR matrix, b and x (device pointers).  The first call
- * on a device looks up the array's device address and the solver's
- * co-residency limit for that device (the device current at the call); make
- * that first call before any stream capture.  All calls share the one array:
+ * owns and passes the CSR matrix, b and x (device pointers).  Every call looks
+ * up the array's device address in the current context (so a context reset
+ * between calls is harmless); the first call on a device also queries the
+ * solver's co-residency limit for that device (the device current at the
+ * call).  Make that first call before any stream capture.  All calls share the one array:
  * calls that overlap on the GPU (on different streams or host threads) race
  * and give wrong results; serialise them.  The array keeps the last call's
  * contents; the call clears the counters it needs at its start.  Status

@@ -32,8 +32,9 @@ EXPORTS = [
     "mpg_csr_download", "mpg_particles_reserve", "mpg_fill_ref", "mpg_fill_uniform", "mpg_particles_upload",
     "mpg_particles_download", "mpg_particles_count", "mpg_mixed_download", "mpg_mixed_upload",
     "mpg_charge_download", "mpg_weight_charge", "mpg_solve", "mpg_weight_efield", "mpg_move", "mpg_step",
-    "mpg_sort", "mpg_cell_starts", "mpg_get_field", "mpg_set_field", "mpg_cg_csr", "mpg_cg_csr_noalloc", "mpg_mg_hierarchy",
+    "mpg_sort", "mpg_cell_starts", "mpg_set_barrier_test", "mpg_get_field", "mpg_set_field", "mpg_cg_csr", "mpg_cg_csr_noalloc", "mpg_mg_hierarchy",
     "mpg_batch_create", "mpg_batch_destroy", "mpg_batch_last_error", "mpg_batch_set_tuning", "mpg_batch_admit",
+    "mpg_batch_prepare", "mpg_batch_admit_prepared", "mpg_run_prep_destroy",
     "mpg_batch_step", "mpg_batch_run_info", "mpg_batch_run_phi", "mpg_batch_run_particles", "mpg_batch_retire",
 ]
 NOALLOC_MAX_N = 131072
@@ -138,6 +139,7 @@ def load():
         "mpg_step": ([P, D, I, C.POINTER(StepStats)], I),
         "mpg_sort": ([P], I),
         "mpg_cell_starts": ([P, I64, P], I),
+        "mpg_set_barrier_test": ([P, I, C.c_uint], I),
         "mpg_get_field": ([P, I, P], I),
         "mpg_set_field": ([P, I, P], I),
         "mpg_cg_csr": ([P, I64, P, P, P, P, P, D, I, C.POINTER(I), C.POINTER(D)], I),
@@ -148,6 +150,9 @@ def load():
         "mpg_batch_last_error": ([P, C.c_char_p, I], I),
         "mpg_batch_set_tuning": ([P, I, I], I),
         "mpg_batch_admit": ([P, C.POINTER(RunDesc), C.POINTER(I)], I),
+        "mpg_batch_prepare": ([C.POINTER(RunDesc), C.POINTER(P)], I),
+        "mpg_batch_admit_prepared": ([P, P, C.POINTER(I)], I),
+        "mpg_run_prep_destroy": ([P], I),
         "mpg_batch_step": ([P, I, C.POINTER(BatchStats)], I),
         "mpg_batch_run_info": ([P, I, C.POINTER(RunInfo)], I),
         "mpg_batch_run_phi": ([P, I, P], I),
@@ -396,6 +401,11 @@ class Ctx:
     def sort(self):
         self._ck(self.L.mpg_sort(self.h))
 
+    def barrier_test(self, skip_block=-1, poll_limit=0):
+        """Make the field solves' grid barriers time out (block skip_block
+        does not arrive; waits give up after poll_limit polls); -1 turns it off."""
+        self._ck(self.L.mpg_set_barrier_test(self.h, int(skip_block), int(poll_limit)))
+
     def cell_starts(self):
         """start[e] = first list position of cell e after the last sort (T + 1 entries)."""
         a = np.zeros(self.T + 1, np.int64)
@@ -445,17 +455,30 @@ class Batch:
     def tuning(self, cg_threads=512, sort_interval=10):
         self._ck(self.L.mpg_batch_set_tuning(self.h, cg_threads, sort_interval))
 
-    def admit(self, n_side, n_particles, seed, q=-1.0, m=1.0, weight=None, vth=0.05, drift=(0.0, 0.0, 0.0),
-              rho_background=None, dt=0.01, tol=1e-10, max_iter=5000, steps=100, allow=()):
+    @staticmethod
+    def desc(n_side, n_particles, seed, q=-1.0, m=1.0, weight=None, vth=0.05, drift=(0.0, 0.0, 0.0),
+             rho_background=None, dt=0.01, tol=1e-10, max_iter=5000, steps=100):
         w = (1.0 / n_particles) if weight is None else weight
         rho = (-q * w * n_particles) if rho_background is None else rho_background
-        d = RunDesc(n_side, int(n_particles), seed, q, m, w, vth, (C.c_double * 3)(*drift), rho, dt, tol, max_iter,
-                    steps)
+        return RunDesc(n_side, int(n_particles), seed, q, m, w, vth, (C.c_double * 3)(*drift), rho, dt, tol,
+                       max_iter, steps)
+
+    def admit(self, n_side, n_particles, seed, allow=(), **kw):
+        d = self.desc(n_side, n_particles, seed, **kw)
         slot = C.c_int(-1)
         rc = self._ck(self.L.mpg_batch_admit(self.h, C.byref(d), C.byref(slot)), allow=allow)
         if rc != OK:
             return None
         self.n_nodes[slot.value] = (n_side + 1) ** 3
+        return slot.value
+
+    def admit_prepared(self, prep, allow=()):
+        """Admit a RunPrep (host part already done); None when it does not fit now."""
+        slot = C.c_int(-1)
+        rc = self._ck(self.L.mpg_batch_admit_prepared(self.h, prep.h, C.byref(slot)), allow=allow)
+        if rc != OK:
+            return None
+        self.n_nodes[slot.value] = (prep.n_side + 1) ** 3
         return slot.value
 
     def step(self, n=1, allow=()):
@@ -487,3 +510,29 @@ class Batch:
     def retire(self, slot):
         self._ck(self.L.mpg_batch_retire(self.h, slot))
         self.n_nodes.pop(slot, None)
+
+
+class RunPrep:
+    """The host part of a batch admission (mpg_batch_prepare): safe to build on
+    any thread while another thread steps a batch."""
+
+    def __init__(self, n_side, n_particles, seed, **kw):
+        self.L = load()
+        self.n_side = n_side
+        d = Batch.desc(n_side, n_particles, seed, **kw)
+        h = C.c_void_p()
+        rc = self.L.mpg_batch_prepare(C.byref(d), C.byref(h))
+        if rc != OK:
+            raise MpgError(rc, "mpg_batch_prepare failed")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.mpg_run_prep_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

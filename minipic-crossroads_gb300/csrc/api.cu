@@ -337,9 +337,15 @@ int ensure_cg_work(mpg_ctx *c, int64_t n) {
   return MPG_OK;
 }
 
-int sync_stats(mpg_ctx *c) {
+// device statistics to the host (no status check)
+int fetch_stats(mpg_ctx *c) {
   CK(cudaMemcpyAsync(c->h_stats, c->d_stats, sizeof(DevStats), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
+  return MPG_OK;
+}
+
+int sync_stats(mpg_ctx *c) {
+  TRY(fetch_stats(c));
   if (c->h_stats->bar_error) return fail(c, MPG_ERR_TIMEOUT, "solver grid barrier timed out");
   return MPG_OK;
 }
@@ -492,14 +498,15 @@ int sort_work(mpg_ctx *c, SortWork &w) {
     dfree(c, c->sort_perm);
     dfree(c, c->sort_long);
     TRY(dalloc(c, &c->sort_perm, std::max<int64_t>(c->cap, 1)));
-    TRY(dalloc(c, &c->sort_long, c->cap / 32 + 2));
+    TRY(dalloc(c, &c->sort_long, c->cap / 32 + 3));
     c->sort_perm_cap = c->cap;
   }
   w.cnt = c->sort_cnt;
   w.start = c->sort_start;
   w.perm = c->sort_perm;
   w.long_count = c->sort_long;
-  w.long_list = c->sort_long + 1;
+  w.long_list = c->sort_long + 2;
+  w.list_len = c->cap / 32 + 1;
   w.scan_scratch = c->scan_scratch;
   w.scan_len = c->scan_len;
   w.long_blocks = sort_long_blocks(c->device);
@@ -515,7 +522,7 @@ int sort_mixed(mpg_ctx *c) {
   TRY(sort_work(c, w));
   const int other = 1 - c->cur;
   launch_mixed_sort(c->stream, c->mp[c->cur], c->n, c->mp[other], c->dm.T, w, c->d_count);
-  c->launches += 9;
+  c->launches += 10;
   CKL();
   c->cur = other;
   c->starts_valid = true;
@@ -529,7 +536,7 @@ int sort_plain(mpg_ctx *c) {
   TRY(sort_work(c, w));
   const int other = 1 - c->cur;
   launch_plain_sort(c->stream, c->pp[c->cur], c->n, c->pp[other], c->dm.T, w, c->d_count);
-  c->launches += 9;
+  c->launches += 10;
   CKL();
   CK(cudaMemcpyAsync(c->h_count, c->d_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
@@ -584,13 +591,15 @@ int one_step(mpg_ctx *c, double dt, mpg_step_stats *acc_st, bool &sorted) {
       sorted = true;
     }
   } else {
-    // the plain form compacts whenever particles were removed (particle_list.cpp:148-164)
-    TRY(sync_stats(c));
+    // the plain form compacts whenever particles were removed (particle_list.cpp:148-164),
+    // also after a failed solve, so that the list stays consistent
+    TRY(fetch_stats(c));
     if (c->h_stats->n_killed > 0) {
       TRY(compact_plain(c));
       CK(cudaMemsetAsync(&c->d_stats->n_killed, 0, sizeof(unsigned long long), c->stream));
       acc_st->n_killed += (int64_t)c->h_stats->n_killed;
     }
+    if (c->h_stats->bar_error) return fail(c, MPG_ERR_TIMEOUT, "solver grid barrier timed out");
   }
   ev_record(c, 5);
   if (c->timing) {
@@ -639,6 +648,7 @@ int upload_mesh(mpg_ctx *c) {
   CK(cudaMemcpyAsync(d.nodes, h.nodes.data(), sizeof(double) * 3 * h.N, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(d.bnd, h.bnd.data(), h.N, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(d.mnbr, h.nbr_opp.data(), sizeof(uint4) * h.T, cudaMemcpyHostToDevice, s));
+  // walk record per tet: J^-1 (9 floats), E (3 floats, written by the E-field pass)
   std::vector<float> rec(12 * h.T), ratio;
   for (int64_t t = 0; t < h.T; ++t) {
     for (int q = 0; q < 9; ++q) rec[12 * t + q] = (float)h.jinv[9 * t + q];
@@ -1597,8 +1607,10 @@ int mpg_step(mpg_ctx *c, double dt, int n_steps, mpg_step_stats *st) {
   TRY(zero_stats(c));
   const int64_t launches0 = c->launches;
   bool sorted = false;
-  for (int i = 0; i < n_steps; ++i) TRY(one_step(c, dt, &acc, sorted));
-  TRY(sync_stats(c));
+  int rc = MPG_OK;
+  for (int i = 0; i < n_steps && rc == MPG_OK; ++i) rc = one_step(c, dt, &acc, sorted);
+  // the counts are brought up to date after a failed step too
+  TRY(fetch_stats(c));
   TRY(finish_counts_mixed(c, sorted));
   const DevStats &h = *c->h_stats;
   acc.ke = h.ke;
@@ -1618,8 +1630,13 @@ int mpg_step(mpg_ctx *c, double dt, int n_steps, mpg_step_stats *st) {
   else
     c->n_live = c->n;
   acc.n_alive = c->n_live;
-  acc.status = h.solver_fail ? MPG_ERR_NOT_CONVERGED : (h.n_limit ? MPG_ERR_WALK_LIMIT : MPG_OK);
+  acc.status = rc ? rc
+                  : h.bar_error ? MPG_ERR_TIMEOUT
+                  : h.solver_fail ? MPG_ERR_NOT_CONVERGED
+                  : (h.n_limit ? MPG_ERR_WALK_LIMIT : MPG_OK);
   if (st) *st = acc;
+  if (rc) return rc;  // the failed step set the message
+  if (h.bar_error) return fail(c, MPG_ERR_TIMEOUT, "solver grid barrier timed out");
   if (h.solver_fail) return fail(c, MPG_ERR_NOT_CONVERGED, "a field solve reached max_iter");
   if (h.n_limit) return fail(c, MPG_ERR_WALK_LIMIT, "%llu particles hit max_crossings", h.n_limit);
   return MPG_OK;
@@ -1636,6 +1653,13 @@ int mpg_sort(mpg_ctx *c) {
     TRY(sort_plain(c));
   }
   CK(cudaStreamSynchronize(c->stream));
+  return MPG_OK;
+}
+
+int mpg_set_barrier_test(mpg_ctx *c, int skip_block, unsigned poll_limit) {
+  ENTER(c);
+  c->cg.bar_skip = skip_block >= 0 ? skip_block + 1 : 0;
+  c->cg.bar_limit = poll_limit;
   return MPG_OK;
 }
 

@@ -672,6 +672,18 @@ struct Run {
 
 }  // namespace
 
+// host-side part of an admission (mpg_batch_prepare): the run's mesh, its
+// uniform stencil and the tables uploaded at admission
+struct mpg_run_prep {
+  mpg_run_desc d{};
+  HostMesh hm;
+  int off[kND] = {};
+  double s64[kND] = {};
+  std::vector<float> recv, ratio;
+  std::vector<double> bg;
+  std::vector<int32_t> n2c_off, c2n;
+};
+
 struct mpg_batch {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -1055,15 +1067,80 @@ int mpg_batch_set_tuning(mpg_batch *b, int cg_threads, int sort_interval) {
   return MPG_OK;
 }
 
-int mpg_batch_admit(mpg_batch *b, const mpg_run_desc *d, int *slot) {
-  if (!b || !d || !slot) return MPG_ERR_ARG;
-  BCK(cudaSetDevice(b->device));
-  *slot = -1;
+int mpg_batch_prepare(const mpg_run_desc *d, mpg_run_prep **out) {
+  if (!d || !out) return MPG_ERR_ARG;
+  *out = nullptr;
   // n >= 4: the stencil is read off the centre node's row, whose 14
   // neighbours must all be interior nodes
   if (d->n_side < 4 || d->n_particles < 0 || !(d->m > 0) || !(d->dt > 0) || !(d->tol > 0) || d->max_iter < 1 ||
       d->steps < 0)
-    return bfail(b, MPG_ERR_ARG, "bad run descriptor");
+    return MPG_ERR_ARG;
+  if (6LL * d->n_side * d->n_side * d->n_side >= (int64_t)MPG_WALL) return MPG_ERR_ARG;
+  mpg_run_prep *p = new (std::nothrow) mpg_run_prep();
+  if (!p) return MPG_ERR_ARG;
+  p->d = *d;
+  // mesh and stencil on the host
+  mpg_mesh_desc md{};
+  md.nx = md.ny = md.nz = d->n_side;
+  md.split = MPG_SPLIT_KUHN6;
+  md.lo = 0.0;
+  md.hi = 1.0;
+  md.mapping = MPG_MAP_NONE;
+  HostMesh &hm = p->hm;
+  std::string err;
+  int rc = host_mesh_generate(md, hm, err);
+  if (rc) {
+    delete p;
+    return rc;
+  }
+  std::vector<int32_t> rp, col;
+  std::vector<double> val;
+  host_csr_assemble(hm, 1, rp, col, val);
+  // stencil: the row of the centre node (all 15 neighbours interior for n >= 4)
+  const int64_t c = (int64_t)(d->n_side / 2) * (d->n_side + 1) * (d->n_side + 1) +
+                    (int64_t)(d->n_side / 2) * (d->n_side + 1) + d->n_side / 2;
+  if (rp[c + 1] - rp[c] != kND) {
+    delete p;
+    return MPG_ERR_MESH;
+  }
+  for (int k = 0; k < kND; ++k) {
+    p->off[k] = col[rp[c] + k] - (int32_t)c;
+    p->s64[k] = val[rp[c] + k];
+  }
+  p->recv.resize(12 * hm.T);
+  for (int64_t t = 0; t < hm.T; ++t) {
+    for (int q = 0; q < 9; ++q) p->recv[12 * t + q] = (float)hm.jinv[9 * t + q];
+    p->recv[12 * t + 9] = p->recv[12 * t + 10] = p->recv[12 * t + 11] = 0.f;
+  }
+  host_fill_ratio(hm, p->ratio);
+  host_background(hm, d->rho_background, p->bg);
+  host_charge_slots(hm, p->n2c_off, p->c2n);
+  *out = p;
+  return MPG_OK;
+}
+
+int mpg_run_prep_destroy(mpg_run_prep *p) {
+  delete p;
+  return MPG_OK;
+}
+
+int mpg_batch_admit(mpg_batch *b, const mpg_run_desc *d, int *slot) {
+  if (!b || !d || !slot) return MPG_ERR_ARG;
+  *slot = -1;
+  mpg_run_prep *p = nullptr;
+  const int rc = mpg_batch_prepare(d, &p);
+  if (rc) return bfail(b, rc, rc == MPG_ERR_MESH ? "unexpected stencil size" : "bad run descriptor");
+  const int rc2 = mpg_batch_admit_prepared(b, p, slot);
+  mpg_run_prep_destroy(p);
+  return rc2;
+}
+
+int mpg_batch_admit_prepared(mpg_batch *b, const mpg_run_prep *p, int *slot) {
+  if (!b || !p || !slot) return MPG_ERR_ARG;
+  BCK(cudaSetDevice(b->device));
+  *slot = -1;
+  const mpg_run_desc *d = &p->d;
+  const HostMesh &hm = p->hm;
   int used_runs = 0, s = -1;
   for (int k = 0; k < kMaxSlots; ++k) {
     if (b->runs[k].used)
@@ -1076,26 +1153,6 @@ int mpg_batch_admit(mpg_batch *b, const mpg_run_desc *d, int *slot) {
   if (b->used + need > b->budget) return bfail(b, MPG_ERR_CAPACITY, "device-memory budget exhausted");
   if (b->n + d->n_particles > b->cap && b->n > 0) BTRY(batch_sort(b));
   if (b->n + d->n_particles > b->cap) return bfail(b, MPG_ERR_CAPACITY, "particle capacity exhausted");
-  if (6LL * d->n_side * d->n_side * d->n_side >= (int64_t)MPG_WALL)
-    return bfail(b, MPG_ERR_ARG, "run mesh too large for 24-bit cell ids");
-  // mesh and stencil on the host
-  mpg_mesh_desc md{};
-  md.nx = md.ny = md.nz = d->n_side;
-  md.split = MPG_SPLIT_KUHN6;
-  md.lo = 0.0;
-  md.hi = 1.0;
-  md.mapping = MPG_MAP_NONE;
-  HostMesh hm;
-  std::string err;
-  int rc = host_mesh_generate(md, hm, err);
-  if (rc) return bfail(b, rc, "%s", err.c_str());
-  std::vector<int32_t> rp, col;
-  std::vector<double> val;
-  host_csr_assemble(hm, 1, rp, col, val);
-  // stencil: the row of the centre node (all 15 neighbours interior for n >= 2)
-  const int64_t c = (int64_t)(d->n_side / 2) * (d->n_side + 1) * (d->n_side + 1) +
-                    (int64_t)(d->n_side / 2) * (d->n_side + 1) + d->n_side / 2;
-  if (rp[c + 1] - rp[c] != kND) return bfail(b, MPG_ERR_MESH, "unexpected stencil size %d", rp[c + 1] - rp[c]);
   Run &r = b->runs[s];
   r = Run();
   r.used = true;
@@ -1106,9 +1163,9 @@ int mpg_batch_admit(mpg_batch *b, const mpg_run_desc *d, int *slot) {
   SlotDev &v = r.dev;
   v = SlotDev();
   for (int k = 0; k < kND; ++k) {
-    v.off[k] = col[rp[c] + k] - (int32_t)c;
-    v.s64[k] = val[rp[c] + k];
-    v.s32[k] = (float)val[rp[c] + k];
+    v.off[k] = p->off[k];
+    v.s64[k] = p->s64[k];
+    v.s32[k] = (float)p->s64[k];
   }
   v.T = hm.T;
   v.N = hm.N;
@@ -1124,7 +1181,12 @@ int mpg_batch_admit(mpg_batch *b, const mpg_run_desc *d, int *slot) {
   const double wq = fabs(d->weight * d->q);
   v.quantum = wq > 0 ? wq / 33554432.0 : 1.0;
   v.Q = (int)llround(d->weight * d->q / v.quantum);
-  // device buffers of the run
+  // device buffers of the run (freed again if an allocation fails)
+  auto undo = [&](int rc) {
+    free_run(r);
+    r = Run();
+    return rc;
+  };
   float4 *rec;
   uint4 *nbr;
   int4 *tets;
@@ -1134,44 +1196,27 @@ int mpg_batch_admit(mpg_batch *b, const mpg_run_desc *d, int *slot) {
   double *rhs, *phi, *bg, *r64;
   float *f[7];
   double *parts;
-  BTRY(balloc(b, &r, &rec, 3 * hm.T));
-  BTRY(balloc(b, &r, &nbr, hm.T));
-  BTRY(balloc(b, &r, &tets, hm.T));
-  BTRY(balloc(b, &r, &bnd, hm.N));
-  BTRY(balloc(b, &r, &ratio, hm.T));
-  BTRY(balloc(b, &r, &acc, 4 * hm.T));
   int32_t *n2c_off;
   int4 *c2n;
-  BTRY(balloc(b, &r, &n2c_off, hm.N + 1));
-  BTRY(balloc(b, &r, &c2n, hm.T));
-  BTRY(balloc(b, &r, &rhs, hm.N));
-  BTRY(balloc(b, &r, &phi, hm.N));
-  BTRY(balloc(b, &r, &bg, hm.N));
-  BTRY(balloc(b, &r, &r64, hm.N));
-  for (int k = 0; k < 7; ++k) BTRY(balloc(b, &r, &f[k], hm.N));
-  BTRY(balloc(b, &r, &parts, 8 * kMaxParts));
   double *phi_prev;
-  BTRY(balloc(b, &r, &phi_prev, hm.N));
-  std::vector<float> recv(12 * hm.T), ratio_h;
-  for (int64_t t = 0; t < hm.T; ++t) {
-    for (int q = 0; q < 9; ++q) recv[12 * t + q] = (float)hm.jinv[9 * t + q];
-    recv[12 * t + 9] = recv[12 * t + 10] = recv[12 * t + 11] = 0.f;
-  }
-  host_fill_ratio(hm, ratio_h);
-  std::vector<double> bgh;
-  host_background(hm, d->rho_background, bgh);
+  if (balloc(b, &r, &rec, 3 * hm.T) || balloc(b, &r, &nbr, hm.T) || balloc(b, &r, &tets, hm.T) ||
+      balloc(b, &r, &bnd, hm.N) || balloc(b, &r, &ratio, hm.T) || balloc(b, &r, &acc, 4 * hm.T) ||
+      balloc(b, &r, &n2c_off, hm.N + 1) || balloc(b, &r, &c2n, hm.T) || balloc(b, &r, &rhs, hm.N) ||
+      balloc(b, &r, &phi, hm.N) || balloc(b, &r, &bg, hm.N) || balloc(b, &r, &r64, hm.N) ||
+      balloc(b, &r, &parts, 8 * kMaxParts) || balloc(b, &r, &phi_prev, hm.N))
+    return undo(MPG_ERR_CUDA);
+  for (int k = 0; k < 7; ++k)
+    if (balloc(b, &r, &f[k], hm.N)) return undo(MPG_ERR_CUDA);
   cudaStream_t st = b->stream;
-  BCK(cudaMemcpyAsync(rec, recv.data(), sizeof(float) * 12 * hm.T, cudaMemcpyHostToDevice, st));
+  BCK(cudaMemcpyAsync(rec, p->recv.data(), sizeof(float) * 12 * hm.T, cudaMemcpyHostToDevice, st));
   BCK(cudaMemcpyAsync(nbr, hm.nbr_opp.data(), sizeof(uint4) * hm.T, cudaMemcpyHostToDevice, st));
   BCK(cudaMemcpyAsync(tets, hm.tets.data(), sizeof(int4) * hm.T, cudaMemcpyHostToDevice, st));
   BCK(cudaMemcpyAsync(bnd, hm.bnd.data(), hm.N, cudaMemcpyHostToDevice, st));
-  BCK(cudaMemcpyAsync(ratio, ratio_h.data(), sizeof(float) * hm.T, cudaMemcpyHostToDevice, st));
-  BCK(cudaMemcpyAsync(bg, bgh.data(), sizeof(double) * hm.N, cudaMemcpyHostToDevice, st));
+  BCK(cudaMemcpyAsync(ratio, p->ratio.data(), sizeof(float) * hm.T, cudaMemcpyHostToDevice, st));
+  BCK(cudaMemcpyAsync(bg, p->bg.data(), sizeof(double) * hm.N, cudaMemcpyHostToDevice, st));
   BCK(cudaMemsetAsync(acc, 0, sizeof(unsigned long long) * 4 * hm.T, st));
-  std::vector<int32_t> offh, c2nh;
-  host_charge_slots(hm, offh, c2nh);
-  BCK(cudaMemcpyAsync(n2c_off, offh.data(), sizeof(int32_t) * (hm.N + 1), cudaMemcpyHostToDevice, st));
-  BCK(cudaMemcpyAsync(c2n, c2nh.data(), sizeof(int32_t) * 4 * hm.T, cudaMemcpyHostToDevice, st));
+  BCK(cudaMemcpyAsync(n2c_off, p->n2c_off.data(), sizeof(int32_t) * (hm.N + 1), cudaMemcpyHostToDevice, st));
+  BCK(cudaMemcpyAsync(c2n, p->c2n.data(), sizeof(int32_t) * 4 * hm.T, cudaMemcpyHostToDevice, st));
   BCK(cudaMemsetAsync(phi, 0, sizeof(double) * hm.N, st));
   v.rec = rec;
   v.nbr = nbr;

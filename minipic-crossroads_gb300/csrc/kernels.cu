@@ -385,14 +385,23 @@ __global__ void __launch_bounds__(kThreads) k_plain_move(PlainParts P, int64_t n
   block_totals_push(&bt, ff{ke_hi, (float)(ke - (double)ke_hi)}, killed, cross, limit, st);
 }
 
-// stable compaction: count live particles per 4096-particle tile
+// Stable compaction by warp ballots over 4096-particle tiles.  A tile is
+// four rounds of 1024 consecutive particles; in a round thread t holds
+// particle t of the round, so every load and store of a warp covers
+// consecutive particles.  A particle's destination is the tile's offset +
+// the live particles of the tile's earlier rounds + those of earlier warps in
+// its round (a scan of 32 warp counts) + those of lower lanes in its warp
+// (popc of the ballot below the lane).
 __global__ void __launch_bounds__(kScanThreads) k_count_live(const int32_t *__restrict__ cell, int64_t n,
                                                              uint32_t *__restrict__ tile_cnt) {
   __shared__ uint32_t wt[32];
-  const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanPer;
+  const int64_t base = (int64_t)blockIdx.x * kScanTile + threadIdx.x;
   uint32_t s = 0;
-  for (int i = 0; i < kScanPer; ++i)
-    if (base + i < n && cell[base + i] >= 0) ++s;
+#pragma unroll
+  for (int r = 0; r < kScanPer; ++r) {
+    const int64_t e = base + (int64_t)r * kScanThreads;
+    if (e < n && cell[e] >= 0) ++s;
+  }
   uint32_t tot;
   block_exclusive_scan(s, wt, tot);
   if (threadIdx.x == 0) tile_cnt[blockIdx.x] = tot;
@@ -401,29 +410,44 @@ __global__ void __launch_bounds__(kScanThreads) k_count_live(const int32_t *__re
 __global__ void __launch_bounds__(kScanThreads) k_compact_plain(PlainParts P, int64_t n, PlainParts Q,
                                                                 const uint32_t *__restrict__ tile_off,
                                                                 int64_t ntiles, uint32_t *d_count) {
-  __shared__ uint32_t wt[32];
-  const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanPer;
-  uint32_t s = 0;
-  bool live[kScanPer];
-  for (int i = 0; i < kScanPer; ++i) {
-    live[i] = base + i < n && P.cell[base + i] >= 0;
-    s += live[i];
-  }
-  uint32_t tot;
-  uint32_t dst = block_exclusive_scan(s, wt, tot) + tile_off[blockIdx.x];
-  for (int i = 0; i < kScanPer; ++i) {
-    if (!live[i]) continue;
-    const int64_t a = base + i;
-    Q.cell[dst] = P.cell[a];
-    for (int d = 0; d < 3; ++d) {
-      Q.x[d * Q.cap + dst] = P.x[d * P.cap + a];
-      Q.xr[d * Q.cap + dst] = P.xr[d * P.cap + a];
-      Q.v[d * Q.cap + dst] = P.v[d * P.cap + a];
+  __shared__ uint32_t wcnt[32];
+  __shared__ uint32_t round_total;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t base = (int64_t)blockIdx.x * kScanTile + threadIdx.x;
+  uint32_t off = tile_off[blockIdx.x];
+  for (int r = 0; r < kScanPer; ++r) {
+    const int64_t e = base + (int64_t)r * kScanThreads;
+    const bool live = e < n && P.cell[e] >= 0;
+    const unsigned bal = __ballot_sync(0xffffffffu, live);
+    if (lane == 0) wcnt[wid] = __popc(bal);
+    __syncthreads();
+    if (wid == 0) {
+      const uint32_t c = lane < (kScanThreads >> 5) ? wcnt[lane] : 0u;
+      uint32_t x = c;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+      }
+      if (lane < (kScanThreads >> 5)) wcnt[lane] = x - c;  // exclusive
+      if (lane == 31) round_total = x;
     }
-    Q.w[dst] = P.w[a];
-    Q.sp[dst] = P.sp[a];
-    if (P.id) Q.id[dst] = P.id[a];
-    ++dst;
+    __syncthreads();
+    if (live) {
+      const uint32_t dst = off + wcnt[wid] + __popc(bal & ((1u << lane) - 1u));
+      Q.cell[dst] = P.cell[e];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        Q.x[d * Q.cap + dst] = P.x[d * P.cap + e];
+        Q.xr[d * Q.cap + dst] = P.xr[d * P.cap + e];
+        Q.v[d * Q.cap + dst] = P.v[d * P.cap + e];
+      }
+      Q.w[dst] = P.w[e];
+      Q.sp[dst] = P.sp[e];
+      if (P.id) Q.id[dst] = P.id[e];
+    }
+    off += round_total;
+    __syncthreads();
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) *d_count = tile_off[ntiles];
 }
@@ -444,8 +468,11 @@ __global__ void __launch_bounds__(kScanThreads) k_compact_plain(PlainParts P, in
 // range, and k_mixed_convert sums each node's range.  Integer addition is
 // associative, so the result does not depend on the grouping.  Every lane of
 // the warp must call this; lanes with key < 0 contribute nothing.
-__device__ __forceinline__ void deposit_fixed_warp(unsigned long long *__restrict__ acc, const int4 *__restrict__ c2n,
-                                                   int key, float b1, float b2, float b3, int Q) {
+// `slots(key)` gives the four slot indices of cell `key`; it is called by
+// the lanes that issue a run's atomics only.
+template <class Slots>
+__device__ __forceinline__ void deposit_fixed_warp_t(unsigned long long *__restrict__ acc, Slots slots, int key,
+                                                     float b1, float b2, float b3, int Q) {
   // |Q| <= 2^25 quanta, so a run of up to 32 lanes sums to < 2^30 in int32
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -467,7 +494,7 @@ __device__ __forceinline__ void deposit_fixed_warp(unsigned long long *__restric
     c2 = __reduce_add_sync(FULL, c2);
     c3 = __reduce_add_sync(FULL, c3);
     if (lane == 0 && key >= 0) {
-      const int4 q = c2n[key];
+      const int4 q = slots(key);
       atomicAdd(acc + q.x, (unsigned long long)(long long)c0);
       atomicAdd(acc + q.y, (unsigned long long)(long long)c1);
       atomicAdd(acc + q.z, (unsigned long long)(long long)c2);
@@ -493,12 +520,18 @@ __device__ __forceinline__ void deposit_fixed_warp(unsigned long long *__restric
   const int sn = __shfl_down_sync(FULL, seg, 1);
   const bool tail = lane == 31 || sn != seg;
   if (tail && key >= 0) {
-    const int4 q = c2n[key];
+    const int4 q = slots(key);
     atomicAdd(acc + q.x, (unsigned long long)(long long)c0);
     atomicAdd(acc + q.y, (unsigned long long)(long long)c1);
     atomicAdd(acc + q.z, (unsigned long long)(long long)c2);
     atomicAdd(acc + q.w, (unsigned long long)(long long)c3);
   }
+}
+
+// slot indices from the tet table c2n (a load per run)
+__device__ __forceinline__ void deposit_fixed_warp(unsigned long long *__restrict__ acc, const int4 *__restrict__ c2n,
+                                                   int key, float b1, float b2, float b3, int Q) {
+  deposit_fixed_warp_t(acc, [&](int k) { return c2n[k]; }, key, b1, b2, b3, Q);
 }
 
 __global__ void __launch_bounds__(kThreads) k_mixed_deposit(MixedParts P, int64_t n, const int4 *__restrict__ c2n,
@@ -764,16 +797,23 @@ __global__ void k_cell_slots(const uint32_t *__restrict__ c, int64_t n, const ui
 }
 
 // ranges of up to kSortLocal entries are sorted by one thread (insertion sort,
-// in registers and L1); longer ones are listed for k_cell_order_long
+// in registers and L1); ranges of up to kSortWarp entries are listed for
+// k_cell_order_warp (one warp each), longer ones for k_cell_order_long (one
+// block each).  The two lists share one buffer: medium ranges from the
+// front (counter long_count[0]), long ones from the back (long_count[1]).
 constexpr int kSortLocal = 32;
+constexpr int kSortWarp = 1024;
 __global__ void k_cell_order(const uint32_t *__restrict__ start, int64_t T, uint32_t *__restrict__ perm,
-                             uint32_t *__restrict__ long_list, uint32_t *__restrict__ long_count) {
+                             uint32_t *__restrict__ lists, int64_t list_len, uint32_t *__restrict__ long_count) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= T) return;
   const uint32_t lo = start[e], m = start[e + 1] - lo;
   if (m < 2) return;
   if (m > (uint32_t)kSortLocal) {
-    long_list[atomicAdd(long_count, 1u)] = (uint32_t)e;
+    if (m <= (uint32_t)kSortWarp)
+      lists[atomicAdd(long_count, 1u)] = (uint32_t)e;
+    else
+      lists[list_len - 1 - atomicAdd(long_count + 1, 1u)] = (uint32_t)e;
     return;
   }
   uint32_t a[kSortLocal];
@@ -810,6 +850,45 @@ __device__ __forceinline__ uint32_t merge_split(const uint32_t *a, uint32_t la, 
   return lo;
 }
 
+// Medium ranges, one warp each (warp-stride over the list): a bitonic sort of
+// the range padded to the next power of two, in the warp's shared-memory
+// slice, with warp-level synchronisation only.
+constexpr int kWarpSortThreads = 256;
+__global__ void __launch_bounds__(kWarpSortThreads) k_cell_order_warp(const uint32_t *__restrict__ start,
+                                                                     const uint32_t *__restrict__ lists,
+                                                                     const uint32_t *__restrict__ long_count,
+                                                                     uint32_t *__restrict__ perm) {
+  __shared__ uint32_t sm[(kWarpSortThreads / 32) * kSortWarp];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint32_t *a = sm + wid * kSortWarp;
+  const uint32_t nl = long_count[0];
+  const uint32_t nwarps = gridDim.x * (kWarpSortThreads / 32);
+  for (uint32_t li = blockIdx.x * (kWarpSortThreads / 32) + wid; li < nl; li += nwarps) {
+    const uint32_t e = lists[li];
+    const uint32_t lo = start[e], m = start[e + 1] - lo;
+    uint32_t P = 64;
+    while (P < m) P <<= 1;
+    for (uint32_t i = lane; i < P; i += 32) a[i] = i < m ? perm[lo + i] : 0xFFFFFFFFu;
+    __syncwarp();
+    for (uint32_t k = 2; k <= P; k <<= 1)
+      for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+        for (uint32_t i = lane; i < P; i += 32) {
+          const uint32_t ixj = i ^ j;
+          if (ixj > i) {
+            const uint32_t x = a[i], y = a[ixj];
+            if ((x > y) == ((i & k) == 0)) {
+              a[i] = y;
+              a[ixj] = x;
+            }
+          }
+        }
+        __syncwarp();
+      }
+    for (uint32_t i = lane; i < m; i += 32) perm[lo + i] = a[i];
+    __syncwarp();
+  }
+}
+
 // Long ranges, one block each (grid-stride over the list): tiles of
 // kLongTile entries are sorted in shared memory (bitonic), then runs are
 // merged pairwise (merge path split over the block's threads) between the
@@ -817,15 +896,16 @@ __device__ __forceinline__ uint32_t merge_split(const uint32_t *a, uint32_t la, 
 constexpr int kLongThreads = 1024;
 constexpr int kLongTile = 4096;
 __global__ void __launch_bounds__(kLongThreads) k_cell_order_long(const uint32_t *__restrict__ start,
-                                                                  const uint32_t *__restrict__ long_list,
+                                                                  const uint32_t *__restrict__ lists,
+                                                                  int64_t list_len,
                                                                   const uint32_t *__restrict__ long_count,
                                                                   uint32_t *__restrict__ perm,
                                                                   uint32_t *__restrict__ tmp) {
   __shared__ uint32_t sm[kLongTile];
-  const uint32_t nl = *long_count;
+  const uint32_t nl = long_count[1];
   const int tid = threadIdx.x;
   for (uint32_t li = blockIdx.x; li < nl; li += gridDim.x) {
-    const uint32_t e = long_list[li];
+    const uint32_t e = lists[list_len - 1 - li];
     const uint32_t lo = start[e], m = start[e + 1] - lo;
     uint32_t *a = perm + lo;
     for (uint32_t t0 = 0; t0 < m; t0 += kLongTile) {
@@ -1251,13 +1331,15 @@ template <bool kMixed>
 static void cell_sort_order(cudaStream_t s, const uint32_t *keys, int64_t n, int64_t T, const SortWork &w,
                             uint32_t *tmp, uint32_t *d_count) {
   cudaMemsetAsync(w.cnt, 0, sizeof(uint32_t) * T, s);
-  cudaMemsetAsync(w.long_count, 0, sizeof(uint32_t), s);
+  cudaMemsetAsync(w.long_count, 0, 2 * sizeof(uint32_t), s);
   if (n > 0) k_cell_hist<kMixed><<<grid_for(n), kThreads, 0, s>>>(keys, n, w.cnt);
   scan_u32(s, w.cnt, w.start, T, w.scan_scratch, w.scan_len);
   cudaMemsetAsync(w.cnt, 0, sizeof(uint32_t) * T, s);
   if (n > 0) k_cell_slots<kMixed><<<grid_for(n), kThreads, 0, s>>>(keys, n, w.start, w.cnt, w.perm);
-  k_cell_order<<<grid_for(T), kThreads, 0, s>>>(w.start, T, w.perm, w.long_list, w.long_count);
-  k_cell_order_long<<<w.long_blocks, kLongThreads, 0, s>>>(w.start, w.long_list, w.long_count, w.perm, tmp);
+  k_cell_order<<<grid_for(T), kThreads, 0, s>>>(w.start, T, w.perm, w.long_list, w.list_len, w.long_count);
+  k_cell_order_warp<<<w.long_blocks * 4, kWarpSortThreads, 0, s>>>(w.start, w.long_list, w.long_count, w.perm);
+  k_cell_order_long<<<w.long_blocks, kLongThreads, 0, s>>>(w.start, w.long_list, w.list_len, w.long_count, w.perm,
+                                                            tmp);
   k_copy_u32<<<1, 1, 0, s>>>(w.start + T, d_count);
 }
 void launch_mixed_sort(cudaStream_t s, const MixedParts &P, int64_t n, const MixedParts &Q, int64_t T,

@@ -92,7 +92,13 @@ __device__ __forceinline__ void level_ijk(const MgLevelDev &L, int64_t r, unsign
 }
 
 // restriction r_{l+1}[C] = sum_delta w(delta) t_l[2C + delta] over the 27 fine
-// nodes around 2C (w = 1/2 per non-zero component); zero on Dirichlet rows
+// nodes around 2C (w = 1/2 per non-zero component); zero on Dirichlet rows.
+// The host's Galerkin product leaves Dirichlet fine nodes out of P (on an odd
+// cell count the far boundary node 2C + 1 is one of the 27); this sum reads
+// them, which is the same because t is exactly zero on every Dirichlet row of
+// every level: the right-hand side r is zero there (the PCG residual of the
+// identity rows, and restrict_at's own zero on coarse Dirichlet rows), so
+// t = r - A (omega D^-1 r) = 0 - 1 * 0 on those rows.
 __device__ __forceinline__ float restrict_at(const MgLevelDev &F, const MgLevelDev &Cl, int64_t C) {
   if (Cl.bnd[C]) return 0.f;
   unsigned I, J, K;
@@ -142,6 +148,8 @@ __device__ __forceinline__ float dinv_at(const CgMgArgs &a, int l, const float *
   return (CST && l == 0) ? a.mg.dinv0 : dinv[j];
 }
 
+// Invariant relied on by restrict_at: on a Dirichlet (identity) row r = 0,
+// hence out = 0 there.
 template <int ND, bool CST, typename R>
 __device__ __forceinline__ void presmooth_residual(const CgMgArgs &a, int l, int64_t lo, int64_t hi, R rv,
                                                    float *__restrict__ out) {
@@ -632,10 +640,9 @@ int run_cg_mg(cudaStream_t s, const DiaMatrix &A, const MgDev &mg, const double 
   int cap = max_blocks;
   if (w.block_cap > 0 && w.block_cap < cap) cap = w.block_cap;
   const int nb = (int)(want < cap ? want : cap);
-  if (cudaMemsetAsync(&st->bar_count, 0, sizeof(unsigned), s) != cudaSuccess) return MPG_ERR_CUDA;
-  static const int mode0 = 0;
-  if (cudaMemcpyAsync(&st->bar_mode, &mode0, sizeof(int), cudaMemcpyHostToDevice, s) != cudaSuccess)
-    return MPG_ERR_CUDA;
+  CgWork wb = w;
+  wb.bar_mode = 0;  // the multigrid solver uses the fence + volatile-polling barrier
+  if (barrier_setup(s, st, wb)) return MPG_ERR_CUDA;
   void *args[] = {&a};
   cudaError_t e = cudaLaunchCooperativeKernel(mg_kernel_of(A.ndiag, A.constant != 0, th), dim3(nb), dim3(th), args, 0, s);
   return e == cudaSuccess ? MPG_OK : MPG_ERR_CUDA;

@@ -39,6 +39,11 @@ struct DevStats {
   unsigned int bar_gen;
   int bar_error;
   int bar_mode;  // 0: fence + volatile polling, 1: release/acquire
+  // test of the time-out path (mpg_set_barrier_test): block bar_skip - 1
+  // skips its arrivals (0 = none); bar_limit = polls before a wait gives up
+  // (0 = the default 2^22)
+  int bar_skip;
+  unsigned int bar_limit;
 };
 
 // -------------------------------------------------------------------------
@@ -48,9 +53,11 @@ struct DevStats {
 // (the host zeroes it before each launch).  Arrival is one release-reduction,
 // the wait is an acquire load, so the block's writes before the barrier are
 // visible to every block after it.  The wait is bounded: after ~2^22 polls
-// (about a second with the back-off) the block raises bar_error and returns
-// false; every later barrier sees the flag and returns false at once, so all
-// blocks leave the kernel.  `epoch` is a per-block counter (thread 0 only).
+// (about a second with the back-off; bar_limit when set) the block raises
+// bar_error and returns false; every later barrier sees the flag and returns
+// false at once, so all blocks leave the kernel.  `epoch` is a per-block
+// counter (thread 0 only).  A block named by bar_skip does not arrive (the
+// host-set test of this time-out path).
 __device__ __forceinline__ bool grid_barrier(DevStats *st, unsigned nblocks, unsigned &epoch) {
   __shared__ int ok;
   __syncthreads();
@@ -60,7 +67,10 @@ __device__ __forceinline__ bool grid_barrier(DevStats *st, unsigned nblocks, uns
     const unsigned target = epoch * nblocks;
     unsigned *cnt = &st->bar_count;
     const int mode = st->bar_mode;
-    if (mode == 0) {
+    const unsigned limit = st->bar_limit ? st->bar_limit : (1u << 22);
+    if (st->bar_skip == (int)blockIdx.x + 1) {
+      // no arrival (time-out test)
+    } else if (mode == 0) {
       // fence + relaxed arrival, volatile polling, fence
       __threadfence();
       atomicAdd(cnt, 1u);
@@ -80,7 +90,7 @@ __device__ __forceinline__ bool grid_barrier(DevStats *st, unsigned nblocks, uns
           ok = 0;
           break;
         }
-        if (spins > (1u << 22)) {
+        if (spins > limit) {
           atomicExch(&st->bar_error, 1);
           ok = 0;
           break;

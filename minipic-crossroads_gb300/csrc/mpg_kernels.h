@@ -80,10 +80,12 @@ void launch_mixed_move(cudaStream_t s, const MixedParts &P, int64_t n, const Dev
                        float dt, int kill, int max_cross, unsigned long long *acc, DevStats *st);
 // Scratch of the stable cell sort: per-cell counts and starts (start holds
 // T + 1 entries: the first sorted position of every cell, start[T] = count),
-// the permutation (one uint32 per particle slot), the list of cells with long
-// ranges (cap / 32 + 1 entries) and its counter, the scan scratch.
+// the permutation (one uint32 per particle slot), the lists of cells with
+// medium and long ranges (list_len >= cap / 32 + 1 entries in all) and their
+// two counters, the scan scratch.
 struct SortWork {
   uint32_t *cnt = nullptr, *start = nullptr, *perm = nullptr, *long_list = nullptr, *long_count = nullptr;
+  int64_t list_len = 0;
   uint32_t *scan_scratch = nullptr;
   int64_t scan_len = 0;
   int long_blocks = 1;
@@ -162,6 +164,8 @@ struct CgWork {
   double inner_safety = 0.5;
   int threads = 512;  // block size of the cooperative solver kernels (256, 512 or 1024)
   int bar_mode = 0;   // grid barrier flavour (0: fence + volatile polling, 1: release/acquire)
+  int bar_skip = 0;   // time-out test: block bar_skip - 1 skips its barrier arrivals (0 = none)
+  unsigned bar_limit = 0;  // polls before a barrier wait gives up (0 = the default)
   int block_cap = 0;  // > 0: at most this many blocks in the mixed solver's grid
 };
 // Geometric multigrid preconditioner of the mixed solver (mg.cu, mg_host.cpp):
@@ -214,3 +218,6 @@ int run_bicgstab(cudaStream_t s, int64_t n, const int32_t *rowptr, const int32_t
                  const double *b, double *x, double tol, int max_iter, double *work, double *red_dev,
                  double *red_host, int *iters, double *resid);
 int cg_max_blocks(int device, int threads);
+// zeroes the grid-barrier counter of st and sets its flavour and time-out
+// test fields from w, on stream s, before a cooperative launch
+int barrier_setup(cudaStream_t s, DevStats *st, const CgWork &w);

@@ -2,14 +2,32 @@
 //
 // Shared by the single-run kernel (kernels.cu) and the batched kernel
 // (batch.cu), so that a run advanced alone and a run advanced inside a batch
-// execute the same arithmetic.  The per-tet tables are run-local:
-// rec[3*e .. 3*e+2] = J^-1 (9 floats) + E (3 floats), nbr[e] = neighbour and
-// vertex permutation per face (indexed by the opposite vertex).
+// execute the same arithmetic.  The per-tet tables are reached through a
+// table policy `Tab` with
+//   load(e, r0, r1, r2): the tet's record, J^-1 (9 floats) + E (3 floats),
+//   face(e, k): the neighbour word of the face opposite vertex k of tet e
+//               (neighbour | vertex permutation << 24, MPG_WALL = wall).
+// RecTab3 reads the tables rec[3*e .. 3*e+2] and nbr[e] as needed (the
+// neighbour word only when the particle reaches a face).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include "mpg_device.cuh"
+
+struct RecTab3 {
+  const float4 *__restrict__ rec;
+  const uint4 *__restrict__ nbr;
+  __device__ __forceinline__ void load(uint32_t e, float4 &r0, float4 &r1, float4 &r2) const {
+    r0 = rec[3 * e];
+    r1 = rec[3 * e + 1];
+    r2 = rec[3 * e + 2];
+  }
+  __device__ __forceinline__ uint32_t face(uint32_t e, int k) const {
+    const uint4 nb4 = nbr[e];
+    return k == 0 ? nb4.x : k == 1 ? nb4.y : k == 2 ? nb4.z : nb4.w;
+  }
+};
 
 // Boris push with B = 0 (the two half kicks of particle_move.hpp:376-387,
 // hk = dt q/(2m)), then the walk across faces until dt is used up
@@ -17,13 +35,15 @@
 // through the vertex permutation; the entered face's coordinate is exactly
 // 0.  Returns the number of face crossings; *dead is set when the particle
 // left through an absorbing wall, *limit when max_cross was reached.
-__device__ __forceinline__ int mixed_walk(const float4 *__restrict__ rec, const uint4 *__restrict__ nbr, uint32_t &e,
-                                          float &l1, float &l2, float &l3, float &vx, float &vy, float &vz,
-                                          const float hk, const float dt, const int kill, const int max_cross,
-                                          bool &dead, bool &limit) {
+// The record of the start tet e is given in (r0, r1, r2); on return they
+// hold the record of the final tet.
+template <class Tab>
+__device__ __forceinline__ int mixed_walk_t(Tab &tab, uint32_t &e, float4 &r0, float4 &r1, float4 &r2, float &l1,
+                                            float &l2, float &l3, float &vx, float &vy, float &vz, const float hk,
+                                            const float dt, const int kill, const int max_cross, bool &dead,
+                                            bool &limit) {
   dead = false;
   limit = false;
-  float4 r0 = rec[3 * e], r1 = rec[3 * e + 1], r2 = rec[3 * e + 2];
   // Boris push with B = 0: the two half kicks of particle_move.hpp:376-387
   vx = __fmaf_rn(hk, r2.y, vx);
   vy = __fmaf_rn(hk, r2.z, vy);
@@ -76,8 +96,7 @@ __device__ __forceinline__ int mixed_walk(const float4 *__restrict__ rec, const 
                    __fmaf_rn(tmin, u3, l3)};
     nl[kmin] = 0.f;
     tleft = tleft - tmin;
-    const uint4 nb4 = nbr[e];
-    const uint32_t w = kmin == 0 ? nb4.x : kmin == 1 ? nb4.y : kmin == 2 ? nb4.z : nb4.w;
+    const uint32_t w = tab.face(e, kmin);
     const uint32_t nb = w & 0xFFFFFFu;
     if (nb == MPG_WALL) {
       if (kill) {
@@ -124,9 +143,18 @@ __device__ __forceinline__ int mixed_walk(const float4 *__restrict__ rec, const 
     l1 = ml[1];
     l2 = ml[2];
     l3 = ml[3];
-    r0 = rec[3 * e];
-    r1 = rec[3 * e + 1];
-    r2 = rec[3 * e + 2];
+    tab.load(e, r0, r1, r2);
   }
   return it;
+}
+
+// the walk on run-local tables rec[3*e ..] / nbr[e] (batch engine)
+__device__ __forceinline__ int mixed_walk(const float4 *__restrict__ rec, const uint4 *__restrict__ nbr, uint32_t &e,
+                                          float &l1, float &l2, float &l3, float &vx, float &vy, float &vz,
+                                          const float hk, const float dt, const int kill, const int max_cross,
+                                          bool &dead, bool &limit) {
+  RecTab3 tab{rec, nbr};
+  float4 r0, r1, r2;
+  tab.load(e, r0, r1, r2);
+  return mixed_walk_t(tab, e, r0, r1, r2, l1, l2, l3, vx, vy, vz, hk, dt, kill, max_cross, dead, limit);
 }

@@ -139,18 +139,21 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg64(Cg64Args a) {
 }
 
 // ---------------------------------------------------------------------------
-// plain FP64 CG on the DIA form: the CG_solve.hpp:54-114 recurrence, two grid
-// barriers per iteration.  ND is the exact diagonal count (15 for the Kuhn
-// split, 27 in general; the host pads with zero diagonals of offset 0), so
-// the diagonal loop unrolls without branches and all gathers of a row can be
-// in flight at once.
+// plain FP64 CG on the DIA form: the CG_solve.hpp:54-114 recurrence in its
+// own order (p = beta p + r, q = A p, p.q, x += alpha p, r -= alpha q, r.r),
+// three grid barriers per iteration.  GB300's FP64 pipe runs about 1/64 of
+// the FP32 rate, so the kernel is bound by FP64 instructions, not bytes: p is
+// formed once per row (a barrier before the product reads it) instead of
+// once per neighbour, and every multiply-add is one fused FP64 instruction
+// (15 for the product, 5 for the updates and dots per row).  ND is the exact
+// diagonal count (15 for the Kuhn split, 27 in general; the host pads with
+// zero diagonals of offset 0), so the diagonal loop unrolls without branches.
 struct Cg64DiaArgs {
   DiaMatrix A;
   const double *__restrict__ b;
   double *x;
   double *r;
-  double *p0;
-  double *p1;
+  double *p;
   double *q;
   double *partials;
   double tol2;
@@ -170,21 +173,22 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg64_dia(Cg64DiaArgs a) {
   double *P0 = a.partials, *P1 = a.partials + nb, *P2 = a.partials + 2 * nb;
   const double *__restrict__ val = a.A.val64;
   const uint8_t *__restrict__ bnd = a.A.bnd;
+  double *__restrict__ p = a.p;
   double rr = 0.0, bb = 0.0;
+  // r = b - A x (CG_solve.hpp:62-63); rho0 = b.b, rho = r.r
   for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
     double s = 0.0;
     if (bnd[i]) {
-      s += 1.0 * a.x[i];
+      s = a.x[i];
     } else {
 #pragma unroll
-      for (int d = 0; d < ND; ++d) {
-        s += val[d * n + i] * a.x[dia_nb(i, a.A.off[d], a.A.nwrap)];
-      }
+      for (int d = 0; d < ND; ++d) s = __fma_rn(val[d * n + i], a.x[dia_nb(i, a.A.off[d], a.A.nwrap)], s);
     }
-    const double ri = -1.0 * s + 1.0 * a.b[i];
+    const double bi = a.b[i];
+    const double ri = bi - s;
     a.r[i] = ri;
-    rr += ri * ri;
-    bb += a.b[i] * a.b[i];
+    rr = __fma_rn(ri, ri, rr);
+    bb = __fma_rn(bi, bi, bb);
   }
   double t = block_sum(rr, red);
   if (threadIdx.x == 0) P0[bid] = t;
@@ -203,38 +207,36 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg64_dia(Cg64DiaArgs a) {
         status = 1;
         break;
       }
+      // p = beta p + r (CG_solve.hpp:77-82)
       const double beta = iter == 0 ? 0.0 : rho / rho_old;
-      double *pk = (iter & 1) ? a.p1 : a.p0;
-      const double *pp = (iter & 1) ? a.p0 : a.p1;
-      const bool first = iter == 0;
+      for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x)
+        p[i] = iter == 0 ? a.r[i] : __fma_rn(beta, p[i], a.r[i]);
+      if (!grid_barrier(a.st, nb, epoch)) return;
+      // q = A p (:85), p.q (:87)
       double pq = 0.0;
       for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-        const double pki = first ? a.r[i] : beta * pp[i] + 1.0 * a.r[i];
+        const double pi = p[i];
         double s = 0.0;
         if (bnd[i]) {
-          s += 1.0 * pki;
+          s = pi;
         } else {
 #pragma unroll
-          for (int d = 0; d < ND; ++d) {
-                const int64_t j = dia_nb(i, a.A.off[d], a.A.nwrap);
-            const double pj = first ? a.r[j] : beta * pp[j] + 1.0 * a.r[j];
-            s += val[d * n + i] * pj;
-          }
+          for (int d = 0; d < ND; ++d) s = __fma_rn(val[d * n + i], p[dia_nb(i, a.A.off[d], a.A.nwrap)], s);
         }
-        pk[i] = pki;
         a.q[i] = s;
-        pq += pki * s;
+        pq = __fma_rn(pi, s, pq);
       }
       t = block_sum(pq, red);
       if (threadIdx.x == 0) P2[bid] = t;
       if (!grid_barrier(a.st, nb, epoch)) return;
       const double alpha = rho / grid_total(P2, nb, &bcast);
+      // x += alpha p (:92), r -= alpha q (:96), rho = r.r (:100)
       rr = 0.0;
       for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-        a.x[i] = 1.0 * a.x[i] + alpha * pk[i];
-        const double ri = 1.0 * a.r[i] + -alpha * a.q[i];
+        a.x[i] = __fma_rn(alpha, p[i], a.x[i]);
+        const double ri = __fma_rn(-alpha, a.q[i], a.r[i]);
         a.r[i] = ri;
-        rr += ri * ri;
+        rr = __fma_rn(ri, ri, rr);
       }
       t = block_sum(rr, red);
       if (threadIdx.x == 0) P0[bid] = t;
@@ -619,14 +621,26 @@ static int grid_for_rows(int64_t n, int max_blocks, int threads) {
   return (int)want;
 }
 
-static int coop_launch(cudaStream_t s, void *fn, int nb, int threads, void *arg, DevStats *st, int bar_mode) {
-  if (nb < 1) return MPG_ERR_CUDA;
+// the barrier fields of DevStats for one cooperative launch: the counter
+// starts at zero, the flavour and the time-out test settings come from w
+int barrier_setup(cudaStream_t s, DevStats *st, const CgWork &w) {
   static const int modes[2] = {0, 1};
-  // the barrier counter starts at zero for every launch
   if (cudaMemsetAsync(&st->bar_count, 0, sizeof(unsigned), s) != cudaSuccess) return MPG_ERR_CUDA;
-  if (cudaMemcpyAsync(&st->bar_mode, &modes[bar_mode ? 1 : 0], sizeof(int), cudaMemcpyHostToDevice, s) !=
+  if (cudaMemcpyAsync(&st->bar_mode, &modes[w.bar_mode ? 1 : 0], sizeof(int), cudaMemcpyHostToDevice, s) !=
       cudaSuccess)
     return MPG_ERR_CUDA;
+  // pageable sources are staged by the copy before it returns
+  const int skip = w.bar_skip;
+  const unsigned limit = w.bar_limit;
+  if (cudaMemcpyAsync(&st->bar_skip, &skip, sizeof(int), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+      cudaMemcpyAsync(&st->bar_limit, &limit, sizeof(unsigned), cudaMemcpyHostToDevice, s) != cudaSuccess)
+    return MPG_ERR_CUDA;
+  return MPG_OK;
+}
+
+static int coop_launch(cudaStream_t s, void *fn, int nb, int threads, void *arg, DevStats *st, const CgWork &w) {
+  if (nb < 1) return MPG_ERR_CUDA;
+  if (barrier_setup(s, st, w)) return MPG_ERR_CUDA;
   void *args[] = {arg};
   cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(nb), dim3(threads), args, 0, s);
   return e == cudaSuccess ? MPG_OK : MPG_ERR_CUDA;
@@ -651,7 +665,7 @@ int run_cg64(cudaStream_t s, int device, int64_t n, const int32_t *rowptr, const
   a.st = st;
   (void)device;
   const int th = threads_of(w);
-  return coop_launch(s, kernel_of(0, th), grid_for_rows(n, w.max_blocks, th), th, &a, st, w.bar_mode);
+  return coop_launch(s, kernel_of(0, th), grid_for_rows(n, w.max_blocks, th), th, &a, st, w);
 }
 
 int run_cg64_dia(cudaStream_t s, const DiaMatrix &A, const double *b, double *x, double tol, int max_iter, CgWork &w,
@@ -661,8 +675,7 @@ int run_cg64_dia(cudaStream_t s, const DiaMatrix &A, const double *b, double *x,
   a.b = b;
   a.x = x;
   a.r = w.r;
-  a.p0 = w.p0;
-  a.p1 = w.p1;
+  a.p = w.p0;
   a.q = w.q;
   a.partials = w.partials;
   a.tol2 = tol * tol;
@@ -670,7 +683,7 @@ int run_cg64_dia(cudaStream_t s, const DiaMatrix &A, const double *b, double *x,
   a.st = st;
   const int th = threads_of(w);
   return coop_launch(s, kernel_of(A.ndiag <= 15 ? 1 : 2, th), grid_for_rows(A.n, w.max_blocks, th), th, &a, st,
-                     w.bar_mode);
+                     w);
 }
 
 int run_cg_mixed(cudaStream_t s, const DiaMatrix &A, const double *b, double *x, double tol, double inner_tol,
@@ -692,7 +705,7 @@ int run_cg_mixed(cudaStream_t s, const DiaMatrix &A, const double *b, double *x,
   const int kind = (A.ndiag <= 15 ? 3 : 4) + (A.constant ? 2 : 0);
   int cap = 128 * kRecOf(th) < w.max_blocks ? 128 * kRecOf(th) : w.max_blocks;
   if (w.block_cap > 0 && w.block_cap < cap) cap = w.block_cap;
-  return coop_launch(s, kernel_of(kind, th), grid_for_rows(A.n, cap, th), th, &a, st, w.bar_mode);
+  return coop_launch(s, kernel_of(kind, th), grid_for_rows(A.n, cap, th), th, &a, st, w);
 }
 
 // CG_solve.hpp:115-206, one host round trip per dot product
@@ -778,9 +791,10 @@ static_assert(sizeof(DevStats) <= kNoAllocStatsBytes, "DevStats must fit its scr
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 namespace {
+// per device: the solver's co-residency limit (a property of the device and
+// the kernel, unchanged by a context reset)
 struct NoAllocDevice {
   bool ready = false;
-  unsigned char *base = nullptr;  // device address of g_noalloc_scratch on this device
   int max_blocks = 0;
 };
 constexpr int kNoAllocDevices = 64;
@@ -802,22 +816,25 @@ extern "C" int mpg_cg_csr_noalloc(void *stream, int64_t n, const int32_t *d_rowp
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
     NoAllocDevice &d = g_noalloc_dev[dev];
     if (!d.ready) {
-      // one-time set-up on this device (the device is current)
-      void *p = nullptr;
-      e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-      if (e != cudaSuccess || !p) return MPG_ERR_CUDA;
+      // first call on this device (the device is current)
       int mb = cg_max_blocks(dev, 512);
       if (mb > kNoAllocMaxBlocks) mb = kNoAllocMaxBlocks;
       if (mb < 1) return MPG_ERR_CUDA;
-      d.base = static_cast<unsigned char *>(p);
       d.max_blocks = mb;
       d.ready = true;
     }
     nd = d;
   }
+  // The array's device address in the current context, looked up on every
+  // call (no allocation): after a context reset the module is loaded again
+  // and the array may sit elsewhere, so a saved address could be stale.
+  void *base_p = nullptr;
+  e = cudaGetSymbolAddress(&base_p, g_noalloc_scratch);
+  if (e != cudaSuccess || !base_p) return MPG_ERR_CUDA;
+  unsigned char *base = static_cast<unsigned char *>(base_p);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  DevStats *st = reinterpret_cast<DevStats *>(nd.base);
-  double *dbl = reinterpret_cast<double *>(nd.base + kNoAllocStatsBytes);
+  DevStats *st = reinterpret_cast<DevStats *>(base);
+  double *dbl = reinterpret_cast<double *>(base + kNoAllocStatsBytes);
   CgWork w;
   w.partials = dbl;
   w.r = dbl + kNoAllocPartials;

@@ -632,18 +632,24 @@ static int cg_impl(const orc_mesh *m, const double *rhs, double *x, double tol, 
   if (resid_out) *resid_out = rho0 > 0 ? sqrt(rho / rho0) : 0.0;
   if (rho == 0) return 0;
   int iter = 0;
+  // the vector updates are elementwise: the same result on any thread count
+  const int nt = nthr(nthreads);
   for (; iter < max_iter; ++iter) {
     if (iter == 0) {
       p = r;
     } else {
       beta = rho / rho_old;
+#pragma omp parallel for num_threads(nt) schedule(static) if (nt > 1)
       for (int64_t i = 0; i < N; ++i) p[i] = beta * p[i] + 1.0 * r[i];
     }
     orc_spmv(m, p.data(), q.data(), nthreads);
     alpha = dot(p.data(), q.data(), N, nthreads);
     alpha = rho / alpha;
-    for (int64_t i = 0; i < N; ++i) x[i] = 1.0 * x[i] + alpha * p[i];
-    for (int64_t i = 0; i < N; ++i) r[i] = 1.0 * r[i] + -alpha * q[i];
+#pragma omp parallel for num_threads(nt) schedule(static) if (nt > 1)
+    for (int64_t i = 0; i < N; ++i) {
+      x[i] = 1.0 * x[i] + alpha * p[i];
+      r[i] = 1.0 * r[i] + -alpha * q[i];
+    }
     rho_old = rho;
     rho = dot(r.data(), r.data(), N, nthreads);
     if (rho / rho0 < tol * tol) break;
@@ -926,6 +932,60 @@ extern "C" int64_t orc_sort_by_cell(int64_t n, const int32_t *cell, int64_t T, i
   return m;
 }
 
+/* Stable compaction (mode 1) on nt threads: the same order and values as the
+ * serial loop.  Each thread stages its chunk's live particles, then writes
+ * them at the chunk's offset (the live count of the chunks before it). */
+static int64_t compact_stable_par(int64_t n, int32_t *cell, double *x, double *xref, double *v, double *w, int32_t *sp,
+                                  int64_t *id, int nt) {
+  std::vector<int64_t> cnt(nt + 1, 0);
+  struct Stage {
+    std::vector<int32_t> cell, sp;
+    std::vector<double> x, xref, v, w;
+    std::vector<int64_t> id;
+  };
+  std::vector<Stage> st(nt);
+#pragma omp parallel num_threads(nt)
+  {
+#ifdef _OPENMP
+    const int t = omp_get_thread_num();
+#else
+    const int t = 0;
+#endif
+    const int64_t lo = n * t / nt, hi = n * (t + 1) / nt;
+    Stage &S = st[t];
+    for (int64_t p = lo; p < hi; ++p) {
+      if (cell[p] < 0) continue;
+      S.cell.push_back(cell[p]);
+      for (int d = 0; d < 3; ++d) {
+        S.x.push_back(x[3 * p + d]);
+        S.xref.push_back(xref[3 * p + d]);
+        S.v.push_back(v[3 * p + d]);
+      }
+      if (w) S.w.push_back(w[p]);
+      if (sp) S.sp.push_back(sp[p]);
+      if (id) S.id.push_back(id[p]);
+    }
+    cnt[t + 1] = (int64_t)S.cell.size();
+#pragma omp barrier
+#pragma omp single
+    for (int k = 0; k < nt; ++k) cnt[k + 1] += cnt[k];
+    const int64_t o = cnt[t];
+    const int64_t m = (int64_t)S.cell.size();
+    for (int64_t k = 0; k < m; ++k) {
+      cell[o + k] = S.cell[k];
+      for (int d = 0; d < 3; ++d) {
+        x[3 * (o + k) + d] = S.x[3 * k + d];
+        xref[3 * (o + k) + d] = S.xref[3 * k + d];
+        v[3 * (o + k) + d] = S.v[3 * k + d];
+      }
+      if (w) w[o + k] = S.w[k];
+      if (sp) sp[o + k] = S.sp[k];
+      if (id) id[o + k] = S.id[k];
+    }
+  }
+  return cnt[nt];
+}
+
 extern "C" double orc_kinetic(int64_t n, const double *v, const double *w, const int32_t *sp, const double *mass,
                               int nthreads) {
   // PIC.cpp:191-200
@@ -1097,7 +1157,10 @@ extern "C" int orc_step(orc_mesh *m, const orc_step_cfg *c, double dt, int64_t *
   orc_push(m, np, cell, E, v, vref, sp, qm.data(), dt, c->nthreads);
   s.n_walk_limit = orc_walk(m, np, cell, x, xref, v, vref, dt, c->kill, c->max_cross, &s.n_killed, &s.n_cross,
                             c->nthreads);
-  np = orc_compact(c->compact_mode, np, cell, x, xref, v, w, sp, id);
+  if (c->compact_mode == 1 && nthr(c->nthreads) > 1)
+    np = compact_stable_par(np, cell, x, xref, v, w, sp, id, nthr(c->nthreads));
+  else
+    np = orc_compact(c->compact_mode, np, cell, x, xref, v, w, sp, id);
   // compaction does not carry vref: it is recomputed by the next push
   s.ke = orc_kinetic(np, v, w, sp, mass, c->nthreads);
   s.n_alive = np;

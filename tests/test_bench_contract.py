@@ -26,6 +26,7 @@ def test_reference_arm_line():
         assert k in d, k
     assert d["impl"] == "reference" and d["unit"] == "particle-steps/s" and d["higher_is_better"] is True
     assert d["value"] > 0 and d["steps"] == 3 and d["warmup"] == 3
+    assert d["cpu_baseline"]["steps_timed"] == 3 and d["cpu_baseline"]["steps_requested"] == 3
     cb = d["cpu_baseline"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
     e = d["e2e"]

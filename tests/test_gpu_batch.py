@@ -45,6 +45,39 @@ def test_run_alone_equals_run_in_mix(mpg):
     assert mix.info(a).steps_done == 8 and mix.info(c).steps_done == 8
 
 
+def test_run_admitted_mid_flight_equals_run_alone(mpg):
+    """Continuous batching: run B is prepared on the host while run A is
+    resident, admitted after A has taken 5 steps, then both step together.
+    B's phi and particle set equal those of B stepped alone in its own batch
+    (admitted from the same preparation), bit for bit."""
+    mix = mpg.Batch(0, budget_bytes=4 << 30, particle_capacity=1 << 20)
+    alone = mpg.Batch(0, budget_bytes=4 << 30, particle_capacity=1 << 20)
+    mix.tuning(512, 3)
+    alone.tuning(512, 3)
+    a = mix.admit(10, 50000, 41, vth=0.08, drift=(0.05, 0, 0), steps=30)
+    for _ in range(5):
+        assert mix.step(1).rc == 0
+    prep = mpg.RunPrep(12, 60000, 42, vth=0.05, steps=12)
+    b_mix = mix.admit_prepared(prep)
+    b_alone = alone.admit_prepared(prep)
+    prep.close()
+    assert b_mix is not None and b_alone is not None
+    for _ in range(8):
+        assert mix.step(1).rc == 0
+        assert alone.step(1).rc == 0
+    p1, p2 = mix.phi(b_mix), alone.phi(b_alone)
+    assert (p1.view(np.uint64) == p2.view(np.uint64)).all()
+    x1 = _sorted_state(*mix.particles(b_mix))
+    x2 = _sorted_state(*alone.particles(b_alone))
+    assert len(x1[0]) == len(x2[0])
+    for u, w in zip(x1, x2):
+        assert (u == w).all()
+    i1, i2 = mix.info(b_mix), alone.info(b_alone)
+    assert i1.n_alive == i2.n_alive and i1.steps_done == i2.steps_done == 8
+    assert i1.solver_iters == i2.solver_iters
+    assert mix.info(a).steps_done == 13
+
+
 def test_batch_run_matches_single_run(mpg):
     n_side, n, seed, dt = 10, 40000, 5, 0.01
     bt = mpg.Batch(0, budget_bytes=4 << 30, particle_capacity=1 << 20)

@@ -286,7 +286,7 @@ def test_config1_full_run_matches_oracle(mpg, orc, capsys):
         assert rc == 0
         assert st.n_alive == ost.n_alive, s
         assert st.n_killed == ost.n_killed, s
-        assert st.n_crossings == ost.n_crossings, s
+        assert st.n_crossings == ost.n_cross, s
         assert abs(st.ke - ost.ke) <= 1e-10 * ost.ke, s
         exits += st.n_killed
         if s % 10 == 9:
