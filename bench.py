@@ -342,23 +342,34 @@ def batch_admit(bt, r, steps=None):
 
 
 def autotune(mpg, runs, device=0):
-    """Pick the batch solver's block size and the sort interval on a sample."""
+    """Pick the batch engine's block size, step form (one persistent launch
+    per step or one launch per phase) and sort interval on a sample of runs:
+    first block size x step form at sort interval 10, then the best of those
+    at sort intervals 5 and 20."""
     sample = runs[: min(24, len(runs))]
     cap = sum(r["n_particles"] for r in sample)
     results = []
-    for th, si in ((256, 10), (512, 10), (1024, 10), (512, 5), (512, 20)):
+
+    def trial(th, fused, si):
         bt = mpg.Batch(device, budget_bytes=64 << 30, particle_capacity=cap)
-        bt.tuning(th, si)
+        bt.tuning(th, si, fused=fused)
         for r in sample:
             batch_admit(bt, r, steps=1000)
         bt.step(2)
         st = bt.step(8)
-        results.append((st.particle_steps / max(st.ms, 1e-9), th, si))
         bt.close()
+        results.append((st.particle_steps / max(st.ms, 1e-9), th, fused, si))
+
+    for th in (256, 512, 1024):
+        for fused in (True, False):
+            trial(th, fused, 10)
+    _, th, fused, _ = max(results)
+    for si in (5, 20):
+        trial(th, fused, si)
     best = max(results)
-    return {"cg_threads": best[1], "sort_interval": best[2],
-            "tried": [{"cg_threads": th, "sort_interval": si, "particle_steps_per_ms": round(v, 1)}
-                      for v, th, si in results]}
+    return {"cg_threads": best[1], "fused": best[2], "sort_interval": best[3],
+            "tried": [{"cg_threads": th, "fused": fu, "sort_interval": si, "particle_steps_per_ms": round(v, 1)}
+                      for v, th, fu, si in results]}
 
 
 def _by_id(d, n_ids):
@@ -450,7 +461,7 @@ def run_ensemble(mpg, args, device=0):
     tune = autotune(mpg, runs, device)
     cap = sum(r["n_particles"] for r in runs)
     bt = mpg.Batch(device, budget_bytes=150 << 30, max_runs=256, particle_capacity=cap)
-    bt.tuning(tune["cg_threads"], tune["sort_interval"])
+    bt.tuning(tune["cg_threads"], tune["sort_interval"], fused=tune["fused"])
     t0 = time.perf_counter()
     for r in runs:
         assert batch_admit(bt, r) is not None
@@ -547,7 +558,7 @@ def run_serving(mpg, args, device=0):
     tune = autotune(mpg, [r for r in runs if r["n_side"] < 64], device)
     cap = 200 << 20
     bt = mpg.Batch(device, budget_bytes=150 << 30, max_runs=256, particle_capacity=cap)
-    bt.tuning(tune["cg_threads"], tune["sort_interval"])
+    bt.tuning(tune["cg_threads"], tune["sort_interval"], fused=tune["fused"])
     pool = ThreadPoolExecutor(max_workers=max(2, min(8, (os.cpu_count() or 2) // 2)))
 
     def prepare(r):

@@ -208,9 +208,10 @@ int mpg_cg_csr(mpg_ctx *ctx, int64_t n, const int32_t *d_rowptr, const int32_t *
 /* ---- batched ensemble / serving (no counterpart in the reference) --------
  * Many independent runs (each: Kuhn-split unit cube n^3, one species,
  * volume-uniform fill, absorbing walls, mixed precision) resident on one GPU
- * and advanced together: one launch per phase of the step for all active runs
- * (charge conversion, field solve, E field, fused push/walk/deposit), the
- * step captured in a CUDA graph.  The field operator of a batched run is the
+ * and advanced together: one persistent launch per step for all active runs
+ * (charge conversion, field solve, E field, fused push/walk/deposit, with
+ * grid barriers between them; mpg_batch_set_fused), the step captured in a
+ * CUDA graph.  The field operator of a batched run is the
  * uniform Kuhn stencil of its mesh (constant coefficients, FP32 inside FP64
  * refinement).  Runs are admitted against a device-memory budget, step
  * until their requested step count and are retired to free their slot.
@@ -260,6 +261,10 @@ int mpg_batch_destroy(mpg_batch *b);
 int mpg_batch_last_error(mpg_batch *b, char *buf, int len);
 /* block size of the batched solver (256, 512, 1024) and cell-sort interval */
 int mpg_batch_set_tuning(mpg_batch *b, int cg_threads, int sort_interval);
+/* on (the default): each batch step is one persistent cooperative launch
+ * whose phases (charge -> rhs, field solves, E, push/walk/deposit) are
+ * separated by grid barriers; off: one launch per phase.  Same results. */
+int mpg_batch_set_fused(mpg_batch *b, int on);
 /* MPG_ERR_CAPACITY when the budget, the particle capacity or the slots are exhausted */
 int mpg_batch_admit(mpg_batch *b, const mpg_run_desc *desc, int *slot);
 /* mpg_batch_admit in two parts, so that the host work of an admission can

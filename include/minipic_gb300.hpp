@@ -14,6 +14,7 @@
 // print-and-skip behaviour on over-capacity (particle_fill.hpp:61-64).
 #pragma once
 
+#include <algorithm>
 #include <array>
 #include <chrono>
 #include <cmath>
@@ -182,7 +183,15 @@ class Mesh {  // mesh.hpp:59-267 (single rank; node/elem gids == lids)
     physToReference(ref, phys, e);
     return ref[0] >= 0 && ref[1] >= 0 && ref[2] >= 0 && ref[0] + ref[1] + ref[2] <= 1;
   }
-  // mesh.cpp:794-822 (nodes and elems files; one rank)
+  // Mesh::dump_data (mesh.cpp:794-910), one rank (file suffix 000): nodes,
+  // elems, faces, edges, owned faces and edges, boundary faces and edges.
+  // Faces and edges carry the reference's gids: their sorted node-gid tuples
+  // in lexicographic order (mesh.cpp:271-303; on a periodic mesh a face on
+  // the x = nx node plane is renamed to the x = 0 plane first, mesh.cpp:61-76;
+  // edges are not renamed).  A face (edge) is on the boundary when the mean
+  // of its node coordinates, mapped onto [-1,1], is within 1e-8 of -1 or +1
+  // in some axis (mesh.cpp:602-625).  Numbers go out with the stream's
+  // default precision, like the reference's.
   void dump_data() const {
     std::ofstream out("nodes-000.dat");
     for (LO i = 0; i < num_nodes; ++i)
@@ -192,6 +201,52 @@ class Mesh {  // mesh.hpp:59-267 (single rank; node/elem gids == lids)
       oe << e << ' ';
       for (int i = 0; i < 4; ++i) oe << tets_[4 * e + i] << ' ';
       oe << '\n';
+    }
+    const int64_t plane = (int64_t)(desc_.ny + 1) * (desc_.nz + 1);
+    static const int fn[4][3] = {{0, 1, 3}, {1, 2, 3}, {0, 3, 2}, {0, 2, 1}};
+    std::vector<std::array<int64_t, 3>> faces;
+    faces.reserve(4 * (size_t)num_elems);
+    for (LO e = 0; e < num_elems; ++e)
+      for (int f = 0; f < 4; ++f) {
+        std::array<int64_t, 3> t = {tets_[4 * e + fn[f][0]], tets_[4 * e + fn[f][1]], tets_[4 * e + fn[f][2]]};
+        if (is_periodic && t[0] / plane == desc_.nx && t[1] / plane == desc_.nx && t[2] / plane == desc_.nx)
+          for (auto &g : t) g -= (int64_t)desc_.nx * plane;
+        std::sort(t.begin(), t.end());
+        faces.push_back(t);
+      }
+    std::sort(faces.begin(), faces.end());
+    faces.erase(std::unique(faces.begin(), faces.end()), faces.end());
+    std::vector<std::array<int64_t, 2>> edges;
+    edges.reserve(6 * (size_t)num_elems);
+    for (LO e = 0; e < num_elems; ++e)
+      for (int j = 0; j < 3; ++j)
+        for (int k = j + 1; k < 4; ++k) {
+          int64_t a = tets_[4 * e + j], b = tets_[4 * e + k];
+          edges.push_back({std::min(a, b), std::max(a, b)});
+        }
+    std::sort(edges.begin(), edges.end());
+    edges.erase(std::unique(edges.begin(), edges.end()), edges.end());
+    std::ofstream of("faces-000.dat"), oed("edges-000.dat"), oof("owned-faces-000.dat"),
+        ooe("owned-edges-000.dat"), obf("boundary-faces-000.dat"), obe("boundary-edges-000.dat");
+    const double almost_one = 0.99999999, mid = 0.5 * (desc_.lo + desc_.hi), half = 0.5 * (desc_.hi - desc_.lo);
+    auto on_boundary = [&](const int64_t *g, int m) {
+      for (int d = 0; d < 3; ++d) {
+        double s = 0.0;
+        for (int q = 0; q < m; ++q) s += nodes_[3 * g[q] + d];
+        const double u = (s / m - mid) / half;
+        if (u <= -almost_one || u >= almost_one) return true;
+      }
+      return false;
+    };
+    for (size_t i = 0; i < faces.size(); ++i) {
+      of << i << ' ' << faces[i][0] << ' ' << faces[i][1] << ' ' << faces[i][2] << ' ' << '\n';
+      oof << i << '\n';
+      if (on_boundary(faces[i].data(), 3)) obf << i << '\n';
+    }
+    for (size_t i = 0; i < edges.size(); ++i) {
+      oed << i << ' ' << edges[i][0] << ' ' << edges[i][1] << ' ' << '\n';
+      ooe << i << '\n';
+      if (on_boundary(edges[i].data(), 2)) obe << i << '\n';
     }
   }
 

@@ -33,7 +33,8 @@ EXPORTS = [
     "mpg_particles_download", "mpg_particles_count", "mpg_mixed_download", "mpg_mixed_upload",
     "mpg_charge_download", "mpg_weight_charge", "mpg_solve", "mpg_weight_efield", "mpg_move", "mpg_step",
     "mpg_sort", "mpg_cell_starts", "mpg_set_barrier_test", "mpg_get_field", "mpg_set_field", "mpg_cg_csr", "mpg_cg_csr_noalloc", "mpg_mg_hierarchy",
-    "mpg_batch_create", "mpg_batch_destroy", "mpg_batch_last_error", "mpg_batch_set_tuning", "mpg_batch_admit",
+    "mpg_batch_create", "mpg_batch_destroy", "mpg_batch_last_error", "mpg_batch_set_tuning", "mpg_batch_set_fused",
+    "mpg_batch_admit",
     "mpg_batch_prepare", "mpg_batch_admit_prepared", "mpg_run_prep_destroy",
     "mpg_batch_step", "mpg_batch_run_info", "mpg_batch_run_phi", "mpg_batch_run_particles", "mpg_batch_retire",
 ]
@@ -149,6 +150,7 @@ def load():
         "mpg_batch_destroy": ([P], I),
         "mpg_batch_last_error": ([P, C.c_char_p, I], I),
         "mpg_batch_set_tuning": ([P, I, I], I),
+        "mpg_batch_set_fused": ([P, I], I),
         "mpg_batch_admit": ([P, C.POINTER(RunDesc), C.POINTER(I)], I),
         "mpg_batch_prepare": ([C.POINTER(RunDesc), C.POINTER(P)], I),
         "mpg_batch_admit_prepared": ([P, P, C.POINTER(I)], I),
@@ -452,8 +454,10 @@ class Batch:
             raise MpgError(rc, buf.value.decode())
         return rc
 
-    def tuning(self, cg_threads=512, sort_interval=10):
+    def tuning(self, cg_threads=512, sort_interval=10, fused=None):
         self._ck(self.L.mpg_batch_set_tuning(self.h, cg_threads, sort_interval))
+        if fused is not None:
+            self._ck(self.L.mpg_batch_set_fused(self.h, int(fused)))
 
     @staticmethod
     def desc(n_side, n_particles, seed, q=-1.0, m=1.0, weight=None, vth=0.05, drift=(0.0, 0.0, 0.0),

@@ -84,10 +84,9 @@ struct SlotStat {
 // ---------------------------------------------------------------------------
 // also forms the solver's initial guess: 2 phi[n-1] - phi[n-2] once two
 // solutions exist (the count is advanced by the solver after it finishes)
-__global__ void k_batch_convert(const SlotDev *__restrict__ slots, const int2 *__restrict__ plan) {
-  const int2 pl = plan[blockIdx.x];
-  const SlotDev &S = slots[pl.x];
-  const int64_t i = (int64_t)pl.y * blockDim.x + threadIdx.x;
+constexpr int kPlanChunk = 256;  // elements (nodes or tets) per plan entry
+
+__device__ __forceinline__ void batch_convert_at(const SlotDev &S, int64_t i) {
   if (i >= S.N) return;
   const int h = *S.hist;
   if (h >= 2) {
@@ -105,10 +104,12 @@ __global__ void k_batch_convert(const SlotDev *__restrict__ slots, const int2 *_
   S.rhs[i] = r;
 }
 
-__global__ void k_batch_efield(const SlotDev *__restrict__ slots, const int2 *__restrict__ plan) {
+__global__ void k_batch_convert(const SlotDev *__restrict__ slots, const int2 *__restrict__ plan) {
   const int2 pl = plan[blockIdx.x];
-  const SlotDev &S = slots[pl.x];
-  const int64_t t = (int64_t)pl.y * blockDim.x + threadIdx.x;
+  batch_convert_at(slots[pl.x], (int64_t)pl.y * kPlanChunk + threadIdx.x);
+}
+
+__device__ __forceinline__ void batch_efield_at(const SlotDev &S, int64_t t) {
   if (t >= S.T) return;
   const int4 nd = S.tets[t];
   const double f0 = S.phi[nd.x];
@@ -124,6 +125,11 @@ __global__ void k_batch_efield(const SlotDev *__restrict__ slots, const int2 *__
   ulonglong2 *a2 = reinterpret_cast<ulonglong2 *>(S.acc + 4 * t);
   a2[0] = make_ulonglong2(0ull, 0ull);
   a2[1] = make_ulonglong2(0ull, 0ull);
+}
+
+__global__ void k_batch_efield(const SlotDev *__restrict__ slots, const int2 *__restrict__ plan) {
+  const int2 pl = plan[blockIdx.x];
+  batch_efield_at(slots[pl.x], (int64_t)pl.y * kPlanChunk + threadIdx.x);
 }
 
 // warp-aggregated fixed-point deposit keyed by the full cellsp word (runs
@@ -195,8 +201,8 @@ constexpr int kMoveThreads = 256;
 // contiguous, so a lane's particles mostly belong to one run: the lane keeps
 // that run's statistics in registers (kinetic energy per unit mass in
 // float-float) and adds them to the run's counters when its run changes.
-__global__ void __launch_bounds__(kMoveThreads) k_batch_move(MixedParts P, int64_t n, const SlotDev *__restrict__ slots,
-                                                             SlotStat *stats, int kill) {
+__device__ __forceinline__ void batch_move_body(MixedParts P, int64_t n, const SlotDev *__restrict__ slots,
+                                                SlotStat *stats, int kill) {
   const int lane = threadIdx.x & 31;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -282,6 +288,11 @@ __global__ void __launch_bounds__(kMoveThreads) k_batch_move(MixedParts P, int64
     batch_deposit_warp(slots, key, d1, d2, d3, dq);
   }
   flush();
+}
+
+__global__ void __launch_bounds__(kMoveThreads) k_batch_move(MixedParts P, int64_t n, const SlotDev *__restrict__ slots,
+                                                             SlotStat *stats, int kill) {
+  batch_move_body(P, n, slots, stats, kill);
 }
 
 // resident blocks of the persistent batch move on the current device (one wave)
@@ -659,6 +670,58 @@ void *batch_cg_kernel(int th) {
   return th <= 256 ? (void *)k_batch_cg<256> : th <= 512 ? (void *)k_batch_cg<512> : (void *)k_batch_cg<1024>;
 }
 
+// One persistent cooperative launch per batch step: the four phases of the
+// step separated by grid barriers (bounded waits, as in the single-run
+// solvers; a time-out ends the launch in every block).
+//   1 charge -> rhs and the initial guess, grid-stride over the node plan;
+//   2 the runs' field solves: block b < n_cg_blocks works its solver items
+//     (each run's CTA group synchronises on its own group barrier), the
+//     other blocks go straight to the barrier;
+//   3 E per tet (and zeroed charge slots), grid-stride over the tet plan;
+//   4 the fused push/walk/deposit over the particle array.
+struct BatchStepArgs {
+  const SlotDev *slots;
+  SlotStat *stats;
+  const int2 *conv_plan, *ef_plan, *block_items;
+  const int4 *items;
+  int n_conv, n_ef, n_cg_blocks;
+  MixedParts P;
+  int64_t n;
+  DevStats *gbar;
+};
+
+template <int TH>
+__global__ void __launch_bounds__(TH, 1024 / TH) k_batch_step(BatchStepArgs a) {
+  static_assert(TH % kPlanChunk == 0, "block size is a multiple of the plan chunk");
+  constexpr int kPer = TH / kPlanChunk;  // plan entries per block and pass
+  unsigned epoch = 0;
+  const int sub = threadIdx.x / kPlanChunk, t = threadIdx.x % kPlanChunk;
+  for (int e = blockIdx.x * kPer + sub; e < a.n_conv; e += gridDim.x * kPer) {
+    const int2 pl = a.conv_plan[e];
+    batch_convert_at(a.slots[pl.x], (int64_t)pl.y * kPlanChunk + t);
+  }
+  if (!grid_barrier(a.gbar, gridDim.x, epoch)) return;
+  if ((int)blockIdx.x < a.n_cg_blocks) {
+    const int2 rng = a.block_items[blockIdx.x];
+    for (int k = rng.x; k < rng.y; ++k) {
+      const int4 w = a.items[k];
+      solve_run<TH>(a.slots[w.x], &a.stats[w.x], w.y, w.z);
+      __syncthreads();
+    }
+  }
+  if (!grid_barrier(a.gbar, gridDim.x, epoch)) return;
+  for (int e = blockIdx.x * kPer + sub; e < a.n_ef; e += gridDim.x * kPer) {
+    const int2 pl = a.ef_plan[e];
+    batch_efield_at(a.slots[pl.x], (int64_t)pl.y * kPlanChunk + t);
+  }
+  if (!grid_barrier(a.gbar, gridDim.x, epoch)) return;
+  if (a.n > 0) batch_move_body(a.P, a.n, a.slots, a.stats, 1);
+}
+
+void *batch_step_kernel(int th) {
+  return th <= 256 ? (void *)k_batch_step<256> : th <= 512 ? (void *)k_batch_step<512> : (void *)k_batch_step<1024>;
+}
+
 // ---------------------------------------------------------------------------
 struct Run {
   bool used = false, active = false, finished = false;
@@ -705,6 +768,11 @@ struct mpg_batch {
   int64_t plan_cap_conv = 0, plan_cap_ef = 0, plan_cap_items = 0, plan_cap_blocks = 0;
   bool plan_dirty = true;
   int max_cg_blocks = 0;
+  // one persistent launch per step (k_batch_step) or one launch per phase
+  bool fused = true;
+  int max_step_blocks = 0;   // co-resident blocks of k_batch_step at cg_threads
+  DevStats *d_gbar = nullptr;  // grid barrier of k_batch_step
+  DevStats *h_gbar = nullptr;
   // sort scratch
   int64_t *d_base = nullptr;
   uint32_t *d_cnt = nullptr, *d_start = nullptr, *d_scan = nullptr, *d_count = nullptr, *h_count = nullptr;
@@ -808,7 +876,7 @@ int build_plans(mpg_batch *b) {
   // solver: runs bigger than rows_per_cta get several CTAs (their items come
   // first in each CTA's list, one multi-CTA item per CTA); the rest are dealt
   // to the least-loaded CTA
-  const int G = std::max(1, b->max_cg_blocks);
+  const int G = std::max(1, b->fused ? b->max_step_blocks : b->max_cg_blocks);
   const int64_t rows_per_cta = 24 * 1024;
   std::vector<std::vector<int4>> per(G);
   std::vector<int64_t> load(G, 0);
@@ -902,6 +970,27 @@ int batch_sort(mpg_batch *b) {
 int enqueue_step(mpg_batch *b) {
   cudaStream_t s = b->stream;
   BCK(cudaMemsetAsync(b->d_stats, 0, sizeof(SlotStat) * kMaxSlots, s));
+  if (b->fused) {
+    // one persistent cooperative launch for all phases of the step
+    BCK(cudaMemsetAsync(b->d_gbar, 0, sizeof(DevStats), s));
+    BatchStepArgs a;
+    a.slots = b->d_slots;
+    a.stats = b->d_stats;
+    a.conv_plan = b->d_conv_plan;
+    a.ef_plan = b->d_ef_plan;
+    a.block_items = b->d_block_items;
+    a.items = b->d_items;
+    a.n_conv = b->n_conv_blocks;
+    a.n_ef = b->n_ef_blocks;
+    a.n_cg_blocks = b->n_cg_blocks;
+    a.P = b->mp[b->cur];
+    a.n = b->n;
+    a.gbar = b->d_gbar;
+    void *args[] = {(void *)&a};
+    BCK(cudaLaunchCooperativeKernel(batch_step_kernel(b->cg_threads), dim3(b->max_step_blocks),
+                                    dim3(b->cg_threads), args, 0, s));
+    return MPG_OK;
+  }
   if (b->n_conv_blocks) k_batch_convert<<<b->n_conv_blocks, 256, 0, s>>>(b->d_slots, b->d_conv_plan);
   if (b->n_cg_blocks) {
     void *args[] = {(void *)&b->d_slots, (void *)&b->d_stats, (void *)&b->d_items, (void *)&b->d_block_items};
@@ -926,8 +1015,9 @@ int step_once(mpg_batch *b, double &ms) {
       b->gexec = nullptr;
     }
   }
-  const int n_launch = (b->n_conv_blocks ? 1 : 0) + (b->n_cg_blocks ? 1 : 0) + (b->n_ef_blocks ? 1 : 0) +
-                       (b->n > 0 ? 1 : 0);
+  const int n_launch = b->fused ? 1
+                                : (b->n_conv_blocks ? 1 : 0) + (b->n_cg_blocks ? 1 : 0) + (b->n_ef_blocks ? 1 : 0) +
+                                      (b->n > 0 ? 1 : 0);
   BCK(cudaEventRecord(b->ev0, b->stream));
   bool ran = false;
   if (b->use_graph && b->graph_ok) {
@@ -963,7 +1053,10 @@ int step_once(mpg_batch *b, double &ms) {
   b->launches += n_launch;
   BCK(cudaEventRecord(b->ev1, b->stream));
   BCK(cudaMemcpyAsync(b->h_stats, b->d_stats, sizeof(SlotStat) * kMaxSlots, cudaMemcpyDeviceToHost, b->stream));
+  if (b->fused) BCK(cudaMemcpyAsync(b->h_gbar, b->d_gbar, sizeof(DevStats), cudaMemcpyDeviceToHost, b->stream));
   BCK(cudaStreamSynchronize(b->stream));
+  if (b->fused && b->h_gbar->bar_error)
+    for (int s = 0; s < kMaxSlots; ++s) b->h_stats[s].bar_error = 1;  // the step ended early for every run
   float f = 0.f;
   BCK(cudaEventElapsedTime(&f, b->ev0, b->ev1));
   ms = f;
@@ -1008,13 +1101,17 @@ int mpg_batch_create(int device, int64_t budget_bytes, int max_runs, int64_t par
       balloc(b, nullptr, &b->d_hist, kMaxSlots))
     return bail(MPG_ERR_CUDA);
   if (cudaMallocHost(&b->h_stats, sizeof(SlotStat) * kMaxSlots) != cudaSuccess ||
-      cudaMallocHost(&b->h_count, sizeof(uint32_t)) != cudaSuccess)
+      cudaMallocHost(&b->h_count, sizeof(uint32_t)) != cudaSuccess ||
+      cudaMallocHost(&b->h_gbar, sizeof(DevStats)) != cudaSuccess)
     return bail(MPG_ERR_CUDA);
+  if (balloc(b, nullptr, &b->d_gbar, 1)) return bail(MPG_ERR_CUDA);
   int sms = 0, occ = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_cg_kernel(b->cg_threads), b->cg_threads, 0);
   b->max_cg_blocks = sms * occ;
-  if (b->max_cg_blocks < 1) return bail(MPG_ERR_CUDA);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_step_kernel(b->cg_threads), b->cg_threads, 0);
+  b->max_step_blocks = sms * occ;
+  if (b->max_cg_blocks < 1 || b->max_step_blocks < 1) return bail(MPG_ERR_CUDA);
   *out = b;
   return MPG_OK;
 }
@@ -1030,9 +1127,10 @@ int mpg_batch_destroy(mpg_batch *b) {
     cudaFree(b->mp[k].v);
   }
   void *ps[] = {b->d_slots, b->d_stats, b->d_base, b->d_count, b->d_hist, b->d_conv_plan, b->d_ef_plan,
-                b->d_block_items, b->d_items, b->d_cnt, b->d_start, b->d_scan};
+                b->d_block_items, b->d_items, b->d_cnt, b->d_start, b->d_scan, b->d_gbar};
   for (void *p : ps)
     if (p) cudaFree(p);
+  if (b->h_gbar) cudaFreeHost(b->h_gbar);
   if (b->h_stats) cudaFreeHost(b->h_stats);
   if (b->h_count) cudaFreeHost(b->h_count);
   if (b->gexec) cudaGraphExecDestroy(b->gexec);
@@ -1060,8 +1158,12 @@ int mpg_batch_set_tuning(mpg_batch *b, int cg_threads, int sort_interval) {
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_cg_kernel(cg_threads), cg_threads, 0);
   if (sms * occ < 1) return bfail(b, MPG_ERR_ARG, "solver block size %d cannot be resident", cg_threads);
+  int occ_step = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_step, batch_step_kernel(cg_threads), cg_threads, 0);
+  if (sms * occ_step < 1) return bfail(b, MPG_ERR_ARG, "step block size %d cannot be resident", cg_threads);
   b->cg_threads = cg_threads;
   b->max_cg_blocks = sms * occ;
+  b->max_step_blocks = sms * occ_step;
   b->sort_interval = sort_interval;
   b->plan_dirty = true;
   return MPG_OK;
@@ -1121,6 +1223,13 @@ int mpg_batch_prepare(const mpg_run_desc *d, mpg_run_prep **out) {
 
 int mpg_run_prep_destroy(mpg_run_prep *p) {
   delete p;
+  return MPG_OK;
+}
+
+int mpg_batch_set_fused(mpg_batch *b, int on) {
+  if (!b) return MPG_ERR_ARG;
+  b->fused = on != 0;
+  b->plan_dirty = true;
   return MPG_OK;
 }
 

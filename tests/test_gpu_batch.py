@@ -78,6 +78,33 @@ def test_run_admitted_mid_flight_equals_run_alone(mpg):
     assert mix.info(a).steps_done == 13
 
 
+def test_fused_step_equals_one_launch_per_phase(mpg):
+    """One persistent launch per batch step (phases behind grid barriers)
+    against one launch per phase, same runs: phi and the particle sets are
+    bit-identical, and a fused step launches one kernel."""
+    bts = []
+    for fused in (True, False):
+        bt = mpg.Batch(0, budget_bytes=4 << 30, particle_capacity=1 << 20)
+        bt.tuning(512, 3, fused=fused)
+        slots = [bt.admit(8, 20000, 61, vth=0.08, steps=20), bt.admit(12, 50000, 62, vth=0.05, steps=20),
+                 bt.admit(10, 30000, 63, vth=0.1, drift=(0.1, 0, 0), steps=20)]
+        bts.append((bt, slots))
+    for k in range(7):
+        sts = [bt.step(1) for bt, _ in bts]
+        assert all(st.rc == 0 for st in sts)
+        if k == 6:
+            assert sts[0].graph == 1 and sts[0].n_launches <= 1 + 10  # one step launch (+ a sort's kernels)
+    (f, fs), (u, us) = bts
+    for a, b in zip(fs, us):
+        assert (f.phi(a).view(np.uint64) == u.phi(b).view(np.uint64)).all()
+        x1, x2 = _sorted_state(*f.particles(a)), _sorted_state(*u.particles(b))
+        for p, q in zip(x1, x2):
+            assert (p == q).all()
+        i1, i2 = f.info(a), u.info(b)
+        assert i1.n_alive == i2.n_alive and i1.solver_iters == i2.solver_iters
+        assert abs(i1.ke - i2.ke) <= 1e-6 * i2.ke
+
+
 def test_batch_run_matches_single_run(mpg):
     n_side, n, seed, dt = 10, 40000, 5, 0.01
     bt = mpg.Batch(0, budget_bytes=4 << 30, particle_capacity=1 << 20)
