@@ -836,6 +836,8 @@ def main():
                     help="cell sort every K steps in the mixed form (default: the workload's, 10)")
     ap.add_argument("--mixed-solver", default="mg", choices=["cg", "mg"],
                     help="inner solver of the mixed form: plain CG or multigrid-preconditioned CG")
+    ap.add_argument("--form", default=None, choices=["mixed", "plain"],
+                    help="form of the timed run (default: plain for the small workload, mixed otherwise)")
     ap.add_argument("--particle-scale", type=float, default=1.0,
                     help="scale the workload's particle counts (small cases for profiler captures; the "
                          "workload name then carries the scale)")
@@ -894,7 +896,8 @@ def main():
     mpg = _pkg()
     mpg.build()
     mpg.load()
-    precision = mpg.PLAIN if args.workload == "small" else mpg.MIXED
+    form = args.form or ("plain" if args.workload == "small" else "mixed")
+    precision = mpg.PLAIN if form == "plain" else mpg.MIXED
     mixed = precision == mpg.MIXED
     ctx = make_ctx(mpg, w, precision, device=local, seed_offset=rank)
     for _ in range(args.warmup):

@@ -473,7 +473,7 @@ __device__ void solve_run(const SlotDev &S, SlotStat *st, const int part, const 
         s = S.phi[i];
       } else {
 #pragma unroll
-        for (int d = 0; d < kND; ++d) s += S.s64[d] * S.phi[i + S.off[d]];
+        for (int d = 0; d < kND; ++d) s = __fma_rn(S.s64[d], S.phi[i + S.off[d]], s);
       }
       const double ri = S.rhs[i] - s;
       S.r64[i] = ri;

@@ -432,7 +432,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mg(CgMgArgs a) {
     return true;
   };
   double bb = 0.0;
-  for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) bb += a.b[i] * a.b[i];
+  for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) bb = __fma_rn(a.b[i], a.b[i], bb);
   double t = block_sum(bb, red);
   if (threadIdx.x == 0) slot64(1, 3)[bid] = t;  // read after the first barrier
   int total_inner = 0, status = 0, sweeps = 0, phase = 0;
@@ -453,11 +453,11 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mg(CgMgArgs a) {
         s = a.x[i];
       } else {
 #pragma unroll
-        for (int d = 0; d < ND; ++d) s += v64[d * n + i] * a.x[dia_nb(i, a.A.off[d], a.A.nwrap)];
+        for (int d = 0; d < ND; ++d) s = __fma_rn(v64[d * n + i], a.x[dia_nb(i, a.A.off[d], a.A.nwrap)], s);
       }
       const double ri = a.b[i] - s;
       a.r64[i] = ri;
-      rr += ri * ri;
+      rr = __fma_rn(ri, ri, rr);
     }
     int set = phase & 1;
     t = block_sum(rr, red);
@@ -570,7 +570,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mg(CgMgArgs a) {
     rho_prev64 = rho64;
     // ---- x += |r64| z  (FP64)
     const double back = sqrt(rho64);
-    for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) a.x[i] += (double)a.z[i] * back;
+    for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) a.x[i] = __fma_rn((double)a.z[i], back, a.x[i]);
     if (!bar()) return;
   }
   if (bid == 0 && threadIdx.x == 0) {

@@ -332,7 +332,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
     for (int k = 0; k < K; ++k) out[k] = v[k];
   };
   double bb = 0.0;
-  for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) bb += a.b[i] * a.b[i];
+  for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) bb = __fma_rn(a.b[i], a.b[i], bb);
   double t = block_sum(bb, red);
   if (threadIdx.x == 0) slot64(1, 3)[bid] = t;  // read after the first barrier
   int total_inner = 0, status = 0, sweeps = 0;
@@ -349,11 +349,11 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
         s = a.x[i];
       } else {
 #pragma unroll
-        for (int d = 0; d < ND; ++d) s += v64[d * n + i] * a.x[dia_nb(i, a.A.off[d], a.A.nwrap)];
+        for (int d = 0; d < ND; ++d) s = __fma_rn(v64[d * n + i], a.x[dia_nb(i, a.A.off[d], a.A.nwrap)], s);
       }
       const double ri = a.b[i] - s;
       a.r64[i] = ri;
-      rr += ri * ri;
+      rr = __fma_rn(ri, ri, rr);
     }
     int set = phase & 1;
     t = block_sum(rr, red);
@@ -536,7 +536,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH) k_cg_mixed(CgMixedArgs a) {
     const double back = sqrt(rho64);
     const float4 *vz = a.v[cur];
     for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x)
-      a.x[i] += dis ? (double)vz[i].w * back * dis[i] : (double)vz[i].w * back;
+      a.x[i] = __fma_rn(dis ? (double)vz[i].w * dis[i] : (double)vz[i].w, back, a.x[i]);
     if (!grid_barrier(a.st, nb, epoch)) return;
   }
   if (bid == 0 && threadIdx.x == 0) {
