@@ -246,6 +246,12 @@ def mg_iter_bytes(n_side, N, coef, periodic=0):
     return b + 4 * m * m + 40 * x * g * g
 
 
+def kuhn_structured(w):
+    """The library walks an unjittered, non-periodic Kuhn cube through its
+    6-type table (mpg_kernels.h KuhnTable)."""
+    return w["jitter"] == 0 and not w.get("periodic", 0) and "ref_fills" not in w and w["n_side"] >= 3
+
+
 def phase_bytes(w, ctx, stats, steps, mpg):
     """Algorithmic bytes per launch of each phase of the mixed step.
 
@@ -265,15 +271,26 @@ def phase_bytes(w, ctx, stats, steps, mpg):
     sweep = (8 * nd + 24 + 20) * N
     if uses_mg(w):
         cg_iter = mg_iter_bytes(w["n_side"], N, coef, w.get("periodic", 0))
+    if kuhn_structured(w):
+        # uniform Kuhn mesh: the walk tables are a 6-type table: per tet E
+        # (16 B) and the charge-slot indices (16 B) are read and its four
+        # 8-byte charge slots written; the E pass reads the node ids (16 B) and
+        # writes E (16 B) per tet
+        move_tet, efield_tet = 16 + 16 + 32, 16 + 16
+        dep = N * (4 + 8 + 1 + 8) + T * 32
+    else:
+        # per tet the walk record (48 B), the neighbour table (16 B) and the
+        # charge-slot indices (16 B) read once and its four 8-byte charge
+        # slots written once; the E pass reads node ids and the record and
+        # writes E; the conversion reads slot offsets, background, flag, rhs
+        # per node and the 4T slots
+        move_tet, efield_tet, dep = 48 + 16 + 16 + 32, 16 + 48 + 12, N * (4 + 8 + 1 + 8) + T * 32
     return {
-        # 28 B read + 28 B write per particle; per tet the walk record (48 B), the
-        # neighbour table (16 B) and the charge-slot indices (16 B) read once and
-        # its four 8-byte charge slots written once
-        "move": P * 56 + T * (48 + 16 + 16 + 32),
+        # 28 B read + 28 B write per particle
+        "move": P * 56 + T * move_tet,
         "solve": iters * cg_iter + 3 * sweep,
-        "efield": T * (16 + 48 + 12) + N * 8,
-        # per node: slot offsets, background, flag, rhs; the 4T charge slots read
-        "deposit": N * (4 + 8 + 1 + 8) + T * 32,
+        "efield": T * efield_tet + N * 8,
+        "deposit": dep,
         "cg_iter_bytes": cg_iter, "iters_per_step": iters,
     }
 

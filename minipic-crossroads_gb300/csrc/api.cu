@@ -663,6 +663,18 @@ int upload_mesh(mpg_ctx *c) {
   TRY(dalloc(c, &d.c2n, h.T));
   CK(cudaMemcpyAsync(d.n2c_off, off.data(), sizeof(int32_t) * (h.N + 1), cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(d.c2n, c2n.data(), sizeof(int32_t) * 4 * h.T, cudaMemcpyHostToDevice, s));
+  // uniform Kuhn meshes: the mixed walk reads the 6-type table (MPG_KUHN_WALK=0
+  // keeps the per-tet records, for comparisons)
+  d.kuhn = 0;
+  const char *kw = getenv("MPG_KUHN_WALK");
+  if (!(kw && atoi(kw) == 0) && host_kuhn_table(h, d.ktab.jinv, d.ktab.face)) {
+    d.ktab.nx = h.d.nx;
+    d.ktab.ny = h.d.ny;
+    d.ktab.nz = h.d.nz;
+    TRY(dalloc(c, &d.etet4, h.T));
+    CK(cudaMemsetAsync(d.etet4, 0, sizeof(float4) * h.T, s));
+    d.kuhn = 1;
+  }
   CK(cudaStreamSynchronize(s));
   return MPG_OK;
 }
@@ -683,6 +695,8 @@ void free_mesh(mpg_ctx *c) {
   dfree(c, d.fill_ratio);
   dfree(c, d.n2c_off);
   dfree(c, d.c2n);
+  dfree(c, d.etet4);
+  d.kuhn = 0;
   d = DevMesh();
 }
 
@@ -1177,7 +1191,7 @@ int mpg_configure(mpg_ctx *c, const mpg_config *cfg) {
     TRY(dalloc(c, &c->Etet, 3 * T));
     TRY(dalloc(c, &c->acc, 4 * T));
     TRY(dalloc(c, &c->acc_node, N));
-    CK(cudaMemsetAsync(c->acc, 0, sizeof(unsigned long long) * 4 * T, c->stream));
+    CK(cudaMemsetAsync(c->acc, 0, sizeof(unsigned long long) * 4 * c->dm.T, c->stream));
     TRY(dalloc(c, &c->sort_cnt, T + 1));
     TRY(dalloc(c, &c->sort_start, T + 1));
     CK(cudaMemsetAsync(c->phi, 0, sizeof(double) * N, c->stream));
@@ -1692,7 +1706,16 @@ int mpg_get_field(mpg_ctx *c, int which, double *host) {
     else
       memset(host, 0, sizeof(double) * N);
   } else if (which == MPG_FIELD_E_TET) {
-    if (c->cfg.precision == MPG_MIXED) {
+    if (c->cfg.precision == MPG_MIXED && c->dm.kuhn) {
+      std::vector<float4> e4(T);
+      CK(cudaMemcpyAsync(e4.data(), c->dm.etet4, sizeof(float4) * T, cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      for (int64_t t = 0; t < T; ++t) {
+        host[3 * t] = e4[t].x;
+        host[3 * t + 1] = e4[t].y;
+        host[3 * t + 2] = e4[t].z;
+      }
+    } else if (c->cfg.precision == MPG_MIXED) {
       std::vector<float> rec(12 * T);
       CK(cudaMemcpyAsync(rec.data(), c->dm.mrec, sizeof(float) * 12 * T, cudaMemcpyDeviceToHost, s));
       CK(cudaStreamSynchronize(s));

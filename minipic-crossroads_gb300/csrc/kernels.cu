@@ -534,6 +534,30 @@ __device__ __forceinline__ void deposit_fixed_warp(unsigned long long *__restric
   deposit_fixed_warp_t(acc, [&](int k) { return c2n[k]; }, key, b1, b2, b3, Q);
 }
 
+// Walk tables of a uniform Kuhn mesh (KuhnTable, staged in shared memory):
+// J^-1 by tet type t % 6, neighbours by hex offset.  A crossing needs no
+// memory access at all; E of the start tet comes from etet4.
+struct KuhnWalk {
+  const float *__restrict__ jinv;   // 6 x 9
+  const uint32_t *__restrict__ fw;  // 6 x 4 face words
+  uint32_t nx, ny, nz;
+  __device__ __forceinline__ void load(uint32_t e, float4 &r0, float4 &r1, float4 &r2) const {
+    const float *J = jinv + 9 * (e % 6u);
+    r0 = make_float4(J[0], J[1], J[2], J[3]);
+    r1 = make_float4(J[4], J[5], J[6], J[7]);
+    r2.x = J[8];  // r2.yzw (E) is used by the kick at the start only
+  }
+  __device__ __forceinline__ uint32_t face(uint32_t e, int k) const {
+    const uint32_t h = e / 6u, ty = e - 6u * h;
+    const uint32_t f = fw[4 * ty + k];
+    const uint32_t nyz = ny * nz, i = h / nyz, rem = h - i * nyz, j = rem / nz, kk = rem - j * nz;
+    const int ni = (int)i + (int)(f & 3u) - 1, nj = (int)j + (int)((f >> 2) & 3u) - 1,
+              nk = (int)kk + (int)((f >> 4) & 3u) - 1;
+    if (ni < 0 || ni >= (int)nx || nj < 0 || nj >= (int)ny || nk < 0 || nk >= (int)nz) return MPG_WALL;
+    return ((f >> 16) << 24) | (6u * (((uint32_t)ni * ny + (uint32_t)nj) * nz + (uint32_t)nk) + ((f >> 8) & 0xFFu));
+  }
+};
+
 __global__ void __launch_bounds__(kThreads) k_mixed_deposit(MixedParts P, int64_t n, const int4 *__restrict__ c2n,
                                                             SpeciesTable S, unsigned long long *__restrict__ acc) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -608,6 +632,24 @@ __global__ void k_efield_mixed(int64_t T, const int4 *__restrict__ tets, float4 
   rec[3 * t + 2] = r2;
 }
 
+// E per tet on a uniform Kuhn mesh: the arithmetic of k_efield_mixed with
+// J^-1 from the 6-type table, written as (Ex, Ey, Ez, 0)
+__global__ void k_efield_kuhn(int64_t T, const int4 *__restrict__ tets, KuhnTable kt, const double *__restrict__ phi,
+                              float4 *__restrict__ etet4) {
+  __shared__ float sj[54];
+  for (int i = threadIdx.x; i < 54; i += blockDim.x) sj[i] = kt.jinv[i / 9][i % 9];
+  __syncthreads();
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T) return;
+  const int4 nd = tets[t];
+  const double f0 = phi[nd.x];
+  const float d1 = (float)(phi[nd.y] - f0), d2 = (float)(phi[nd.z] - f0), d3 = (float)(phi[nd.w] - f0);
+  const float *J = sj + 9 * (int)(t % 6);
+  etet4[t] = make_float4(__fmaf_rn(d3, J[6], __fmaf_rn(d2, J[3], d1 * J[0])),
+                         __fmaf_rn(d3, J[7], __fmaf_rn(d2, J[4], d1 * J[1])),
+                         __fmaf_rn(d3, J[8], __fmaf_rn(d2, J[5], d1 * J[2])), 0.f);
+}
+
 __global__ void __launch_bounds__(kThreads) k_mixed_move(MixedParts P, int64_t n, const float4 *__restrict__ rec,
                                                          const uint4 *__restrict__ nbr,
                                                          const int4 *__restrict__ c2n, SpeciesTable S, float dt,
@@ -661,16 +703,27 @@ __global__ void __launch_bounds__(kThreads) k_mixed_move(MixedParts P, int64_t n
 // grid).  The next chunk's particle record is loaded before the current chunk
 // is processed, so its DRAM latency overlaps the push, walk and deposit of
 // the current one; block totals are formed once per block.  Per particle the
-// arithmetic is that of k_mixed_move.
-__global__ void __launch_bounds__(kThreads) k_mixed_move_persistent(MixedParts P, int64_t n,
+// arithmetic is that of k_mixed_move.  KUHN: the walk tables come from the
+// 6-type table of a uniform Kuhn mesh (same values, bit for bit, as the
+// per-tet records the table was checked against).
+template <bool KUHN>
+__global__ void __launch_bounds__(kThreads, 4) k_mixed_move_persistent(MixedParts P, int64_t n,
                                                                     const float4 *__restrict__ rec,
                                                                     const uint4 *__restrict__ nbr,
+                                                                    const float4 *__restrict__ etet4, KuhnTable kt,
                                                                     const int4 *__restrict__ c2n, SpeciesTable S,
                                                                     float dt, int kill, int max_cross,
                                                                     unsigned long long *__restrict__ acc,
                                                                     DevStats *st) {
   __shared__ BlockTotals bt;
-  block_totals_init(&bt);
+  __shared__ float s_jinv[KUHN ? 54 : 1];
+  __shared__ uint32_t s_face[KUHN ? 24 : 1];
+  if (KUHN) {
+    for (int i = threadIdx.x; i < 54; i += blockDim.x) s_jinv[i] = kt.jinv[i / 9][i % 9];
+    for (int i = threadIdx.x; i < 24; i += blockDim.x) s_face[i] = kt.face[i / 4][i % 4];
+  }
+  block_totals_init(&bt);  // also the barrier after the table stores
+  const KuhnWalk kw{s_jinv, s_face, (uint32_t)kt.nx, (uint32_t)kt.ny, (uint32_t)kt.nz};
   const int lane = threadIdx.x & 31;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const int64_t nchunks = (n + 31) >> 5;
@@ -712,8 +765,19 @@ __global__ void __launch_bounds__(kThreads) k_mixed_move_persistent(MixedParts P
       float l1 = bv.x, l2 = bv.y, l3 = bv.z;
       float vx = bv.w, vy = vv.x, vz = vv.y;
       bool dead, lim;
-      const int it = mixed_walk(rec, nbr, e, l1, l2, l3, vx, vy, vz, 0.5f * dt * S.qm_f[s], dt, kill, max_cross,
-                                dead, lim);
+      int it;
+      if (KUHN) {
+        float4 r0, r1, r2;
+        kw.load(e, r0, r1, r2);
+        const float4 E = etet4[e];
+        r2.y = E.x;
+        r2.z = E.y;
+        r2.w = E.z;
+        it = mixed_walk_t(kw, e, r0, r1, r2, l1, l2, l3, vx, vy, vz, 0.5f * dt * S.qm_f[s], dt, kill, max_cross, dead,
+                          lim);
+      } else {
+        it = mixed_walk(rec, nbr, e, l1, l2, l3, vx, vy, vz, 0.5f * dt * S.qm_f[s], dt, kill, max_cross, dead, lim);
+      }
       limit += lim ? 1u : 0u;
       cross += (unsigned)it;
       if (dead) {
@@ -1289,16 +1353,20 @@ void launch_mixed_deposit(cudaStream_t s, const MixedParts &P, int64_t n, const 
 }
 void launch_mixed_convert(cudaStream_t s, const DevMesh &M, unsigned long long *acc, double quantum, const double *bg,
                           double *rhs) {
-  k_mixed_convert<<<grid_for(M.N), kThreads, 0, s>>>(M.N, M.n2c_off, acc, quantum, bg, M.bnd, rhs, M.nsolve,
-                                                     M.fper ? M.plane : 0);
+  k_mixed_convert<<<grid_for(M.N), kThreads, 0, s>>>(M.N, M.n2c_off, acc, quantum, bg, M.bnd, rhs,
+                                                     M.nsolve, M.fper ? M.plane : 0);
 }
 void launch_node_quanta(cudaStream_t s, const DevMesh &M, const unsigned long long *acc, long long *out) {
   k_node_quanta<<<grid_for(M.N), kThreads, 0, s>>>(M.N, M.n2c_off, acc, out);
 }
 void launch_efield_mixed(cudaStream_t s, const DevMesh &M, const double *phi) {
-  k_efield_mixed<<<grid_for(M.T), kThreads, 0, s>>>(M.T, M.tets, M.mrec, phi);
+  if (M.kuhn)
+    k_efield_kuhn<<<grid_for(M.T), kThreads, 0, s>>>(M.T, M.tets, M.ktab, phi, M.etet4);
+  else
+    k_efield_mixed<<<grid_for(M.T), kThreads, 0, s>>>(M.T, M.tets, M.mrec, phi);
 }
-// resident blocks of the persistent move kernel on the current device (one wave)
+// resident blocks of a persistent move kernel on the current device (one wave)
+template <bool KUHN>
 static unsigned move_wave_blocks() {
   static int cached[64] = {0};
   int dev = 0;
@@ -1307,7 +1375,7 @@ static unsigned move_wave_blocks() {
   if (!cached[dev]) {
     int sms = 0, occ = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mixed_move_persistent, kThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mixed_move_persistent<KUHN>, kThreads, 0);
     cached[dev] = (sms > 0 ? sms : 1) * (occ > 0 ? occ : 1);
   }
   return (unsigned)cached[dev];
@@ -1315,15 +1383,21 @@ static unsigned move_wave_blocks() {
 void launch_mixed_move(cudaStream_t s, const MixedParts &P, int64_t n, const DevMesh &M, const SpeciesTable &S,
                        float dt, int kill, int max_cross, unsigned long long *acc, DevStats *st) {
   if (n <= 0) return;
+  const unsigned want = grid_for(n);
+  if (M.kuhn) {
+    const unsigned wave = move_wave_blocks<true>();
+    k_mixed_move_persistent<true><<<want < wave ? want : wave, kThreads, 0, s>>>(
+        P, n, M.mrec, M.mnbr, M.etet4, M.ktab, M.c2n, S, dt, kill, max_cross, acc, st);
+    return;
+  }
   static const char *env = getenv("MPG_MOVE_KERNEL");
   if (env && atoi(env) == 0) {
     k_mixed_move<<<grid_for(n), kThreads, 0, s>>>(P, n, M.mrec, M.mnbr, M.c2n, S, dt, kill, max_cross, acc, st);
     return;
   }
-  const unsigned wave = move_wave_blocks();
-  const unsigned want = grid_for(n);
-  k_mixed_move_persistent<<<want < wave ? want : wave, kThreads, 0, s>>>(P, n, M.mrec, M.mnbr, M.c2n, S, dt, kill,
-                                                                         max_cross, acc, st);
+  const unsigned wave = move_wave_blocks<false>();
+  k_mixed_move_persistent<false><<<want < wave ? want : wave, kThreads, 0, s>>>(
+      P, n, M.mrec, M.mnbr, M.etet4, M.ktab, M.c2n, S, dt, kill, max_cross, acc, st);
 }
 // the five passes of the stable cell sort; leaves perm[0..count) and start
 // (T + 1 entries) behind, and the count in *d_count

@@ -490,3 +490,65 @@ void host_charge_slots(const HostMesh &m, std::vector<int32_t> &off, std::vector
   for (int64_t t = 0; t < m.T; ++t)
     for (int k = 0; k < 4; ++k) c2n[4 * t + k] = fill[m.tets[4 * t + k]]++;
 }
+
+bool host_kuhn_table(const HostMesh &m, float jinv[6][9], uint32_t face[6][4]) {
+  const mpg_mesh_desc &d = m.d;
+  if (d.split != MPG_SPLIT_KUHN6 || d.mapping != MPG_MAP_NONE || d.periodic) return false;
+  const int64_t nx = d.nx, ny = d.ny, nz = d.nz;
+  if (nx < 3 || ny < 3 || nz < 3 || m.T != 6 * nx * ny * nz) return false;
+  // reference hex (1, 1, 1): all its face neighbours are interior tets
+  const int64_t h0 = (1 * ny + 1) * nz + 1;
+  for (int k = 0; k < 6; ++k) {
+    const int64_t t = 6 * h0 + k;
+    for (int q = 0; q < 9; ++q) jinv[k][q] = (float)m.jinv[9 * t + q];
+    for (int v = 0; v < 4; ++v) {
+      const uint32_t w = m.nbr_opp[4 * t + v];
+      const uint32_t nb = w & 0xFFFFFFu;
+      if (nb == 0xFFFFFFu) return false;
+      const int64_t h = nb / 6, di = h / (ny * nz) - 1, dj = (h / nz) % ny - 1, dk = h % nz - 1;
+      if (di < -1 || di > 1 || dj < -1 || dj > 1 || dk < -1 || dk > 1) return false;
+      face[k][v] = (uint32_t)(di + 1) | (uint32_t)(dj + 1) << 2 | (uint32_t)(dk + 1) << 4 | (nb % 6) << 8 |
+                   (w >> 24) << 16;
+    }
+  }
+  // the corner (x = 4, y = 2, z = 1) of each local vertex, to check the node
+  // numbering of every tet as well
+  const int64_t si = (ny + 1) * (nz + 1), sj = nz + 1;
+  const int64_t base0 = 1 * si + 1 * sj + 1;
+  int corner[6][4];
+  for (int k = 0; k < 6; ++k)
+    for (int q = 0; q < 4; ++q) {
+      const int64_t r = m.tets[4 * (6 * h0 + k) + q] - base0;
+      const int64_t di = r / si, dj = (r % si) / sj, dk = r % sj;
+      if (r < 0 || di > 1 || dj > 1 || dk > 1) return false;
+      corner[k][q] = (int)(4 * di + 2 * dj + dk);
+    }
+  // every tet must match its type's entries bit for bit
+  int bad = 0;
+#pragma omp parallel for schedule(static) reduction(+ : bad)
+  for (int64_t t = 0; t < m.T; ++t) {
+    const int k = (int)(t % 6);
+    for (int q = 0; q < 9; ++q)
+      if ((float)m.jinv[9 * t + q] != jinv[k][q]) ++bad;
+    const int64_t h = t / 6, i = h / (ny * nz), j = (h / nz) % ny, kk = h % nz;
+    const int64_t base = i * si + j * sj + kk;
+    for (int q = 0; q < 4; ++q) {
+      const int c = corner[k][q];
+      if (m.tets[4 * t + q] != base + (c >> 2) * si + ((c >> 1) & 1) * sj + (c & 1)) ++bad;
+    }
+    for (int v = 0; v < 4; ++v) {
+      const uint32_t f = face[k][v];
+      const int64_t ni = i + (int64_t)(f & 3) - 1, nj = j + (int64_t)((f >> 2) & 3) - 1,
+                    nk = kk + (int64_t)((f >> 4) & 3) - 1;
+      uint32_t want;
+      if (ni < 0 || ni >= nx || nj < 0 || nj >= ny || nk < 0 || nk >= nz)
+        want = 0xFFFFFFu;
+      else
+        want = ((f >> 16) << 24) | (uint32_t)(6 * ((ni * ny + nj) * nz + nk) + ((f >> 8) & 0xFF));
+      const uint32_t got = m.nbr_opp[4 * t + v];
+      // a wall carries no permutation
+      if ((got & 0xFFFFFFu) == 0xFFFFFFu ? want != 0xFFFFFFu : got != want) ++bad;
+    }
+  }
+  return bad == 0;
+}

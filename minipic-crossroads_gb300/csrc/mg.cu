@@ -628,6 +628,13 @@ int run_cg_mg(cudaStream_t s, const DiaMatrix &A, const MgDev &mg, const double 
   a.mg.lev[0].t = f + 8 * n;
   a.mg.lev[0].t2 = f + 9 * n;
   a.u = a.mg.lev[0].t;
+  if (!mg.fuse_update) {
+    // without the fused update no pass reads a neighbour's old residual while
+    // the new one is written, so r and s are updated in place: two fine-level
+    // vectors fewer in the working set (L2)
+    a.r[1] = a.r[0];
+    a.s[1] = a.s[0];
+  }
   a.partials = w.partials;
   a.tol2 = tol * tol;
   a.inner_tol2 = inner_tol * inner_tol;

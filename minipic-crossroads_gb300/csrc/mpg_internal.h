@@ -66,6 +66,13 @@ struct MgHostHierarchy {
 bool host_mg_build(const HostMesh &m, const std::vector<int32_t> &rp, const std::vector<int32_t> &col,
                    const std::vector<double> &val, MgHostHierarchy &H, std::string &why, int64_t dense_max = 0);
 
+// The 6-type walk table of a uniform Kuhn mesh (see KuhnTable in
+// mpg_kernels.h): jinv[k][9] and face[k][4] from the tets of one interior hex,
+// then checked against every tet's J^-1 (as the FP32 walk record holds it)
+// and neighbour word.  False when the mesh is not such a mesh or any tet
+// differs (the walk then uses the per-tet records).
+bool host_kuhn_table(const HostMesh &m, float jinv[6][9], uint32_t face[6][4]);
+
 // counter-based generator shared by the jitter and the fills (splitmix64 finaliser)
 static inline uint64_t mpg_mix64(uint64_t z) {
   z += 0x9E3779B97F4A7C15ULL;

@@ -24,6 +24,19 @@ struct MixedParts {
   int64_t cap;
 };
 
+// Uniform Kuhn meshes (unmapped, not periodic): every tet of type k = t % 6
+// has the same J^-1, and its face neighbours sit at the same hex offsets
+// with the same types and vertex permutations, so the mixed walk reads them
+// from this 6-type table instead of per-tet records.  face word per type and
+// opposite vertex: (di+1) | (dj+1) << 2 | (dk+1) << 4 | type' << 8 | perm << 16
+// (di, dj, dk the neighbour hex's offset; the face is a wall when that hex
+// lies outside the grid).
+struct KuhnTable {
+  float jinv[6][9];
+  uint32_t face[6][4];
+  int nx = 0, ny = 0, nz = 0;
+};
+
 struct DevMesh {
   int64_t T = 0, N = 0;
   int4 *tets = nullptr;      // T
@@ -47,6 +60,11 @@ struct DevMesh {
   // c2n[t] holds the slots of tet t's four corners
   int32_t *n2c_off = nullptr;   // N+1
   int4 *c2n = nullptr;          // T
+  // uniform Kuhn meshes: the 6-type walk table, and E per tet as (Ex, Ey, Ez, 0)
+  // (the E-field pass writes etet4 instead of the records' E)
+  int kuhn = 0;
+  KuhnTable ktab;
+  float4 *etet4 = nullptr;      // T
 };
 
 // ---- plain FP64 path ------------------------------------------------------

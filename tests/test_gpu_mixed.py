@@ -253,3 +253,31 @@ def test_extrapolated_initial_guess_same_solution(mpg, form, ws):
             ib += sb.solver_iters
     # the extrapolated start is closer: never more iterations in total
     assert ib <= ia, (ia, ib)
+
+
+def test_kuhn_table_walk_equals_per_tet_records(mpg, monkeypatch):
+    """On a uniform Kuhn mesh the mixed walk reads J^-1 and the neighbours from
+    the 6-type table; against the per-tet records (MPG_KUHN_WALK=0) the state,
+    the per-node charge, phi, E and the counts after several steps with many
+    crossings and wall exits are bit-identical."""
+    runs = []
+    for kw in ("1", "0"):
+        monkeypatch.setenv("MPG_KUHN_WALK", kw)
+        ctx = mpg.Ctx(0)
+        ctx.mesh(12, split=mpg.SPLIT_KUHN6)
+        ctx.configure(precision=mpg.MIXED, deposit=mpg.DEPOSIT_LINEAR, solver=mpg.SOLVER_CG_MG, tol=1e-10,
+                      warm_start=2, kill_on_wall=1, sort_interval=3, rho_background=1.0)
+        n = 60000
+        ctx.reserve(n)
+        ctx.fill_uniform(n // 2, 4, 0, 1.0 / n, drift=(0.3, 0, 0), vth=0.1)
+        ctx.fill_uniform(n // 2, 5, 0, 1.0 / n, drift=(-0.3, 0, 0), vth=0.1)
+        sts = [ctx.step(0.02, 1) for _ in range(7)]
+        runs.append((ctx.mixed_download() + (ctx.charge()[0],), ctx.get_field(mpg.FIELD_PHI),
+                     ctx.get_field(mpg.FIELD_E_TET), [(s.n_alive, s.n_crossings, s.n_killed) for s in sts]))
+        ctx.close()
+    (a, pa, ea, ca), (b, pb, eb, cb) = runs
+    assert ca == cb and sum(k for _, _, k in ca) > 0 and sum(c for _, c, _ in ca) > 0
+    for u, v in zip(a, b):
+        assert (u.view(np.uint8) == v.view(np.uint8)).all()
+    assert (pa.view(np.uint64) == pb.view(np.uint64)).all()
+    assert (ea.view(np.uint64) == eb.view(np.uint64)).all()
