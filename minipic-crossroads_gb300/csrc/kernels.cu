@@ -234,46 +234,46 @@ __global__ void k_efield_plain(int64_t T, const int4 *__restrict__ tets, const d
 __device__ __forceinline__ double plain_intersect(const DevMesh &M, int &e, double x[3], double xr[3], double v[3],
                                                   double vr[3], double dt, double time_remaining, int kill,
                                                   bool &killed) {
-  const double local_dt = dt * time_remaining;
-  double scale_fact = 1.0;
+  const double span = dt * time_remaining;
+  double frac = 1.0;
   int face = -1;
-  double dx_ref[3], xf[3];
+  double dlam[3], lend[3];
   for (int d = 0; d < 3; ++d) {
-    dx_ref[d] = local_dt * vr[d];
-    xf[d] = xr[d] + dx_ref[d];
+    dlam[d] = span * vr[d];
+    lend[d] = xr[d] + dlam[d];
   }
-  if (vr[2] < 0 && xf[2] < 0) {
+  if (vr[2] < 0 && lend[2] < 0) {
     face = 3;
-    scale_fact = -xr[2] / (dx_ref[2]);
+    frac = -xr[2] / (dlam[2]);
   }
-  if (vr[1] < 0 && xf[1] < 0) {
-    const double sfy = -xr[1] / (dx_ref[1]);
-    if (sfy < scale_fact) {
+  if (vr[1] < 0 && lend[1] < 0) {
+    const double fy = -xr[1] / (dlam[1]);
+    if (fy < frac) {
       face = 0;
-      scale_fact = sfy;
+      frac = fy;
     }
   }
-  if (vr[0] < 0 && xf[0] < 0) {
-    const double sfx = -xr[0] / (dx_ref[0]);
-    if (sfx < scale_fact) {
+  if (vr[0] < 0 && lend[0] < 0) {
+    const double fx = -xr[0] / (dlam[0]);
+    if (fx < frac) {
       face = 2;
-      scale_fact = sfx;
+      frac = fx;
     }
   }
-  const double xf_sum = xf[0] + xf[1] + xf[2];
-  const double vr_sum = vr[0] + vr[1] + vr[2];
-  if (vr_sum > 0 && xf_sum > 1) {
-    const double sfs = (1 - xr[0] - xr[1] - xr[2]) / (dx_ref[0] + dx_ref[1] + dx_ref[2]);
-    if (sfs < scale_fact) {
+  const double end_sum = lend[0] + lend[1] + lend[2];
+  const double rate_sum = vr[0] + vr[1] + vr[2];
+  if (rate_sum > 0 && end_sum > 1) {
+    const double fs = (1 - xr[0] - xr[1] - xr[2]) / (dlam[0] + dlam[1] + dlam[2]);
+    if (fs < frac) {
       face = 1;
-      scale_fact = sfs;
+      frac = fs;
     }
   }
   for (int d = 0; d < 3; ++d) {
-    x[d] = x[d] + scale_fact * local_dt * v[d];
-    xr[d] = xr[d] + scale_fact * local_dt * vr[d];
+    x[d] = x[d] + frac * span * v[d];
+    xr[d] = xr[d] + frac * span * vr[d];
   }
-  if (scale_fact < 1) {
+  if (frac < 1) {
     const int4 nb4 = M.nbrs[e];
     const int nb = face == 0 ? nb4.x : face == 1 ? nb4.y : face == 2 ? nb4.z : nb4.w;
     if (nb >= 0) {
@@ -305,7 +305,7 @@ __device__ __forceinline__ double plain_intersect(const DevMesh &M, int &e, doub
       jinv_apply(M.jinv + 9 * (int64_t)e, v, vr);
     }
   }
-  return scale_fact;
+  return frac;
 }
 
 __global__ void __launch_bounds__(kThreads) k_plain_move(PlainParts P, int64_t n, DevMesh M,

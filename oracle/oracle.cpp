@@ -748,49 +748,49 @@ extern "C" void orc_push(const orc_mesh *m, int64_t n, const int32_t *cell, cons
 
 /* ------------------------------------------------------------------------ */
 /* walk: particle_move.hpp:102-124 (loop) and :135-225 (find_intersection)   */
-// returns scale_fact; *killed set when the particle left through an absorbing wall
+// returns the fraction of the sub-step used; *killed set when the particle left through an absorbing wall
 static inline double find_intersection(const orc_mesh *m, int32_t &e, double *x, double *xr, double *v, double *vr,
                                        double dt, double time_remaining, int kill, bool &killed) {
-  const double local_dt = dt * time_remaining;
-  double scale_fact = 1.0;
+  const double span = dt * time_remaining;
+  double frac = 1.0;
   int face = -1;
-  double dx_ref[3], xf[3];
+  double dlam[3], lend[3];
   for (int d = 0; d < 3; ++d) {
-    dx_ref[d] = local_dt * vr[d];
-    xf[d] = xr[d] + dx_ref[d];
+    dlam[d] = span * vr[d];
+    lend[d] = xr[d] + dlam[d];
   }
-  if (vr[2] < 0 && xf[2] < 0) {
+  if (vr[2] < 0 && lend[2] < 0) {
     face = 3;
-    scale_fact = -xr[2] / (dx_ref[2]);
+    frac = -xr[2] / (dlam[2]);
   }
-  if (vr[1] < 0 && xf[1] < 0) {
-    double sfy = -xr[1] / (dx_ref[1]);
-    if (sfy < scale_fact) {
+  if (vr[1] < 0 && lend[1] < 0) {
+    double fy = -xr[1] / (dlam[1]);
+    if (fy < frac) {
       face = 0;
-      scale_fact = sfy;
+      frac = fy;
     }
   }
-  if (vr[0] < 0 && xf[0] < 0) {
-    double sfx = -xr[0] / (dx_ref[0]);
-    if (sfx < scale_fact) {
+  if (vr[0] < 0 && lend[0] < 0) {
+    double fx = -xr[0] / (dlam[0]);
+    if (fx < frac) {
       face = 2;
-      scale_fact = sfx;
+      frac = fx;
     }
   }
-  double xf_sum = xf[0] + xf[1] + xf[2];
-  double vr_sum = vr[0] + vr[1] + vr[2];
-  if (vr_sum > 0 && xf_sum > 1) {
-    double sfs = (1 - xr[0] - xr[1] - xr[2]) / (dx_ref[0] + dx_ref[1] + dx_ref[2]);
-    if (sfs < scale_fact) {
+  double end_sum = lend[0] + lend[1] + lend[2];
+  double rate_sum = vr[0] + vr[1] + vr[2];
+  if (rate_sum > 0 && end_sum > 1) {
+    double fs = (1 - xr[0] - xr[1] - xr[2]) / (dlam[0] + dlam[1] + dlam[2]);
+    if (fs < frac) {
       face = 1;
-      scale_fact = sfs;
+      frac = fs;
     }
   }
   for (int d = 0; d < 3; ++d) {
-    x[d] = x[d] + scale_fact * local_dt * v[d];
-    xr[d] = xr[d] + scale_fact * local_dt * vr[d];
+    x[d] = x[d] + frac * span * v[d];
+    xr[d] = xr[d] + frac * span * vr[d];
   }
-  if (scale_fact < 1) {
+  if (frac < 1) {
     int32_t nb = m->nbrs[4 * e + face];
     if (nb >= 0) {
       // a periodic face wraps x to the other side of the box.  The reference's
@@ -824,7 +824,7 @@ static inline double find_intersection(const orc_mesh *m, int32_t &e, double *x,
       jinv_apply(&m->jinv[9 * e], v, vr);
     }
   }
-  return scale_fact;
+  return frac;
 }
 
 extern "C" int64_t orc_walk(const orc_mesh *m, int64_t n, int32_t *cell, double *x, double *xref, double *v,
