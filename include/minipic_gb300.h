@@ -206,14 +206,15 @@ int mpg_cg_csr(mpg_ctx *ctx, int64_t n, const int32_t *d_rowptr, const int32_t *
                const double *d_b, double *d_x, double tol, int max_iter, int *iters, double *resid);
 
 /* ---- batched ensemble / serving (no counterpart in the reference) --------
- * Many independent runs (each: Kuhn-split unit cube n^3, one species,
- * volume-uniform fill, absorbing walls, mixed precision) resident on one GPU
+ * Many independent runs (each: Kuhn-split unit cube n^3, uniform or with
+ * jittered interior nodes, one species, volume-uniform fill, absorbing
+ * walls, mixed precision) resident on one GPU
  * and advanced together: one persistent launch per step for all active runs
  * (charge conversion, field solve, E field, fused push/walk/deposit, with
  * grid barriers between them; mpg_batch_set_fused), the step captured in a
- * CUDA graph.  The field operator of a batched run is the
- * uniform Kuhn stencil of its mesh (constant coefficients, FP32 inside FP64
- * refinement).  Runs are admitted against a device-memory budget, step
+ * CUDA graph.  The field operator of a batched run is the 15-point Kuhn
+ * stencil of its mesh (constant coefficients on a uniform mesh, per-row
+ * coefficients on a jittered one; FP32 inside FP64 refinement).  Runs are admitted against a device-memory budget, step
  * until their requested step count and are retired to free their slot.
  * A run's results do not depend on which other runs share the batch. */
 typedef struct mpg_batch mpg_batch;
@@ -231,6 +232,8 @@ typedef struct {
   double tol;            /* relative residual of the field solve */
   int max_iter;
   int steps;             /* the run finishes after this many steps */
+  double jitter;         /* interior nodes moved by up to +-jitter h per axis (0: uniform mesh, < 0.5) */
+  uint64_t mesh_seed;    /* jitter seed */
 } mpg_run_desc;
 
 typedef struct {

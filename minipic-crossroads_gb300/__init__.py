@@ -69,7 +69,7 @@ class RunDesc(C.Structure):
     _fields_ = [("n_side", C.c_int), ("n_particles", C.c_int64), ("seed", C.c_uint64), ("q", C.c_double),
                 ("m", C.c_double), ("weight", C.c_double), ("vth", C.c_double), ("drift", C.c_double * 3),
                 ("rho_background", C.c_double), ("dt", C.c_double), ("tol", C.c_double), ("max_iter", C.c_int),
-                ("steps", C.c_int)]
+                ("steps", C.c_int), ("jitter", C.c_double), ("mesh_seed", C.c_uint64)]
 
 
 class RunInfo(C.Structure):
@@ -461,11 +461,11 @@ class Batch:
 
     @staticmethod
     def desc(n_side, n_particles, seed, q=-1.0, m=1.0, weight=None, vth=0.05, drift=(0.0, 0.0, 0.0),
-             rho_background=None, dt=0.01, tol=1e-10, max_iter=5000, steps=100):
+             rho_background=None, dt=0.01, tol=1e-10, max_iter=5000, steps=100, jitter=0.0, mesh_seed=1):
         w = (1.0 / n_particles) if weight is None else weight
         rho = (-q * w * n_particles) if rho_background is None else rho_background
         return RunDesc(n_side, int(n_particles), seed, q, m, w, vth, (C.c_double * 3)(*drift), rho, dt, tol,
-                       max_iter, steps)
+                       max_iter, steps, jitter, mesh_seed)
 
     def admit(self, n_side, n_particles, seed, allow=(), **kw):
         d = self.desc(n_side, n_particles, seed, **kw)

@@ -667,10 +667,13 @@ int upload_mesh(mpg_ctx *c) {
   // keeps the per-tet records, for comparisons)
   d.kuhn = 0;
   const char *kw = getenv("MPG_KUHN_WALK");
-  if (!(kw && atoi(kw) == 0) && host_kuhn_table(h, d.ktab.jinv, d.ktab.face)) {
+  const int64_t nyz = (int64_t)h.d.ny * h.d.nz;
+  if (!(kw && atoi(kw) == 0) && nyz <= (1 << 16) && host_kuhn_table(h, d.ktab.jinv, d.ktab.face)) {
     d.ktab.nx = h.d.nx;
     d.ktab.ny = h.d.ny;
     d.ktab.nz = h.d.nz;
+    d.ktab.mz = ((1ull << 40) + (unsigned long long)h.d.nz - 1) / (unsigned long long)h.d.nz;
+    d.ktab.myz = ((1ull << 40) + (unsigned long long)nyz - 1) / (unsigned long long)nyz;
     TRY(dalloc(c, &d.etet4, h.T));
     CK(cudaMemsetAsync(d.etet4, 0, sizeof(float4) * h.T, s));
     d.kuhn = 1;

@@ -17,9 +17,10 @@
 // drops the particles of retired runs.  The steps run from a captured CUDA
 // graph, re-captured when the set of runs or the particle count changes.
 //
-// The field operator of a batched run is the uniform Kuhn stencil of its mesh
-// (constant coefficients; FP32 inner CG, FP64 outer residual), so runs carry
-// no matrix.  Nothing a kernel computes for one run reads another run's
+// The field operator of a batched run is the 15-point Kuhn stencil of its
+// mesh (FP32 inner CG, FP64 outer residual): constant coefficients on a
+// uniform mesh, so such a run carries no matrix; per-row coefficients (15
+// diagonals, FP64 and FP32 copies) on a mesh with jittered interior nodes.  Nothing a kernel computes for one run reads another run's
 // data, and every per-run reduction has a fixed order, so a run's field and
 // particle state do not depend on which runs share the batch.
 #include <cuda_runtime.h>
@@ -62,6 +63,10 @@ struct SlotDev {
   int off[kND];
   double s64[kND];
   float s32[kND];
+  // jittered mesh: row i's coefficient of diagonal d at v64[d * N + i] (FP64)
+  // and v32 (FP32); null on a uniform mesh (s64 / s32 for every row)
+  const double *v64;
+  const float *v32;
   double quantum;
   int Q;
   float hk, dt;
@@ -473,7 +478,7 @@ __device__ void solve_run(const SlotDev &S, SlotStat *st, const int part, const 
         s = S.phi[i];
       } else {
 #pragma unroll
-        for (int d = 0; d < kND; ++d) s = __fma_rn(S.s64[d], S.phi[i + S.off[d]], s);
+        for (int d = 0; d < kND; ++d) s = __fma_rn(S.v64 ? S.v64[d * S.N + i] : S.s64[d], S.phi[i + S.off[d]], s);
       }
       const double ri = S.rhs[i] - s;
       S.r64[i] = ri;
@@ -524,7 +529,7 @@ __device__ void solve_run(const SlotDev &S, SlotStat *st, const int part, const 
         } else {
           s = 0.f;
 #pragma unroll
-          for (int d = 0; d < kND; ++d) s = __fmaf_rn(S.s32[d], p0[i + S.off[d]], s);
+          for (int d = 0; d < kND; ++d) s = __fmaf_rn(S.v32 ? S.v32[d * S.N + i] : S.s32[d], p0[i + S.off[d]], s);
         }
         q0[i] = s;
         pq = ff_add(pq, ff_prod(pi, s));
@@ -567,7 +572,7 @@ __device__ void solve_run(const SlotDev &S, SlotStat *st, const int part, const 
           for (int d = 0; d < kND; ++d) {
             const int64_t j = i + S.off[d];
             const float rj = __fmaf_rn(-af, qk[j], rk[j]);
-            s = __fmaf_rn(S.s32[d], __fmaf_rn(bf, pk[j], rj), s);
+            s = __fmaf_rn(S.v32 ? S.v32[d * S.N + i] : S.s32[d], __fmaf_rn(bf, pk[j], rj), s);
           }
         }
         rnx[i] = ri;
@@ -742,6 +747,8 @@ struct mpg_run_prep {
   HostMesh hm;
   int off[kND] = {};
   double s64[kND] = {};
+  std::vector<double> d64;  // jittered mesh: per-row coefficients by diagonal (kND x N), else empty
+  std::vector<float> d32;   // the same in FP32
   std::vector<float> recv, ratio;
   std::vector<double> bg;
   std::vector<int32_t> n2c_off, c2n;
@@ -836,7 +843,9 @@ int64_t run_bytes_estimate(const mpg_run_desc &d) {
   // per tet: walk record, neighbours, node ids, fill ratio, 4 charge slots, slot
   // indices; per node: flag, slot offset, rhs, phi, background, r64, previous
   // phi, 7 FP32 solver vectors
-  return T * (48 + 16 + 16 + 4 + 32 + 16) + N * (1 + 4 + 8 * 5 + 4 * 7) + 8 * kMaxParts * 8 + d.n_particles * 56;
+  // (+ 15 FP64 and 15 FP32 coefficients per node on a jittered mesh)
+  return T * (48 + 16 + 16 + 4 + 32 + 16) + N * (1 + 4 + 8 * 5 + 4 * 7 + (d.jitter > 0 ? kND * 12 : 0)) +
+         8 * kMaxParts * 8 + d.n_particles * 56;
 }
 
 int upload_slots(mpg_batch *b) {
@@ -1175,7 +1184,7 @@ int mpg_batch_prepare(const mpg_run_desc *d, mpg_run_prep **out) {
   // n >= 4: the stencil is read off the centre node's row, whose 14
   // neighbours must all be interior nodes
   if (d->n_side < 4 || d->n_particles < 0 || !(d->m > 0) || !(d->dt > 0) || !(d->tol > 0) || d->max_iter < 1 ||
-      d->steps < 0)
+      d->steps < 0 || !(d->jitter >= 0.0 && d->jitter < 0.5))
     return MPG_ERR_ARG;
   if (6LL * d->n_side * d->n_side * d->n_side >= (int64_t)MPG_WALL) return MPG_ERR_ARG;
   mpg_run_prep *p = new (std::nothrow) mpg_run_prep();
@@ -1187,7 +1196,9 @@ int mpg_batch_prepare(const mpg_run_desc *d, mpg_run_prep **out) {
   md.split = MPG_SPLIT_KUHN6;
   md.lo = 0.0;
   md.hi = 1.0;
-  md.mapping = MPG_MAP_NONE;
+  md.mapping = d->jitter > 0.0 ? MPG_MAP_JITTER : MPG_MAP_NONE;
+  md.jitter = d->jitter;
+  md.seed = d->mesh_seed;
   HostMesh &hm = p->hm;
   std::string err;
   int rc = host_mesh_generate(md, hm, err);
@@ -1208,6 +1219,25 @@ int mpg_batch_prepare(const mpg_run_desc *d, mpg_run_prep **out) {
   for (int k = 0; k < kND; ++k) {
     p->off[k] = col[rp[c] + k] - (int32_t)c;
     p->s64[k] = val[rp[c] + k];
+  }
+  if (d->jitter > 0.0) {
+    // every interior row has the centre row's 15 offsets (jittering moves
+    // nodes, not the connectivity); boundary rows stay zero (identity rows)
+    const int64_t N = hm.N;
+    p->d64.assign((size_t)kND * N, 0.0);
+    for (int64_t r = 0; r < N; ++r) {
+      if (hm.bnd[r]) continue;
+      for (int32_t k = rp[r]; k < rp[r + 1]; ++k) {
+        int dd = 0;
+        while (dd < kND && p->off[dd] != col[k] - (int32_t)r) ++dd;
+        if (dd == kND) {
+          delete p;
+          return MPG_ERR_MESH;
+        }
+        p->d64[(size_t)dd * N + r] = val[k];
+      }
+    }
+    p->d32.assign(p->d64.begin(), p->d64.end());
   }
   p->recv.resize(12 * hm.T);
   for (int64_t t = 0; t < hm.T; ++t) {
@@ -1316,6 +1346,10 @@ int mpg_batch_admit_prepared(mpg_batch *b, const mpg_run_prep *p, int *slot) {
     return undo(MPG_ERR_CUDA);
   for (int k = 0; k < 7; ++k)
     if (balloc(b, &r, &f[k], hm.N)) return undo(MPG_ERR_CUDA);
+  double *v64 = nullptr;
+  float *v32 = nullptr;
+  if (!p->d64.empty() && (balloc(b, &r, &v64, kND * hm.N) || balloc(b, &r, &v32, kND * hm.N)))
+    return undo(MPG_ERR_CUDA);
   cudaStream_t st = b->stream;
   BCK(cudaMemcpyAsync(rec, p->recv.data(), sizeof(float) * 12 * hm.T, cudaMemcpyHostToDevice, st));
   BCK(cudaMemcpyAsync(nbr, hm.nbr_opp.data(), sizeof(uint4) * hm.T, cudaMemcpyHostToDevice, st));
@@ -1327,6 +1361,12 @@ int mpg_batch_admit_prepared(mpg_batch *b, const mpg_run_prep *p, int *slot) {
   BCK(cudaMemcpyAsync(n2c_off, p->n2c_off.data(), sizeof(int32_t) * (hm.N + 1), cudaMemcpyHostToDevice, st));
   BCK(cudaMemcpyAsync(c2n, p->c2n.data(), sizeof(int32_t) * 4 * hm.T, cudaMemcpyHostToDevice, st));
   BCK(cudaMemsetAsync(phi, 0, sizeof(double) * hm.N, st));
+  if (v64) {
+    BCK(cudaMemcpyAsync(v64, p->d64.data(), sizeof(double) * p->d64.size(), cudaMemcpyHostToDevice, st));
+    BCK(cudaMemcpyAsync(v32, p->d32.data(), sizeof(float) * p->d32.size(), cudaMemcpyHostToDevice, st));
+  }
+  v.v64 = v64;
+  v.v32 = v32;
   v.rec = rec;
   v.nbr = nbr;
   v.tets = tets;

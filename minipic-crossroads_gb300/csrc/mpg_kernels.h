@@ -35,6 +35,9 @@ struct KuhnTable {
   float jinv[6][9];
   uint32_t face[6][4];
   int nx = 0, ny = 0, nz = 0;
+  // ceil(2^40 / d) for d = nz and d = ny nz: exact division of hex indices
+  // (< 2^24) by a multiply and a shift, for ny nz <= 2^16
+  unsigned long long mz = 0, myz = 0;
 };
 
 struct DevMesh {

@@ -281,3 +281,29 @@ def test_kuhn_table_walk_equals_per_tet_records(mpg, monkeypatch):
         assert (u.view(np.uint8) == v.view(np.uint8)).all()
     assert (pa.view(np.uint64) == pb.view(np.uint64)).all()
     assert (ea.view(np.uint64) == eb.view(np.uint64)).all()
+
+
+@pytest.mark.parametrize("n_side,n", [(12, 40000), (40, 400000)])
+def test_kuhn_move_deposit_matches_oracle(mpg, orc, n_side, n):
+    """The fused move deposits the new positions (warp runs into per-(cell,
+    corner) slots, walk on the 6-type Kuhn table with the multiply-shift hex
+    split); after steps with crossings, wall exits and a sort in between,
+    the per-node charge equals the oracle's fixed-point deposit of the
+    particle state, bit for bit."""
+    ctx = mpg.Ctx(0)
+    ctx.mesh(n_side, split=mpg.SPLIT_KUHN6)
+    ctx.configure(precision=mpg.MIXED, deposit=mpg.DEPOSIT_LINEAR, solver=mpg.SOLVER_CG_MG, tol=1e-10,
+                  warm_start=2, kill_on_wall=1, sort_interval=2, rho_background=1.0)
+    ctx.reserve(n)
+    ctx.fill_uniform(n // 2, 7, 0, 1.0 / n, drift=(0.4, 0, 0), vth=0.1)
+    ctx.fill_uniform(n // 2, 8, 0, 1.0 / n, drift=(-0.4, 0, 0), vth=0.1)
+    m = orc.Mesh(n_side, split=6)
+    killed = 0
+    for _ in range(3):
+        st = ctx.step(0.02, 1)
+        killed += st.n_killed
+        acc, quantum, qfix = ctx.charge()
+        cs, b, v = ctx.mixed_download()
+        assert (acc == orc.deposit_fixed(m, cs, b, qfix)).all()
+    assert killed > 0
+    ctx.close()
