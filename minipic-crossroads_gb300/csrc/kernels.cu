@@ -718,6 +718,20 @@ __global__ void __launch_bounds__(kThreads) k_mixed_move(MixedParts P, int64_t n
 // arithmetic is that of k_mixed_move.  KUHN: the walk tables come from the
 // 6-type table of a uniform Kuhn mesh (same values, bit for bit, as the
 // per-tet records the table was checked against).
+//
+// Crossing particles walk in full warps: a chunk's lanes kick their particle
+// and look for the first exit only; a particle that stays in its tet is
+// finished and deposited with the chunk, one that leaves it goes, in its
+// kicked state, to the warp's queue in shared memory.  Each time 32 are
+// queued the warp walks them together from that state (the same operations
+// as an uninterrupted walk, so the results are bit for bit those of walking
+// every particle in its own chunk) and deposits them; the rest are walked
+// after the last chunk.  Without the queue every chunk runs the crossing
+// code about twice (some lane almost always crosses), with a third of the
+// lanes active.
+constexpr int kMoveWarps = kThreads / 32;
+constexpr int kMoveQueue = 64;  // per warp: fewer than 32 wait, up to 32 join per chunk
+
 template <bool KUHN>
 __global__ void __launch_bounds__(kThreads, 4) k_mixed_move_persistent(MixedParts P, int64_t n,
                                                                     const float4 *__restrict__ rec,
@@ -730,17 +744,94 @@ __global__ void __launch_bounds__(kThreads, 4) k_mixed_move_persistent(MixedPart
   __shared__ BlockTotals bt;
   __shared__ float s_jinv[KUHN ? 54 : 1];
   __shared__ uint32_t s_face[KUHN ? 24 : 1];
+  // queued particles of each warp: index (< 2^31, the particle capacity
+  // bound), cellsp word, barycentrics, kicked velocity
+  __shared__ uint32_t q_u[kMoveWarps][2][kMoveQueue];
+  __shared__ float q_f[kMoveWarps][6][kMoveQueue];
   if (KUHN) {
     for (int i = threadIdx.x; i < 54; i += blockDim.x) s_jinv[i] = kt.jinv[i / 9][i % 9];
     for (int i = threadIdx.x; i < 24; i += blockDim.x) s_face[i] = kt.face[i / 4][i % 4];
   }
   block_totals_init(&bt);  // also the barrier after the table stores
   const KuhnWalk kw{s_jinv, s_face, (uint32_t)kt.nx, (uint32_t)kt.ny, (uint32_t)kt.nz, kt.mz, kt.myz};
-  const int lane = threadIdx.x & 31;
+  const RecTab3 rt{rec, nbr};
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  uint32_t *const qp = q_u[wib][0], *const qc = q_u[wib][1];
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const int64_t nchunks = (n + 31) >> 5;
   ff ke = {0.f, 0.f};
   unsigned killed = 0, cross = 0, limit = 0;
+  int qn = 0;  // queued particles of this warp (warp-uniform)
+  // the walk tables of tet e
+  auto load_rec = [&](uint32_t e, float4 &r0, float4 &r1, float4 &r2) {
+    if (KUHN)
+      kw.load(e, r0, r1, r2);
+    else
+      rt.load(e, r0, r1, r2);
+  };
+  // full walk of a kicked particle from (e, l), then its store, statistics
+  // and deposit key; every lane of the warp calls it (live = has a particle)
+  auto finish = [&](bool live, uint32_t p, uint32_t cs, float l1, float l2, float l3, float vx, float vy, float vz) {
+    int dep_key = -1;
+    float d1 = 0.f, d2 = 0.f, d3 = 0.f;
+    int dq = 0;
+    if (live) {
+      const int s = (int)(cs >> 24);
+      uint32_t e = cs & 0xFFFFFFu;
+      float4 r0, r1, r2;
+      load_rec(e, r0, r1, r2);
+      bool dead, lim, stopped;
+      int it;
+      if (KUHN) {
+        KuhnWalk tab = kw;
+        it = mixed_walk_from<false>(tab, e, r0, r1, r2, l1, l2, l3, vx, vy, vz, dt, kill, max_cross, dead, lim,
+                                    stopped);
+      } else {
+        RecTab3 tab = rt;
+        it = mixed_walk_from<false>(tab, e, r0, r1, r2, l1, l2, l3, vx, vy, vz, dt, kill, max_cross, dead, lim,
+                                    stopped);
+      }
+      limit += lim ? 1u : 0u;
+      cross += (unsigned)it;
+      if (dead) {
+        killed += 1;
+        P.c[p] = MPG_DEAD;
+      } else {
+        if (e != (cs & 0xFFFFFFu)) P.c[p] = ((uint32_t)s << 24) | e;
+        P.b[p] = make_float4(l1, l2, l3, vx);
+        P.v[p] = make_float2(vy, vz);
+        ke = ff_add(ke, ff{S.half_wm_f[s] * __fmaf_rn(vz, vz, __fmaf_rn(vy, vy, vx * vx)), 0.f});
+        dep_key = (int)e;
+        d1 = l1;
+        d2 = l2;
+        d3 = l3;
+        dq = (int)S.qfix[s];
+      }
+    }
+    deposit_fixed_warp(acc, c2n, dep_key, d1, d2, d3, dq);
+  };
+  // walk the queued particles [qn - m, qn) in lanes 0 .. m-1
+  auto drain = [&](int m) {
+    __syncwarp();
+    const int slot = qn - m + lane;
+    const bool live = lane < m;
+    uint32_t p = 0, cs = MPG_DEAD;
+    float l1 = 0.f, l2 = 0.f, l3 = 0.f, vx = 0.f, vy = 0.f, vz = 0.f;
+    if (live) {
+      p = qp[slot];
+      cs = qc[slot];
+      l1 = q_f[wib][0][slot];
+      l2 = q_f[wib][1][slot];
+      l3 = q_f[wib][2][slot];
+      vx = q_f[wib][3][slot];
+      vy = q_f[wib][4][slot];
+      vz = q_f[wib][5][slot];
+    }
+    __syncwarp();
+    qn -= m;
+    finish(live, p, cs, l1, l2, l3, vx, vy, vz);
+  };
   int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   // prefetched record of this lane's particle in chunk c
   uint32_t cs_n = MPG_DEAD;
@@ -771,32 +862,33 @@ __global__ void __launch_bounds__(kThreads, 4) k_mixed_move_persistent(MixedPart
     int dep_key = -1;
     float d1 = 0.f, d2 = 0.f, d3 = 0.f;
     int dq = 0;
+    bool queue = false;
+    float l1 = bv.x, l2 = bv.y, l3 = bv.z;
+    float vx = bv.w, vy = vv.x, vz = vv.y;
     if (p < n && cs != MPG_DEAD) {
       const int s = (int)(cs >> 24);
       uint32_t e = cs & 0xFFFFFFu;
-      float l1 = bv.x, l2 = bv.y, l3 = bv.z;
-      float vx = bv.w, vy = vv.x, vz = vv.y;
-      bool dead, lim;
-      int it;
+      float4 r0, r1, r2;
       if (KUHN) {
-        float4 r0, r1, r2;
         kw.load(e, r0, r1, r2);
         const float4 E = etet4[e];
         r2.y = E.x;
         r2.z = E.y;
         r2.w = E.z;
-        it = mixed_walk_t(kw, e, r0, r1, r2, l1, l2, l3, vx, vy, vz, 0.5f * dt * S.qm_f[s], dt, kill, max_cross, dead,
-                          lim);
       } else {
-        it = mixed_walk(rec, nbr, e, l1, l2, l3, vx, vy, vz, 0.5f * dt * S.qm_f[s], dt, kill, max_cross, dead, lim);
+        rt.load(e, r0, r1, r2);
       }
-      limit += lim ? 1u : 0u;
-      cross += (unsigned)it;
-      if (dead) {
-        killed += 1;
-        P.c[p] = MPG_DEAD;
+      mixed_kick(0.5f * dt * S.qm_f[s], r2, vx, vy, vz);
+      bool dead, lim;
+      if (KUHN) {
+        KuhnWalk tab = kw;
+        mixed_walk_from<true>(tab, e, r0, r1, r2, l1, l2, l3, vx, vy, vz, dt, kill, max_cross, dead, lim, queue);
       } else {
-        if (e != (cs & 0xFFFFFFu)) P.c[p] = ((uint32_t)s << 24) | e;
+        RecTab3 tab = rt;
+        mixed_walk_from<true>(tab, e, r0, r1, r2, l1, l2, l3, vx, vy, vz, dt, kill, max_cross, dead, lim, queue);
+      }
+      if (!queue) {
+        // stays in its tet: l advanced by dt, nothing else changes
         P.b[p] = make_float4(l1, l2, l3, vx);
         P.v[p] = make_float2(vy, vz);
         ke = ff_add(ke, ff{S.half_wm_f[s] * __fmaf_rn(vz, vz, __fmaf_rn(vy, vy, vx * vx)), 0.f});
@@ -809,7 +901,22 @@ __global__ void __launch_bounds__(kThreads, 4) k_mixed_move_persistent(MixedPart
     }
     // every lane of the warp is here (c is uniform across the warp)
     deposit_fixed_warp(acc, c2n, dep_key, d1, d2, d3, dq);
+    const unsigned qm = __ballot_sync(FULL, queue);
+    if (queue) {
+      const int slot = qn + __popc(qm & ((1u << lane) - 1u));
+      qp[slot] = (uint32_t)p;
+      qc[slot] = cs;
+      q_f[wib][0][slot] = l1;
+      q_f[wib][1][slot] = l2;
+      q_f[wib][2][slot] = l3;
+      q_f[wib][3][slot] = vx;
+      q_f[wib][4][slot] = vy;
+      q_f[wib][5][slot] = vz;
+    }
+    qn += __popc(qm);
+    if (qn >= 32) drain(32);
   }
+  if (qn > 0) drain(qn);
   block_totals_push(&bt, ke, killed, cross, limit, st);
 }
 

@@ -29,28 +29,36 @@ struct RecTab3 {
   }
 };
 
-// Boris push with B = 0 (the two half kicks of particle_move.hpp:376-387,
-// hk = dt q/(2m)), then the walk across faces until dt is used up
-// (particle_move.hpp:110-121).  Barycentrics are carried across each face
-// through the vertex permutation; the entered face's coordinate is exactly
-// 0.  Returns the number of face crossings; *dead is set when the particle
-// left through an absorbing wall, *limit when max_cross was reached.
-// The record of the start tet e is given in (r0, r1, r2); on return they
-// hold the record of the final tet.
-template <class Tab>
-__device__ __forceinline__ int mixed_walk_t(Tab &tab, uint32_t &e, float4 &r0, float4 &r1, float4 &r2, float &l1,
-                                            float &l2, float &l3, float &vx, float &vy, float &vz, const float hk,
-                                            const float dt, const int kill, const int max_cross, bool &dead,
-                                            bool &limit) {
+// Boris push with B = 0: the two half kicks of particle_move.hpp:376-387
+// (hk = dt q/(2m)) with E of the start tet in r2.yzw
+__device__ __forceinline__ void mixed_kick(const float hk, const float4 &r2, float &vx, float &vy, float &vz) {
+  vx = __fmaf_rn(hk, r2.y, vx);
+  vy = __fmaf_rn(hk, r2.z, vy);
+  vz = __fmaf_rn(hk, r2.w, vz);
+  vx = __fmaf_rn(hk, r2.y, vx);
+  vy = __fmaf_rn(hk, r2.z, vy);
+  vz = __fmaf_rn(hk, r2.w, vz);
+}
+
+// The walk of a kicked particle across faces until dt is used up
+// (particle_move.hpp:110-121), from tet e with barycentrics (l1, l2, l3).
+// Barycentrics are carried across each face through the vertex
+// permutation; the entered face's coordinate is exactly 0.  Returns the
+// number of face crossings; *dead is set when the particle left through an
+// absorbing wall, *limit when max_cross was reached.  The record of the
+// start tet e is given in (r0, r1, r2); on return they hold the record of
+// the final tet.  STOP: return as soon as the first step finds an exit
+// before dt, with *stopped set and nothing changed, so that the walk can be
+// run again from the same state later (the move kernel gathers such
+// particles to walk them in full warps).
+template <bool STOP, class Tab>
+__device__ __forceinline__ int mixed_walk_from(Tab &tab, uint32_t &e, float4 &r0, float4 &r1, float4 &r2, float &l1,
+                                               float &l2, float &l3, float &vx, float &vy, float &vz, const float dt,
+                                               const int kill, const int max_cross, bool &dead, bool &limit,
+                                               bool &stopped) {
   dead = false;
   limit = false;
-  // Boris push with B = 0: the two half kicks of particle_move.hpp:376-387
-  vx = __fmaf_rn(hk, r2.y, vx);
-  vy = __fmaf_rn(hk, r2.z, vy);
-  vz = __fmaf_rn(hk, r2.w, vz);
-  vx = __fmaf_rn(hk, r2.y, vx);
-  vy = __fmaf_rn(hk, r2.z, vy);
-  vz = __fmaf_rn(hk, r2.w, vz);
+  stopped = false;
   float tleft = dt;
   int entry = -1;  // vertex opposite the face the particle entered through
   int it = 0;
@@ -84,6 +92,10 @@ __device__ __forceinline__ int mixed_walk_t(Tab &tab, uint32_t &e, float4 &r0, f
       l1 = __fmaf_rn(tleft, u1, l1);
       l2 = __fmaf_rn(tleft, u2, l2);
       l3 = __fmaf_rn(tleft, u3, l3);
+      break;
+    }
+    if (STOP) {
+      stopped = true;
       break;
     }
     if (it >= max_cross) {
@@ -146,6 +158,18 @@ __device__ __forceinline__ int mixed_walk_t(Tab &tab, uint32_t &e, float4 &r0, f
     tab.load(e, r0, r1, r2);
   }
   return it;
+}
+
+// kick and full walk from the start tet e (record in r0, r1, r2)
+template <class Tab>
+__device__ __forceinline__ int mixed_walk_t(Tab &tab, uint32_t &e, float4 &r0, float4 &r1, float4 &r2, float &l1,
+                                            float &l2, float &l3, float &vx, float &vy, float &vz, const float hk,
+                                            const float dt, const int kill, const int max_cross, bool &dead,
+                                            bool &limit) {
+  mixed_kick(hk, r2, vx, vy, vz);
+  bool stopped;
+  return mixed_walk_from<false>(tab, e, r0, r1, r2, l1, l2, l3, vx, vy, vz, dt, kill, max_cross, dead, limit,
+                                stopped);
 }
 
 // the walk on run-local tables rec[3*e ..] / nbr[e] (batch engine)
