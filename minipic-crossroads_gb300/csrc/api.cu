@@ -668,7 +668,7 @@ int upload_mesh(mpg_ctx *c) {
   d.kuhn = 0;
   const char *kw = getenv("MPG_KUHN_WALK");
   const int64_t nyz = (int64_t)h.d.ny * h.d.nz;
-  if (!(kw && atoi(kw) == 0) && nyz <= (1 << 16) && host_kuhn_table(h, d.ktab.jinv, d.ktab.face)) {
+  if (!(kw && atoi(kw) == 0) && nyz <= (1 << 16) && host_kuhn_table(h, d.ktab.jinv, d.ktab.face, d.ktab.noff)) {
     d.ktab.nx = h.d.nx;
     d.ktab.ny = h.d.ny;
     d.ktab.nz = h.d.nz;

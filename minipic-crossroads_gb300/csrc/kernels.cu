@@ -645,18 +645,26 @@ __global__ void k_efield_mixed(int64_t T, const int4 *__restrict__ tets, float4 
 }
 
 // E per tet on a uniform Kuhn mesh: the arithmetic of k_efield_mixed with
-// J^-1 from the 6-type table, written as (Ex, Ey, Ez, 0)
-__global__ void k_efield_kuhn(int64_t T, const int4 *__restrict__ tets, KuhnTable kt, const double *__restrict__ phi,
+// J^-1 from the 6-type table, written as (Ex, Ey, Ez, 0); the node ids come
+// from the hex index and the type's corner offsets (no tet table read)
+__global__ void k_efield_kuhn(int64_t T, KuhnTable kt, const double *__restrict__ phi,
                               float4 *__restrict__ etet4) {
   __shared__ float sj[54];
+  __shared__ int32_t so[24];
   for (int i = threadIdx.x; i < 54; i += blockDim.x) sj[i] = kt.jinv[i / 9][i % 9];
+  for (int i = threadIdx.x; i < 24; i += blockDim.x) so[i] = kt.noff[i / 4][i % 4];
   __syncthreads();
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= T) return;
-  const int4 nd = tets[t];
-  const double f0 = phi[nd.x];
-  const float d1 = (float)(phi[nd.y] - f0), d2 = (float)(phi[nd.z] - f0), d3 = (float)(phi[nd.w] - f0);
-  const float *J = sj + 9 * (int)(t % 6);
+  const uint32_t h = (uint32_t)t / 6u, ty = (uint32_t)t - 6u * h;
+  const uint32_t nyz = (uint32_t)(kt.ny * kt.nz), i = div_magic40(h, kt.myz), rem = h - i * nyz,
+                 j = div_magic40(rem, kt.mz), k = rem - j * (uint32_t)kt.nz;
+  const int64_t base = ((int64_t)i * (kt.ny + 1) + j) * (kt.nz + 1) + k;
+  const int32_t *o = so + 4 * ty;
+  const double f0 = phi[base + o[0]];
+  const float d1 = (float)(phi[base + o[1]] - f0), d2 = (float)(phi[base + o[2]] - f0),
+              d3 = (float)(phi[base + o[3]] - f0);
+  const float *J = sj + 9 * ty;
   etet4[t] = make_float4(__fmaf_rn(d3, J[6], __fmaf_rn(d2, J[3], d1 * J[0])),
                          __fmaf_rn(d3, J[7], __fmaf_rn(d2, J[4], d1 * J[1])),
                          __fmaf_rn(d3, J[8], __fmaf_rn(d2, J[5], d1 * J[2])), 0.f);
@@ -1480,7 +1488,7 @@ void launch_node_quanta(cudaStream_t s, const DevMesh &M, const unsigned long lo
 }
 void launch_efield_mixed(cudaStream_t s, const DevMesh &M, const double *phi) {
   if (M.kuhn)
-    k_efield_kuhn<<<grid_for(M.T), kThreads, 0, s>>>(M.T, M.tets, M.ktab, phi, M.etet4);
+    k_efield_kuhn<<<grid_for(M.T), kThreads, 0, s>>>(M.T, M.ktab, phi, M.etet4);
   else
     k_efield_mixed<<<grid_for(M.T), kThreads, 0, s>>>(M.T, M.tets, M.mrec, phi);
 }

@@ -491,7 +491,7 @@ void host_charge_slots(const HostMesh &m, std::vector<int32_t> &off, std::vector
     for (int k = 0; k < 4; ++k) c2n[4 * t + k] = fill[m.tets[4 * t + k]]++;
 }
 
-bool host_kuhn_table(const HostMesh &m, float jinv[6][9], uint32_t face[6][4]) {
+bool host_kuhn_table(const HostMesh &m, float jinv[6][9], uint32_t face[6][4], int32_t noff[6][4]) {
   const mpg_mesh_desc &d = m.d;
   if (d.split != MPG_SPLIT_KUHN6 || d.mapping != MPG_MAP_NONE || d.periodic) return false;
   const int64_t nx = d.nx, ny = d.ny, nz = d.nz;
@@ -522,6 +522,7 @@ bool host_kuhn_table(const HostMesh &m, float jinv[6][9], uint32_t face[6][4]) {
       const int64_t di = r / si, dj = (r % si) / sj, dk = r % sj;
       if (r < 0 || di > 1 || dj > 1 || dk > 1) return false;
       corner[k][q] = (int)(4 * di + 2 * dj + dk);
+      noff[k][q] = (int32_t)(di * si + dj * sj + dk);
     }
   // every tet must match its type's entries bit for bit
   int bad = 0;

@@ -71,7 +71,7 @@ bool host_mg_build(const HostMesh &m, const std::vector<int32_t> &rp, const std:
 // then checked against every tet's J^-1 (as the FP32 walk record holds it)
 // and neighbour word.  False when the mesh is not such a mesh or any tet
 // differs (the walk then uses the per-tet records).
-bool host_kuhn_table(const HostMesh &m, float jinv[6][9], uint32_t face[6][4]);
+bool host_kuhn_table(const HostMesh &m, float jinv[6][9], uint32_t face[6][4], int32_t noff[6][4]);
 
 // counter-based generator shared by the jitter and the fills (splitmix64 finaliser)
 static inline uint64_t mpg_mix64(uint64_t z) {

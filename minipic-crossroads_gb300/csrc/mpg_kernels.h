@@ -34,6 +34,7 @@ struct MixedParts {
 struct KuhnTable {
   float jinv[6][9];
   uint32_t face[6][4];
+  int32_t noff[6][4];  // node index of each type's corners minus the hex's first node (i, j, k)
   int nx = 0, ny = 0, nz = 0;
   // ceil(2^40 / d) for d = nz and d = ny nz: exact division of hex indices
   // (< 2^24) by a multiply and a shift, for ny nz <= 2^16
