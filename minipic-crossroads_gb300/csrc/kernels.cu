@@ -1007,13 +1007,19 @@ __global__ void k_cell_order(const uint32_t *__restrict__ start, int64_t T, uint
       lists[list_len - 1 - atomicAdd(long_count + 1, 1u)] = (uint32_t)e;
     return;
   }
-  uint32_t a[kSortLocal];
-  bool sorted = true;
-  for (uint32_t k = 0; k < m; ++k) {
-    a[k] = perm[lo + k];
-    if (k && a[k] < a[k - 1]) sorted = false;
+  // most ranges are in order already (claimed by one warp run): check them
+  // in place before anything goes to the local array
+  {
+    uint32_t prev = perm[lo], k = 1;
+    for (; k < m; ++k) {
+      const uint32_t x = perm[lo + k];
+      if (x < prev) break;
+      prev = x;
+    }
+    if (k == m) return;
   }
-  if (sorted) return;
+  uint32_t a[kSortLocal];
+  for (uint32_t k = 0; k < m; ++k) a[k] = perm[lo + k];
   for (uint32_t k = 1; k < m; ++k) {
     const uint32_t x = a[k];
     int j = (int)k - 1;
@@ -1148,19 +1154,42 @@ __global__ void __launch_bounds__(kLongThreads) k_cell_order_long(const uint32_t
 
 // sorted slot i < count takes input record perm[i]; slots [count, n) are
 // dead (the grid bound n stays the old count until the host reads the new one)
+// four particles per thread (strided by the block), their permutation
+// entries first, so that twelve record loads are in flight per thread
+constexpr int kGatherPer = 4;
 __global__ void k_sort_gather_mixed(MixedParts P, int64_t n, MixedParts Q, const uint32_t *__restrict__ perm,
                                     const uint32_t *__restrict__ count) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  if (i >= (int64_t)*count) {
-    Q.c[i] = MPG_DEAD;
-    return;
+  const int64_t cnt = (int64_t)*count;
+  const int64_t base = (int64_t)blockIdx.x * blockDim.x * kGatherPer + threadIdx.x;
+  uint32_t src[kGatherPer];
+#pragma unroll
+  for (int u = 0; u < kGatherPer; ++u) {
+    const int64_t i = base + (int64_t)u * blockDim.x;
+    src[u] = i < cnt ? perm[i] : 0u;
   }
-  const uint32_t p = perm[i];
-  Q.c[i] = P.c[p];
-  Q.b[i] = P.b[p];
-  Q.v[i] = P.v[p];
-  if (P.id) Q.id[i] = P.id[p];
+  uint32_t c[kGatherPer];
+  float4 b[kGatherPer];
+  float2 v[kGatherPer];
+#pragma unroll
+  for (int u = 0; u < kGatherPer; ++u) {
+    if (base + (int64_t)u * blockDim.x < cnt) {
+      c[u] = P.c[src[u]];
+      b[u] = P.b[src[u]];
+      v[u] = P.v[src[u]];
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < kGatherPer; ++u) {
+    const int64_t i = base + (int64_t)u * blockDim.x;
+    if (i < cnt) {
+      Q.c[i] = c[u];
+      Q.b[i] = b[u];
+      Q.v[i] = v[u];
+      if (P.id) Q.id[i] = P.id[src[u]];
+    } else if (i < n) {
+      Q.c[i] = MPG_DEAD;
+    }
+  }
 }
 
 __global__ void k_sort_gather_plain(PlainParts P, PlainParts Q, const uint32_t *__restrict__ perm,
@@ -1546,7 +1575,8 @@ static void cell_sort_order(cudaStream_t s, const uint32_t *keys, int64_t n, int
 void launch_mixed_sort(cudaStream_t s, const MixedParts &P, int64_t n, const MixedParts &Q, int64_t T,
                        const SortWork &w, uint32_t *d_count) {
   cell_sort_order<true>(s, P.c, n, T, w, Q.c, d_count);
-  if (n > 0) k_sort_gather_mixed<<<grid_for(n), kThreads, 0, s>>>(P, n, Q, w.perm, d_count);
+  if (n > 0)
+    k_sort_gather_mixed<<<grid_for((n + kGatherPer - 1) / kGatherPer), kThreads, 0, s>>>(P, n, Q, w.perm, d_count);
 }
 void launch_plain_sort(cudaStream_t s, const PlainParts &P, int64_t n, const PlainParts &Q, int64_t T,
                        const SortWork &w, uint32_t *d_count) {
