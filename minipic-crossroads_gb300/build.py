@@ -26,7 +26,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-fn
 
 CU_SOURCES = ["kernels.cu", "solver.cu", "mg.cu", "api.cu", "batch.cu"]
 CXX_SOURCES = ["mesh_host.cpp", "mg_host.cpp"]
-HEADERS = ["mpg_internal.h", "mpg_kernels.h", "mpg_device.cuh", "mpg_walk.cuh"]
+HEADERS = ["mpg_internal.h", "mpg_kernels.h", "mpg_device.cuh", "mpg_walk.cuh", "mpg_mg.cuh"]
 
 
 def nvcc():

@@ -37,6 +37,7 @@
 #include "minipic_gb300.h"
 #include "mpg_internal.h"
 #include "mpg_kernels.h"
+#include "mpg_mg.cuh"
 #include "mpg_walk.cuh"
 
 namespace {
@@ -67,6 +68,9 @@ struct SlotDev {
   // and v32 (FP32); null on a uniform mesh (s64 / s32 for every row)
   const double *v64;
   const float *v32;
+  // multigrid state of a run solved by one CTA (its inner solve is then the
+  // multigrid-preconditioned CG of the single-run solver); null: plain inner CG
+  const mgpass::CgMgArgs *mg;
   double quantum;
   int Q;
   float hk, dt;
@@ -425,6 +429,106 @@ __device__ __forceinline__ bool group_barrier(SlotStat *st, int nparts, unsigned
   return ok != 0;
 }
 
+// u = M r for a run held by one CTA: the single-run solver's V-cycle with
+// every level on this block (block barriers between dependent passes).
+// Level 0's first pre-smoothing residual (from rf) is in place.
+template <bool CST>
+__device__ void batch_vcycle(const mgpass::CgMgArgs &a, const float *rf) {
+  using namespace mgpass;
+  auto bsync = [&]() {
+    __syncthreads();
+    return true;
+  };
+  const MgDev &mg = a.mg;
+  const int nl = mg.nlev;
+  __syncthreads();
+  if (mg.nu0 == 2) {
+    const float *__restrict__ t1 = mg.lev[0].t2;
+    presmooth_residual<kND, CST>(a, 0, 0, mg.lev[0].n, [&](int64_t j) { return t1[j]; }, mg.lev[0].t);
+    __syncthreads();
+  }
+  restrict_rows(a, 0, 0, mg.lev[1].n);
+  __syncthreads();
+  for (int l = 1; l < nl - 1; ++l) {
+    if (mg.nu1 == 2)
+      level_down_twice<kND, CST>(a, l, 0, mg.lev[l].n, 0, mg.lev[l + 1].n, bsync);
+    else
+      level_down<kND, CST>(a, l, 0, mg.lev[l].n, 0, mg.lev[l + 1].n, bsync);
+  }
+  dense_solve_rows(mg, threadIdx.x >> 5, blockDim.x >> 5);
+  __syncthreads();
+  for (int l = nl - 2; l >= 1; --l) {
+    if (mg.nu1 == 2)
+      level_up_twice<kND, CST>(a, l, 0, mg.lev[l].n, mg.lev[l].r, mg.lev[l + 1].t, bsync);
+    else
+      level_up<kND, CST>(a, l, 0, mg.lev[l].n, mg.lev[l].r, mg.lev[l + 1].t, bsync);
+  }
+  if (mg.nu0 == 2)
+    level_up_twice<kND, CST>(a, 0, 0, mg.lev[0].n, rf, mg.lev[1].t, bsync);
+  else
+    level_up<kND, CST>(a, 0, 0, mg.lev[0].n, rf, mg.lev[1].t, bsync);
+}
+
+// inner solve of one FP64 refinement sweep for a one-CTA run with a
+// multigrid hierarchy: PCG on A z = r64 / |r64| in the single-reduction form
+// of the single-run solver (one block reduction of four float-float dots
+// per iteration), z starting at 0, the search direction restarted each sweep
+template <bool CST>
+__device__ void batch_mg_inner(const mgpass::CgMgArgs &a, int64_t n, double scale, float stop_rel,
+                               int &total_inner, int max_iter, ff *smf) {
+  using namespace mgpass;
+  float *__restrict__ r = a.r[0];
+  float *__restrict__ s = a.s[0];
+  float *__restrict__ p = a.p;
+  float *__restrict__ z = a.z;
+  float *__restrict__ w = a.w;
+  const float *__restrict__ u = a.u;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    r[i] = (float)(a.r64[i] * scale);
+    z[i] = 0.f;
+    p[i] = 0.f;
+    s[i] = 0.f;
+  }
+  __syncthreads();
+  presmooth_residual<kND, CST>(a, 0, 0, n, [&](int64_t j) { return r[j]; }, first_residual(a));
+  ff gam0 = {0.f, 0.f}, gam_prev = {0.f, 0.f};
+  bool have_dir = false;
+  for (int k = 0;; ++k) {
+    batch_vcycle<CST>(a, r);
+    ff v[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+      const float ui = u[i];
+      const float wi = level_apply<kND, CST>(a, 0, [&](int64_t j) { return u[j]; }, i);
+      const float si = s[i];
+      w[i] = wi;
+      v[0] = ff_add(v[0], ff_prod(r[i], ui));
+      v[1] = ff_add(v[1], ff_prod(wi, ui));
+      v[2] = ff_add(v[2], ff_prod(ui, si));
+      v[3] = ff_add(v[3], ff_prod(p[i], si));
+    }
+    block_sum_ff<4>(v, smf);
+    const ff G = v[0];
+    if (k == 0) gam0 = G;
+    if (!(G.hi > 0.f) || G.hi <= stop_rel * gam0.hi || total_inner >= max_iter) break;
+    const float beta = have_dir ? G.hi / gam_prev.hi : 0.f;
+    const ff den = ff_add(ff_add(v[1], ff_mulf(v[2], 2.f * beta)), ff_mulf(ff_mulf(v[3], beta), beta));
+    const float alpha = G.hi / den.hi;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+      const float pi = __fmaf_rn(beta, p[i], u[i]);
+      const float si = __fmaf_rn(beta, s[i], w[i]);
+      p[i] = pi;
+      s[i] = si;
+      z[i] = __fmaf_rn(alpha, pi, z[i]);
+      r[i] = __fmaf_rn(-alpha, si, r[i]);
+    }
+    __syncthreads();
+    presmooth_residual<kND, CST>(a, 0, 0, n, [&](int64_t j) { return r[j]; }, first_residual(a));
+    gam_prev = G;
+    have_dir = true;
+    ++total_inner;
+  }
+}
+
 template <int TH>
 __device__ void solve_run(const SlotDev &S, SlotStat *st, const int part, const int nparts) {
   __shared__ double red[32];
@@ -502,6 +606,17 @@ __device__ void solve_run(const SlotDev &S, SlotStat *st, const int part, const 
       break;
     }
     const double scale = 1.0 / sqrt(rho64);
+    if (S.mg && nparts == 1) {
+      const float stop_rel = (float)fmax(S.inner_tol2, S.safety2 * S.tol2 * rho0 / rho64);
+      if (S.v32)
+        batch_mg_inner<false>(*S.mg, n, scale, stop_rel, total_inner, S.max_iter, smf);
+      else
+        batch_mg_inner<true>(*S.mg, n, scale, stop_rel, total_inner, S.max_iter, smf);
+      const double back = sqrt(rho64);
+      for (int64_t i = threadIdx.x; i < n; i += blockDim.x) S.phi[i] += (double)S.z[i] * back;
+      __syncthreads();
+      continue;
+    }
     float *r0 = S.r[0], *p0 = S.p[0];
     ff rs = {0.f, 0.f};
     for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
@@ -752,6 +867,10 @@ struct mpg_run_prep {
   std::vector<float> recv, ratio;
   std::vector<double> bg;
   std::vector<int32_t> n2c_off, c2n;
+  // multigrid hierarchy of the run's operator (runs whose grid coarsens to at
+  // most kBatchDenseMax interior unknowns; the others keep the plain inner CG)
+  bool has_mg = false;
+  MgHostHierarchy mg;
 };
 
 struct mpg_batch {
@@ -837,6 +956,8 @@ void free_run(Run &r) {
   r.bytes = 0;
 }
 
+constexpr int64_t kBatchDenseMax = 400;  // interior unknowns of a run's coarsest multigrid level
+
 int64_t run_bytes_estimate(const mpg_run_desc &d) {
   const int64_t n = d.n_side;
   const int64_t T = 6 * n * n * n, N = (n + 1) * (n + 1) * (n + 1);
@@ -844,8 +965,113 @@ int64_t run_bytes_estimate(const mpg_run_desc &d) {
   // indices; per node: flag, slot offset, rhs, phi, background, r64, previous
   // phi, 7 FP32 solver vectors
   // (+ 15 FP64 and 15 FP32 coefficients per node on a jittered mesh)
+  // (+ a multigrid hierarchy: level-0 D^-1, flags and three vectors, the
+  // coarser levels' stencils and vectors (< N / 7 nodes), the dense inverse)
   return T * (48 + 16 + 16 + 4 + 32 + 16) + N * (1 + 4 + 8 * 5 + 4 * 7 + (d.jitter > 0 ? kND * 12 : 0)) +
-         8 * kMaxParts * 8 + d.n_particles * 56;
+         8 * kMaxParts * 8 + d.n_particles * 56 + N * 40 + kBatchDenseMax * kBatchDenseMax * 4 + (16 << 10);
+}
+
+// device copy of a run's multigrid hierarchy, and the solver state
+// (mgpass::CgMgArgs) pointing into the run's own vectors; one CTA runs the
+// run's V-cycles (batch_vcycle)
+int upload_run_mg(mpg_batch *b, Run &r, const mpg_run_prep &p, const SlotDev &v, mgpass::CgMgArgs **out) {
+  const MgHostHierarchy &H = p.mg;
+  cudaStream_t st = b->stream;
+  mgpass::CgMgArgs a{};
+  MgDev &m = a.mg;
+  m.nlev = (int)H.lev.size();
+  if (m.nlev < 2 || m.nlev > kMgMaxLevels) return bfail(b, MPG_ERR_ARG, "multigrid hierarchy of %d levels", m.nlev);
+  for (int l = 0; l < m.nlev; ++l) {
+    const MgHostLevel &h = H.lev[l];
+    MgLevelDev &L = m.lev[l];
+    L.gx = h.gx;
+    L.gy = h.gy;
+    L.gz = h.gz;
+    L.px = h.px ? 1 : 0;
+    L.sj = h.gz;
+    L.si = h.gy * h.gz;
+    L.n = (int64_t)h.gx * h.gy * h.gz;
+    float *dinv, *e, *t, *t2;
+    uint8_t *bnd;
+    BTRY(balloc(b, &r, &dinv, L.n));
+    BTRY(balloc(b, &r, &bnd, L.n));
+    BTRY(balloc(b, &r, &e, L.n));
+    BTRY(balloc(b, &r, &t, L.n));
+    BTRY(balloc(b, &r, &t2, L.n));
+    BCK(cudaMemcpyAsync(dinv, h.dinv.data(), sizeof(float) * L.n, cudaMemcpyHostToDevice, st));
+    BCK(cudaMemcpyAsync(bnd, h.bnd.data(), L.n, cudaMemcpyHostToDevice, st));
+    BCK(cudaMemsetAsync(e, 0, sizeof(float) * L.n, st));
+    BCK(cudaMemsetAsync(t, 0, sizeof(float) * L.n, st));
+    BCK(cudaMemsetAsync(t2, 0, sizeof(float) * L.n, st));
+    L.dinv = dinv;
+    L.bnd = bnd;
+    L.e = e;
+    L.t = t;
+    L.t2 = t2;
+    L.r = nullptr;  // level 0's right-hand side is the PCG residual
+    if (l > 0) {
+      float *val, *rr;
+      BTRY(balloc(b, &r, &val, 27 * L.n));
+      BTRY(balloc(b, &r, &rr, L.n));
+      BCK(cudaMemcpyAsync(val, h.val.data(), sizeof(float) * 27 * L.n, cudaMemcpyHostToDevice, st));
+      BCK(cudaMemsetAsync(rr, 0, sizeof(float) * L.n, st));
+      L.val = val;
+      L.r = rr;
+    }
+  }
+  m.ngrid = m.nlev - 1;
+  m.dense_m = (int)H.dense_idx.size();
+  int32_t *idx;
+  float *inv, *dr;
+  BTRY(balloc(b, &r, &idx, m.dense_m));
+  BTRY(balloc(b, &r, &inv, (int64_t)m.dense_m * m.dense_m));
+  BTRY(balloc(b, &r, &dr, m.dense_m));
+  BCK(cudaMemcpyAsync(idx, H.dense_idx.data(), sizeof(int32_t) * m.dense_m, cudaMemcpyHostToDevice, st));
+  BCK(cudaMemcpyAsync(inv, H.dense_inv.data(), sizeof(float) * H.dense_inv.size(), cudaMemcpyHostToDevice, st));
+  BCK(cudaMemsetAsync(dr, 0, sizeof(float) * m.dense_m, st));
+  m.dense_idx = idx;
+  m.dense_inv = inv;
+  m.dense_r = dr;
+  m.omega = 0.8f;
+  m.nu0 = 2;
+  m.nu1 = 1;
+  m.reliable = 0;
+  m.fuse_update = 0;
+  // level 0: the run's 15-point stencil, constant on a uniform mesh
+  DiaMatrix &A = a.A;
+  A.n = m.lev[0].n;
+  A.nwrap = 0;
+  A.ndiag = kND;
+  A.constant = v.v32 ? 0 : 1;
+  A.val32 = const_cast<float *>(v.v32);
+  A.val64 = const_cast<double *>(v.v64);
+  A.bnd = v.bnd;
+  for (int k = 0; k < kND; ++k) {
+    A.off[k] = p.off[k];
+    A.cst[k] = (float)p.s64[k];
+    if (p.off[k] == 0 && p.s64[k] != 0.0) m.dinv0 = (float)(1.0 / p.s64[k]);
+  }
+  a.b = v.rhs;
+  a.x = v.phi;
+  a.r64 = v.r64;
+  a.r[0] = a.r[1] = v.r[0];
+  a.s[0] = a.s[1] = v.q[1];
+  a.w = v.q[0];
+  a.p = v.p[0];
+  a.z = v.z;
+  a.u = m.lev[0].t;
+  a.partials = v.partials;
+  a.tol2 = v.tol2;
+  a.inner_tol2 = v.inner_tol2;
+  a.safety2 = v.safety2;
+  a.max_iter = v.max_iter;
+  a.st = nullptr;
+  mgpass::CgMgArgs *d;
+  BTRY(balloc(b, &r, &d, 1));
+  BCK(cudaMemcpyAsync(d, &a, sizeof(a), cudaMemcpyHostToDevice, st));
+  BCK(cudaStreamSynchronize(st));
+  *out = d;
+  return MPG_OK;
 }
 
 int upload_slots(mpg_batch *b) {
@@ -894,7 +1120,8 @@ int build_plans(mpg_batch *b) {
   std::sort(order.begin(), order.end(), [&](int a, int c) { return b->runs[a].N > b->runs[c].N; });
   for (int s : order) {
     const int64_t N = b->runs[s].N;
-    int parts = (int)std::min<int64_t>(kMaxParts, (N + rows_per_cta - 1) / rows_per_cta);
+    // a run with a multigrid hierarchy runs its V-cycles on one CTA
+    int parts = b->runs[s].dev.mg ? 1 : (int)std::min<int64_t>(kMaxParts, (N + rows_per_cta - 1) / rows_per_cta);
     if (parts > 1 && next + parts <= G) {
       for (int q = 0; q < parts; ++q) {
         per[next + q].insert(per[next + q].begin(), make_int4(s, q, parts, 0));
@@ -1247,6 +1474,11 @@ int mpg_batch_prepare(const mpg_run_desc *d, mpg_run_prep **out) {
   host_fill_ratio(hm, p->ratio);
   host_background(hm, d->rho_background, p->bg);
   host_charge_slots(hm, p->n2c_off, p->c2n);
+  {
+    const char *e = getenv("MPG_BATCH_MG");
+    std::string why;
+    if (!(e && atoi(e) == 0)) p->has_mg = host_mg_build(hm, rp, col, val, p->mg, why, kBatchDenseMax);
+  }
   *out = p;
   return MPG_OK;
 }
@@ -1390,6 +1622,12 @@ int mpg_batch_admit_prepared(mpg_batch *b, const mpg_run_prep *p, int *slot) {
   v.phi_prev = phi_prev;
   v.hist = b->d_hist + s;
   BCK(cudaMemsetAsync(v.hist, 0, sizeof(int), st));
+  v.mg = nullptr;
+  if (p->has_mg) {
+    mgpass::CgMgArgs *dargs;
+    if (upload_run_mg(b, r, *p, v, &dargs)) return undo(MPG_ERR_CUDA);
+    v.mg = dargs;
+  }
   // fill: append the run's particles, species field = slot
   DevMesh dm;
   dm.T = hm.T;

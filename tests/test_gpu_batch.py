@@ -182,3 +182,52 @@ def test_jittered_run_matches_single_run_and_mix(mpg):
     x1, x2 = _sorted_state(*mix.particles(s_mix)), _sorted_state(*bt.particles(s))
     for u, w in zip(x1, x2):
         assert (u == w).all()
+
+
+def test_multigrid_runs_match_single_run_and_cg(mpg, monkeypatch):
+    """Runs whose grid coarsens (here 16^3 and 24^3, one of them jittered)
+    solve with the multigrid-preconditioned CG on one CTA: against the
+    single-run mixed path (phi within 1e-7 relative, kinetic energy within
+    1e-5) and against the batch's own plain inner CG (MPG_BATCH_MG=0, phi
+    within 1e-7), with several times fewer iterations; stepped alone or in a
+    mix, bit-identical."""
+    dt = 0.01
+    specs = [dict(n_side=16, n=60000, seed=31, jitter=0.0), dict(n_side=24, n=80000, seed=32, jitter=0.15)]
+
+    def batch(specs_in, mg=True):
+        monkeypatch.setenv("MPG_BATCH_MG", "1" if mg else "0")
+        bt = mpg.Batch(0, budget_bytes=4 << 30, particle_capacity=1 << 20)
+        bt.tuning(512, 0)
+        slots = [bt.admit(s["n_side"], s["n"], s["seed"], vth=0.05, dt=dt, steps=10, jitter=s["jitter"], mesh_seed=5)
+                 for s in specs_in]
+        return bt, slots
+
+    bt, slots = batch(specs)
+    cg, cg_slots = batch(specs, mg=False)
+    mix, mix_slots = batch([dict(n_side=9, n=10000, seed=3, jitter=0.0)] + specs)
+    ctxs = []
+    for s in specs:
+        ctx = mpg.Ctx(0)
+        ctx.mesh(s["n_side"], split=mpg.SPLIT_KUHN6, mapping=mpg.MAP_JITTER if s["jitter"] else mpg.MAP_NONE,
+                 jitter=s["jitter"], seed=5)
+        ctx.configure(precision=mpg.MIXED, deposit=mpg.DEPOSIT_LINEAR, solver=mpg.SOLVER_CG, tol=1e-10,
+                      max_iter=5000, warm_start=1, kill_on_wall=1, rho_background=1.0)
+        ctx.reserve(s["n"])
+        ctx.fill_uniform(s["n"], s["seed"], 0, 1.0 / s["n"], vth=0.05)
+        ctxs.append(ctx)
+    for k in range(4):
+        assert bt.step(1).rc == 0 and cg.step(1).rc == 0 and mix.step(1).rc == 0
+        sts = [ctx.step(dt, 1) for ctx in ctxs]
+        for s, st in zip(slots, sts):
+            bi = bt.info(s)
+            assert abs(bi.ke - st.ke) <= 1e-5 * st.ke, (k, bi.ke, st.ke)
+    for s, c, ctx in zip(slots, cg_slots, ctxs):
+        pb, pc, pcg = bt.phi(s), ctx.get_field(mpg.FIELD_PHI), cg.phi(c)
+        assert np.abs(pb - pc).max() <= 1e-7 * np.abs(pc).max()
+        assert np.abs(pb - pcg).max() <= 1e-7 * np.abs(pcg).max()
+        assert 3 * bt.info(s).solver_iters < cg.info(c).solver_iters, (bt.info(s).solver_iters, cg.info(c).solver_iters)
+    for s, m in zip(slots, mix_slots[1:]):
+        assert (bt.phi(s).view(np.uint64) == mix.phi(m).view(np.uint64)).all()
+        x1, x2 = _sorted_state(*bt.particles(s)), _sorted_state(*mix.particles(m))
+        for u, w in zip(x1, x2):
+            assert (u == w).all()
