@@ -429,53 +429,67 @@ __device__ __forceinline__ bool group_barrier(SlotStat *st, int nparts, unsigned
   return ok != 0;
 }
 
-// u = M r for a run held by one CTA: the single-run solver's V-cycle with
-// every level on this block (block barriers between dependent passes).
-// Level 0's first pre-smoothing residual (from rf) is in place.
-template <bool CST>
-__device__ void batch_vcycle(const mgpass::CgMgArgs &a, const float *rf) {
+// The run's CTA group: part `part` of `nparts` takes the rows
+// [n part / nparts, n (part + 1) / nparts) of every level; `sync` is the
+// group barrier (a block barrier for a one-CTA run).
+struct GroupRows {
+  int part, nparts;
+  __device__ void of(int64_t n, int64_t &lo, int64_t &hi) const {
+    lo = n * part / nparts;
+    hi = n * (part + 1) / nparts;
+  }
+};
+
+// u = M r: the single-run solver's V-cycle with every level on the run's
+// CTA group (group barriers between dependent passes).  Level 0's first
+// pre-smoothing residual (from rf) is in place on this part's rows.
+template <bool CST, typename Sync>
+__device__ bool batch_vcycle(const mgpass::CgMgArgs &a, const float *rf, const GroupRows g, Sync sync) {
   using namespace mgpass;
-  auto bsync = [&]() {
-    __syncthreads();
-    return true;
-  };
   const MgDev &mg = a.mg;
   const int nl = mg.nlev;
-  __syncthreads();
+  int64_t lo, hi, clo, chi;
+  if (!sync()) return false;
+  g.of(mg.lev[0].n, lo, hi);
   if (mg.nu0 == 2) {
     const float *__restrict__ t1 = mg.lev[0].t2;
-    presmooth_residual<kND, CST>(a, 0, 0, mg.lev[0].n, [&](int64_t j) { return t1[j]; }, mg.lev[0].t);
-    __syncthreads();
+    presmooth_residual<kND, CST>(a, 0, lo, hi, [&](int64_t j) { return t1[j]; }, mg.lev[0].t);
+    if (!sync()) return false;
   }
-  restrict_rows(a, 0, 0, mg.lev[1].n);
-  __syncthreads();
+  g.of(mg.lev[1].n, clo, chi);
+  restrict_rows(a, 0, clo, chi);
+  if (!sync()) return false;
   for (int l = 1; l < nl - 1; ++l) {
-    if (mg.nu1 == 2)
-      level_down_twice<kND, CST>(a, l, 0, mg.lev[l].n, 0, mg.lev[l + 1].n, bsync);
-    else
-      level_down<kND, CST>(a, l, 0, mg.lev[l].n, 0, mg.lev[l + 1].n, bsync);
+    g.of(mg.lev[l].n, lo, hi);
+    g.of(mg.lev[l + 1].n, clo, chi);
+    const bool ok = mg.nu1 == 2 ? level_down_twice<kND, CST>(a, l, lo, hi, clo, chi, sync)
+                                : level_down<kND, CST>(a, l, lo, hi, clo, chi, sync);
+    if (!ok) return false;
   }
-  dense_solve_rows(mg, threadIdx.x >> 5, blockDim.x >> 5);
-  __syncthreads();
+  const int nw = blockDim.x >> 5;
+  dense_solve_rows(mg, g.part * nw + (threadIdx.x >> 5), g.nparts * nw);
+  if (!sync()) return false;
   for (int l = nl - 2; l >= 1; --l) {
-    if (mg.nu1 == 2)
-      level_up_twice<kND, CST>(a, l, 0, mg.lev[l].n, mg.lev[l].r, mg.lev[l + 1].t, bsync);
-    else
-      level_up<kND, CST>(a, l, 0, mg.lev[l].n, mg.lev[l].r, mg.lev[l + 1].t, bsync);
+    g.of(mg.lev[l].n, lo, hi);
+    const bool ok = mg.nu1 == 2 ? level_up_twice<kND, CST>(a, l, lo, hi, mg.lev[l].r, mg.lev[l + 1].t, sync)
+                                : level_up<kND, CST>(a, l, lo, hi, mg.lev[l].r, mg.lev[l + 1].t, sync);
+    if (!ok) return false;
   }
-  if (mg.nu0 == 2)
-    level_up_twice<kND, CST>(a, 0, 0, mg.lev[0].n, rf, mg.lev[1].t, bsync);
-  else
-    level_up<kND, CST>(a, 0, 0, mg.lev[0].n, rf, mg.lev[1].t, bsync);
+  g.of(mg.lev[0].n, lo, hi);
+  return mg.nu0 == 2 ? level_up_twice<kND, CST>(a, 0, lo, hi, rf, mg.lev[1].t, sync)
+                     : level_up<kND, CST>(a, 0, lo, hi, rf, mg.lev[1].t, sync);
 }
 
-// inner solve of one FP64 refinement sweep for a one-CTA run with a
-// multigrid hierarchy: PCG on A z = r64 / |r64| in the single-reduction form
-// of the single-run solver (one block reduction of four float-float dots
-// per iteration), z starting at 0, the search direction restarted each sweep
-template <bool CST>
-__device__ void batch_mg_inner(const mgpass::CgMgArgs &a, int64_t n, double scale, float stop_rel,
-                               int &total_inner, int max_iter, ff *smf) {
+// inner solve of one FP64 refinement sweep for a run with a multigrid
+// hierarchy: PCG on A z = r64 / |r64| in the single-reduction form of the
+// single-run solver (one all-reduce of four float-float dots per iteration,
+// through the part records and the group barrier when the run has several
+// CTAs, summed in part order), z starting at 0, the search direction
+// restarted each sweep.  False when a group barrier timed out.
+template <bool CST, typename Sync>
+__device__ bool batch_mg_inner(const mgpass::CgMgArgs &a, const GroupRows g, Sync sync, double scale,
+                               float stop_rel, int &total_inner, int max_iter, ff *smf, double *partials,
+                               int &phase) {
   using namespace mgpass;
   float *__restrict__ r = a.r[0];
   float *__restrict__ s = a.s[0];
@@ -483,20 +497,22 @@ __device__ void batch_mg_inner(const mgpass::CgMgArgs &a, int64_t n, double scal
   float *__restrict__ z = a.z;
   float *__restrict__ w = a.w;
   const float *__restrict__ u = a.u;
-  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+  int64_t lo, hi;
+  g.of(a.mg.lev[0].n, lo, hi);
+  for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
     r[i] = (float)(a.r64[i] * scale);
     z[i] = 0.f;
     p[i] = 0.f;
     s[i] = 0.f;
   }
-  __syncthreads();
-  presmooth_residual<kND, CST>(a, 0, 0, n, [&](int64_t j) { return r[j]; }, first_residual(a));
+  if (!sync()) return false;
+  presmooth_residual<kND, CST>(a, 0, lo, hi, [&](int64_t j) { return r[j]; }, first_residual(a));
   ff gam0 = {0.f, 0.f}, gam_prev = {0.f, 0.f};
   bool have_dir = false;
   for (int k = 0;; ++k) {
-    batch_vcycle<CST>(a, r);
+    if (!batch_vcycle<CST>(a, r, g, sync)) return false;
     ff v[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
       const float ui = u[i];
       const float wi = level_apply<kND, CST>(a, 0, [&](int64_t j) { return u[j]; }, i);
       const float si = s[i];
@@ -507,13 +523,34 @@ __device__ void batch_mg_inner(const mgpass::CgMgArgs &a, int64_t n, double scal
       v[3] = ff_add(v[3], ff_prod(p[i], si));
     }
     block_sum_ff<4>(v, smf);
+    if (g.nparts > 1) {
+      // part records (two float4 per part, sets alternating by phase), then
+      // every part sums them in part order
+      float4 *rec = reinterpret_cast<float4 *>(partials + (size_t)(phase & 1) * 4 * kMaxParts);
+      if (threadIdx.x == 0) {
+        rec[2 * g.part] = make_float4(v[0].hi, v[0].lo, v[1].hi, v[1].lo);
+        rec[2 * g.part + 1] = make_float4(v[2].hi, v[2].lo, v[3].hi, v[3].lo);
+      }
+      ++phase;
+      if (!sync()) return false;
+      ff t[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+      for (int q = 0; q < g.nparts; ++q) {
+        const float4 x = rec[2 * q], y = rec[2 * q + 1];
+        t[0] = ff_add(t[0], ff{x.x, x.y});
+        t[1] = ff_add(t[1], ff{x.z, x.w});
+        t[2] = ff_add(t[2], ff{y.x, y.y});
+        t[3] = ff_add(t[3], ff{y.z, y.w});
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) v[q] = t[q];
+    }
     const ff G = v[0];
     if (k == 0) gam0 = G;
     if (!(G.hi > 0.f) || G.hi <= stop_rel * gam0.hi || total_inner >= max_iter) break;
     const float beta = have_dir ? G.hi / gam_prev.hi : 0.f;
     const ff den = ff_add(ff_add(v[1], ff_mulf(v[2], 2.f * beta)), ff_mulf(ff_mulf(v[3], beta), beta));
     const float alpha = G.hi / den.hi;
-    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
       const float pi = __fmaf_rn(beta, p[i], u[i]);
       const float si = __fmaf_rn(beta, s[i], w[i]);
       p[i] = pi;
@@ -521,12 +558,13 @@ __device__ void batch_mg_inner(const mgpass::CgMgArgs &a, int64_t n, double scal
       z[i] = __fmaf_rn(alpha, pi, z[i]);
       r[i] = __fmaf_rn(-alpha, si, r[i]);
     }
-    __syncthreads();
-    presmooth_residual<kND, CST>(a, 0, 0, n, [&](int64_t j) { return r[j]; }, first_residual(a));
+    if (!sync()) return false;
+    presmooth_residual<kND, CST>(a, 0, lo, hi, [&](int64_t j) { return r[j]; }, first_residual(a));
     gam_prev = G;
     have_dir = true;
     ++total_inner;
   }
+  return true;
 }
 
 template <int TH>
@@ -606,15 +644,18 @@ __device__ void solve_run(const SlotDev &S, SlotStat *st, const int part, const 
       break;
     }
     const double scale = 1.0 / sqrt(rho64);
-    if (S.mg && nparts == 1) {
+    if (S.mg) {
       const float stop_rel = (float)fmax(S.inner_tol2, S.safety2 * S.tol2 * rho0 / rho64);
-      if (S.v32)
-        batch_mg_inner<false>(*S.mg, n, scale, stop_rel, total_inner, S.max_iter, smf);
-      else
-        batch_mg_inner<true>(*S.mg, n, scale, stop_rel, total_inner, S.max_iter, smf);
+      const GroupRows g{part, nparts};
+      auto gsync = [&]() { return group_barrier(st, nparts, epoch); };
+      const bool ok = S.v32 ? batch_mg_inner<false>(*S.mg, g, gsync, scale, stop_rel, total_inner, S.max_iter, smf,
+                                                    S.partials, phase)
+                            : batch_mg_inner<true>(*S.mg, g, gsync, scale, stop_rel, total_inner, S.max_iter, smf,
+                                                   S.partials, phase);
+      if (!ok) return;
       const double back = sqrt(rho64);
-      for (int64_t i = threadIdx.x; i < n; i += blockDim.x) S.phi[i] += (double)S.z[i] * back;
-      __syncthreads();
+      for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) S.phi[i] += (double)S.z[i] * back;
+      if (!group_barrier(st, nparts, epoch)) return;
       continue;
     }
     float *r0 = S.r[0], *p0 = S.p[0];
@@ -867,8 +908,9 @@ struct mpg_run_prep {
   std::vector<float> recv, ratio;
   std::vector<double> bg;
   std::vector<int32_t> n2c_off, c2n;
-  // multigrid hierarchy of the run's operator (runs whose grid coarsens to at
-  // most kBatchDenseMax interior unknowns; the others keep the plain inner CG)
+  // multigrid hierarchy of the run's operator (runs of at most kBatchMgMaxRows
+  // nodes whose grid coarsens to at most kBatchDenseMax interior unknowns; the
+  // others keep the plain inner CG)
   bool has_mg = false;
   MgHostHierarchy mg;
 };
@@ -957,6 +999,10 @@ void free_run(Run &r) {
 }
 
 constexpr int64_t kBatchDenseMax = 400;  // interior unknowns of a run's coarsest multigrid level
+// runs up to this many nodes solve with multigrid on one CTA; larger ones keep
+// the plain inner CG on several CTAs (one CTA's passes over ~2^18 rows would
+// cost more than the multi-CTA CG saves)
+constexpr int64_t kBatchMgMaxRows = 1 << 16;
 
 int64_t run_bytes_estimate(const mpg_run_desc &d) {
   const int64_t n = d.n_side;
@@ -1113,6 +1159,8 @@ int build_plans(mpg_batch *b) {
   // to the least-loaded CTA
   const int G = std::max(1, b->fused ? b->max_step_blocks : b->max_cg_blocks);
   const int64_t rows_per_cta = 24 * 1024;
+  int64_t rows_per_mg_cta = 12 * 1024;
+  if (const char *e = getenv("MPG_BATCH_MG_ROWS")) rows_per_mg_cta = std::max<int64_t>(1024, atoll(e));
   std::vector<std::vector<int4>> per(G);
   std::vector<int64_t> load(G, 0);
   int next = 0;
@@ -1120,8 +1168,10 @@ int build_plans(mpg_batch *b) {
   std::sort(order.begin(), order.end(), [&](int a, int c) { return b->runs[a].N > b->runs[c].N; });
   for (int s : order) {
     const int64_t N = b->runs[s].N;
-    // a run with a multigrid hierarchy runs its V-cycles on one CTA
-    int parts = b->runs[s].dev.mg ? 1 : (int)std::min<int64_t>(kMaxParts, (N + rows_per_cta - 1) / rows_per_cta);
+    // a run with a multigrid hierarchy takes fewer rows per CTA: its
+    // iterations are few and each is a dozen latency-bound passes
+    const int64_t rows = b->runs[s].dev.mg ? rows_per_mg_cta : rows_per_cta;
+    int parts = (int)std::min<int64_t>(kMaxParts, (N + rows - 1) / rows);
     if (parts > 1 && next + parts <= G) {
       for (int q = 0; q < parts; ++q) {
         per[next + q].insert(per[next + q].begin(), make_int4(s, q, parts, 0));
@@ -1477,7 +1527,8 @@ int mpg_batch_prepare(const mpg_run_desc *d, mpg_run_prep **out) {
   {
     const char *e = getenv("MPG_BATCH_MG");
     std::string why;
-    if (!(e && atoi(e) == 0)) p->has_mg = host_mg_build(hm, rp, col, val, p->mg, why, kBatchDenseMax);
+    if (!(e && atoi(e) == 0) && hm.N <= kBatchMgMaxRows)
+      p->has_mg = host_mg_build(hm, rp, col, val, p->mg, why, kBatchDenseMax);
   }
   *out = p;
   return MPG_OK;
