@@ -214,7 +214,10 @@ int mpg_cg_csr(mpg_ctx *ctx, int64_t n, const int32_t *d_rowptr, const int32_t *
  * grid barriers between them; mpg_batch_set_fused), the step captured in a
  * CUDA graph.  The field operator of a batched run is the 15-point Kuhn
  * stencil of its mesh (constant coefficients on a uniform mesh, per-row
- * coefficients on a jittered one; FP32 inside FP64 refinement).  Runs are admitted against a device-memory budget, step
+ * coefficients on a jittered one; FP32 inside FP64 refinement), its inner
+ * solve multigrid-preconditioned CG with a per-run hierarchy for meshes of
+ * 9^3 cells and more, up to 2^20 nodes, and plain CG otherwise.  Runs are
+ * admitted against a device-memory budget, step
  * until their requested step count and are retired to free their slot.
  * A run's results do not depend on which other runs share the batch. */
 typedef struct mpg_batch mpg_batch;

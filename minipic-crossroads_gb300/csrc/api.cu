@@ -58,6 +58,9 @@ struct mpg_ctx {
   long long *acc_node = nullptr;      // per-node quanta for downloads (N)
   bool acc_valid = false;
   bool needs_sort = false;  // particles added or replaced since the last cell sort
+  // a cell sort's permutation (sort_perm) whose gather is left to the next
+  // move, which reads the particles through it into the other buffer
+  bool gather_pending = false;
   double inner_tol = 1e-5;  // relative residual target of the mixed solver's FP32 inner CG
 
   int precision = MPG_PLAIN;  // precision of the allocated particle arrays
@@ -374,8 +377,10 @@ int phase_deposit_plain(mpg_ctx *c) {
   return MPG_OK;
 }
 
+int settle_sort(mpg_ctx *c);
 int phase_deposit_mixed(mpg_ctx *c) {
   if (!c->acc_valid) {
+    TRY(settle_sort(c));
     ensure_qfix(c);
     CK(cudaMemsetAsync(c->acc, 0, sizeof(unsigned long long) * 4 * c->dm.T, c->stream));
     launch_mixed_deposit(c->stream, c->mp[c->cur], c->n, c->dm, c->sp, c->acc);
@@ -517,6 +522,7 @@ int sort_work(mpg_ctx *c, SortWork &w) {
 // is read back at the next host sync; the slots [count, n) of the new buffer
 // are dead, so the grid bound n stays valid until then.
 int sort_mixed(mpg_ctx *c) {
+  TRY(settle_sort(c));
   c->needs_sort = false;
   SortWork w;
   TRY(sort_work(c, w));
@@ -526,6 +532,34 @@ int sort_mixed(mpg_ctx *c) {
   CKL();
   c->cur = other;
   c->starts_valid = true;
+  return MPG_OK;
+}
+
+// The cell sort of mpg_step: permutation, start offsets and count only; the
+// gather is the next move's (launch_mixed_move_sorted), one pass over the
+// particle records fewer.  Any other use of the particle list completes the
+// gather first (settle_sort).
+int sort_mixed_deferred(mpg_ctx *c) {
+  TRY(settle_sort(c));
+  c->needs_sort = false;
+  SortWork w;
+  TRY(sort_work(c, w));
+  launch_mixed_sort_order(c->stream, c->mp[c->cur], c->n, c->mp[1 - c->cur], c->dm.T, w, c->d_count);
+  c->launches += 9;
+  CKL();
+  c->gather_pending = true;
+  c->starts_valid = true;
+  return MPG_OK;
+}
+
+int settle_sort(mpg_ctx *c) {
+  if (!c->gather_pending) return MPG_OK;
+  const int other = 1 - c->cur;
+  launch_mixed_gather(c->stream, c->mp[c->cur], c->n, c->mp[other], c->sort_perm, c->d_count);
+  c->launches += 1;
+  CKL();
+  c->cur = other;
+  c->gather_pending = false;
   return MPG_OK;
 }
 
@@ -574,7 +608,14 @@ int one_step(mpg_ctx *c, double dt, mpg_step_stats *acc_st, bool &sorted) {
   // memset is timed with the E-field phase, the move phase is the kernel)
   if (mixed) CK(cudaMemsetAsync(c->acc, 0, sizeof(unsigned long long) * 4 * c->dm.T, c->stream));
   ev_record(c, 3);
-  if (mixed) {
+  if (mixed && c->gather_pending) {
+    // the last step's cell sort: read through its permutation, write sorted
+    const int other = 1 - c->cur;
+    launch_mixed_move_sorted(c->stream, c->mp[c->cur], c->n, c->mp[other], c->sort_perm, c->d_count, c->dm, c->sp,
+                             (float)dt, c->cfg.kill_on_wall, c->cfg.max_crossings, c->acc, c->d_stats);
+    c->cur = other;
+    c->gather_pending = false;
+  } else if (mixed) {
     launch_mixed_move(c->stream, c->mp[c->cur], c->n, c->dm, c->sp, (float)dt, c->cfg.kill_on_wall,
                       c->cfg.max_crossings, c->acc, c->d_stats);
   } else {
@@ -587,7 +628,7 @@ int one_step(mpg_ctx *c, double dt, mpg_step_stats *acc_st, bool &sorted) {
   c->step_count++;
   if (mixed) {
     if (c->cfg.sort_interval > 0 && c->step_count % c->cfg.sort_interval == 0) {
-      TRY(sort_mixed(c));
+      TRY(sort_mixed_deferred(c));
       sorted = true;
     }
   } else {
@@ -955,6 +996,7 @@ int mpg_mg_hierarchy(const mpg_mesh_desc *mesh, int64_t dense_max, int level, in
 
 int mpg_mesh_build(mpg_ctx *c, const mpg_mesh_desc *d) {
   ENTER(c);
+  TRY(settle_sort(c));
   if (!d) return fail(c, MPG_ERR_ARG, "null mesh descriptor");
   CK(cudaStreamSynchronize(c->stream));
   free_particles(c);
@@ -1027,6 +1069,7 @@ int mpg_species_set(mpg_ctx *c, int i, double q, double m) {
 
 int mpg_configure(mpg_ctx *c, const mpg_config *cfg) {
   ENTER(c);
+  TRY(settle_sort(c));
   if (!cfg) return fail(c, MPG_ERR_ARG, "null config");
   if (!c->has_mesh) return fail(c, MPG_ERR_STATE, "no mesh: call mpg_mesh_build first");
   if (cfg->precision != MPG_PLAIN && cfg->precision != MPG_MIXED) return fail(c, MPG_ERR_ARG, "bad precision");
@@ -1234,6 +1277,7 @@ int mpg_csr_download(mpg_ctx *c, int32_t *rowptr, int32_t *col, double *val) {
 
 int mpg_particles_reserve(mpg_ctx *c, int64_t capacity) {
   ENTER(c);
+  TRY(settle_sort(c));
   if (capacity <= 0 || capacity >= (1LL << 31)) return fail(c, MPG_ERR_ARG, "capacity out of range");
   if (c->parts_alloc && c->n > 0 && !(c->cap == capacity && c->precision == c->cfg.precision))
     return fail(c, MPG_ERR_STATE, "cannot resize a non-empty particle list");
@@ -1253,6 +1297,7 @@ int mpg_particles_count(mpg_ctx *c, int64_t *n) {
 
 int mpg_fill_ref(mpg_ctx *c, int nppe, int type, double density, const double vel[3], double temp) {
   ENTER(c);
+  TRY(settle_sort(c));
   TRY(ensure_particles(c));
   if (nppe < 1 || type < 0 || type >= MPG_MAX_SPECIES) return fail(c, MPG_ERR_ARG, "bad nppe or type");
   const int64_t add = c->hm.T * (int64_t)nppe;
@@ -1295,6 +1340,7 @@ int mpg_fill_ref(mpg_ctx *c, int nppe, int type, double density, const double ve
 int mpg_fill_uniform(mpg_ctx *c, int64_t n, uint64_t seed, int type, double weight, const double drift[3],
                      double vth) {
   ENTER(c);
+  TRY(settle_sort(c));
   TRY(ensure_particles(c));
   if (n < 0 || type < 0 || type >= MPG_MAX_SPECIES) return fail(c, MPG_ERR_ARG, "bad count or type");
   if (c->n + n > c->cap) return fail(c, MPG_ERR_CAPACITY, "fill of %lld exceeds capacity", (long long)n);
@@ -1318,6 +1364,7 @@ int mpg_fill_uniform(mpg_ctx *c, int64_t n, uint64_t seed, int type, double weig
 int mpg_particles_upload(mpg_ctx *c, int64_t n, const int32_t *cell, const double *x, const double *xref,
                          const double *v, const double *w, const int32_t *species, const int64_t *id) {
   ENTER(c);
+  TRY(settle_sort(c));
   TRY(ensure_particles(c));
   if (n < 0 || n > c->cap) return fail(c, MPG_ERR_CAPACITY, "upload of %lld exceeds capacity", (long long)n);
   if (n > 0 && (!cell || !xref || !v)) return fail(c, MPG_ERR_ARG, "cell, xref and v are required");
@@ -1402,6 +1449,7 @@ int mpg_particles_upload(mpg_ctx *c, int64_t n, const int32_t *cell, const doubl
 int mpg_particles_download(mpg_ctx *c, int64_t cap, int64_t *nout, int32_t *cell, double *x, double *xref, double *v,
                            double *w, int32_t *species, int64_t *id) {
   ENTER(c);
+  TRY(settle_sort(c));
   if (!c->parts_alloc) {
     if (nout) *nout = 0;
     return MPG_OK;
@@ -1445,6 +1493,7 @@ int mpg_particles_download(mpg_ctx *c, int64_t cap, int64_t *nout, int32_t *cell
 
 int mpg_mixed_download(mpg_ctx *c, int64_t cap, int64_t *nout, uint32_t *cellsp, float *b, float *v) {
   ENTER(c);
+  TRY(settle_sort(c));
   if (!c->parts_alloc || c->precision != MPG_MIXED) return fail(c, MPG_ERR_STATE, "no mixed particle state");
   const int64_t n = c->n;
   if (nout) *nout = n;
@@ -1468,6 +1517,7 @@ int mpg_mixed_download(mpg_ctx *c, int64_t cap, int64_t *nout, uint32_t *cellsp,
 
 int mpg_mixed_upload(mpg_ctx *c, int64_t n, const uint32_t *cellsp, const float *b, const float *v) {
   ENTER(c);
+  TRY(settle_sort(c));
   TRY(ensure_particles(c));
   if (c->precision != MPG_MIXED) return fail(c, MPG_ERR_STATE, "context is not in mixed precision");
   if (n < 0 || n > c->cap) return fail(c, MPG_ERR_CAPACITY, "upload exceeds capacity");
@@ -1524,6 +1574,7 @@ int mpg_mixed_upload(mpg_ctx *c, int64_t n, const uint32_t *cellsp, const float 
 
 int mpg_charge_download(mpg_ctx *c, int64_t *acc, double *quantum, int64_t *qfix) {
   ENTER(c);
+  TRY(settle_sort(c));
   if (!c->configured) return fail(c, MPG_ERR_STATE, "not configured");
   if (c->cfg.precision != MPG_MIXED) return fail(c, MPG_ERR_STATE, "charge accumulator exists in the mixed form only");
   ensure_qfix(c);
@@ -1547,6 +1598,7 @@ int mpg_charge_download(mpg_ctx *c, int64_t *acc, double *quantum, int64_t *qfix
 
 int mpg_weight_charge(mpg_ctx *c) {
   ENTER(c);
+  TRY(settle_sort(c));
   TRY(ensure_particles(c));
   if (c->cfg.precision == MPG_MIXED) {
     c->acc_valid = false;
@@ -1580,6 +1632,7 @@ int mpg_weight_efield(mpg_ctx *c) {
 
 int mpg_move(mpg_ctx *c, double dt, mpg_step_stats *st) {
   ENTER(c);
+  TRY(settle_sort(c));
   TRY(ensure_particles(c));
   mpg_step_stats acc{};
   TRY(zero_stats(c));
@@ -1661,6 +1714,7 @@ int mpg_step(mpg_ctx *c, double dt, int n_steps, mpg_step_stats *st) {
 
 int mpg_sort(mpg_ctx *c) {
   ENTER(c);
+  TRY(settle_sort(c));
   TRY(ensure_particles(c));
   if (c->cfg.precision == MPG_MIXED) {
     TRY(sort_mixed(c));

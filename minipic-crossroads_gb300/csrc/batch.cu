@@ -999,10 +999,9 @@ void free_run(Run &r) {
 }
 
 constexpr int64_t kBatchDenseMax = 400;  // interior unknowns of a run's coarsest multigrid level
-// runs up to this many nodes solve with multigrid on one CTA; larger ones keep
-// the plain inner CG on several CTAs (one CTA's passes over ~2^18 rows would
-// cost more than the multi-CTA CG saves)
-constexpr int64_t kBatchMgMaxRows = 1 << 16;
+// runs up to this many nodes solve with multigrid (on a CTA group of
+// rows_per_mg_cta nodes per CTA, at most kMaxParts CTAs)
+constexpr int64_t kBatchMgMaxRows = 1 << 20;
 
 int64_t run_bytes_estimate(const mpg_run_desc &d) {
   const int64_t n = d.n_side;

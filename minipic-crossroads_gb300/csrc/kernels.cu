@@ -741,7 +741,9 @@ constexpr int kMoveWarps = kThreads / 32;
 constexpr int kMoveQueue = 64;  // per warp: fewer than 32 wait, up to 32 join per chunk
 
 template <bool KUHN>
-__global__ void __launch_bounds__(kThreads, 4) k_mixed_move_persistent(MixedParts P, int64_t n,
+__global__ void __launch_bounds__(kThreads, 4) k_mixed_move_persistent(MixedParts P, int64_t n, MixedParts Q,
+                                                                    const uint32_t *__restrict__ perm,
+                                                                    const uint32_t *__restrict__ d_count,
                                                                     const float4 *__restrict__ rec,
                                                                     const uint4 *__restrict__ nbr,
                                                                     const float4 *__restrict__ etet4, KuhnTable kt,
@@ -768,6 +770,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_mixed_move_persistent(MixedPart
   uint32_t *const qp = q_u[wib][0], *const qc = q_u[wib][1];
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const int64_t nchunks = (n + 31) >> 5;
+  const bool sorted_in = perm != nullptr;
+  const int64_t cnt = sorted_in ? (int64_t)*d_count : n;
   ff ke = {0.f, 0.f};
   unsigned killed = 0, cross = 0, limit = 0;
   int qn = 0;  // queued particles of this warp (warp-uniform)
@@ -804,11 +808,11 @@ __global__ void __launch_bounds__(kThreads, 4) k_mixed_move_persistent(MixedPart
       cross += (unsigned)it;
       if (dead) {
         killed += 1;
-        P.c[p] = MPG_DEAD;
+        Q.c[p] = MPG_DEAD;
       } else {
-        if (e != (cs & 0xFFFFFFu)) P.c[p] = ((uint32_t)s << 24) | e;
-        P.b[p] = make_float4(l1, l2, l3, vx);
-        P.v[p] = make_float2(vy, vz);
+        if (sorted_in || e != (cs & 0xFFFFFFu)) Q.c[p] = ((uint32_t)s << 24) | e;
+        Q.b[p] = make_float4(l1, l2, l3, vx);
+        Q.v[p] = make_float2(vy, vz);
         ke = ff_add(ke, ff{S.half_wm_f[s] * __fmaf_rn(vz, vz, __fmaf_rn(vy, vy, vx * vx)), 0.f});
         dep_key = (int)e;
         d1 = l1;
@@ -841,39 +845,39 @@ __global__ void __launch_bounds__(kThreads, 4) k_mixed_move_persistent(MixedPart
     finish(live, p, cs, l1, l2, l3, vx, vy, vz);
   };
   int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  // the record of particle i (input perm[i] when fused with a sort's
+  // gather, whose slots [count, n) are dead in Q)
+  auto fetch = [&](int64_t i, uint32_t &cs_, float4 &bv_, float2 &vv_) {
+    cs_ = MPG_DEAD;
+    if (i >= cnt) {
+      if (sorted_in && i < n) Q.c[i] = MPG_DEAD;
+      return;
+    }
+    const int64_t src = sorted_in ? (int64_t)perm[i] : i;
+    cs_ = P.c[src];
+    bv_ = P.b[src];
+    vv_ = P.v[src];
+    if (sorted_in && P.id) Q.id[i] = P.id[src];
+  };
   // prefetched record of this lane's particle in chunk c
   uint32_t cs_n = MPG_DEAD;
   float4 bv_n = make_float4(0.f, 0.f, 0.f, 0.f);
   float2 vv_n = make_float2(0.f, 0.f);
-  {
-    const int64_t p = c * 32 + lane;
-    if (c < nchunks && p < n) {
-      cs_n = P.c[p];
-      bv_n = P.b[p];
-      vv_n = P.v[p];
-    }
-  }
+  if (c < nchunks) fetch(c * 32 + lane, cs_n, bv_n, vv_n);
   for (; c < nchunks; c += nw) {
     const int64_t p = c * 32 + lane;
     const uint32_t cs = cs_n;
     const float4 bv = bv_n;
     const float2 vv = vv_n;
-    {
-      const int64_t q = (c + nw) * 32 + lane;
-      cs_n = MPG_DEAD;
-      if (c + nw < nchunks && q < n) {
-        cs_n = P.c[q];
-        bv_n = P.b[q];
-        vv_n = P.v[q];
-      }
-    }
+    cs_n = MPG_DEAD;
+    if (c + nw < nchunks) fetch((c + nw) * 32 + lane, cs_n, bv_n, vv_n);
     int dep_key = -1;
     float d1 = 0.f, d2 = 0.f, d3 = 0.f;
     int dq = 0;
     bool queue = false;
     float l1 = bv.x, l2 = bv.y, l3 = bv.z;
     float vx = bv.w, vy = vv.x, vz = vv.y;
-    if (p < n && cs != MPG_DEAD) {
+    if (p < cnt && cs != MPG_DEAD) {
       const int s = (int)(cs >> 24);
       uint32_t e = cs & 0xFFFFFFu;
       float4 r0, r1, r2;
@@ -897,8 +901,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_mixed_move_persistent(MixedPart
       }
       if (!queue) {
         // stays in its tet: l advanced by dt, nothing else changes
-        P.b[p] = make_float4(l1, l2, l3, vx);
-        P.v[p] = make_float2(vy, vz);
+        if (sorted_in) Q.c[p] = cs;
+        Q.b[p] = make_float4(l1, l2, l3, vx);
+        Q.v[p] = make_float2(vy, vz);
         ke = ff_add(ke, ff{S.half_wm_f[s] * __fmaf_rn(vz, vz, __fmaf_rn(vy, vy, vx * vx)), 0.f});
         dep_key = (int)e;
         d1 = l1;
@@ -1536,24 +1541,35 @@ static unsigned move_wave_blocks() {
   }
   return (unsigned)cached[dev];
 }
-void launch_mixed_move(cudaStream_t s, const MixedParts &P, int64_t n, const DevMesh &M, const SpeciesTable &S,
-                       float dt, int kill, int max_cross, unsigned long long *acc, DevStats *st) {
-  if (n <= 0) return;
+static void move_persistent(cudaStream_t s, const MixedParts &P, int64_t n, const MixedParts &Q,
+                            const uint32_t *perm, const uint32_t *d_count, const DevMesh &M, const SpeciesTable &S,
+                            float dt, int kill, int max_cross, unsigned long long *acc, DevStats *st) {
   const unsigned want = grid_for(n);
   if (M.kuhn) {
     const unsigned wave = move_wave_blocks<true>();
     k_mixed_move_persistent<true><<<want < wave ? want : wave, kThreads, 0, s>>>(
-        P, n, M.mrec, M.mnbr, M.etet4, M.ktab, M.c2n, S, dt, kill, max_cross, acc, st);
-    return;
+        P, n, Q, perm, d_count, M.mrec, M.mnbr, M.etet4, M.ktab, M.c2n, S, dt, kill, max_cross, acc, st);
+  } else {
+    const unsigned wave = move_wave_blocks<false>();
+    k_mixed_move_persistent<false><<<want < wave ? want : wave, kThreads, 0, s>>>(
+        P, n, Q, perm, d_count, M.mrec, M.mnbr, M.etet4, M.ktab, M.c2n, S, dt, kill, max_cross, acc, st);
   }
+}
+void launch_mixed_move(cudaStream_t s, const MixedParts &P, int64_t n, const DevMesh &M, const SpeciesTable &S,
+                       float dt, int kill, int max_cross, unsigned long long *acc, DevStats *st) {
+  if (n <= 0) return;
   static const char *env = getenv("MPG_MOVE_KERNEL");
-  if (env && atoi(env) == 0) {
+  if (!M.kuhn && env && atoi(env) == 0) {
     k_mixed_move<<<grid_for(n), kThreads, 0, s>>>(P, n, M.mrec, M.mnbr, M.c2n, S, dt, kill, max_cross, acc, st);
     return;
   }
-  const unsigned wave = move_wave_blocks<false>();
-  k_mixed_move_persistent<false><<<want < wave ? want : wave, kThreads, 0, s>>>(
-      P, n, M.mrec, M.mnbr, M.etet4, M.ktab, M.c2n, S, dt, kill, max_cross, acc, st);
+  move_persistent(s, P, n, P, nullptr, nullptr, M, S, dt, kill, max_cross, acc, st);
+}
+void launch_mixed_move_sorted(cudaStream_t s, const MixedParts &P, int64_t n, const MixedParts &Q,
+                              const uint32_t *perm, const uint32_t *d_count, const DevMesh &M, const SpeciesTable &S,
+                              float dt, int kill, int max_cross, unsigned long long *acc, DevStats *st) {
+  if (n <= 0) return;
+  move_persistent(s, P, n, Q, perm, d_count, M, S, dt, kill, max_cross, acc, st);
 }
 // the five passes of the stable cell sort; leaves perm[0..count) and start
 // (T + 1 entries) behind, and the count in *d_count
@@ -1572,11 +1588,19 @@ static void cell_sort_order(cudaStream_t s, const uint32_t *keys, int64_t n, int
                                                             tmp);
   k_copy_u32<<<1, 1, 0, s>>>(w.start + T, d_count);
 }
+void launch_mixed_sort_order(cudaStream_t s, const MixedParts &P, int64_t n, const MixedParts &Q, int64_t T,
+                             const SortWork &w, uint32_t *d_count) {
+  cell_sort_order<true>(s, P.c, n, T, w, Q.c, d_count);
+}
+void launch_mixed_gather(cudaStream_t s, const MixedParts &P, int64_t n, const MixedParts &Q, const uint32_t *perm,
+                         const uint32_t *d_count) {
+  if (n > 0)
+    k_sort_gather_mixed<<<grid_for((n + kGatherPer - 1) / kGatherPer), kThreads, 0, s>>>(P, n, Q, perm, d_count);
+}
 void launch_mixed_sort(cudaStream_t s, const MixedParts &P, int64_t n, const MixedParts &Q, int64_t T,
                        const SortWork &w, uint32_t *d_count) {
-  cell_sort_order<true>(s, P.c, n, T, w, Q.c, d_count);
-  if (n > 0)
-    k_sort_gather_mixed<<<grid_for((n + kGatherPer - 1) / kGatherPer), kThreads, 0, s>>>(P, n, Q, w.perm, d_count);
+  launch_mixed_sort_order(s, P, n, Q, T, w, d_count);
+  launch_mixed_gather(s, P, n, Q, w.perm, d_count);
 }
 void launch_plain_sort(cudaStream_t s, const PlainParts &P, int64_t n, const PlainParts &Q, int64_t T,
                        const SortWork &w, uint32_t *d_count) {

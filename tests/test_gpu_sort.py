@@ -90,3 +90,32 @@ def test_sort_long_cell_ranges_and_repeatability(mpg, orc):
         assert (cs2 == cs[perm]).all()
         assert (ctx.cell_starts() == start).all()
     assert (runs[0][0] == runs[1][0]).all() and (runs[0][1] == runs[1][1]).all()
+
+
+def test_sort_gather_fused_into_next_move(mpg):
+    """mpg_step leaves the gather of its cell sort to the next move, which
+    reads the particles through the permutation into the other buffer; any
+    other use of the list completes the gather first.  Nine steps in one call
+    (sorts after steps 3 and 6 fused into the moves of steps 4 and 7) equal
+    nine single steps with a download after each (every gather completed on
+    its own), bit for bit: particle state, charge, phi."""
+    runs = []
+    for single in (False, True):
+        ctx = _ctx(mpg, mpg.MIXED, n_side=10, jitter=0.2, sort_interval=3, track_ids=1)
+        n = 60000
+        ctx.reserve(n)
+        ctx.fill_uniform(n // 2, 41, 0, 1.0 / n, drift=(0.3, 0, 0), vth=0.1)
+        ctx.fill_uniform(n // 2, 42, 0, 1.0 / n, drift=(-0.3, 0, 0), vth=0.1)
+        if single:
+            for _ in range(9):
+                ctx.step(0.02, 1)
+                ctx.mixed_download()
+        else:
+            ctx.step(0.02, 9)
+        runs.append((ctx.mixed_download(), ctx.download()["id"], ctx.charge()[0], ctx.get_field(mpg.FIELD_PHI)))
+        ctx.close()
+    (a, ida, qa, pa), (b, idb, qb, pb) = runs
+    for u, v in zip(a, b):
+        assert (u.view(np.uint8) == v.view(np.uint8)).all()
+    assert (ida == idb).all() and (qa == qb).all()
+    assert (pa.view(np.uint64) == pb.view(np.uint64)).all()
