@@ -59,8 +59,11 @@ struct mpg_ctx {
   bool acc_valid = false;
   bool needs_sort = false;  // particles added or replaced since the last cell sort
   // a cell sort's permutation (sort_perm) whose gather is left to the next
-  // move, which reads the particles through it into the other buffer
+  // move, which reads the particles through it into the other buffer; the
+  // list in mp[cur] then still has n_presort slots (n may already hold the
+  // sorted count)
   bool gather_pending = false;
+  int64_t n_presort = 0;
   double inner_tol = 1e-5;  // relative residual target of the mixed solver's FP32 inner CG
 
   int precision = MPG_PLAIN;  // precision of the allocated particle arrays
@@ -380,10 +383,11 @@ int phase_deposit_plain(mpg_ctx *c) {
 int settle_sort(mpg_ctx *c);
 int phase_deposit_mixed(mpg_ctx *c) {
   if (!c->acc_valid) {
-    TRY(settle_sort(c));
+    // the deposit does not depend on the order: with a gather pending it
+    // reads the unsorted list (its dead slots deposit nothing)
     ensure_qfix(c);
     CK(cudaMemsetAsync(c->acc, 0, sizeof(unsigned long long) * 4 * c->dm.T, c->stream));
-    launch_mixed_deposit(c->stream, c->mp[c->cur], c->n, c->dm, c->sp, c->acc);
+    launch_mixed_deposit(c->stream, c->mp[c->cur], c->gather_pending ? c->n_presort : c->n, c->dm, c->sp, c->acc);
     c->acc_valid = true;
     c->launches += 1;
   }
@@ -548,6 +552,7 @@ int sort_mixed_deferred(mpg_ctx *c) {
   c->launches += 9;
   CKL();
   c->gather_pending = true;
+  c->n_presort = c->n;
   c->starts_valid = true;
   return MPG_OK;
 }
@@ -592,8 +597,9 @@ int one_step(mpg_ctx *c, double dt, mpg_step_stats *acc_st, bool &sorted) {
   const bool mixed = c->cfg.precision == MPG_MIXED;
   if (mixed && c->cfg.sort_interval > 0 && c->needs_sort) {
     // freshly filled or uploaded particles are in arbitrary cell order: sort
-    // before the first step instead of after sort_interval steps
-    TRY(sort_mixed(c));
+    // before the first step instead of after sort_interval steps (its gather
+    // is this step's move)
+    TRY(sort_mixed_deferred(c));
     sorted = true;
   }
   ev_record(c, 0);
@@ -1491,6 +1497,20 @@ int mpg_particles_download(mpg_ctx *c, int64_t cap, int64_t *nout, int32_t *cell
   return MPG_OK;
 }
 
+// Device address of host memory that the device can read and write (page
+// locked and mapped: cudaHostAlloc'ed or cudaHostRegister'ed), else null.
+// Such buffers are read and written by the pack kernels directly over the
+// host link, without a staging copy in device memory.
+static void *mapped_host(const void *p) {
+  if (!p) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 int mpg_mixed_download(mpg_ctx *c, int64_t cap, int64_t *nout, uint32_t *cellsp, float *b, float *v) {
   ENTER(c);
   TRY(settle_sort(c));
@@ -1499,6 +1519,14 @@ int mpg_mixed_download(mpg_ctx *c, int64_t cap, int64_t *nout, uint32_t *cellsp,
   if (nout) *nout = n;
   if (cap < n) return fail(c, MPG_ERR_CAPACITY, "download buffer too small");
   cudaStream_t s = c->stream;
+  float *hb = static_cast<float *>(mapped_host(b)), *hv = static_cast<float *>(mapped_host(v));
+  if (n > 0 && hb && hv) {
+    launch_mixed_unpack(s, c->mp[c->cur], n, hb, hv);
+    CKL();
+    if (cellsp) CK(cudaMemcpyAsync(cellsp, c->mp[c->cur].c, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return MPG_OK;
+  }
   float *sb, *sv;
   CK(cudaMallocAsync((void **)&sb, sizeof(float) * 3 * (n > 0 ? n : 1), s));
   CK(cudaMallocAsync((void **)&sv, sizeof(float) * 3 * (n > 0 ? n : 1), s));
@@ -1523,21 +1551,29 @@ int mpg_mixed_upload(mpg_ctx *c, int64_t n, const uint32_t *cellsp, const float 
   if (n < 0 || n > c->cap) return fail(c, MPG_ERR_CAPACITY, "upload exceeds capacity");
   // staged upload: the words are validated on the device before they replace
   // the resident state, so a rejected upload leaves the context unchanged
+  // (mapped host buffers: validated and packed from host memory directly)
   cudaStream_t s = c->stream;
   const int64_t nn = n > 0 ? n : 1;
+  const uint32_t *hc = static_cast<const uint32_t *>(mapped_host(cellsp));
+  const float *hb = static_cast<const float *>(mapped_host(b)), *hv = static_cast<const float *>(mapped_host(v));
+  const bool direct = n > 0 && hc && hb && hv;
   uint32_t *sc;
   float *sb, *sv;
   unsigned long long *chk;
-  CK(cudaMallocAsync((void **)&sc, sizeof(uint32_t) * nn, s));
-  CK(cudaMallocAsync((void **)&sb, sizeof(float) * 3 * nn, s));
-  CK(cudaMallocAsync((void **)&sv, sizeof(float) * 3 * nn, s));
+  const int64_t ns = direct ? 1 : nn;
+  CK(cudaMallocAsync((void **)&sc, sizeof(uint32_t) * ns, s));
+  CK(cudaMallocAsync((void **)&sb, sizeof(float) * 3 * ns, s));
+  CK(cudaMallocAsync((void **)&sv, sizeof(float) * 3 * ns, s));
   CK(cudaMallocAsync((void **)&chk, 2 * sizeof(unsigned long long), s));
   uint32_t wmask = 0;
   for (int k = 0; k < MPG_MAX_SPECIES; ++k)
     if (c->weight_set[k]) wmask |= 1u << k;
   unsigned long long h_chk[2] = {~0ull, 0ull};
   CK(cudaMemcpyAsync(chk, h_chk, sizeof(h_chk), cudaMemcpyHostToDevice, s));
-  if (n > 0) {
+  if (direct) {
+    launch_mixed_check(s, hc, n, c->hm.T, wmask, chk);
+    CKL();
+  } else if (n > 0) {
     CK(cudaMemcpyAsync(sc, cellsp, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(sb, b, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(sv, v, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, s));
@@ -1553,6 +1589,10 @@ int mpg_mixed_upload(mpg_ctx *c, int64_t n, const uint32_t *cellsp, const float 
       rc = fail(c, MPG_ERR_ARG, "cellsp[%lld] out of range", (long long)i);
     else
       rc = fail(c, MPG_ERR_STATE, "species %u has no weight (fill or upload it first)", cellsp[i] >> 24);
+  } else if (direct) {
+    CK(cudaMemcpyAsync(c->mp[c->cur].c, cellsp, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, s));
+    launch_mixed_pack(s, hb, hv, c->mp[c->cur], n);
+    CKL();
   } else if (n > 0) {
     CK(cudaMemcpyAsync(c->mp[c->cur].c, sc, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s));
     launch_mixed_pack(s, sb, sv, c->mp[c->cur], n);

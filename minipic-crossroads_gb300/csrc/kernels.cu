@@ -1412,14 +1412,57 @@ __global__ void k_mixed_check(const uint32_t *__restrict__ cs, int64_t n, int64_
   if ((threadIdx.x & 31) == 0 && live) atomicAdd(&out[1], (unsigned long long)live);
 }
 
-__global__ void k_mixed_pack(const float *__restrict__ b, const float *__restrict__ v, MixedParts X, int64_t n) {
-  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+// Host layout (b and v as float[3] per particle) <-> device records.  A
+// warp moves its 32 particles' 384-byte spans of b and v as 24 float4 each,
+// through shared memory, so that every access to the host arrays (which may
+// be mapped host memory, read and written over the host link) is a full
+// 16-byte vector; arrays not 16-byte aligned, and the last partial warp, go
+// element by element.
+constexpr int kPackWarps = kThreads / 32;
+__global__ void __launch_bounds__(kThreads) k_mixed_pack(const float *__restrict__ b, const float *__restrict__ v,
+                                                         MixedParts X, int64_t n) {
+  __shared__ float4 sm[kPackWarps][2][24];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int64_t p0 = ((int64_t)blockIdx.x * blockDim.x) + 32 * wib, p = p0 + lane;
+  const bool vec = ((reinterpret_cast<uintptr_t>(b) | reinterpret_cast<uintptr_t>(v)) & 15u) == 0 && p0 + 32 <= n;
+  if (vec) {
+    if (lane < 24) {
+      sm[wib][0][lane] = reinterpret_cast<const float4 *>(b + 3 * p0)[lane];
+      sm[wib][1][lane] = reinterpret_cast<const float4 *>(v + 3 * p0)[lane];
+    }
+    __syncwarp();
+    const float *fb = reinterpret_cast<const float *>(sm[wib][0]), *fv = reinterpret_cast<const float *>(sm[wib][1]);
+    X.b[p] = make_float4(fb[3 * lane], fb[3 * lane + 1], fb[3 * lane + 2], fv[3 * lane]);
+    X.v[p] = make_float2(fv[3 * lane + 1], fv[3 * lane + 2]);
+    return;
+  }
   if (p >= n) return;
   X.b[p] = make_float4(b[3 * p], b[3 * p + 1], b[3 * p + 2], v[3 * p]);
   X.v[p] = make_float2(v[3 * p + 1], v[3 * p + 2]);
 }
-__global__ void k_mixed_unpack(MixedParts X, int64_t n, float *__restrict__ b, float *__restrict__ v) {
-  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(kThreads) k_mixed_unpack(MixedParts X, int64_t n, float *__restrict__ b,
+                                                           float *__restrict__ v) {
+  __shared__ float4 sm[kPackWarps][2][24];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int64_t p0 = ((int64_t)blockIdx.x * blockDim.x) + 32 * wib, p = p0 + lane;
+  const bool vec = ((reinterpret_cast<uintptr_t>(b) | reinterpret_cast<uintptr_t>(v)) & 15u) == 0 && p0 + 32 <= n;
+  if (vec) {
+    const float4 a = X.b[p];
+    const float2 c = X.v[p];
+    float *fb = reinterpret_cast<float *>(sm[wib][0]), *fv = reinterpret_cast<float *>(sm[wib][1]);
+    fb[3 * lane] = a.x;
+    fb[3 * lane + 1] = a.y;
+    fb[3 * lane + 2] = a.z;
+    fv[3 * lane] = a.w;
+    fv[3 * lane + 1] = c.x;
+    fv[3 * lane + 2] = c.y;
+    __syncwarp();
+    if (lane < 24) {
+      reinterpret_cast<float4 *>(b + 3 * p0)[lane] = sm[wib][0][lane];
+      reinterpret_cast<float4 *>(v + 3 * p0)[lane] = sm[wib][1][lane];
+    }
+    return;
+  }
   if (p >= n) return;
   const float4 a = X.b[p];
   const float2 c = X.v[p];

@@ -307,3 +307,40 @@ def test_kuhn_move_deposit_matches_oracle(mpg, orc, n_side, n):
         assert (acc == orc.deposit_fixed(m, cs, b, qfix)).all()
     assert killed > 0
     ctx.close()
+
+
+def test_mixed_upload_download_from_mapped_host_memory(mpg):
+    """Page-locked mapped host buffers (cudaHostAlloc, here through torch's
+    pinned allocator) are validated, packed and unpacked by the device
+    directly over the host link: the same particle state as through staged
+    copies of pageable buffers, and a rejected upload (a cell out of range)
+    leaves the resident state unchanged."""
+    torch = pytest.importorskip("torch")
+    ctx = _ctx(mpg, n_side=10, jitter=0.0)
+    n = 50000
+    ctx.reserve(n)
+    ctx.fill_uniform(n, 9, 0, 1.0 / n, drift=(0.2, 0, 0), vth=0.05)
+    ctx.step(0.01, 2)
+    cs, b, v = ctx.mixed_download()
+
+    def pinned(a):
+        t = torch.empty(a.nbytes, dtype=torch.uint8, pin_memory=True).numpy().view(a.dtype).reshape(a.shape)
+        np.copyto(t, a)
+        return t
+
+    pc, pb, pv = pinned(cs), pinned(b), pinned(v)
+    out = tuple(pinned(np.zeros_like(a)) for a in (cs, b, v))
+    c2, b2, v2 = ctx.mixed_download(out=out)
+    assert (c2 == cs).all() and (b2 == b).all() and (v2 == v).all()
+    bad = pinned(cs)
+    bad[123] = (bad[123] & 0xFF000000) | 0xFFFFF0
+    with pytest.raises(mpg.MpgError):
+        ctx.mixed_upload(bad, pb, pv)
+    c3, b3, v3 = ctx.mixed_download()
+    assert (c3 == cs).all() and (b3 == b).all() and (v3 == v).all()
+    # a modified state goes in through the mapped buffers and comes back the same
+    pb[:, 0] *= 0.5
+    ctx.mixed_upload(pc, pb, pv)
+    c4, b4, v4 = ctx.mixed_download()
+    assert (c4 == pc).all() and (b4 == pb).all() and (v4 == pv).all()
+    ctx.close()
