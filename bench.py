@@ -362,7 +362,8 @@ def autotune(mpg, runs, device=0):
     """Pick the batch engine's block size, step form (one persistent launch
     per step or one launch per phase) and sort interval on a sample of runs:
     first block size x step form at sort interval 10, then the best of those
-    at sort intervals 5 and 20."""
+    at sort intervals 5 and 20.  The one-launch form is kept unless one launch
+    per phase is more than 1 % faster at the same block size."""
     sample = runs[: min(24, len(runs))]
     cap = sum(r["n_particles"] for r in sample)
     results = []
@@ -381,9 +382,12 @@ def autotune(mpg, runs, device=0):
         for fused in (True, False):
             trial(th, fused, 10)
     _, th, fused, _ = max(results)
+    rate = {(t, f): v for v, t, f, _ in results}
+    if not fused and rate[(th, True)] * 1.01 >= rate[(th, False)]:
+        fused = True
     for si in (5, 20):
         trial(th, fused, si)
-    best = max(results)
+    best = max((r for r in results if r[1] == th and r[2] == fused), key=lambda r: r[0])
     return {"cg_threads": best[1], "fused": best[2], "sort_interval": best[3],
             "tried": [{"cg_threads": th, "fused": fu, "sort_interval": si, "particle_steps_per_ms": round(v, 1)}
                       for v, th, fu, si in results]}
