@@ -210,7 +210,8 @@ def test_reference_problem_steps_match_oracle(mpg, orc):
 
 
 def test_config1_plain_steps_match_oracle(mpg, orc):
-    # configs[0] shape at reduced count: Kuhn [0,1]^3, e- uniform, background, CG 1e-10, absorbing
+    # the 10^3 Kuhn plain configuration at a reduced count: Kuhn [0,1]^3, e- uniform, background, CG 1e-10,
+    # absorbing walls
     n_side, n = 10, 20000
     ctx, m = _mesh_pair(mpg, orc, n_side, 6, 0.0, 1.0)
     ctx.configure(precision=mpg.PLAIN, deposit=mpg.DEPOSIT_LINEAR, solver=mpg.SOLVER_CG, tol=1e-10,
