@@ -479,7 +479,11 @@ def accuracy_vs_plain(mpg, w, steps, device=0):
 def run_ensemble(mpg, args, device=0):
     import numpy as np
     runs = ensemble_trace()
-    tune = autotune(mpg, runs, device)
+    if args.batch_form:
+        # fixed tuning instead of the autotuner (profiler captures)
+        tune = {"cg_threads": 1024, "fused": args.batch_form == "fused", "sort_interval": 10, "tried": []}
+    else:
+        tune = autotune(mpg, runs, device)
     cap = sum(r["n_particles"] for r in runs)
     bt = mpg.Batch(device, budget_bytes=150 << 30, max_runs=256, particle_capacity=cap)
     bt.tuning(tune["cg_threads"], tune["sort_interval"], fused=tune["fused"])
@@ -500,7 +504,10 @@ def run_ensemble(mpg, args, device=0):
         graph = max(graph, st.graph)
     clk = clocks.stop()
     bt.close()
-    seq_s, seq_detail = plain_sequential_time(mpg, runs, device)
+    if args.no_plain:
+        seq_s, seq_detail = float("nan"), {"skipped": "--no-plain"}
+    else:
+        seq_s, seq_detail = plain_sequential_time(mpg, runs, device)
     seq = sum(r["n_particles"] * r["steps"] for r in runs) / seq_s
     value = ps / (ms * 1e-3)
     return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": len(lat), "warmup": 0,
@@ -849,6 +856,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the 48^3 configuration key")
+    ap.add_argument("--batch-form", default=None, choices=["fused", "phases"],
+                    help="ensemble: fixed batch tuning (1024-thread solver blocks, sort interval 10) with this "
+                         "step form instead of the autotuner")
     ap.add_argument("--accuracy-steps", type=int, default=None,
                     help="steps of the mixed-vs-FP64 comparison (default: the configuration's step count)")
     ap.add_argument("--warm-start", type=int, default=2, choices=[0, 1, 2, 3],
