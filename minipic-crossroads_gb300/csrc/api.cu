@@ -1521,9 +1521,11 @@ int mpg_mixed_download(mpg_ctx *c, int64_t cap, int64_t *nout, uint32_t *cellsp,
   cudaStream_t s = c->stream;
   float *hb = static_cast<float *>(mapped_host(b)), *hv = static_cast<float *>(mapped_host(v));
   if (n > 0 && hb && hv) {
-    launch_mixed_unpack(s, c->mp[c->cur], n, hb, hv);
+    uint32_t *hc = static_cast<uint32_t *>(mapped_host(cellsp));
+    launch_mixed_unpack(s, c->mp[c->cur], n, hb, hv, hc);
     CKL();
-    if (cellsp) CK(cudaMemcpyAsync(cellsp, c->mp[c->cur].c, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, s));
+    if (cellsp && !hc)
+      CK(cudaMemcpyAsync(cellsp, c->mp[c->cur].c, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     return MPG_OK;
   }
@@ -1570,8 +1572,11 @@ int mpg_mixed_upload(mpg_ctx *c, int64_t n, const uint32_t *cellsp, const float 
     if (c->weight_set[k]) wmask |= 1u << k;
   unsigned long long h_chk[2] = {~0ull, 0ull};
   CK(cudaMemcpyAsync(chk, h_chk, sizeof(h_chk), cudaMemcpyHostToDevice, s));
+  const int other = 1 - c->cur;
   if (direct) {
-    launch_mixed_check(s, hc, n, c->hm.T, wmask, chk);
+    // checked and packed into the free buffer in one pass over the host
+    // arrays; it replaces the resident list only if every word passed
+    launch_mixed_pack_checked(s, hc, hb, hv, c->mp[other], n, c->hm.T, wmask, chk);
     CKL();
   } else if (n > 0) {
     CK(cudaMemcpyAsync(sc, cellsp, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, s));
@@ -1590,9 +1595,9 @@ int mpg_mixed_upload(mpg_ctx *c, int64_t n, const uint32_t *cellsp, const float 
     else
       rc = fail(c, MPG_ERR_STATE, "species %u has no weight (fill or upload it first)", cellsp[i] >> 24);
   } else if (direct) {
-    CK(cudaMemcpyAsync(c->mp[c->cur].c, cellsp, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, s));
-    launch_mixed_pack(s, hb, hv, c->mp[c->cur], n);
-    CKL();
+    if (c->mp[c->cur].id && c->mp[other].id)
+      CK(cudaMemcpyAsync(c->mp[other].id, c->mp[c->cur].id, sizeof(int64_t) * n, cudaMemcpyDeviceToDevice, s));
+    c->cur = other;
   } else if (n > 0) {
     CK(cudaMemcpyAsync(c->mp[c->cur].c, sc, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s));
     launch_mixed_pack(s, sb, sv, c->mp[c->cur], n);

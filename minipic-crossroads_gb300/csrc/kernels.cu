@@ -1419,11 +1419,31 @@ __global__ void k_mixed_check(const uint32_t *__restrict__ cs, int64_t n, int64_
 // 16-byte vector; arrays not 16-byte aligned, and the last partial warp, go
 // element by element.
 constexpr int kPackWarps = kThreads / 32;
+// With cs (checked packing): the cell words go to X.c as well, each one
+// checked as k_mixed_check does (first bad index and live count in out).
 __global__ void __launch_bounds__(kThreads) k_mixed_pack(const float *__restrict__ b, const float *__restrict__ v,
-                                                         MixedParts X, int64_t n) {
+                                                         MixedParts X, int64_t n, const uint32_t *__restrict__ cs,
+                                                         int64_t T, uint32_t weight_mask,
+                                                         unsigned long long *__restrict__ out) {
   __shared__ float4 sm[kPackWarps][2][24];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int64_t p0 = ((int64_t)blockIdx.x * blockDim.x) + 32 * wib, p = p0 + lane;
+  if (cs) {
+    unsigned live = 0;
+    if (p < n) {
+      const uint32_t w = cs[p];
+      X.c[p] = w;
+      if (w != MPG_DEAD) {
+        const uint32_t sp = w >> 24;
+        if ((int64_t)(w & 0xFFFFFFu) >= T || sp >= MPG_MAX_SPECIES || !((weight_mask >> sp) & 1u))
+          atomicMin(&out[0], (unsigned long long)p);
+        else
+          live = 1;
+      }
+    }
+    live = __reduce_add_sync(0xffffffffu, live);
+    if (lane == 0 && live) atomicAdd(&out[1], (unsigned long long)live);
+  }
   const bool vec = ((reinterpret_cast<uintptr_t>(b) | reinterpret_cast<uintptr_t>(v)) & 15u) == 0 && p0 + 32 <= n;
   if (vec) {
     if (lane < 24) {
@@ -1441,10 +1461,11 @@ __global__ void __launch_bounds__(kThreads) k_mixed_pack(const float *__restrict
   X.v[p] = make_float2(v[3 * p + 1], v[3 * p + 2]);
 }
 __global__ void __launch_bounds__(kThreads) k_mixed_unpack(MixedParts X, int64_t n, float *__restrict__ b,
-                                                           float *__restrict__ v) {
+                                                           float *__restrict__ v, uint32_t *__restrict__ cs) {
   __shared__ float4 sm[kPackWarps][2][24];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int64_t p0 = ((int64_t)blockIdx.x * blockDim.x) + 32 * wib, p = p0 + lane;
+  if (cs && p < n) cs[p] = X.c[p];
   const bool vec = ((reinterpret_cast<uintptr_t>(b) | reinterpret_cast<uintptr_t>(v)) & 15u) == 0 && p0 + 32 <= n;
   if (vec) {
     const float4 a = X.b[p];
@@ -1680,14 +1701,18 @@ void launch_cols_to_rows(cudaStream_t s, const double *cols, double *rows, int64
   if (n > 0) k_cols_to_rows<<<grid_for(n), kThreads, 0, s>>>(cols, rows, n, cap);
 }
 void launch_mixed_pack(cudaStream_t s, const float *b, const float *v, MixedParts X, int64_t n) {
-  if (n > 0) k_mixed_pack<<<grid_for(n), kThreads, 0, s>>>(b, v, X, n);
+  if (n > 0) k_mixed_pack<<<grid_for(n), kThreads, 0, s>>>(b, v, X, n, nullptr, 0, 0u, nullptr);
+}
+void launch_mixed_pack_checked(cudaStream_t s, const uint32_t *cs, const float *b, const float *v, MixedParts X,
+                               int64_t n, int64_t T, uint32_t weight_mask, unsigned long long *out) {
+  if (n > 0) k_mixed_pack<<<grid_for(n), kThreads, 0, s>>>(b, v, X, n, cs, T, weight_mask, out);
 }
 void launch_mixed_check(cudaStream_t s, const uint32_t *cs, int64_t n, int64_t T, uint32_t weight_mask,
                         unsigned long long *out) {
   if (n > 0) k_mixed_check<<<grid_for(n), kThreads, 0, s>>>(cs, n, T, weight_mask, out);
 }
-void launch_mixed_unpack(cudaStream_t s, const MixedParts X, int64_t n, float *b, float *v) {
-  if (n > 0) k_mixed_unpack<<<grid_for(n), kThreads, 0, s>>>(X, n, b, v);
+void launch_mixed_unpack(cudaStream_t s, const MixedParts X, int64_t n, float *b, float *v, uint32_t *cs) {
+  if (n > 0) k_mixed_unpack<<<grid_for(n), kThreads, 0, s>>>(X, n, b, v, cs);
 }
 void launch_plain_to_mixed(cudaStream_t s, const PlainParts &P, int64_t n0, int64_t n, const MixedParts &X) {
   if (n > 0) k_plain_to_mixed<<<grid_for(n), kThreads, 0, s>>>(P, n0, n, X);

@@ -343,4 +343,11 @@ def test_mixed_upload_download_from_mapped_host_memory(mpg):
     ctx.mixed_upload(pc, pb, pv)
     c4, b4, v4 = ctx.mixed_download()
     assert (c4 == pc).all() and (b4 == pb).all() and (v4 == pv).all()
+    # and steps on exactly as the same state uploaded from pageable copies
+    ctx.step(0.01, 1)
+    c5, b5, v5 = ctx.mixed_download(out=out)
+    ctx.mixed_upload(np.array(pc), np.array(pb), np.array(pv))
+    ctx.step(0.01, 1)
+    c6, b6, v6 = ctx.mixed_download()
+    assert (c5 == c6).all() and (b5 == b6).all() and (v5 == v6).all()
     ctx.close()
