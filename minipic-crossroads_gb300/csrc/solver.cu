@@ -776,9 +776,10 @@ int run_bicgstab(cudaStream_t s, int64_t n, const int32_t *rp, const int32_t *co
 // The scratch of the solve lives in one file-scope static device array: the
 // device-side counters (DevStats, 256 B), the per-block partial sums (8 x
 // kNoAllocMaxBlocks doubles) and the vectors r, p, p', q (MPG_NOALLOC_MAX_N
-// doubles each).  Host code never uses the array's name as an address: the
-// first call on a device (with that device current) asks the runtime for the
-// array's device address with cudaGetSymbolAddress and caches it per device.
+// doubles each).  Host code never uses the array's name as an address: every
+// call asks the runtime for the array's device address in the current
+// context with cudaGetSymbolAddress (only the co-residency limit is cached
+// per device).
 namespace {
 constexpr int kNoAllocMaxBlocks = 4096;
 constexpr size_t kNoAllocStatsBytes = 256;
