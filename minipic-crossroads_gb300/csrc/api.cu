@@ -1574,9 +1574,12 @@ int mpg_mixed_upload(mpg_ctx *c, int64_t n, const uint32_t *cellsp, const float 
   CK(cudaMemcpyAsync(chk, h_chk, sizeof(h_chk), cudaMemcpyHostToDevice, s));
   const int other = 1 - c->cur;
   if (direct) {
-    // checked and packed into the free buffer in one pass over the host
-    // arrays; it replaces the resident list only if every word passed
-    launch_mixed_pack_checked(s, hc, hb, hv, c->mp[other], n, c->hm.T, wmask, chk);
+    // checked, packed into the free buffer and deposited in one pass over
+    // the host arrays (the deposit costs nothing beside the reads over the
+    // host link); it replaces the resident list only if every word passed
+    ensure_qfix(c);
+    CK(cudaMemsetAsync(c->acc, 0, sizeof(unsigned long long) * 4 * c->dm.T, s));
+    launch_mixed_pack_checked(s, hc, hb, hv, c->mp[other], n, c->hm.T, wmask, chk, c->dm, c->sp, c->acc);
     CKL();
   } else if (n > 0) {
     CK(cudaMemcpyAsync(sc, cellsp, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, s));
@@ -1608,10 +1611,13 @@ int mpg_mixed_upload(mpg_ctx *c, int64_t n, const uint32_t *cellsp, const float 
   CK(cudaFreeAsync(sv, s));
   CK(cudaFreeAsync(chk, s));
   CK(cudaStreamSynchronize(s));
-  if (rc != MPG_OK) return rc;
+  if (rc != MPG_OK) {
+    if (direct) c->acc_valid = false;  // the slots hold a partial deposit of the rejected list
+    return rc;
+  }
   c->n = n;
   c->n_live = (int64_t)h_chk[1];
-  c->acc_valid = false;
+  c->acc_valid = direct;  // the direct path deposited the new list
   c->needs_sort = true;
   c->starts_valid = false;
   return MPG_OK;

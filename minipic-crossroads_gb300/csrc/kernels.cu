@@ -1420,14 +1420,20 @@ __global__ void k_mixed_check(const uint32_t *__restrict__ cs, int64_t n, int64_
 // element by element.
 constexpr int kPackWarps = kThreads / 32;
 // With cs (checked packing): the cell words go to X.c as well, each one
-// checked as k_mixed_check does (first bad index and live count in out).
+// checked as k_mixed_check does (first bad index and live count in out), and
+// with acc the charge of every checked live particle is deposited as
+// k_mixed_deposit does (the same integer sums; the slots are zeroed first).
 __global__ void __launch_bounds__(kThreads) k_mixed_pack(const float *__restrict__ b, const float *__restrict__ v,
                                                          MixedParts X, int64_t n, const uint32_t *__restrict__ cs,
                                                          int64_t T, uint32_t weight_mask,
-                                                         unsigned long long *__restrict__ out) {
+                                                         unsigned long long *__restrict__ out,
+                                                         const int4 *__restrict__ c2n, SpeciesTable S,
+                                                         unsigned long long *__restrict__ acc) {
   __shared__ float4 sm[kPackWarps][2][24];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int64_t p0 = ((int64_t)blockIdx.x * blockDim.x) + 32 * wib, p = p0 + lane;
+  int key = -1;  // the cell whose charge this lane deposits
+  int Q = 0;
   if (cs) {
     unsigned live = 0;
     if (p < n) {
@@ -1435,16 +1441,20 @@ __global__ void __launch_bounds__(kThreads) k_mixed_pack(const float *__restrict
       X.c[p] = w;
       if (w != MPG_DEAD) {
         const uint32_t sp = w >> 24;
-        if ((int64_t)(w & 0xFFFFFFu) >= T || sp >= MPG_MAX_SPECIES || !((weight_mask >> sp) & 1u))
+        if ((int64_t)(w & 0xFFFFFFu) >= T || sp >= MPG_MAX_SPECIES || !((weight_mask >> sp) & 1u)) {
           atomicMin(&out[0], (unsigned long long)p);
-        else
+        } else {
           live = 1;
+          key = (int)(w & 0xFFFFFFu);
+          Q = (int)S.qfix[sp];
+        }
       }
     }
     live = __reduce_add_sync(0xffffffffu, live);
     if (lane == 0 && live) atomicAdd(&out[1], (unsigned long long)live);
   }
   const bool vec = ((reinterpret_cast<uintptr_t>(b) | reinterpret_cast<uintptr_t>(v)) & 15u) == 0 && p0 + 32 <= n;
+  float4 bw = make_float4(0.f, 0.f, 0.f, 0.f);
   if (vec) {
     if (lane < 24) {
       sm[wib][0][lane] = reinterpret_cast<const float4 *>(b + 3 * p0)[lane];
@@ -1452,13 +1462,16 @@ __global__ void __launch_bounds__(kThreads) k_mixed_pack(const float *__restrict
     }
     __syncwarp();
     const float *fb = reinterpret_cast<const float *>(sm[wib][0]), *fv = reinterpret_cast<const float *>(sm[wib][1]);
-    X.b[p] = make_float4(fb[3 * lane], fb[3 * lane + 1], fb[3 * lane + 2], fv[3 * lane]);
+    bw = make_float4(fb[3 * lane], fb[3 * lane + 1], fb[3 * lane + 2], fv[3 * lane]);
+    X.b[p] = bw;
     X.v[p] = make_float2(fv[3 * lane + 1], fv[3 * lane + 2]);
-    return;
+  } else if (p < n) {
+    bw = make_float4(b[3 * p], b[3 * p + 1], b[3 * p + 2], v[3 * p]);
+    X.b[p] = bw;
+    X.v[p] = make_float2(v[3 * p + 1], v[3 * p + 2]);
   }
-  if (p >= n) return;
-  X.b[p] = make_float4(b[3 * p], b[3 * p + 1], b[3 * p + 2], v[3 * p]);
-  X.v[p] = make_float2(v[3 * p + 1], v[3 * p + 2]);
+  // every lane of the warp is here (acc is uniform across the grid)
+  if (acc) deposit_fixed_warp(acc, c2n, key, bw.x, bw.y, bw.z, Q);
 }
 __global__ void __launch_bounds__(kThreads) k_mixed_unpack(MixedParts X, int64_t n, float *__restrict__ b,
                                                            float *__restrict__ v, uint32_t *__restrict__ cs) {
@@ -1701,11 +1714,14 @@ void launch_cols_to_rows(cudaStream_t s, const double *cols, double *rows, int64
   if (n > 0) k_cols_to_rows<<<grid_for(n), kThreads, 0, s>>>(cols, rows, n, cap);
 }
 void launch_mixed_pack(cudaStream_t s, const float *b, const float *v, MixedParts X, int64_t n) {
-  if (n > 0) k_mixed_pack<<<grid_for(n), kThreads, 0, s>>>(b, v, X, n, nullptr, 0, 0u, nullptr);
+  if (n > 0)
+    k_mixed_pack<<<grid_for(n), kThreads, 0, s>>>(b, v, X, n, nullptr, 0, 0u, nullptr, nullptr, SpeciesTable{},
+                                                  nullptr);
 }
 void launch_mixed_pack_checked(cudaStream_t s, const uint32_t *cs, const float *b, const float *v, MixedParts X,
-                               int64_t n, int64_t T, uint32_t weight_mask, unsigned long long *out) {
-  if (n > 0) k_mixed_pack<<<grid_for(n), kThreads, 0, s>>>(b, v, X, n, cs, T, weight_mask, out);
+                               int64_t n, int64_t T, uint32_t weight_mask, unsigned long long *out,
+                               const DevMesh &M, const SpeciesTable &S, unsigned long long *acc) {
+  if (n > 0) k_mixed_pack<<<grid_for(n), kThreads, 0, s>>>(b, v, X, n, cs, T, weight_mask, out, M.c2n, S, acc);
 }
 void launch_mixed_check(cudaStream_t s, const uint32_t *cs, int64_t n, int64_t T, uint32_t weight_mask,
                         unsigned long long *out) {

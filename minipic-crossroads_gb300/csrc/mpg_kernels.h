@@ -150,9 +150,11 @@ void launch_fill_ref(cudaStream_t s, const PlainParts &P, int64_t n0, int nppe, 
 void launch_rows_to_cols(cudaStream_t s, const double *rows, double *cols, int64_t n, int64_t cap);
 void launch_cols_to_rows(cudaStream_t s, const double *cols, double *rows, int64_t n, int64_t cap);
 void launch_mixed_pack(cudaStream_t s, const float *b, const float *v, MixedParts X, int64_t n);
-// the pack with the cell words copied to X.c and checked as launch_mixed_check does
+// the pack with the cell words copied to X.c and checked as launch_mixed_check
+// does; with acc (zeroed) also the deposit of launch_mixed_deposit
 void launch_mixed_pack_checked(cudaStream_t s, const uint32_t *cs, const float *b, const float *v, MixedParts X,
-                               int64_t n, int64_t T, uint32_t weight_mask, unsigned long long *out);
+                               int64_t n, int64_t T, uint32_t weight_mask, unsigned long long *out,
+                               const DevMesh &M, const SpeciesTable &S, unsigned long long *acc);
 // cs (optional): the cell words as well
 void launch_mixed_unpack(cudaStream_t s, const MixedParts X, int64_t n, float *b, float *v, uint32_t *cs = nullptr);
 // out[0] = lowest invalid index (caller sets it to all ones), out[1] += live entries

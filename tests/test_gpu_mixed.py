@@ -341,12 +341,15 @@ def test_mixed_upload_download_from_mapped_host_memory(mpg):
     # a modified state goes in through the mapped buffers and comes back the same
     pb[:, 0] *= 0.5
     ctx.mixed_upload(pc, pb, pv)
+    acc_mapped = ctx.charge()[0]  # deposited by the upload's own pass
     c4, b4, v4 = ctx.mixed_download()
     assert (c4 == pc).all() and (b4 == pb).all() and (v4 == pv).all()
     # and steps on exactly as the same state uploaded from pageable copies
+    ctx.mixed_upload(pc, pb, pv)
     ctx.step(0.01, 1)
     c5, b5, v5 = ctx.mixed_download(out=out)
     ctx.mixed_upload(np.array(pc), np.array(pb), np.array(pv))
+    assert (ctx.charge()[0] == acc_mapped).all()  # deposited by the deposit kernel
     ctx.step(0.01, 1)
     c6, b6, v6 = ctx.mixed_download()
     assert (c5 == c6).all() and (b5 == b6).all() and (v5 == v6).all()
