@@ -542,13 +542,14 @@ int sort_mixed(mpg_ctx *c) {
 // The cell sort of mpg_step: permutation, start offsets and count only; the
 // gather is the next move's (launch_mixed_move_sorted), one pass over the
 // particle records fewer.  Any other use of the particle list completes the
-// gather first (settle_sort).
-int sort_mixed_deferred(mpg_ctx *c) {
+// gather first (settle_sort).  have_hist: the move that wrote the list
+// counted its particles per cell into the sort's counters.
+int sort_mixed_deferred(mpg_ctx *c, bool have_hist) {
   TRY(settle_sort(c));
   c->needs_sort = false;
   SortWork w;
   TRY(sort_work(c, w));
-  launch_mixed_sort_order(c->stream, c->mp[c->cur], c->n, c->mp[1 - c->cur], c->dm.T, w, c->d_count);
+  launch_mixed_sort_order(c->stream, c->mp[c->cur], c->n, c->mp[1 - c->cur], c->dm.T, w, c->d_count, have_hist);
   c->launches += 9;
   CKL();
   c->gather_pending = true;
@@ -599,7 +600,7 @@ int one_step(mpg_ctx *c, double dt, mpg_step_stats *acc_st, bool &sorted) {
     // freshly filled or uploaded particles are in arbitrary cell order: sort
     // before the first step instead of after sort_interval steps (its gather
     // is this step's move)
-    TRY(sort_mixed_deferred(c));
+    TRY(sort_mixed_deferred(c, false));
     sorted = true;
   }
   ev_record(c, 0);
@@ -613,17 +614,28 @@ int one_step(mpg_ctx *c, double dt, mpg_step_stats *acc_st, bool &sorted) {
   // the move deposits the new positions' charge into zeroed slots (the
   // memset is timed with the E-field phase, the move phase is the kernel)
   if (mixed) CK(cudaMemsetAsync(c->acc, 0, sizeof(unsigned long long) * 4 * c->dm.T, c->stream));
+  // a step that ends with a cell sort has the move count the particles per
+  // cell for it (its deposit runs are the sort's counting pass)
+  const bool sort_after =
+      mixed && c->cfg.sort_interval > 0 && (c->step_count + 1) % c->cfg.sort_interval == 0;
+  uint32_t *hist = nullptr;
+  if (sort_after) {
+    SortWork w;
+    TRY(sort_work(c, w));
+    hist = w.cnt;
+    CK(cudaMemsetAsync(hist, 0, sizeof(uint32_t) * c->dm.T, c->stream));
+  }
   ev_record(c, 3);
   if (mixed && c->gather_pending) {
     // the last step's cell sort: read through its permutation, write sorted
     const int other = 1 - c->cur;
     launch_mixed_move_sorted(c->stream, c->mp[c->cur], c->n, c->mp[other], c->sort_perm, c->d_count, c->dm, c->sp,
-                             (float)dt, c->cfg.kill_on_wall, c->cfg.max_crossings, c->acc, c->d_stats);
+                             (float)dt, c->cfg.kill_on_wall, c->cfg.max_crossings, c->acc, c->d_stats, hist);
     c->cur = other;
     c->gather_pending = false;
   } else if (mixed) {
     launch_mixed_move(c->stream, c->mp[c->cur], c->n, c->dm, c->sp, (float)dt, c->cfg.kill_on_wall,
-                      c->cfg.max_crossings, c->acc, c->d_stats);
+                      c->cfg.max_crossings, c->acc, c->d_stats, hist);
   } else {
     launch_plain_move(c->stream, c->pp[c->cur], c->n, c->dm, c->Etet, c->sp, dt, c->cfg.kill_on_wall,
                       c->cfg.max_crossings, c->d_stats);
@@ -633,8 +645,8 @@ int one_step(mpg_ctx *c, double dt, mpg_step_stats *acc_st, bool &sorted) {
   ev_record(c, 4);
   c->step_count++;
   if (mixed) {
-    if (c->cfg.sort_interval > 0 && c->step_count % c->cfg.sort_interval == 0) {
-      TRY(sort_mixed_deferred(c));
+    if (sort_after) {
+      TRY(sort_mixed_deferred(c, true));
       sorted = true;
     }
   } else {

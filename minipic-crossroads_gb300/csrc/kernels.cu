@@ -469,10 +469,13 @@ __global__ void __launch_bounds__(kScanThreads) k_compact_plain(PlainParts P, in
 // associative, so the result does not depend on the grouping.  Every lane of
 // the warp must call this; lanes with key < 0 contribute nothing.
 // `slots(key)` gives the four slot indices of cell `key`; it is called by
-// the lanes that issue a run's atomics only.
+// the lanes that issue a run's atomics only.  With hist, the run's length is
+// added to hist[key] as well: the particles per cell of the next cell sort
+// (k_cell_hist's counts, taken from the deposit's runs at no extra pass).
 template <class Slots>
 __device__ __forceinline__ void deposit_fixed_warp_t(unsigned long long *__restrict__ acc, Slots slots, int key,
-                                                     float b1, float b2, float b3, int Q) {
+                                                     float b1, float b2, float b3, int Q,
+                                                     uint32_t *__restrict__ hist) {
   // |Q| <= 2^25 quanta, so a run of up to 32 lanes sums to < 2^30 in int32
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -499,6 +502,7 @@ __device__ __forceinline__ void deposit_fixed_warp_t(unsigned long long *__restr
       atomicAdd(acc + q.y, (unsigned long long)(long long)c1);
       atomicAdd(acc + q.z, (unsigned long long)(long long)c2);
       atomicAdd(acc + q.w, (unsigned long long)(long long)c3);
+      if (hist) atomicAdd(hist + key, 32u);
     }
     return;
   }
@@ -525,13 +529,15 @@ __device__ __forceinline__ void deposit_fixed_warp_t(unsigned long long *__restr
     atomicAdd(acc + q.y, (unsigned long long)(long long)c1);
     atomicAdd(acc + q.z, (unsigned long long)(long long)c2);
     atomicAdd(acc + q.w, (unsigned long long)(long long)c3);
+    if (hist) atomicAdd(hist + key, (unsigned)(lane - seg + 1));
   }
 }
 
 // slot indices from the tet table c2n (a load per run)
 __device__ __forceinline__ void deposit_fixed_warp(unsigned long long *__restrict__ acc, const int4 *__restrict__ c2n,
-                                                   int key, float b1, float b2, float b3, int Q) {
-  deposit_fixed_warp_t(acc, [&](int k) { return c2n[k]; }, key, b1, b2, b3, Q);
+                                                   int key, float b1, float b2, float b3, int Q,
+                                                   uint32_t *__restrict__ hist = nullptr) {
+  deposit_fixed_warp_t(acc, [&](int k) { return c2n[k]; }, key, b1, b2, b3, Q, hist);
 }
 
 // Walk tables of a uniform Kuhn mesh (KuhnTable, staged in shared memory):
@@ -750,7 +756,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_mixed_move_persistent(MixedPart
                                                                     const int4 *__restrict__ c2n, SpeciesTable S,
                                                                     float dt, int kill, int max_cross,
                                                                     unsigned long long *__restrict__ acc,
-                                                                    DevStats *st) {
+                                                                    uint32_t *__restrict__ hist, DevStats *st) {
   __shared__ BlockTotals bt;
   __shared__ float s_jinv[KUHN ? 54 : 1];
   __shared__ uint32_t s_face[KUHN ? 24 : 1];
@@ -821,7 +827,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_mixed_move_persistent(MixedPart
         dq = (int)S.qfix[s];
       }
     }
-    deposit_fixed_warp(acc, c2n, dep_key, d1, d2, d3, dq);
+    deposit_fixed_warp(acc, c2n, dep_key, d1, d2, d3, dq, hist);
   };
   // walk the queued particles [qn - m, qn) in lanes 0 .. m-1
   auto drain = [&](int m) {
@@ -913,7 +919,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_mixed_move_persistent(MixedPart
       }
     }
     // every lane of the warp is here (c is uniform across the warp)
-    deposit_fixed_warp(acc, c2n, dep_key, d1, d2, d3, dq);
+    deposit_fixed_warp(acc, c2n, dep_key, d1, d2, d3, dq, hist);
     const unsigned qm = __ballot_sync(FULL, queue);
     if (queue) {
       const int slot = qn + __popc(qm & ((1u << lane) - 1u));
@@ -1620,42 +1626,47 @@ static unsigned move_wave_blocks() {
 }
 static void move_persistent(cudaStream_t s, const MixedParts &P, int64_t n, const MixedParts &Q,
                             const uint32_t *perm, const uint32_t *d_count, const DevMesh &M, const SpeciesTable &S,
-                            float dt, int kill, int max_cross, unsigned long long *acc, DevStats *st) {
+                            float dt, int kill, int max_cross, unsigned long long *acc, uint32_t *hist,
+                            DevStats *st) {
   const unsigned want = grid_for(n);
   if (M.kuhn) {
     const unsigned wave = move_wave_blocks<true>();
     k_mixed_move_persistent<true><<<want < wave ? want : wave, kThreads, 0, s>>>(
-        P, n, Q, perm, d_count, M.mrec, M.mnbr, M.etet4, M.ktab, M.c2n, S, dt, kill, max_cross, acc, st);
+        P, n, Q, perm, d_count, M.mrec, M.mnbr, M.etet4, M.ktab, M.c2n, S, dt, kill, max_cross, acc, hist, st);
   } else {
     const unsigned wave = move_wave_blocks<false>();
     k_mixed_move_persistent<false><<<want < wave ? want : wave, kThreads, 0, s>>>(
-        P, n, Q, perm, d_count, M.mrec, M.mnbr, M.etet4, M.ktab, M.c2n, S, dt, kill, max_cross, acc, st);
+        P, n, Q, perm, d_count, M.mrec, M.mnbr, M.etet4, M.ktab, M.c2n, S, dt, kill, max_cross, acc, hist, st);
   }
 }
 void launch_mixed_move(cudaStream_t s, const MixedParts &P, int64_t n, const DevMesh &M, const SpeciesTable &S,
-                       float dt, int kill, int max_cross, unsigned long long *acc, DevStats *st) {
+                       float dt, int kill, int max_cross, unsigned long long *acc, DevStats *st, uint32_t *hist) {
   if (n <= 0) return;
   static const char *env = getenv("MPG_MOVE_KERNEL");
-  if (!M.kuhn && env && atoi(env) == 0) {
+  if (!M.kuhn && env && atoi(env) == 0 && !hist) {
     k_mixed_move<<<grid_for(n), kThreads, 0, s>>>(P, n, M.mrec, M.mnbr, M.c2n, S, dt, kill, max_cross, acc, st);
     return;
   }
-  move_persistent(s, P, n, P, nullptr, nullptr, M, S, dt, kill, max_cross, acc, st);
+  move_persistent(s, P, n, P, nullptr, nullptr, M, S, dt, kill, max_cross, acc, hist, st);
 }
 void launch_mixed_move_sorted(cudaStream_t s, const MixedParts &P, int64_t n, const MixedParts &Q,
                               const uint32_t *perm, const uint32_t *d_count, const DevMesh &M, const SpeciesTable &S,
-                              float dt, int kill, int max_cross, unsigned long long *acc, DevStats *st) {
+                              float dt, int kill, int max_cross, unsigned long long *acc, DevStats *st,
+                              uint32_t *hist) {
   if (n <= 0) return;
-  move_persistent(s, P, n, Q, perm, d_count, M, S, dt, kill, max_cross, acc, st);
+  move_persistent(s, P, n, Q, perm, d_count, M, S, dt, kill, max_cross, acc, hist, st);
 }
 // the five passes of the stable cell sort; leaves perm[0..count) and start
 // (T + 1 entries) behind, and the count in *d_count
+// (have_hist: w.cnt already holds the particles per cell, counted by the move)
 template <bool kMixed>
 static void cell_sort_order(cudaStream_t s, const uint32_t *keys, int64_t n, int64_t T, const SortWork &w,
-                            uint32_t *tmp, uint32_t *d_count) {
-  cudaMemsetAsync(w.cnt, 0, sizeof(uint32_t) * T, s);
+                            uint32_t *tmp, uint32_t *d_count, bool have_hist = false) {
   cudaMemsetAsync(w.long_count, 0, 2 * sizeof(uint32_t), s);
-  if (n > 0) k_cell_hist<kMixed><<<grid_for(n), kThreads, 0, s>>>(keys, n, w.cnt);
+  if (!have_hist) {
+    cudaMemsetAsync(w.cnt, 0, sizeof(uint32_t) * T, s);
+    if (n > 0) k_cell_hist<kMixed><<<grid_for(n), kThreads, 0, s>>>(keys, n, w.cnt);
+  }
   scan_u32(s, w.cnt, w.start, T, w.scan_scratch, w.scan_len);
   cudaMemsetAsync(w.cnt, 0, sizeof(uint32_t) * T, s);
   if (n > 0) k_cell_slots<kMixed><<<grid_for(n), kThreads, 0, s>>>(keys, n, w.start, w.cnt, w.perm);
@@ -1666,8 +1677,8 @@ static void cell_sort_order(cudaStream_t s, const uint32_t *keys, int64_t n, int
   k_copy_u32<<<1, 1, 0, s>>>(w.start + T, d_count);
 }
 void launch_mixed_sort_order(cudaStream_t s, const MixedParts &P, int64_t n, const MixedParts &Q, int64_t T,
-                             const SortWork &w, uint32_t *d_count) {
-  cell_sort_order<true>(s, P.c, n, T, w, Q.c, d_count);
+                             const SortWork &w, uint32_t *d_count, bool have_hist) {
+  cell_sort_order<true>(s, P.c, n, T, w, Q.c, d_count, have_hist);
 }
 void launch_mixed_gather(cudaStream_t s, const MixedParts &P, int64_t n, const MixedParts &Q, const uint32_t *perm,
                          const uint32_t *d_count) {

@@ -98,14 +98,19 @@ void launch_mixed_convert(cudaStream_t s, const DevMesh &M, unsigned long long *
 // per-node quanta (N) from the slots
 void launch_node_quanta(cudaStream_t s, const DevMesh &M, const unsigned long long *acc, long long *out);
 void launch_efield_mixed(cudaStream_t s, const DevMesh &M, const double *phi);
+// hist (optional, zeroed T entries): the moved live particles per cell are
+// added to it, the counts the next cell sort needs (launch_mixed_sort_order
+// with have_hist)
 void launch_mixed_move(cudaStream_t s, const MixedParts &P, int64_t n, const DevMesh &M, const SpeciesTable &S,
-                       float dt, int kill, int max_cross, unsigned long long *acc, DevStats *st);
+                       float dt, int kill, int max_cross, unsigned long long *acc, DevStats *st,
+                       uint32_t *hist = nullptr);
 // the move fused with the gather of a cell sort (launch_mixed_sort_order):
 // particle i of the result is input particle perm[i] of P, moved, written to
 // Q; *d_count is the sorted count, Q's slots [count, n) are marked dead
 void launch_mixed_move_sorted(cudaStream_t s, const MixedParts &P, int64_t n, const MixedParts &Q,
                               const uint32_t *perm, const uint32_t *d_count, const DevMesh &M, const SpeciesTable &S,
-                              float dt, int kill, int max_cross, unsigned long long *acc, DevStats *st);
+                              float dt, int kill, int max_cross, unsigned long long *acc, DevStats *st,
+                              uint32_t *hist = nullptr);
 // Scratch of the stable cell sort: per-cell counts and starts (start holds
 // T + 1 entries: the first sorted position of every cell, start[T] = count),
 // the permutation (one uint32 per particle slot), the lists of cells with
@@ -126,9 +131,11 @@ struct SortWork {
 void launch_mixed_sort(cudaStream_t s, const MixedParts &P, int64_t n, const MixedParts &Q, int64_t T,
                        const SortWork &w, uint32_t *d_count);
 // the first four passes of launch_mixed_sort (permutation, starts, count;
-// Q.c is their scratch) and its last one, the gather
+// Q.c is their scratch) and its last one, the gather.  have_hist: w.cnt
+// already holds the live particles per cell of P (counted by the move that
+// wrote P), so the counting pass is left out.
 void launch_mixed_sort_order(cudaStream_t s, const MixedParts &P, int64_t n, const MixedParts &Q, int64_t T,
-                             const SortWork &w, uint32_t *d_count);
+                             const SortWork &w, uint32_t *d_count, bool have_hist = false);
 void launch_mixed_gather(cudaStream_t s, const MixedParts &P, int64_t n, const MixedParts &Q, const uint32_t *perm,
                          const uint32_t *d_count);
 void launch_plain_sort(cudaStream_t s, const PlainParts &P, int64_t n, const PlainParts &Q, int64_t T,

@@ -119,3 +119,32 @@ def test_sort_gather_fused_into_next_move(mpg):
         assert (u.view(np.uint8) == v.view(np.uint8)).all()
     assert (ida == idb).all() and (qa == qb).all()
     assert (pa.view(np.uint64) == pb.view(np.uint64)).all()
+
+
+def test_step_sort_counts_from_the_move_equal_a_separate_sort(mpg):
+    """A step that ends with a cell sort takes the sort's particles per cell
+    from the move's deposit runs instead of a counting pass: three steps
+    with sort_interval=3 (sorted before step 1 and after step 3) equal, bit
+    for bit, a sort, three unsorted steps and a sort by mpg_sort (its own
+    counting pass): the permutation (ids), every record, the cell starts and
+    the charge."""
+    runs = []
+    for fused in (True, False):
+        ctx = _ctx(mpg, mpg.MIXED, n_side=10, jitter=0.2, sort_interval=3 if fused else 0, track_ids=1)
+        n = 60000
+        ctx.reserve(n)
+        ctx.fill_uniform(n // 2, 51, 0, 1.0 / n, drift=(0.3, 0, 0), vth=0.2)
+        ctx.fill_uniform(n // 2, 52, 0, 1.0 / n, drift=(-0.3, 0, 0), vth=0.2)
+        if fused:
+            ctx.step(0.02, 3)
+        else:
+            ctx.sort()
+            ctx.step(0.02, 3)
+            ctx.sort()
+        runs.append((ctx.mixed_download(), ctx.download()["id"], ctx.cell_starts(), ctx.charge()[0]))
+        ctx.close()
+    (a, ida, sa, qa), (b, idb, sb, qb) = runs
+    assert len(ida) == len(idb)
+    for u, v in zip(a, b):
+        assert (u.view(np.uint8) == v.view(np.uint8)).all()
+    assert (ida == idb).all() and (sa == sb).all() and (qa == qb).all()
