@@ -477,9 +477,11 @@ int phase_solve(mpg_ctx *c) {
   return MPG_OK;
 }
 
-int phase_efield(mpg_ctx *c) {
+// zero_acc (mixed form): the charge slots are cleared alongside, for the
+// move's deposit
+int phase_efield(mpg_ctx *c, bool zero_acc) {
   if (c->cfg.precision == MPG_MIXED)
-    launch_efield_mixed(c->stream, c->dm, c->phi);
+    launch_efield_mixed(c->stream, c->dm, c->phi, zero_acc ? c->acc : nullptr, zero_acc ? 4 * c->dm.T : 0);
   else
     launch_efield_plain(c->stream, c->dm, c->phi, c->Etet);
   c->launches += 1;
@@ -608,12 +610,11 @@ int one_step(mpg_ctx *c, double dt, mpg_step_stats *acc_st, bool &sorted) {
   ev_record(c, 1);
   TRY(phase_solve(c));
   ev_record(c, 2);
-  TRY(phase_efield(c));
+  // the move deposits the new positions' charge into zeroed slots, cleared
+  // by the E-field pass (timed with the E-field phase)
+  TRY(phase_efield(c, mixed));
   CK(cudaMemsetAsync(&c->d_stats->ke, 0, sizeof(double), c->stream));
   c->starts_valid = false;
-  // the move deposits the new positions' charge into zeroed slots (the
-  // memset is timed with the E-field phase, the move phase is the kernel)
-  if (mixed) CK(cudaMemsetAsync(c->acc, 0, sizeof(unsigned long long) * 4 * c->dm.T, c->stream));
   // a step that ends with a cell sort has the move count the particles per
   // cell for it (its deposit runs are the sort's counting pass)
   const bool sort_after =
@@ -1688,7 +1689,7 @@ int mpg_solve(mpg_ctx *c, int *iters, double *resid) {
 int mpg_weight_efield(mpg_ctx *c) {
   ENTER(c);
   if (!c->configured) return fail(c, MPG_ERR_STATE, "not configured");
-  TRY(phase_efield(c));
+  TRY(phase_efield(c, false));
   CK(cudaStreamSynchronize(c->stream));
   return MPG_OK;
 }

@@ -650,30 +650,72 @@ __global__ void k_efield_mixed(int64_t T, const int4 *__restrict__ tets, float4 
   rec[3 * t + 2] = r2;
 }
 
-// E per tet on a uniform Kuhn mesh: the arithmetic of k_efield_mixed with
-// J^-1 from the 6-type table, written as (Ex, Ey, Ez, 0); the node ids come
-// from the hex index and the type's corner offsets (no tet table read)
-__global__ void k_efield_kuhn(int64_t T, KuhnTable kt, const double *__restrict__ phi,
-                              float4 *__restrict__ etet4) {
+// E per tet of a uniform Kuhn mesh, one thread per hex: node ids come from
+// the hex index and the table's corner offsets (no tet array is read).  All
+// six tets of a hex have the hex's first node as their vertex 0, so the
+// seven FP64 differences phi_c - phi_0 over the hex's other corners are
+// formed and rounded to FP32 once per hex (the per-tet form needs eighteen
+// on the narrow FP64 pipe, which bounded it), and each tet picks its three;
+// the values are those of the per-tet formula bit for bit.  The block's
+// 6 x 256 results are staged in shared memory and stored coalesced.  With
+// zero, the block also clears its share of the nzero charge slots (the next
+// move deposits into them), overlapping the stores with the FP64 work.
+constexpr int kEfThreads = 256;
+__global__ void __launch_bounds__(kEfThreads) k_efield_kuhn(int64_t T, KuhnTable kt, const double *__restrict__ phi,
+                                                            float4 *__restrict__ etet4,
+                                                            unsigned long long *__restrict__ zero, int64_t nzero) {
   __shared__ float sj[54];
-  __shared__ int32_t so[24];
+  __shared__ int sc[24];                     // corner (4 di + 2 dj + dk) of vertex q of type ty
+  __shared__ float sd[kEfThreads * 9];       // per thread: phi_c - phi_0 for c = 0..7 (stride 9)
+  __shared__ float4 se[6 * kEfThreads];
+  const int64_t SJ = kt.nz + 1, SI = (int64_t)(kt.ny + 1) * SJ;
   for (int i = threadIdx.x; i < 54; i += blockDim.x) sj[i] = kt.jinv[i / 9][i % 9];
-  for (int i = threadIdx.x; i < 24; i += blockDim.x) so[i] = kt.noff[i / 4][i % 4];
+  for (int i = threadIdx.x; i < 24; i += blockDim.x) {
+    const int64_t o = kt.noff[i / 4][i % 4], di = o / SI, dj = (o - di * SI) / SJ, dk = o - di * SI - dj * SJ;
+    sc[i] = (int)(4 * di + 2 * dj + dk);
+  }
   __syncthreads();
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= T) return;
-  const uint32_t h = (uint32_t)t / 6u, ty = (uint32_t)t - 6u * h;
-  const uint32_t nyz = (uint32_t)(kt.ny * kt.nz), i = div_magic40(h, kt.myz), rem = h - i * nyz,
-                 j = div_magic40(rem, kt.mz), k = rem - j * (uint32_t)kt.nz;
-  const int64_t base = ((int64_t)i * (kt.ny + 1) + j) * (kt.nz + 1) + k;
-  const int32_t *o = so + 4 * ty;
-  const double f0 = phi[base + o[0]];
-  const float d1 = (float)(phi[base + o[1]] - f0), d2 = (float)(phi[base + o[2]] - f0),
-              d3 = (float)(phi[base + o[3]] - f0);
-  const float *J = sj + 9 * ty;
-  etet4[t] = make_float4(__fmaf_rn(d3, J[6], __fmaf_rn(d2, J[3], d1 * J[0])),
-                         __fmaf_rn(d3, J[7], __fmaf_rn(d2, J[4], d1 * J[1])),
-                         __fmaf_rn(d3, J[8], __fmaf_rn(d2, J[5], d1 * J[2])), 0.f);
+  const int64_t H = T / 6, h0 = (int64_t)blockIdx.x * kEfThreads, h = h0 + threadIdx.x;
+  if (h < H) {
+    const uint32_t nyz = (uint32_t)(kt.ny * kt.nz), i = div_magic40((uint32_t)h, kt.myz),
+                   rem = (uint32_t)h - i * nyz, j = div_magic40(rem, kt.mz), k = rem - j * (uint32_t)kt.nz;
+    const int64_t base = ((int64_t)i * (kt.ny + 1) + j) * SJ + k;
+    const double f0 = phi[base];
+    float *d = sd + 9 * threadIdx.x;
+    d[0] = 0.f;
+    d[1] = (float)(phi[base + 1] - f0);
+    d[2] = (float)(phi[base + SJ] - f0);
+    d[3] = (float)(phi[base + SJ + 1] - f0);
+    d[4] = (float)(phi[base + SI] - f0);
+    d[5] = (float)(phi[base + SI + 1] - f0);
+    d[6] = (float)(phi[base + SI + SJ] - f0);
+    d[7] = (float)(phi[base + SI + SJ + 1] - f0);
+#pragma unroll
+    for (int ty = 0; ty < 6; ++ty) {
+      const float d1 = d[sc[4 * ty + 1]], d2 = d[sc[4 * ty + 2]], d3 = d[sc[4 * ty + 3]];
+      const float *J = sj + 9 * ty;
+      se[6 * threadIdx.x + ty] = make_float4(__fmaf_rn(d3, J[6], __fmaf_rn(d2, J[3], d1 * J[0])),
+                                             __fmaf_rn(d3, J[7], __fmaf_rn(d2, J[4], d1 * J[1])),
+                                             __fmaf_rn(d3, J[8], __fmaf_rn(d2, J[5], d1 * J[2])), 0.f);
+    }
+  }
+  __syncthreads();
+  const int64_t t0 = 6 * h0, nt = T - t0 < 6 * kEfThreads ? T - t0 : 6 * kEfThreads;
+  for (int q = threadIdx.x; q < nt; q += kEfThreads) etet4[t0 + q] = se[q];
+  if (zero) {
+    // this block's share [z0, z1) of the slots, in 16-byte stores where aligned
+    const int64_t z0 = nzero * blockIdx.x / gridDim.x, z1 = nzero * (blockIdx.x + 1) / gridDim.x;
+    int64_t a = z0;
+    if (a & 1) {  // to a 16-byte boundary (the slots start on one)
+      if (threadIdx.x == 0 && a < z1) zero[a] = 0ull;
+      ++a;
+    }
+    if (a > z1) a = z1;
+    const int64_t npair = (z1 - a) >> 1;
+    uint4 *zp = reinterpret_cast<uint4 *>(zero + a);
+    for (int64_t q = threadIdx.x; q < npair; q += kEfThreads) zp[q] = make_uint4(0u, 0u, 0u, 0u);
+    if (threadIdx.x == 0 && ((z1 - a) & 1)) zero[z1 - 1] = 0ull;
+  }
 }
 
 __global__ void __launch_bounds__(kThreads) k_mixed_move(MixedParts P, int64_t n, const float4 *__restrict__ rec,
@@ -1603,11 +1645,15 @@ void launch_mixed_convert(cudaStream_t s, const DevMesh &M, unsigned long long *
 void launch_node_quanta(cudaStream_t s, const DevMesh &M, const unsigned long long *acc, long long *out) {
   k_node_quanta<<<grid_for(M.N), kThreads, 0, s>>>(M.N, M.n2c_off, acc, out);
 }
-void launch_efield_mixed(cudaStream_t s, const DevMesh &M, const double *phi) {
-  if (M.kuhn)
-    k_efield_kuhn<<<grid_for(M.T), kThreads, 0, s>>>(M.T, M.ktab, phi, M.etet4);
-  else
+void launch_efield_mixed(cudaStream_t s, const DevMesh &M, const double *phi, unsigned long long *zero,
+                         int64_t nzero) {
+  if (M.kuhn) {
+    k_efield_kuhn<<<(unsigned)((M.T / 6 + kEfThreads - 1) / kEfThreads), kEfThreads, 0, s>>>(M.T, M.ktab, phi,
+                                                                                            M.etet4, zero, nzero);
+  } else {
     k_efield_mixed<<<grid_for(M.T), kThreads, 0, s>>>(M.T, M.tets, M.mrec, phi);
+    if (zero && nzero > 0) cudaMemsetAsync(zero, 0, sizeof(unsigned long long) * nzero, s);
+  }
 }
 // resident blocks of a persistent move kernel on the current device (one wave)
 template <bool KUHN>

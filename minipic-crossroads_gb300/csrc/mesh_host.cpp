@@ -524,6 +524,10 @@ bool host_kuhn_table(const HostMesh &m, float jinv[6][9], uint32_t face[6][4], i
       corner[k][q] = (int)(4 * di + 2 * dj + dk);
       noff[k][q] = (int32_t)(di * si + dj * sj + dk);
     }
+  // the per-hex E-field pass relies on vertex 0 of every type being the
+  // hex's first node
+  for (int k = 0; k < 6; ++k)
+    if (corner[k][0] != 0) return false;
   // every tet must match its type's entries bit for bit
   int bad = 0;
 #pragma omp parallel for schedule(static) reduction(+ : bad)

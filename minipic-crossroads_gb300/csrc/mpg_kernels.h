@@ -97,7 +97,10 @@ void launch_mixed_convert(cudaStream_t s, const DevMesh &M, unsigned long long *
                           double *rhs);
 // per-node quanta (N) from the slots
 void launch_node_quanta(cudaStream_t s, const DevMesh &M, const unsigned long long *acc, long long *out);
-void launch_efield_mixed(cudaStream_t s, const DevMesh &M, const double *phi);
+// zero (optional): nzero charge slots cleared alongside (by the E kernel
+// itself on a uniform Kuhn mesh)
+void launch_efield_mixed(cudaStream_t s, const DevMesh &M, const double *phi, unsigned long long *zero = nullptr,
+                         int64_t nzero = 0);
 // hist (optional, zeroed T entries): the moved live particles per cell are
 // added to it, the counts the next cell sort needs (launch_mixed_sort_order
 // with have_hist)
