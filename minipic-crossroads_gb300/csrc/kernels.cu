@@ -1042,17 +1042,33 @@ __global__ void k_cell_hist(const uint32_t *__restrict__ c, int64_t n, uint32_t 
   if (rank == 0 && key != MPG_DEAD) atomicAdd(&cnt[key], (unsigned)len);
 }
 
+// Each thread takes kSlotsPer particles, kThreads apart (each warp sees
+// kSlotsPer runs of 32 consecutive particles), so that their slot claims and
+// start loads are in flight together: one claim is an atomic whose result
+// the thread waits for, and the pass is bound by that latency.
+constexpr int kSlotsPer = 4;
 template <bool kMixed>
 __global__ void k_cell_slots(const uint32_t *__restrict__ c, int64_t n, const uint32_t *__restrict__ start,
                              uint32_t *__restrict__ fill, uint32_t *__restrict__ perm) {
-  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t key = sort_key<kMixed>(c, p, n);
-  int first, rank, len;
-  cell_run(key, first, rank, len);
-  uint32_t base = 0;
-  if (rank == 0 && key != MPG_DEAD) base = atomicAdd(&fill[key], (unsigned)len);
-  base = __shfl_sync(0xffffffffu, base, first);
-  if (key != MPG_DEAD) perm[start[key] + base + (uint32_t)rank] = (uint32_t)p;
+  const int64_t p0 = (int64_t)blockIdx.x * blockDim.x * kSlotsPer + threadIdx.x;
+  uint32_t key[kSlotsPer], base[kSlotsPer], st[kSlotsPer];
+  int first[kSlotsPer], rank[kSlotsPer], len[kSlotsPer];
+#pragma unroll
+  for (int u = 0; u < kSlotsPer; ++u) {
+    key[u] = sort_key<kMixed>(c, p0 + (int64_t)u * blockDim.x, n);
+    cell_run(key[u], first[u], rank[u], len[u]);
+  }
+#pragma unroll
+  for (int u = 0; u < kSlotsPer; ++u) {
+    base[u] = 0;
+    if (rank[u] == 0 && key[u] != MPG_DEAD) base[u] = atomicAdd(&fill[key[u]], (unsigned)len[u]);
+    st[u] = key[u] != MPG_DEAD ? start[key[u]] : 0u;
+  }
+#pragma unroll
+  for (int u = 0; u < kSlotsPer; ++u) {
+    const uint32_t b = __shfl_sync(0xffffffffu, base[u], first[u]);
+    if (key[u] != MPG_DEAD) perm[st[u] + b + (uint32_t)rank[u]] = (uint32_t)(p0 + (int64_t)u * blockDim.x);
+  }
 }
 
 // ranges of up to kSortLocal entries are sorted by one thread (insertion sort,
@@ -1076,15 +1092,21 @@ __global__ void k_cell_order(const uint32_t *__restrict__ start, int64_t T, uint
     return;
   }
   // most ranges are in order already (claimed by one warp run): check them
-  // in place before anything goes to the local array
+  // in place before anything goes to the local array, four loads at a time
   {
     uint32_t prev = perm[lo], k = 1;
-    for (; k < m; ++k) {
+    bool ok = true;
+    for (; ok && k + 4 <= m; k += 4) {
+      const uint32_t x0 = perm[lo + k], x1 = perm[lo + k + 1], x2 = perm[lo + k + 2], x3 = perm[lo + k + 3];
+      ok = prev <= x0 && x0 <= x1 && x1 <= x2 && x2 <= x3;
+      prev = x3;
+    }
+    for (; ok && k < m; ++k) {
       const uint32_t x = perm[lo + k];
-      if (x < prev) break;
+      ok = prev <= x;
       prev = x;
     }
-    if (k == m) return;
+    if (ok) return;
   }
   uint32_t a[kSortLocal];
   for (uint32_t k = 0; k < m; ++k) a[k] = perm[lo + k];
@@ -1730,7 +1752,9 @@ static void cell_sort_order(cudaStream_t s, const uint32_t *keys, int64_t n, int
   }
   scan_u32(s, w.cnt, w.start, T, w.scan_scratch, w.scan_len);
   cudaMemsetAsync(w.cnt, 0, sizeof(uint32_t) * T, s);
-  if (n > 0) k_cell_slots<kMixed><<<grid_for(n), kThreads, 0, s>>>(keys, n, w.start, w.cnt, w.perm);
+  if (n > 0)
+    k_cell_slots<kMixed><<<grid_for((n + kSlotsPer - 1) / kSlotsPer), kThreads, 0, s>>>(keys, n, w.start, w.cnt,
+                                                                                       w.perm);
   k_cell_order<<<grid_for(T), kThreads, 0, s>>>(w.start, T, w.perm, w.long_list, w.list_len, w.long_count);
   k_cell_order_warp<<<w.long_blocks * 4, kWarpSortThreads, 0, s>>>(w.start, w.long_list, w.long_count, w.perm);
   k_cell_order_long<<<w.long_blocks, kLongThreads, 0, s>>>(w.start, w.long_list, w.list_len, w.long_count, w.perm,
