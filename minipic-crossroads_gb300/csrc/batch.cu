@@ -105,8 +105,7 @@ __device__ __forceinline__ void batch_convert_at(const SlotDev &S, int64_t i) {
   } else if (h == 1) {
     S.phi_prev[i] = S.phi[i];
   }
-  long long a = 0;
-  for (int32_t q = S.n2c_off[i]; q < S.n2c_off[i + 1]; ++q) a += (long long)S.acc[q];
+  const long long a = slot_sum(S.acc, S.n2c_off[i], S.n2c_off[i + 1]);
   double r = -((double)a * S.quantum);
   if (S.bg) r += S.bg[i];
   if (S.bnd[i]) r = 0.0;

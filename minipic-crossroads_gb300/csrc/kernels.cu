@@ -600,26 +600,10 @@ __global__ void __launch_bounds__(kThreads) k_mixed_deposit(MixedParts P, int64_
 // charge quanta of node i: the sum of its slot range acc[off[i] .. off[i+1])
 // (one thread per node; the slots are zeroed before the next deposit by the
 // E-field pass or a memset, which is cheaper than zeroing them here, behind
-// the reads).  The range is read in 16-byte loads, four slots per iteration into four
-// partial sums (integer sums: the result does not depend on the grouping),
-// so each thread has several loads in flight; acc starts on a 16-byte
-// boundary (a device allocation), so an even slot index is one too.
+// the reads)
 __device__ __forceinline__ long long node_quanta(int64_t i, const int32_t *__restrict__ off,
                                                  const unsigned long long *__restrict__ acc) {
-  int32_t q = off[i];
-  const int32_t e = off[i + 1];
-  long long a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-  if ((q & 1) && q < e) a0 += (long long)acc[q++];
-  for (; q + 4 <= e; q += 4) {
-    const ulonglong2 x = *reinterpret_cast<const ulonglong2 *>(acc + q);
-    const ulonglong2 y = *reinterpret_cast<const ulonglong2 *>(acc + q + 2);
-    a0 += (long long)x.x;
-    a1 += (long long)x.y;
-    a2 += (long long)y.x;
-    a3 += (long long)y.y;
-  }
-  for (; q < e; ++q) a0 += (long long)acc[q];
-  return (a0 + a1) + (a2 + a3);
+  return slot_sum(acc, off[i], off[i + 1]);
 }
 
 // Periodic meshes (plane > 0): the ghost plane's quanta are folded into

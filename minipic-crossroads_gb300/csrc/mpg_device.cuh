@@ -104,6 +104,27 @@ __device__ __forceinline__ bool grid_barrier(DevStats *st, unsigned nblocks, uns
   return ok != 0;
 }
 
+// sum of the fixed-point charge slots acc[lo .. hi) as a signed integer, in
+// 16-byte loads, four slots per iteration into four partial sums (integer
+// sums: the grouping does not change the result), so that a thread has
+// several loads in flight; acc must start on a 16-byte boundary (a device
+// allocation does), so an even slot index is one too
+__device__ __forceinline__ long long slot_sum(const unsigned long long *__restrict__ acc, int32_t lo, int32_t hi) {
+  int32_t q = lo;
+  long long a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+  if ((q & 1) && q < hi) a0 += (long long)acc[q++];
+  for (; q + 4 <= hi; q += 4) {
+    const ulonglong2 x = *reinterpret_cast<const ulonglong2 *>(acc + q);
+    const ulonglong2 y = *reinterpret_cast<const ulonglong2 *>(acc + q + 2);
+    a0 += (long long)x.x;
+    a1 += (long long)x.y;
+    a2 += (long long)y.x;
+    a3 += (long long)y.y;
+  }
+  for (; q < hi; ++q) a0 += (long long)acc[q];
+  return (a0 + a1) + (a2 + a3);
+}
+
 // block-wide sum of one double per thread (blockDim.x multiple of 32, <= 1024);
 // deterministic for a fixed block size.  Result valid in thread 0.  The last
 // stage runs in warp 0 as a shuffle tree (FP64 is a slow pipe on this chip, so
