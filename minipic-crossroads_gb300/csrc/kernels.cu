@@ -1055,13 +1055,41 @@ __global__ void k_cell_slots(const uint32_t *__restrict__ c, int64_t n, const ui
   }
 }
 
-// ranges of up to kSortLocal entries are sorted by one thread (insertion sort,
-// in registers and L1); ranges of up to kSortWarp entries are listed for
+// ranges of up to kSortLocal entries are sorted by one thread (a sorting
+// network in registers); ranges of up to kSortWarp entries are listed for
 // k_cell_order_warp (one warp each), longer ones for k_cell_order_long (one
 // block each).  The two lists share one buffer: medium ranges from the
 // front (counter long_count[0]), long ones from the back (long_count[1]).
 constexpr int kSortLocal = 32;
 constexpr int kSortWarp = 1024;
+
+// Ascending sort of a[0..m), m <= N (N a power of two), in registers: the
+// entries padded to N with the largest key, then a bitonic sorting network
+// whose loops unroll completely (every index a constant), so nothing goes
+// through local memory.
+template <int N>
+__device__ __forceinline__ void sort_range_net(uint32_t *__restrict__ a, uint32_t m) {
+  uint32_t v[N];
+#pragma unroll
+  for (int k = 0; k < N; ++k) v[k] = (uint32_t)k < m ? a[k] : 0xFFFFFFFFu;
+#pragma unroll
+  for (int k = 2; k <= N; k <<= 1)
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1)
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        const int l = i ^ j;
+        if (l > i) {
+          const uint32_t x = v[i], y = v[l];
+          const bool up = (i & k) == 0;
+          v[i] = up ? min(x, y) : max(x, y);
+          v[l] = up ? max(x, y) : min(x, y);
+        }
+      }
+#pragma unroll
+  for (int k = 0; k < N; ++k)
+    if ((uint32_t)k < m) a[k] = v[k];
+}
 __global__ void k_cell_order(const uint32_t *__restrict__ start, int64_t T, uint32_t *__restrict__ perm,
                              uint32_t *__restrict__ lists, int64_t list_len, uint32_t *__restrict__ long_count) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1092,18 +1120,10 @@ __global__ void k_cell_order(const uint32_t *__restrict__ start, int64_t T, uint
     }
     if (ok) return;
   }
-  uint32_t a[kSortLocal];
-  for (uint32_t k = 0; k < m; ++k) a[k] = perm[lo + k];
-  for (uint32_t k = 1; k < m; ++k) {
-    const uint32_t x = a[k];
-    int j = (int)k - 1;
-    while (j >= 0 && a[j] > x) {
-      a[j + 1] = a[j];
-      --j;
-    }
-    a[j + 1] = x;
-  }
-  for (uint32_t k = 0; k < m; ++k) perm[lo + k] = a[k];
+  if (m <= 16)
+    sort_range_net<16>(perm + lo, m);
+  else
+    sort_range_net<32>(perm + lo, m);
 }
 
 // number of entries of a taken among the first d outputs of the merge of
