@@ -1064,14 +1064,19 @@ constexpr int kSortLocal = 32;
 constexpr int kSortWarp = 1024;
 
 // Ascending sort of a[0..m), m <= N (N a power of two), in registers: the
-// entries padded to N with the largest key, then a bitonic sorting network
-// whose loops unroll completely (every index a constant), so nothing goes
-// through local memory.
+// entries padded to N with the largest key; a range found in order (most are:
+// claimed by one warp run) is left as it is, any other goes through a bitonic
+// sorting network whose loops unroll completely (every index a constant), so
+// nothing goes through local memory, and is written back.
 template <int N>
 __device__ __forceinline__ void sort_range_net(uint32_t *__restrict__ a, uint32_t m) {
   uint32_t v[N];
 #pragma unroll
   for (int k = 0; k < N; ++k) v[k] = (uint32_t)k < m ? a[k] : 0xFFFFFFFFu;
+  bool in_order = true;
+#pragma unroll
+  for (int k = 0; k + 1 < N; ++k) in_order = in_order && v[k] <= v[k + 1];  // the padding is in order too
+  if (in_order) return;
 #pragma unroll
   for (int k = 2; k <= N; k <<= 1)
 #pragma unroll
@@ -1102,23 +1107,6 @@ __global__ void k_cell_order(const uint32_t *__restrict__ start, int64_t T, uint
     else
       lists[list_len - 1 - atomicAdd(long_count + 1, 1u)] = (uint32_t)e;
     return;
-  }
-  // most ranges are in order already (claimed by one warp run): check them
-  // in place before anything goes to the local array, four loads at a time
-  {
-    uint32_t prev = perm[lo], k = 1;
-    bool ok = true;
-    for (; ok && k + 4 <= m; k += 4) {
-      const uint32_t x0 = perm[lo + k], x1 = perm[lo + k + 1], x2 = perm[lo + k + 2], x3 = perm[lo + k + 3];
-      ok = prev <= x0 && x0 <= x1 && x1 <= x2 && x2 <= x3;
-      prev = x3;
-    }
-    for (; ok && k < m; ++k) {
-      const uint32_t x = perm[lo + k];
-      ok = prev <= x;
-      prev = x;
-    }
-    if (ok) return;
   }
   if (m <= 16)
     sort_range_net<16>(perm + lo, m);
