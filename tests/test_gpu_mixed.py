@@ -255,16 +255,18 @@ def test_extrapolated_initial_guess_same_solution(mpg, form, ws):
     assert ib <= ia, (ia, ib)
 
 
-def test_kuhn_table_walk_equals_per_tet_records(mpg, monkeypatch):
+@pytest.mark.parametrize("shape", [12, (10, 7, 13)])
+def test_kuhn_table_walk_equals_per_tet_records(mpg, monkeypatch, shape):
     """On a uniform Kuhn mesh the mixed walk reads J^-1 and the neighbours from
-    the 6-type table; against the per-tet records (MPG_KUHN_WALK=0) the state,
-    the per-node charge, phi, E and the counts after several steps with many
-    crossings and wall exits are bit-identical."""
+    the 6-type table and E is formed per hex; against the per-tet records
+    (MPG_KUHN_WALK=0) the state, the per-node charge, phi, E and the counts
+    after several steps with many crossings and wall exits are bit-identical
+    (a cube, and a box with three different cell counts)."""
     runs = []
     for kw in ("1", "0"):
         monkeypatch.setenv("MPG_KUHN_WALK", kw)
         ctx = mpg.Ctx(0)
-        ctx.mesh(12, split=mpg.SPLIT_KUHN6)
+        ctx.mesh(shape, split=mpg.SPLIT_KUHN6)
         ctx.configure(precision=mpg.MIXED, deposit=mpg.DEPOSIT_LINEAR, solver=mpg.SOLVER_CG_MG, tol=1e-10,
                       warm_start=2, kill_on_wall=1, sort_interval=3, rho_background=1.0)
         n = 60000
